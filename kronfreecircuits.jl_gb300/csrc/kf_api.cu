@@ -1,0 +1,208 @@
+// extern "C" entry points of libkfgpu.so (declared in include/kfgpu.h).  Each converts a
+// kf::Error (or any C++ exception) into its status code and records the message for
+// kf_last_error; nothing throws across the C boundary.
+#include <cstring>
+#include <limits>
+
+#include "kf_internal.h"
+
+namespace kf {
+void build_op(const kf_op_desc *desc, kf_op *op);
+void free_op(kf_op *op);
+void solve_dispatch(kf_op *op, const kf_solver_opts &o, int m, const double *X0, const double *seed, double *E_out,
+                    double *V_out, kf_solve_stats &st);
+
+static thread_local std::string g_last_error;
+void set_last_error(const std::string &msg) { g_last_error = msg; }
+
+template <typename F>
+static int guarded(F &&f) {
+    try {
+        f();
+        return KF_OK;
+    } catch (const Error &e) {
+        set_last_error(e.what());
+        return e.code;
+    } catch (const std::bad_alloc &) {
+        set_last_error("host allocation failed");
+        return KF_ENOMEM;
+    } catch (const std::exception &e) {
+        set_last_error(e.what());
+        return KF_EINVAL;
+    }
+}
+}  // namespace kf
+
+using namespace kf;
+
+extern "C" {
+
+int kf_version(void) { return KFGPU_VERSION; }
+
+int kf_last_error(char *buf, size_t len) {
+    if (!buf || len == 0) return KF_EINVAL;
+    std::strncpy(buf, g_last_error.c_str(), len - 1);
+    buf[len - 1] = '\0';
+    return KF_OK;
+}
+
+int kf_op_create(const kf_op_desc *desc, kf_op **out) {
+    return guarded([&] {
+        KF_REQUIRE(out != nullptr, KF_EINVAL, "kf_op_create: out is NULL");
+        *out = nullptr;
+        kf_op *op = new kf_op();
+        try {
+            KF_CUDA(cudaGetDevice(&op->device));
+            KF_CUDA(cudaStreamCreateWithFlags(&op->stream, cudaStreamNonBlocking));
+            build_op(desc, op);
+        } catch (...) {
+            free_op(op);
+            delete op;
+            throw;
+        }
+        *out = op;
+    });
+}
+
+int kf_op_destroy(kf_op *op) {
+    return guarded([&] {
+        if (!op) return;
+        cudaStreamSynchronize(op->stream);
+        free_op(op);
+        delete op;
+    });
+}
+
+int kf_op_size(const kf_op *op, int64_t *n) {
+    return guarded([&] {
+        KF_REQUIRE(op && n, KF_EINVAL, "kf_op_size: NULL argument");
+        *n = op->N;
+    });
+}
+
+static bool ranges_overlap(const void *a, size_t na, const void *b, size_t nb) {
+    const char *pa = (const char *)a, *pb = (const char *)b;
+    return pa < pb + nb && pb < pa + na;
+}
+
+int kf_op_apply(kf_op *op, const void *X, void *Y, int64_t ldx, int64_t ldy, int64_t b, int32_t flags) {
+    return guarded([&] {
+        KF_REQUIRE(op != nullptr, KF_EINVAL, "kf_op_apply: op is NULL");
+        const int64_t N = op->N;
+        KF_REQUIRE(b >= 0, KF_EDIM, "mul!: negative block width");
+        KF_REQUIRE(ldx >= N && ldy >= N, KF_EDIM,
+                   "KronFreeOperator of size (" + std::to_string(N) + ", " + std::to_string(N) +
+                       ") applied to x with " + std::to_string(ldx) + " rows");
+        if (b == 0) return;
+        KF_REQUIRE(X && Y, KF_EINVAL, "kf_op_apply: NULL block");
+        const size_t es = (flags & KF_F32) ? 4 : 8;
+        const size_t bx = ((size_t)(b - 1) * ldx + N) * es, by = ((size_t)(b - 1) * ldy + N) * es;
+        KF_REQUIRE(!ranges_overlap(X, bx, Y, by), KF_EALIAS, "mul!: y must not alias x");
+        cudaStream_t s = op->stream;
+        if (flags & KF_HOST) {
+            void *dX = nullptr, *dY = nullptr;
+            KF_CUDA(cudaMallocAsync(&dX, (size_t)N * b * es, s));
+            KF_CUDA(cudaMallocAsync(&dY, (size_t)N * b * es, s));
+            KF_CUDA(cudaMemcpy2DAsync(dX, N * es, X, ldx * es, N * es, b, cudaMemcpyHostToDevice, s));
+            launch_apply(op, (flags & KF_F32) != 0, dX, dY, N, N, b, 1, 0, nullptr, 0, 0, s);
+            KF_CUDA(cudaMemcpy2DAsync(Y, ldy * es, dY, N * es, N * es, b, cudaMemcpyDeviceToHost, s));
+            KF_CUDA(cudaFreeAsync(dX, s));
+            KF_CUDA(cudaFreeAsync(dY, s));
+            KF_CUDA(cudaStreamSynchronize(s));
+        } else {
+            launch_apply(op, (flags & KF_F32) != 0, X, Y, ldx, ldy, b, 1, 0, nullptr, 0, 0, s);
+        }
+    });
+}
+
+int kf_op_apply_axpby(kf_op *op, const void *X, void *Y, const void *Z, int64_t ld, int64_t b, double alpha,
+                      double beta, double gamma, int32_t flags) {
+    return guarded([&] {
+        KF_REQUIRE(op != nullptr, KF_EINVAL, "kf_op_apply_axpby: op is NULL");
+        KF_REQUIRE(!(flags & KF_HOST), KF_EINVAL, "kf_op_apply_axpby: device pointers only");
+        KF_REQUIRE(ld >= op->N && b >= 0, KF_EDIM, "kf_op_apply_axpby: bad block shape");
+        if (b == 0) return;
+        const size_t es = (flags & KF_F32) ? 4 : 8;
+        const size_t bx = ((size_t)(b - 1) * ld + op->N) * es;
+        KF_REQUIRE(!ranges_overlap(X, bx, Y, bx), KF_EALIAS, "mul!: y must not alias x");
+        KF_REQUIRE(Z == nullptr || !ranges_overlap(Z, bx, Y, bx), KF_EALIAS, "kf_op_apply_axpby: y must not alias z");
+        launch_apply(op, (flags & KF_F32) != 0, X, Y, ld, ld, b, alpha, beta, Z, ld, Z ? gamma : 0.0, op->stream);
+    });
+}
+
+int kf_op_diagonal(kf_op *op, double *out) {
+    return guarded([&] {
+        KF_REQUIRE(op && out, KF_EINVAL, "kf_op_diagonal: NULL argument");
+        std::memcpy(out, op->h_fulldiag.data(), sizeof(double) * op->N);
+    });
+}
+
+int kf_op_gershgorin(kf_op *op, double *out) {
+    return guarded([&] {
+        KF_REQUIRE(op && out, KF_EINVAL, "kf_op_gershgorin: NULL argument");
+        *out = op->gershgorin;
+    });
+}
+
+int kf_op_get_stream(kf_op *op, void **stream) {
+    return guarded([&] {
+        KF_REQUIRE(op && stream, KF_EINVAL, "kf_op_get_stream: NULL argument");
+        *stream = (void *)op->stream;
+    });
+}
+
+int kf_op_set_stream(kf_op *op, void *stream) {
+    return guarded([&] {
+        KF_REQUIRE(op != nullptr, KF_EINVAL, "kf_op_set_stream: op is NULL");
+        KF_CUDA(cudaStreamSynchronize(op->stream));
+        if (op->own_stream) KF_CUDA(cudaStreamDestroy(op->stream));
+        op->stream = (cudaStream_t)stream;
+        op->own_stream = false;
+    });
+}
+
+int kf_op_sync(kf_op *op) {
+    return guarded([&] {
+        KF_REQUIRE(op != nullptr, KF_EINVAL, "kf_op_sync: op is NULL");
+        KF_CUDA(cudaStreamSynchronize(op->stream));
+    });
+}
+
+void kf_solver_opts_default(kf_solver_opts *o, int32_t kind) {
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->kind = kind;
+    o->precision = KF_PREC_F64;
+    o->tol = kind == KF_SOLVER_LANCZOS ? 1e-10 : 1e-8;
+    o->maxiter = kind == KF_SOLVER_LOBPCG ? 1000 : kind == KF_SOLVER_CHEBYSHEV ? 50 : 1000;
+    o->preconditioner = KF_PRECOND_RITZ;
+    o->eta = 0.01;
+    o->guard = 4;
+    o->degree = 100;
+    o->extra = 40;
+    o->rescale_every = 20;
+    o->ortho = KF_ORTHO_SVQB;
+    o->bound = std::numeric_limits<double>::quiet_NaN();
+    o->krylovdim = 0;
+    o->rng_seed = 0x4b46;
+    o->mixed_switch = 2e-6;
+    o->fallback_iters = 3;
+    o->fallback_resid = 0.0;
+}
+
+int kf_solve(kf_op *op, const kf_solver_opts *opts, int32_t m, const double *X0, const double *seed, double *E_out,
+             double *V_out, kf_solve_stats *stats) {
+    return guarded([&] {
+        KF_REQUIRE(op && opts, KF_EINVAL, "kf_solve: NULL argument");
+        kf_solve_stats st;
+        try {
+            solve_dispatch(op, *opts, m, X0, seed, E_out, V_out, st);
+        } catch (...) {
+            if (stats) *stats = st;
+            throw;
+        }
+        if (stats) *stats = st;
+    });
+}
+
+}  // extern "C"

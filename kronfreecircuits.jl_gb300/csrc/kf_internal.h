@@ -1,0 +1,159 @@
+// Internal declarations shared by the translation units of libkfgpu.so.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cmath>
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/kfgpu.h"
+
+namespace kf {
+
+// An error carrying a status code; every extern "C" entry point converts it to its status and
+// records the message for kf_last_error.
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+void set_last_error(const std::string &msg);
+
+#define KF_CUDA(call)                                                                          \
+    do {                                                                                       \
+        cudaError_t e_ = (call);                                                               \
+        if (e_ != cudaSuccess)                                                                 \
+            throw ::kf::Error(e_ == cudaErrorMemoryAllocation ? KF_ENOMEM : KF_ECUDA,          \
+                              std::string(#call) + ": " + cudaGetErrorString(e_));             \
+    } while (0)
+
+#define KF_REQUIRE(cond, code, msg)                                                            \
+    do {                                                                                       \
+        if (!(cond)) throw ::kf::Error((code), (msg));                                         \
+    } while (0)
+
+constexpr int MAXDIMS = 8;     // axes of a state tensor
+constexpr int MAXF = 4;        // non-dense factors of one fused product term
+constexpr int MAXB = 24;       // bands of one banded factor (a periodic order-8 stencil has 16)
+constexpr int MAXT = 16;       // fused product terms of one operator
+constexpr int MAXE = 48;       // stencil entries (products of bands) over all fused terms
+
+// A banded factor in the form the fused kernel reads: per band an offset, and weights
+// w[i * nb + b] (row-major, the band index fastest), zero where i + off[b] leaves [0, n).
+struct BandFactorDev {
+    int axis;
+    int nb;
+    int off[MAXB];
+    int w_off;                 // offset of this factor's weights in the op's weight pool
+};
+
+// One fused product term: a product of banded factors on distinct axes, the coefficient
+// folded into the first factor's weights.
+struct FusedTerm {
+    int nf;
+    BandFactorDev f[MAXF];
+};
+
+// Everything the fused apply kernel needs, passed by value as a kernel parameter.
+struct ApplyPlan {
+    int ndims;
+    int64_t dims[MAXDIMS];
+    int64_t stride[MAXDIMS];
+    int64_t N;
+    int nterms;
+    FusedTerm t[MAXT];
+};
+
+// A dense-containing term, applied as a chain of single-axis products through scratch.
+struct ChainFactor {
+    int axis;
+    int kind;                  // KF_DENSE or KF_BANDED (diag and shift converted to banded)
+    int n;
+    int nb;
+    int off[MAXB];
+    size_t data_off;           // dense: n*n matrix (column-major); banded: n*nb weights
+};
+struct ChainTerm {
+    double coeff;
+    std::vector<ChainFactor> f;
+};
+
+}  // namespace kf
+
+// The operator handle.
+struct kf_op {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = true;
+    kf::ApplyPlan plan{};
+    int64_t N = 0;
+    std::vector<int64_t> dims;
+    // fused diagonal on the device, FP64 and FP32
+    double *d_diag64 = nullptr;
+    float *d_diag32 = nullptr;
+    // banded weight pool (fused terms), FP64 and FP32
+    double *d_w64 = nullptr;
+    float *d_w32 = nullptr;
+    // dense-chain terms and their data (FP64 and FP32 copies)
+    std::vector<kf::ChainTerm> chains;
+    double *d_chain64 = nullptr;
+    float *d_chain32 = nullptr;
+    // scratch for chains: two buffers of N * cap doubles
+    int64_t cap = 0;
+    void *d_scratch = nullptr;
+    size_t scratch_bytes = 0;
+    // host copies of derived data
+    std::vector<double> h_diag;           // fused diagonal (real)
+    double gershgorin = 0;
+    std::vector<double> h_fulldiag;       // full diagonal (fused + kept terms)
+    // host-side term data for the diagonal and gershgorin
+    struct HostFactor { int axis; int kind; int64_t n; std::vector<double> data; std::vector<int64_t> offs; int64_t shift; double factor; };
+    struct HostTerm { double coeff; std::vector<HostFactor> f; };
+    std::vector<HostTerm> kept;
+};
+
+namespace kf {
+
+// kernels of kf_op.cu
+void launch_apply(kf_op *op, bool f32, const void *X, void *Y, int64_t ldx, int64_t ldy, int64_t b,
+                  double alpha, double beta, const void *Z, int64_t ldz, double gamma, cudaStream_t s);
+
+// dense linear algebra on tall-skinny blocks (kf_blas.cu); T = float or double.
+// Column-major blocks with leading dimension ld.
+template <typename T>
+void gram(const T *A, int64_t lda, int ka, const T *B, int64_t ldb, int kb, int64_t N, double *G_dev,
+          double *partials, cudaStream_t s);                 // G = A' B (ka x kb, column-major, FP64)
+size_t gram_partials_size(int ka, int kb, int64_t N);
+template <typename T>
+void update(T *Y, int64_t ldy, int ky, const T *X, int64_t ldx, int kx, const double *C_dev, int ldc,
+            double alpha, double beta, int64_t N, cudaStream_t s);   // Y = alpha X C + beta Y
+template <typename T>
+void colnorms2(const T *X, int64_t ldx, int k, int64_t N, double *out_dev, double *partials, cudaStream_t s);
+template <typename T>
+void residual_precond(const T *X, const T *HX, int64_t ld, int k, int64_t N, const double *theta_dev,
+                      const double *thetap_dev, const double *D_dev, double eta, int mode, T *R, int64_t ldr,
+                      double *norms2_dev, double *partials, cudaStream_t s);
+template <typename T>
+void scale_columns(T *X, int64_t ld, int k, int64_t N, const double *scale_dev, cudaStream_t s);
+template <typename T>
+void fill_normal(T *X, int64_t ld, int k, int64_t N, uint64_t seed, uint64_t stream_id, cudaStream_t s);
+template <typename Ts, typename Td>
+void convert(const Ts *X, int64_t ldx, Td *Y, int64_t ldy, int k, int64_t N, cudaStream_t s);
+template <typename T>
+void copy_block(const T *X, int64_t ldx, T *Y, int64_t ldy, int k, int64_t N, cudaStream_t s);
+template <typename T>
+void residual_block(const T *X, const T *HX, int64_t ld, int k, int64_t N, const double *theta_dev, T *R,
+                    int64_t ldr, cudaStream_t s);    // R = HX - X diag(theta)
+void diag_expectation(const double *D, const double *X, int64_t ld, int k, int64_t N, double *theta_dev,
+                      double *partials, cudaStream_t s);
+
+// small dense FP64 routines on the host (kf_small.cpp); column-major.
+int sym_eig(int n, const double *A, int lda, double *w, double *V, int ldv);   // ascending
+bool cholesky_upper(int n, double *A, int lda);     // A = U'U in place (upper), false if not SPD
+void tri_upper_inverse(int n, const double *U, int ldu, double *Ui, int ldi);
+
+}  // namespace kf

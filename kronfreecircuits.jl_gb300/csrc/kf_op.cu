@@ -1,0 +1,625 @@
+// The Kronecker-free operator: construction from the C descriptor and the apply kernels.
+//
+// Reference semantics (KronFreeCircuits.jl):
+//   src/apply.jl:222-253   construction; all-diagonal terms fused with the constant into one diagonal
+//   src/apply.jl:416-432   mul!(Y, H, X) = diag .* X + sum over kept terms of coeff * (chain of factors) X
+//   src/apply.jl:66-79     banded factor:  Y[t] = sum_b W[i_k, b] X[t + off_b * stride_k] (valid rows)
+//   src/apply.jl:111-118   shift factor:   Y[t] = f X[t - s * stride_k] (valid rows)
+//   src/apply.jl:301-340   dense factor:   the mode-k product with a d_k x d_k matrix
+//
+// GB300 design.  Every non-dense factor is a banded operator (a diagonal is one band at offset
+// 0, a shift one band at offset -s), so every term built only of such factors is a product of
+// banded operators, and all of them are evaluated in ONE pass over X: each thread owns one state
+// index p, decodes its axis indices once, and for a chunk of CB columns accumulates
+//   D[p] X[p] + sum_terms sum_bands (prod_f w_f[i_f, b_f]) X[p + sum_f off_f stride_f]
+// in registers, so X is read from HBM once and Y written once per apply (the neighbour reads hit
+// L1/L2: along the slowest stencil axis the planes p +- k*stride are read by CTAs resident a few
+// waves apart).  The reference's one-pass-per-factor-plus-one-accumulate-pass structure
+// (1 + sum_t (f_t + 1) passes) collapses to one pass.  Terms with dense factors run as chains of
+// single-axis kernels through two scratch blocks, the last factor accumulating into Y.
+#include <algorithm>
+#include <cstring>
+#include <map>
+
+#include "kf_internal.h"
+
+namespace kf {
+
+// ------------------------------------------------------------------------------------------
+// kernels
+
+template <typename T, int CB>
+__global__ void __launch_bounds__(256) k_apply_fused(const ApplyPlan plan, const T *__restrict__ D,
+                                                     const T *__restrict__ W, const T *__restrict__ X,
+                                                     T *__restrict__ Y, int64_t ldx, int64_t ldy, int b,
+                                                     T alpha, T beta, const T *__restrict__ Z, int64_t ldz,
+                                                     T gamma, int epi) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= plan.N) return;
+    int idx[MAXDIMS];
+    {
+        int64_t rem = p;
+#pragma unroll
+        for (int a = 0; a < MAXDIMS; ++a) {
+            if (a < plan.ndims) {
+                idx[a] = (int)(rem % plan.dims[a]);
+                rem /= plan.dims[a];
+            }
+        }
+    }
+    const T dv = D[p];
+    for (int c0 = 0; c0 < b; c0 += CB) {
+        T acc[CB];
+        const T *xb = X + (int64_t)c0 * ldx + p;
+#pragma unroll
+        for (int c = 0; c < CB; ++c) acc[c] = (c0 + c < b) ? dv * xb[(int64_t)c * ldx] : T(0);
+        for (int t = 0; t < plan.nterms; ++t) {
+            const FusedTerm &ft = plan.t[t];
+            if (ft.nf == 1) {
+                const BandFactorDev &f = ft.f[0];
+                const int a = f.axis;
+                const int i = idx[a];
+                const int n = (int)plan.dims[a];
+                const int64_t st = plan.stride[a];
+                const T *w = W + f.w_off + (int64_t)i * f.nb;
+                for (int bb = 0; bb < f.nb; ++bb) {
+                    const int o = f.off[bb];
+                    const int j = i + o;
+                    const T wv = w[bb];
+                    if (j < 0 || j >= n || wv == T(0)) continue;
+                    const T *xs = xb + (int64_t)o * st;
+#pragma unroll
+                    for (int c = 0; c < CB; ++c)
+                        if (c0 + c < b) acc[c] += wv * xs[(int64_t)c * ldx];
+                }
+            } else {  // nf == 2
+                const BandFactorDev &f1 = ft.f[0];
+                const BandFactorDev &f2 = ft.f[1];
+                const int i1 = idx[f1.axis], i2 = idx[f2.axis];
+                const int n1 = (int)plan.dims[f1.axis], n2 = (int)plan.dims[f2.axis];
+                const int64_t s1 = plan.stride[f1.axis], s2 = plan.stride[f2.axis];
+                const T *w1 = W + f1.w_off + (int64_t)i1 * f1.nb;
+                const T *w2 = W + f2.w_off + (int64_t)i2 * f2.nb;
+                for (int b1 = 0; b1 < f1.nb; ++b1) {
+                    const int j1 = i1 + f1.off[b1];
+                    const T wv1 = w1[b1];
+                    if (j1 < 0 || j1 >= n1 || wv1 == T(0)) continue;
+                    for (int b2 = 0; b2 < f2.nb; ++b2) {
+                        const int j2 = i2 + f2.off[b2];
+                        const T wv = wv1 * w2[b2];
+                        if (j2 < 0 || j2 >= n2 || wv == T(0)) continue;
+                        const T *xs = xb + (int64_t)f1.off[b1] * s1 + (int64_t)f2.off[b2] * s2;
+#pragma unroll
+                        for (int c = 0; c < CB; ++c)
+                            if (c0 + c < b) acc[c] += wv * xs[(int64_t)c * ldx];
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < CB; ++c) {
+            if (c0 + c >= b) break;
+            T v = acc[c];
+            if (epi) {
+                v = alpha * v + beta * xb[(int64_t)c * ldx];
+                if (Z != nullptr) v += gamma * Z[(int64_t)(c0 + c) * ldz + p];
+            }
+            Y[(int64_t)(c0 + c) * ldy + p] = v;
+        }
+    }
+}
+
+// dst = alpha * (banded factor along an axis) src  (+ dst when acc); blocks of b columns with
+// leading dimensions ldd, lds.
+template <typename T>
+__global__ void k_axis_banded(T *__restrict__ dst, int64_t ldd, const T *__restrict__ src, int64_t lds,
+                              const T *__restrict__ W, ChainFactor f, int64_t stride, int64_t N, int64_t total,
+                              T alpha, int acc) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= total) return;
+    const int64_t c = t / N, p = t % N;
+    const int i = (int)((p / stride) % f.n);
+    const T *sp = src + c * lds + p;
+    T s = 0;
+    for (int bb = 0; bb < f.nb; ++bb) {
+        const int j = i + f.off[bb];
+        if (j < 0 || j >= f.n) continue;
+        s += W[(int64_t)i * f.nb + bb] * sp[(int64_t)f.off[bb] * stride];
+    }
+    s *= alpha;
+    T *dp = dst + c * ldd + p;
+    *dp = acc ? *dp + s : s;
+}
+
+// dst[l, i, r] = alpha * sum_j A[i, j] src[l, j, r]  (+ dst when acc); A column-major n x n,
+// `left` the stride of the axis; per column of the block (leading dimensions ldd, lds).
+template <typename T>
+__global__ void k_axis_dense(T *__restrict__ dst, int64_t ldd, const T *__restrict__ src, int64_t lds,
+                             const T *__restrict__ A, int n, int64_t left, int64_t N, int64_t total, T alpha,
+                             int acc) {
+    extern __shared__ unsigned char smem_raw[];
+    T *As = reinterpret_cast<T *>(smem_raw);
+    const bool use_smem = (int64_t)n * n * sizeof(T) <= 48 * 1024;
+    if (use_smem) {
+        for (int k = threadIdx.x; k < n * n; k += blockDim.x) As[k] = A[k];
+        __syncthreads();
+    }
+    const T *Ap = use_smem ? As : A;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= total) return;
+    const int64_t c = t / N, p = t % N;
+    const int64_t l = p % left;
+    const int64_t q = p / left;
+    const int i = (int)(q % n);
+    const int64_t r = q / n;
+    const T *sp = src + c * lds + l + left * ((int64_t)n * r);
+    T s = 0;
+    for (int j = 0; j < n; ++j) s += Ap[i + (int64_t)n * j] * sp[left * j];
+    s *= alpha;
+    T *dp = dst + c * ldd + p;
+    *dp = acc ? *dp + s : s;
+}
+
+template <typename T>
+__global__ void k_axpby_cols(T *__restrict__ Y, int64_t ldy, const T *__restrict__ X, int64_t ldx,
+                             const T *__restrict__ Z, int64_t ldz, int64_t N, int b, T alpha, T beta, T gamma) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= N * b) return;
+    const int64_t c = t / N, p = t % N;
+    T v = alpha * Y[c * ldy + p] + beta * X[c * ldx + p];
+    if (Z != nullptr) v += gamma * Z[c * ldz + p];
+    Y[c * ldy + p] = v;
+}
+
+// ------------------------------------------------------------------------------------------
+// host launch
+
+template <typename T>
+static void apply_t(kf_op *op, const T *X, T *Y, int64_t ldx, int64_t ldy, int64_t b, double alpha, double beta,
+                    const T *Z, int64_t ldz, double gamma, cudaStream_t s) {
+    const int64_t N = op->N;
+    const bool f32 = sizeof(T) == 4;
+    const T *D = f32 ? (const T *)op->d_diag32 : (const T *)op->d_diag64;
+    const T *W = f32 ? (const T *)op->d_w32 : (const T *)op->d_w64;
+    const bool chains = !op->chains.empty();
+    const bool trivial_epi = alpha == 1.0 && beta == 0.0 && (Z == nullptr || gamma == 0.0);
+    const int epi = (!chains && !trivial_epi) ? 1 : 0;
+    const unsigned grid = (unsigned)((N + 255) / 256);
+    if (f32)
+        k_apply_fused<T, 16><<<grid, 256, 0, s>>>(op->plan, D, W, X, Y, ldx, ldy, (int)b, (T)alpha, (T)beta, Z, ldz,
+                                                  (T)gamma, epi);
+    else
+        k_apply_fused<T, 8><<<grid, 256, 0, s>>>(op->plan, D, W, X, Y, ldx, ldy, (int)b, (T)alpha, (T)beta, Z, ldz,
+                                                 (T)gamma, epi);
+    KF_CUDA(cudaGetLastError());
+    if (!chains) return;
+    // dense-containing terms: chain through scratch, one contiguous (N x b) block per buffer
+    const size_t need = (size_t)2 * N * b * sizeof(T);
+    if (op->scratch_bytes < need) {
+        if (op->d_scratch) KF_CUDA(cudaFree(op->d_scratch));
+        op->d_scratch = nullptr;
+        op->scratch_bytes = 0;
+        KF_CUDA(cudaMalloc(&op->d_scratch, need));
+        op->scratch_bytes = need;
+    }
+    T *buf[2] = {(T *)op->d_scratch, (T *)op->d_scratch + N * b};
+    const T *cdata = f32 ? (const T *)op->d_chain32 : (const T *)op->d_chain64;
+    const int64_t total = N * b;
+    const unsigned g2 = (unsigned)((total + 255) / 256);
+    for (const ChainTerm &ct : op->chains) {
+        const T *src = X;
+        int64_t lds = ldx;
+        const int nf = (int)ct.f.size();
+        for (int k = 0; k < nf; ++k) {
+            const ChainFactor &f = ct.f[k];
+            const bool last = k == nf - 1;
+            T *dst = last ? Y : buf[k & 1];
+            const int64_t ldd = last ? ldy : N;
+            const T a = last ? (T)ct.coeff : T(1);
+            const int acc = last ? 1 : 0;
+            const int64_t stride = op->plan.stride[f.axis];
+            if (f.kind == KF_DENSE) {
+                const size_t sm = (size_t)f.n * f.n * sizeof(T) <= 48 * 1024 ? (size_t)f.n * f.n * sizeof(T) : 0;
+                k_axis_dense<T><<<g2, 256, sm, s>>>(dst, ldd, src, lds, cdata + f.data_off, f.n, stride, N, total, a,
+                                                    acc);
+            } else {
+                k_axis_banded<T><<<g2, 256, 0, s>>>(dst, ldd, src, lds, cdata + f.data_off, f, stride, N, total, a, acc);
+            }
+            KF_CUDA(cudaGetLastError());
+            src = dst;
+            lds = ldd;
+        }
+    }
+    if (!trivial_epi) {
+        k_axpby_cols<T><<<g2, 256, 0, s>>>(Y, ldy, X, ldx, Z, ldz, N, (int)b, (T)alpha, (T)beta, (T)gamma);
+        KF_CUDA(cudaGetLastError());
+    }
+}
+
+void launch_apply(kf_op *op, bool f32, const void *X, void *Y, int64_t ldx, int64_t ldy, int64_t b, double alpha,
+                  double beta, const void *Z, int64_t ldz, double gamma, cudaStream_t s) {
+    if (b <= 0 || op->N == 0) return;
+    if (f32)
+        apply_t<float>(op, (const float *)X, (float *)Y, ldx, ldy, b, alpha, beta, (const float *)Z, ldz, gamma, s);
+    else
+        apply_t<double>(op, (const double *)X, (double *)Y, ldx, ldy, b, alpha, beta, (const double *)Z, ldz, gamma, s);
+}
+
+// ------------------------------------------------------------------------------------------
+// construction
+
+namespace {
+
+// A factor in banded form on the host: offsets and per-row weights w[i*nb + b], zero where the
+// neighbour i + off leaves the axis.
+struct HBand {
+    int axis;
+    int n;
+    std::vector<int> off;
+    std::vector<double> w;     // n * nb, row-major
+    int nb() const { return (int)off.size(); }
+};
+
+HBand to_band(const kf_factor &f) {
+    HBand h;
+    h.axis = f.axis;
+    h.n = (int)f.n;
+    const int n = h.n;
+    if (f.kind == KF_DIAG) {
+        h.off = {0};
+        h.w.assign(f.data, f.data + n);
+    } else if (f.kind == KF_SHIFT) {
+        // Y[i + s] = f X[i]  <=>  Y[i] = f X[i - s]: one band at offset -s
+        h.off = {(int)(-f.shift)};
+        h.w.assign(n, 0.0);
+        for (int i = 0; i < n; ++i)
+            if (i - f.shift >= 0 && i - f.shift < n) h.w[i] = f.factor;
+    } else {  // banded
+        const int nb = f.nbands;
+        h.off.resize(nb);
+        h.w.assign((size_t)n * nb, 0.0);
+        for (int bb = 0; bb < nb; ++bb) {
+            h.off[bb] = (int)f.offsets[bb];
+            for (int i = 0; i < n; ++i) {
+                const int64_t j = (int64_t)i + f.offsets[bb];
+                if (j >= 0 && j < n) h.w[(size_t)i * nb + bb] = f.data[(size_t)bb * n + i];
+            }
+        }
+    }
+    return h;
+}
+
+// Sum two banded factors on the same axis into one (union of offsets).
+HBand band_sum(const HBand &a, double ca, const HBand &b, double cb) {
+    HBand r;
+    r.axis = a.axis;
+    r.n = a.n;
+    r.off = a.off;
+    for (int o : b.off)
+        if (std::find(r.off.begin(), r.off.end(), o) == r.off.end()) r.off.push_back(o);
+    std::sort(r.off.begin(), r.off.end());
+    const int nb = r.nb();
+    r.w.assign((size_t)r.n * nb, 0.0);
+    auto add = [&](const HBand &h, double c) {
+        for (int bb = 0; bb < h.nb(); ++bb) {
+            const int k = (int)(std::find(r.off.begin(), r.off.end(), h.off[bb]) - r.off.begin());
+            for (int i = 0; i < r.n; ++i) r.w[(size_t)i * nb + k] += c * h.w[(size_t)i * h.nb() + bb];
+        }
+    };
+    add(a, ca);
+    add(b, cb);
+    return r;
+}
+
+bool same_band(const HBand &a, const HBand &b) { return a.axis == b.axis && a.off == b.off && a.w == b.w; }
+
+struct HTerm {
+    double coeff;
+    std::vector<HBand> f;
+};
+
+// Merge fused terms: two terms on the same axes whose factors agree on every axis but one become
+// one term, the differing axis summed (S+ (x) cos + S- (x) cos -> (S+ + S-) (x) cos).
+void merge_terms(std::vector<HTerm> &ts) {
+    bool changed = true;
+    while (changed) {
+        changed = false;
+        for (size_t x = 0; x < ts.size() && !changed; ++x) {
+            for (size_t y = x + 1; y < ts.size() && !changed; ++y) {
+                HTerm &A = ts[x], &B = ts[y];
+                if (A.f.size() != B.f.size()) continue;
+                bool axes_eq = true;
+                for (size_t k = 0; k < A.f.size(); ++k) axes_eq = axes_eq && A.f[k].axis == B.f[k].axis;
+                if (!axes_eq) continue;
+                int diff = -1, ndiff = 0;
+                for (size_t k = 0; k < A.f.size(); ++k)
+                    if (!same_band(A.f[k], B.f[k])) { diff = (int)k; ++ndiff; }
+                if (ndiff > 1) continue;
+                if (ndiff == 0) {
+                    A.coeff += B.coeff;
+                } else {
+                    A.f[diff] = band_sum(A.f[diff], A.coeff, B.f[diff], B.coeff);
+                    A.coeff = 1.0;
+                }
+                ts.erase(ts.begin() + y);
+                changed = true;
+            }
+        }
+    }
+}
+
+double band_infnorm(const kf_factor &f) {
+    const int64_t n = f.n;
+    double m = 0;
+    if (f.kind == KF_DIAG) {
+        for (int64_t i = 0; i < n; ++i) m = std::max(m, std::fabs(f.data[i]));
+    } else if (f.kind == KF_SHIFT) {
+        m = (std::llabs(f.shift) < n) ? std::fabs(f.factor) : 0.0;
+    } else if (f.kind == KF_BANDED) {
+        for (int64_t i = 0; i < n; ++i) {
+            double r = 0;
+            for (int bb = 0; bb < f.nbands; ++bb) {
+                const int64_t j = i + f.offsets[bb];
+                if (j >= 0 && j < n) r += std::fabs(f.data[(size_t)bb * n + i]);
+            }
+            m = std::max(m, r);
+        }
+    } else {
+        for (int64_t i = 0; i < n; ++i) {
+            double r = 0;
+            for (int64_t j = 0; j < n; ++j) r += std::fabs(f.data[i + n * j]);
+            m = std::max(m, r);
+        }
+    }
+    return m;
+}
+
+std::vector<double> factor_diagonal(const kf_factor &f) {
+    const int64_t n = f.n;
+    std::vector<double> d(n, 0.0);
+    if (f.kind == KF_DIAG) {
+        d.assign(f.data, f.data + n);
+    } else if (f.kind == KF_SHIFT) {
+        if (f.shift == 0) d.assign(n, f.factor);
+    } else if (f.kind == KF_BANDED) {
+        for (int bb = 0; bb < f.nbands; ++bb)
+            if (f.offsets[bb] == 0) { d.assign(f.data + (size_t)bb * n, f.data + (size_t)(bb + 1) * n); break; }
+    } else {
+        for (int64_t i = 0; i < n; ++i) d[i] = f.data[i + n * i];
+    }
+    return d;
+}
+
+// acc[p] += c * prod over factors of vec_f[i_axis(p)]
+void add_separable(std::vector<double> &acc, const std::vector<int64_t> &dims, double c,
+                   const std::vector<std::pair<int, std::vector<double>>> &vecs) {
+    const int64_t N = (int64_t)acc.size();
+    const int nd = (int)dims.size();
+    std::vector<int64_t> idx(nd, 0);
+    for (int64_t p = 0; p < N; ++p) {
+        double v = c;
+        for (auto &pv : vecs) v *= pv.second[idx[pv.first]];
+        acc[p] += v;
+        for (int a = 0; a < nd; ++a) {
+            if (++idx[a] < dims[a]) break;
+            idx[a] = 0;
+        }
+    }
+}
+
+}  // namespace
+
+void build_op(const kf_op_desc *desc, kf_op *op) {
+    KF_REQUIRE(desc != nullptr, KF_EINVAL, "KronFreeOperator: descriptor is NULL");
+    KF_REQUIRE(desc->ndims >= 1 && desc->ndims <= MAXDIMS, KF_EINVAL,
+               "KronFreeOperator: ndims must lie in 1:" + std::to_string(MAXDIMS));
+    op->dims.assign(desc->dims, desc->dims + desc->ndims);
+    int64_t N = 1;
+    for (int a = 0; a < desc->ndims; ++a) {
+        KF_REQUIRE(op->dims[a] >= 1, KF_EINVAL, "KronFreeOperator: dims must be positive");
+        N *= op->dims[a];
+    }
+    KF_REQUIRE(N < (int64_t(1) << 31), KF_EINVAL, "KronFreeOperator: prod(dims) must be below 2^31");
+    KF_REQUIRE(desc->block_capacity >= 1, KF_EINVAL, "KronFreeOperator: block_capacity must be positive");
+    KF_REQUIRE(desc->nterms >= 0 && (desc->nterms == 0 || desc->terms != nullptr), KF_EINVAL,
+               "KronFreeOperator: terms is NULL");
+    op->N = N;
+    ApplyPlan &P = op->plan;
+    std::memset(&P, 0, sizeof(P));
+    P.ndims = desc->ndims;
+    P.N = N;
+    int64_t st = 1;
+    for (int a = 0; a < desc->ndims; ++a) {
+        P.dims[a] = op->dims[a];
+        P.stride[a] = st;
+        st *= op->dims[a];
+    }
+    // validate terms (src/apply.jl:226-231, src/apply.jl:160-163)
+    for (int t = 0; t < desc->nterms; ++t) {
+        const kf_term &T = desc->terms[t];
+        KF_REQUIRE(T.nfactors >= 0 && T.nfactors <= desc->ndims && (T.nfactors == 0 || T.factors), KF_EINVAL,
+                   "KronFreeOperator: term " + std::to_string(t + 1) + " has an invalid factor list");
+        for (int k = 0; k < T.nfactors; ++k) {
+            const kf_factor &f = T.factors[k];
+            KF_REQUIRE(f.axis >= 0 && f.axis < desc->ndims, KF_EINVAL,
+                       "KronFreeOperator: factor axis " + std::to_string(f.axis + 1) + " outside 1:" +
+                           std::to_string(desc->ndims));
+            KF_REQUIRE(k == 0 || f.axis > T.factors[k - 1].axis, KF_EINVAL,
+                       "AxisTerm: factor axes must be strictly increasing");
+            KF_REQUIRE(f.n == op->dims[f.axis], KF_EDIM,
+                       "KronFreeOperator: factor on axis " + std::to_string(f.axis + 1) + " has dimension " +
+                           std::to_string(f.n) + ", expected " + std::to_string(op->dims[f.axis]));
+            KF_REQUIRE(f.kind >= KF_DIAG && f.kind <= KF_DENSE, KF_EINVAL, "KronFreeOperator: unknown factor kind");
+            KF_REQUIRE(f.kind == KF_SHIFT || f.data != nullptr, KF_EINVAL, "KronFreeOperator: factor data is NULL");
+            if (f.kind == KF_BANDED) {
+                KF_REQUIRE(f.nbands >= 0 && f.nbands <= MAXB && (f.nbands == 0 || f.offsets), KF_EINVAL,
+                           "KronFreeOperator: a banded factor needs 0.." + std::to_string(MAXB) + " bands");
+            }
+            if (f.kind == KF_DENSE) {
+                KF_REQUIRE(f.n <= 4096, KF_EINVAL, "KronFreeOperator: dense factors are limited to 4096 x 4096");
+            }
+        }
+        KF_REQUIRE(std::isfinite(T.coeff), KF_EINVAL, "KronFreeOperator: a coefficient is not finite");
+    }
+    // fused diagonal (src/apply.jl:234-241, 438-447)
+    std::vector<double> D(N, desc->constant);
+    if (desc->diag) for (int64_t p = 0; p < N; ++p) D[p] += desc->diag[p];
+    std::vector<HTerm> fused;
+    std::vector<ChainTerm> chains_h;
+    std::vector<std::vector<double>> chain_data;
+    double off_norm = 0;
+    op->kept.clear();
+    for (int t = 0; t < desc->nterms; ++t) {
+        const kf_term &T = desc->terms[t];
+        bool alldiag = true, anydense = false;
+        for (int k = 0; k < T.nfactors; ++k) {
+            alldiag = alldiag && T.factors[k].kind == KF_DIAG;
+            anydense = anydense || T.factors[k].kind == KF_DENSE;
+        }
+        if (alldiag) {
+            std::vector<std::pair<int, std::vector<double>>> vecs;
+            for (int k = 0; k < T.nfactors; ++k)
+                vecs.push_back({T.factors[k].axis, std::vector<double>(T.factors[k].data, T.factors[k].data + T.factors[k].n)});
+            add_separable(D, op->dims, T.coeff, vecs);
+            continue;
+        }
+        // a kept term: record it for the diagonal and the Gershgorin bound
+        kf_op::HostTerm ht;
+        ht.coeff = T.coeff;
+        double prod = 1;
+        for (int k = 0; k < T.nfactors; ++k) {
+            const kf_factor &f = T.factors[k];
+            prod *= band_infnorm(f);
+            kf_op::HostFactor hf{f.axis, f.kind, f.n, factor_diagonal(f), {}, f.shift, f.factor};
+            ht.f.push_back(hf);
+        }
+        off_norm += std::fabs(T.coeff) * prod;
+        op->kept.push_back(ht);
+        if (T.coeff == 0.0) continue;
+        HTerm h{T.coeff, {}};
+        for (int k = 0; k < T.nfactors; ++k)
+            if (T.factors[k].kind != KF_DENSE) h.f.push_back(to_band(T.factors[k]));
+        if (!anydense && T.nfactors <= 2) {
+            fused.push_back(h);
+        } else {
+            ChainTerm ct;
+            ct.coeff = T.coeff;
+            size_t bi = 0;
+            for (int k = 0; k < T.nfactors; ++k) {
+                const kf_factor &f = T.factors[k];
+                ChainFactor cf{};
+                cf.axis = f.axis;
+                cf.n = (int)f.n;
+                if (f.kind == KF_DENSE) {
+                    cf.kind = KF_DENSE;
+                    chain_data.push_back(std::vector<double>(f.data, f.data + (size_t)f.n * f.n));
+                } else {
+                    const HBand &hb = h.f[bi++];
+                    cf.kind = KF_BANDED;
+                    cf.nb = hb.nb();
+                    for (int q = 0; q < cf.nb; ++q) cf.off[q] = hb.off[q];
+                    chain_data.push_back(hb.w);
+                }
+                cf.data_off = 0;
+                ct.f.push_back(cf);
+            }
+            chains_h.push_back(ct);
+        }
+    }
+    // merge single-axis and structurally equal fused terms
+    merge_terms(fused);
+    // a fused term beyond the plan's capacity runs as a chain instead
+    int nterms = 0;
+    std::vector<double> pool;
+    for (HTerm &h : fused) {
+        bool fits = nterms < MAXT && (int)h.f.size() >= 1 && (int)h.f.size() <= 2;
+        for (auto &b : h.f) fits = fits && b.nb() <= MAXB;
+        if (!fits) {
+            ChainTerm ct;
+            ct.coeff = h.coeff;
+            for (auto &b : h.f) {
+                ChainFactor cf{};
+                cf.axis = b.axis;
+                cf.n = b.n;
+                cf.kind = KF_BANDED;
+                cf.nb = b.nb();
+                for (int q = 0; q < cf.nb && q < MAXB; ++q) cf.off[q] = b.off[q];
+                KF_REQUIRE(cf.nb <= MAXB, KF_EINVAL, "KronFreeOperator: too many bands in one factor");
+                chain_data.push_back(b.w);
+                ct.f.push_back(cf);
+            }
+            chains_h.push_back(ct);
+            continue;
+        }
+        FusedTerm &ft = P.t[nterms++];
+        ft.nf = (int)h.f.size();
+        for (int k = 0; k < ft.nf; ++k) {
+            HBand &b = h.f[k];
+            BandFactorDev &bf = ft.f[k];
+            bf.axis = b.axis;
+            bf.nb = b.nb();
+            for (int q = 0; q < bf.nb; ++q) bf.off[q] = b.off[q];
+            bf.w_off = (int)pool.size();
+            const double c = (k == 0) ? h.coeff : 1.0;
+            for (double v : b.w) pool.push_back(c * v);
+        }
+    }
+    P.nterms = nterms;
+    // lay out chain data
+    std::vector<double> cpool;
+    {
+        size_t q = 0;
+        for (ChainTerm &ct : chains_h)
+            for (ChainFactor &cf : ct.f) {
+                cf.data_off = cpool.size();
+                cpool.insert(cpool.end(), chain_data[q].begin(), chain_data[q].end());
+                ++q;
+            }
+    }
+    op->chains = chains_h;
+    // host-side derived quantities
+    op->h_diag = D;
+    double dmax = -INFINITY;
+    for (double v : D) dmax = std::max(dmax, v);
+    op->gershgorin = dmax + off_norm;
+    op->h_fulldiag = D;
+    for (auto &ht : op->kept) {
+        std::vector<std::pair<int, std::vector<double>>> vecs;
+        for (auto &hf : ht.f) vecs.push_back({hf.axis, hf.data});
+        add_separable(op->h_fulldiag, op->dims, ht.coeff, vecs);
+    }
+    // upload
+    auto up64 = [&](const std::vector<double> &v, double **d) {
+        if (v.empty()) { *d = nullptr; return; }
+        KF_CUDA(cudaMalloc(d, v.size() * sizeof(double)));
+        KF_CUDA(cudaMemcpyAsync(*d, v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice, op->stream));
+    };
+    auto up32 = [&](const std::vector<double> &v, float **d) {
+        if (v.empty()) { *d = nullptr; return; }
+        std::vector<float> f(v.begin(), v.end());
+        KF_CUDA(cudaMalloc(d, f.size() * sizeof(float)));
+        KF_CUDA(cudaMemcpyAsync(*d, f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice, op->stream));
+        KF_CUDA(cudaStreamSynchronize(op->stream));
+    };
+    up64(D, &op->d_diag64);
+    up32(D, &op->d_diag32);
+    up64(pool, &op->d_w64);
+    up32(pool, &op->d_w32);
+    up64(cpool, &op->d_chain64);
+    up32(cpool, &op->d_chain32);
+    op->cap = desc->block_capacity;
+    KF_CUDA(cudaStreamSynchronize(op->stream));
+}
+
+void free_op(kf_op *op) {
+    cudaFree(op->d_diag64);
+    cudaFree(op->d_diag32);
+    cudaFree(op->d_w64);
+    cudaFree(op->d_w32);
+    cudaFree(op->d_chain64);
+    cudaFree(op->d_chain32);
+    cudaFree(op->d_scratch);
+    if (op->own_stream && op->stream) cudaStreamDestroy(op->stream);
+}
+
+}  // namespace kf

@@ -1,0 +1,1041 @@
+// Eigensolver drivers: LOBPCG, Chebyshev-filtered subspace iteration and Lanczos on the GPU.
+//
+// Reference semantics (KronFreeCircuits.jl):
+//   src/lobpcg.jl:217-301      lobpcg_solve: product seed perturbed by sqrt(eps) along a fixed
+//                              random direction, guard columns g = min(guard, (N-5)/3 - m),
+//                              n_conv_check = m + g, one retry from a random block, acceptance
+//                              on the residual norms of the lowest m
+//   src/lobpcg.jl:51-135       per-Ritz Jacobi preconditioner R_j / hypot(D - theta_j, eta)
+//   src/chebyshev.jl:310-406   Chebyshev-filtered subspace iteration, its locking, guards, degree
+//                              cap, SVQB / Cholesky-QR and final true-residual acceptance
+//   src/solvers.jl:65-75       true residuals and the roundoff floor
+//   src/solvers.jl:85-106      Lanczos
+//
+// The block LOBPCG iteration (the reference calls the unvendored LOBPCGEigensolver 0.1.4): X
+// holds the Ritz vectors (a converged prefix is hard-locked), W the preconditioned residuals of
+// the active columns, P the previous update directions.  Per iteration [W P] is orthogonalised
+// against all of X (classical Gram-Schmidt, twice) and against itself by SVQB (drop directions
+// below a relative cutoff), H is applied to that basis, and Rayleigh-Ritz on
+// [X_active, W, P] gives the new active Ritz pairs; P is the [W P] part of the update.
+//
+// Precision (KF_PREC_MIXED): the bulk of the iterations run with FP32 blocks (FP32 applies,
+// FP32 Gram products accumulated in FP64 across CTAs, FP64 Rayleigh-Ritz on the host); when
+// every active residual is below mixed_switch * ||H|| (or the FP32 residuals stop falling),
+// the block is widened to FP64 and the same iteration finishes in FP64 with FP64 residuals,
+// the last sweep being the FP64 refinement that the acceptance test measures.
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <numeric>
+#include <random>
+
+#include "kf_internal.h"
+
+namespace kf {
+
+// ------------------------------------------------------------------------------------------
+// device / pinned memory helpers
+
+struct DevMem {
+    void *p = nullptr;
+    DevMem() = default;
+    explicit DevMem(size_t bytes) {
+        if (bytes) KF_CUDA(cudaMalloc(&p, bytes));
+    }
+    ~DevMem() {
+        if (p) cudaFree(p);
+    }
+    DevMem(const DevMem &) = delete;
+    DevMem &operator=(const DevMem &) = delete;
+    template <typename T>
+    T *as() const { return (T *)p; }
+};
+
+struct HostMem {
+    void *p = nullptr;
+    explicit HostMem(size_t bytes) { KF_CUDA(cudaMallocHost(&p, bytes ? bytes : 8)); }
+    ~HostMem() {
+        if (p) cudaFreeHost(p);
+    }
+    HostMem(const HostMem &) = delete;
+    HostMem &operator=(const HostMem &) = delete;
+    template <typename T>
+    T *as() const { return (T *)p; }
+};
+
+static double now_s() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+// ------------------------------------------------------------------------------------------
+// SVQB coefficients on the host: for the Gram matrix G (k x k) of a block Z, T (k x r) with
+// Z T orthonormal, dropping directions whose unit-diagonal Gram eigenvalue is below
+// cutoff * the largest (src/chebyshev.jl:68-81).  Returns r.
+static int svqb_coeffs(int k, const double *G, double cutoff, std::vector<double> &T) {
+    std::vector<double> d(k), Gs((size_t)k * k), w(k), U((size_t)k * k);
+    for (int i = 0; i < k; ++i) d[i] = 1.0 / std::sqrt(std::max(G[i + (size_t)k * i], 1e-300));
+    for (int j = 0; j < k; ++j)
+        for (int i = 0; i < k; ++i) Gs[i + (size_t)k * j] = d[i] * G[i + (size_t)k * j] * d[j];
+    if (sym_eig(k, Gs.data(), k, w.data(), U.data(), k) != 0)
+        throw Error(KF_EBREAKDOWN, "SVQB: the Gram eigenproblem did not converge");
+    const double top = w[k - 1];
+    std::vector<int> keep;
+    if (top > 0 && std::isfinite(top))
+        for (int j = 0; j < k; ++j)
+            if (w[j] > cutoff * top) keep.push_back(j);
+    const int r = (int)keep.size();
+    T.assign((size_t)k * std::max(r, 1), 0.0);
+    for (int c = 0; c < r; ++c) {
+        const int j = keep[c];
+        const double s = 1.0 / std::sqrt(w[j]);
+        for (int i = 0; i < k; ++i) T[i + (size_t)k * c] = d[i] * U[i + (size_t)k * j] * s;
+    }
+    return r;
+}
+
+// ------------------------------------------------------------------------------------------
+// LOBPCG on one precision
+
+struct LobParams {
+    double lock_tol;        // a column locks (and counts as converged) below this residual
+    int maxiter;
+    int precond;            // KF_PRECOND_*
+    double eta;
+    int n_conv_check;
+    double cutoff;          // SVQB relative cutoff
+    bool stall_exit;        // FP32 phase: leave when the residuals stop falling
+    int judge_iters;        // warm-start judge: iteration at which ...
+    double judge_resid;     // ... a largest residual above this aborts (0 = off)
+};
+
+struct LobOut {
+    int iters = 0;
+    int64_t nmv = 0;
+    int nlocked = 0;
+    bool converged = false;
+    bool judged_bad = false;
+    std::vector<double> theta, resid;
+};
+
+template <typename T>
+struct LobWork {
+    int64_t N;
+    int w;
+    DevMem X, HX, Xn, HXn, Z, HZ, Zt, Pn, dG, dC, dpart, dth, dthp, dnorm, dD;
+    HostMem hG, hC, hv;
+    LobWork(int64_t N_, int w_)
+        : N(N_), w(w_),
+          X((size_t)N_ * w_ * sizeof(T)), HX((size_t)N_ * w_ * sizeof(T)), Xn((size_t)N_ * w_ * sizeof(T)),
+          HXn((size_t)N_ * w_ * sizeof(T)), Z((size_t)N_ * 2 * w_ * sizeof(T)), HZ((size_t)N_ * 2 * w_ * sizeof(T)),
+          Zt((size_t)N_ * 2 * w_ * sizeof(T)), Pn((size_t)N_ * w_ * sizeof(T)),
+          dG((size_t)9 * w_ * w_ * sizeof(double)), dC((size_t)9 * w_ * w_ * sizeof(double)),
+          dpart(gram_partials_size(3 * w_, 3 * w_, N_)), dth(w_ * sizeof(double)), dthp(w_ * sizeof(double)),
+          dnorm(2 * w_ * sizeof(double)), dD(0),
+          hG((size_t)9 * w_ * w_ * sizeof(double)), hC((size_t)9 * w_ * w_ * sizeof(double)),
+          hv((size_t)4 * w_ * sizeof(double)) {}
+};
+
+template <typename T>
+static void d2h_sync(double *h, const double *d, size_t n, cudaStream_t s) {
+    KF_CUDA(cudaMemcpyAsync(h, d, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    KF_CUDA(cudaStreamSynchronize(s));
+}
+
+static void h2d(double *d, const double *h, size_t n, cudaStream_t s) {
+    KF_CUDA(cudaMemcpyAsync(d, h, n * sizeof(double), cudaMemcpyHostToDevice, s));
+}
+
+// Orthonormalise Zb (N x k, leading dimension N) against X (N x w) and itself, twice; the
+// result lands in `out` (N x r, may be Zt or Z).  Returns r.  `tmp` is an N x k scratch.
+template <typename T>
+static int ortho_against(kf_op *op, LobWork<T> &W, T *Zb, int k, const T *X, int wx, T *tmp, T *&result,
+                         double cutoff, cudaStream_t s) {
+    const int64_t N = W.N;
+    double *G = W.dG.template as<double>();
+    double *part = W.dpart.template as<double>();
+    T *cur = Zb, *other = tmp;
+    int r = k;
+    for (int pass = 0; pass < 2; ++pass) {
+        if (wx > 0) {
+            for (int cgs = 0; cgs < 2; ++cgs) {
+                gram<T>(X, N, wx, cur, N, r, N, G, part, s);
+                update<T>(cur, N, r, X, N, wx, G, wx, -1.0, 1.0, N, s);
+            }
+        }
+        gram<T>(cur, N, r, cur, N, r, N, G, part, s);
+        double *hG = W.hG.template as<double>();
+        d2h_sync<T>(hG, G, (size_t)r * r, s);
+        std::vector<double> Tc;
+        const int r2 = svqb_coeffs(r, hG, cutoff, Tc);
+        if (r2 == 0) { result = cur; return 0; }
+        double *hC = W.hC.template as<double>();
+        std::memcpy(hC, Tc.data(), sizeof(double) * (size_t)r * r2);
+        double *C = W.dC.template as<double>();
+        h2d(C, hC, (size_t)r * r2, s);
+        update<T>(other, N, r2, cur, N, r, C, r, 1.0, 0.0, N, s);
+        std::swap(cur, other);
+        r = r2;
+    }
+    result = cur;
+    return r;
+}
+
+template <typename T>
+static LobOut lobpcg_run(kf_op *op, LobWork<T> &Wk, const double *D, const LobParams &prm, cudaStream_t s,
+                         std::vector<double> &theta) {
+    const int64_t N = Wk.N;
+    const int w = Wk.w;
+    const bool f32 = sizeof(T) == 4;
+    LobOut out;
+    T *X = Wk.X.template as<T>(), *HX = Wk.HX.template as<T>();
+    T *Xn = Wk.Xn.template as<T>(), *HXn = Wk.HXn.template as<T>();
+    T *Z = Wk.Z.template as<T>(), *HZ = Wk.HZ.template as<T>(), *Zt = Wk.Zt.template as<T>();
+    T *Pn = Wk.Pn.template as<T>();
+    double *G = Wk.dG.template as<double>(), *C = Wk.dC.template as<double>();
+    double *part = Wk.dpart.template as<double>();
+    double *hG = Wk.hG.template as<double>(), *hC = Wk.hC.template as<double>();
+    double *dth = Wk.dth.template as<double>(), *dthp = Wk.dthp.template as<double>();
+    double *dnorm = Wk.dnorm.template as<double>();
+    double *hv = Wk.hv.template as<double>();
+
+    // orthonormalise the initial block (in X) and Rayleigh-Ritz on it
+    {
+        T *res = nullptr;
+        const int r = ortho_against<T>(op, Wk, X, w, nullptr, 0, Zt, res, prm.cutoff, s);
+        if (r < w) throw Error(KF_EBREAKDOWN, "LOBPCG: the initial block is numerically rank deficient");
+        if (res != X) copy_block<T>(res, N, X, N, w, N, s);
+        launch_apply(op, f32, X, HX, N, N, w, 1, 0, nullptr, 0, 0, s);
+        out.nmv += w;
+        gram<T>(X, N, w, HX, N, w, N, G, part, s);
+        d2h_sync<T>(hG, G, (size_t)w * w, s);
+        theta.assign(w, 0.0);
+        std::vector<double> V((size_t)w * w);
+        if (sym_eig(w, hG, w, theta.data(), V.data(), w) != 0)
+            throw Error(KF_EBREAKDOWN, "LOBPCG: Rayleigh-Ritz eigenproblem did not converge");
+        std::memcpy(hC, V.data(), sizeof(double) * w * w);
+        h2d(C, hC, (size_t)w * w, s);
+        update<T>(Xn, N, w, X, N, w, C, w, 1.0, 0.0, N, s);
+        update<T>(HXn, N, w, HX, N, w, C, w, 1.0, 0.0, N, s);
+        std::swap(X, Xn);
+        std::swap(HX, HXn);
+    }
+    std::vector<double> res(w, INFINITY);
+    int nl = 0, np = 0, na_prev = w;
+    double best = INFINITY;
+    int since_best = 0;
+    for (int it = 0;; ++it) {
+        const int na = w - nl;
+        // residuals of the active columns, preconditioned into Z[:, 0:na]
+        std::memcpy(hv, theta.data() + nl, sizeof(double) * na);
+        h2d(dth, hv, na, s);
+        h2d(dthp, hv, na, s);
+        if (prm.precond == KF_PRECOND_JACOBI) {
+            // fixed Jacobi: sigma = min(D) - 1, passed in thetap[0]
+            double dmin = op->h_fulldiag.empty() ? 0.0
+                                                 : *std::min_element(op->h_fulldiag.begin(), op->h_fulldiag.end());
+            double sig = dmin - 1.0;
+            h2d(dthp, &sig, 1, s);
+        }
+        const int mode = prm.precond == KF_PRECOND_RITZ ? 0 : prm.precond == KF_PRECOND_JACOBI ? 1 : 2;
+        residual_precond<T>(X + (int64_t)nl * N, HX + (int64_t)nl * N, N, na, N, dth, dthp, D, prm.eta, mode, Z, N,
+                            dnorm, part, s);
+        d2h_sync<T>(hv + w, dnorm, na, s);
+        for (int j = 0; j < na; ++j) res[nl + j] = std::sqrt(hv[w + j]);
+        int newly = 0;
+        while (nl + newly < w && res[nl + newly] <= prm.lock_tol) ++newly;
+        if (newly > 0) {
+            // locked columns never change again: keep both buffers' copies in sync
+            copy_block<T>(X + (int64_t)nl * N, N, Xn + (int64_t)nl * N, N, newly, N, s);
+            copy_block<T>(HX + (int64_t)nl * N, N, HXn + (int64_t)nl * N, N, newly, N, s);
+        }
+        out.iters = it;
+        if (nl + newly >= prm.n_conv_check) {
+            nl += newly;
+            out.converged = true;
+            break;
+        }
+        double worst = 0;
+        for (int j = nl; j < w; ++j) worst = std::max(worst, res[j]);
+        if (!std::isfinite(worst)) throw Error(KF_ENOTFINITE, "LOBPCG: the residual block is not finite");
+        if (prm.judge_resid > 0 && it == prm.judge_iters && worst > prm.judge_resid) {
+            out.judged_bad = true;
+            break;
+        }
+        if (prm.stall_exit) {
+            if (worst < 0.7 * best) {
+                best = worst;
+                since_best = 0;
+            } else if (++since_best >= 6) {
+                break;                                   // FP32 has reached its floor
+            }
+        }
+        if (it >= prm.maxiter) break;
+        // W = Z[:, newly : na] (na2 columns), P = previous Pn[:, newly : na] placed right after it
+        const int na2 = na - newly;
+        T *Wb = Z + (int64_t)newly * N;
+        int nz = na2;
+        if (np > 0) {
+            const int np2 = np - newly;
+            if (np2 > 0) {
+                copy_block<T>(Pn + (int64_t)newly * N, N, Wb + (int64_t)na2 * N, N, np2, N, s);
+                nz += np2;
+            }
+        }
+        nl += newly;
+        // orthonormalise [W P] against X and itself (result in Z or Zt)
+        T *Q = nullptr;
+        const int k = ortho_against<T>(op, Wk, Wb, nz, X, w, Zt, Q, prm.cutoff, s);
+        if (k == 0) throw Error(KF_EBREAKDOWN, "LOBPCG: the search directions vanished");
+        T *Qc = Q;   // in Zt, or in Z at the offset of Wb
+        launch_apply(op, f32, Qc, HZ, N, N, k, 1, 0, nullptr, 0, 0, s);
+        out.nmv += k;
+        // Rayleigh-Ritz on S = [X_act, Q]: A = S' H S assembled from three Gram blocks
+        const int na3 = w - nl;
+        const int ns = na3 + k;
+        T *Xa = X + (int64_t)nl * N, *HXa = HX + (int64_t)nl * N;
+        std::vector<double> A((size_t)ns * ns);
+        gram<T>(Xa, N, na3, HXa, N, na3, N, G, part, s);
+        d2h_sync<T>(hG, G, (size_t)na3 * na3, s);
+        for (int j = 0; j < na3; ++j)
+            for (int i = 0; i < na3; ++i) A[i + (size_t)ns * j] = hG[i + (size_t)na3 * j];
+        gram<T>(Xa, N, na3, HZ, N, k, N, G, part, s);
+        d2h_sync<T>(hG, G, (size_t)na3 * k, s);
+        for (int j = 0; j < k; ++j)
+            for (int i = 0; i < na3; ++i) {
+                A[i + (size_t)ns * (na3 + j)] = hG[i + (size_t)na3 * j];
+                A[(na3 + j) + (size_t)ns * i] = hG[i + (size_t)na3 * j];
+            }
+        gram<T>(Qc, N, k, HZ, N, k, N, G, part, s);
+        d2h_sync<T>(hG, G, (size_t)k * k, s);
+        for (int j = 0; j < k; ++j)
+            for (int i = 0; i < k; ++i) A[(na3 + i) + (size_t)ns * (na3 + j)] = hG[i + (size_t)k * j];
+        std::vector<double> lam(ns), V((size_t)ns * ns);
+        if (sym_eig(ns, A.data(), ns, lam.data(), V.data(), ns) != 0)
+            throw Error(KF_EBREAKDOWN, "LOBPCG: Rayleigh-Ritz eigenproblem did not converge");
+        // C = V[:, 0:na3]  (ns x na3)
+        std::memcpy(hC, V.data(), sizeof(double) * (size_t)ns * na3);
+        h2d(C, hC, (size_t)ns * na3, s);
+        // X_act <- Xa Cx + Q Cz ; HX likewise ; P <- Q Cz
+        T *Xna = Xn + (int64_t)nl * N, *HXna = HXn + (int64_t)nl * N;
+        update<T>(Xna, N, na3, Xa, N, na3, C, ns, 1.0, 0.0, N, s);
+        update<T>(Xna, N, na3, Qc, N, k, C + na3, ns, 1.0, 1.0, N, s);
+        update<T>(HXna, N, na3, HXa, N, na3, C, ns, 1.0, 0.0, N, s);
+        update<T>(HXna, N, na3, HZ, N, k, C + na3, ns, 1.0, 1.0, N, s);
+        update<T>(Pn, N, na3, Qc, N, k, C + na3, ns, 1.0, 0.0, N, s);
+        np = na3;
+        std::swap(X, Xn);
+        std::swap(HX, HXn);
+        for (int j = 0; j < na3; ++j) theta[nl + j] = lam[j];
+        na_prev = na3;
+    }
+    (void)na_prev;
+    // make sure the final block sits in Wk.X / Wk.HX
+    if (X != Wk.X.template as<T>()) {
+        copy_block<T>(X, N, Wk.X.template as<T>(), N, w, N, s);
+        copy_block<T>(HX, N, Wk.HX.template as<T>(), N, w, N, s);
+    }
+    KF_CUDA(cudaStreamSynchronize(s));
+    out.nlocked = nl;
+    out.theta = theta;
+    out.resid = res;
+    return out;
+}
+
+// ------------------------------------------------------------------------------------------
+// host-side seed construction (src/lobpcg.jl:167-190)
+
+// splitmix64-based normal stream on the host, keyed like the reference's MersenneTwister seeds
+struct HostNormal {
+    uint64_t state;
+    bool have = false;
+    double spare = 0;
+    explicit HostNormal(uint64_t seed) : state(seed * 0x9e3779b97f4a7c15ull + 0x4b46) {}
+    uint64_t next() {
+        uint64_t z = (state += 0x9e3779b97f4a7c15ull);
+        z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+        z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+        return z ^ (z >> 31);
+    }
+    double operator()() {
+        if (have) { have = false; return spare; }
+        double u1 = ((next() >> 11) + 1) * (1.0 / 9007199254740993.0);
+        double u2 = (next() >> 11) * (1.0 / 9007199254740992.0);
+        double r = std::sqrt(-2.0 * std::log(u1));
+        spare = r * std::sin(2 * M_PI * u2);
+        have = true;
+        return r * std::cos(2 * M_PI * u2);
+    }
+};
+
+// Each column plus a vector of norm delta * ||column|| along a fixed pseudo-random direction.
+static void perturb_columns(double *X, int64_t N, int k, double delta, uint64_t key) {
+    HostNormal rng(key);
+    std::vector<double> r(N);
+    for (int j = 0; j < k; ++j) {
+        double nc = 0, nr = 0;
+        for (int64_t i = 0; i < N; ++i) {
+            r[i] = rng();
+            nr += r[i] * r[i];
+            nc += X[i + N * j] * X[i + N * j];
+        }
+        const double f = delta * std::sqrt(nc) / std::sqrt(nr);
+        for (int64_t i = 0; i < N; ++i) X[i + N * j] += f * r[i];
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// final FP64 acceptance: sort, true residuals with a fresh apply (src/solvers.jl:65-69)
+
+static void accept_and_copy(kf_op *op, const double *Xd, int w, const std::vector<double> &theta, int m,
+                            double *E_out, double *V_out, std::vector<double> &resid_out, cudaStream_t s) {
+    const int64_t N = op->N;
+    std::vector<int> ord(w);
+    std::iota(ord.begin(), ord.end(), 0);
+    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return theta[a] < theta[b]; });
+    DevMem V((size_t)N * m * sizeof(double)), HV((size_t)N * m * sizeof(double)), dth(m * sizeof(double)),
+        dn(m * sizeof(double)), part(gram_partials_size(1, 1, N));
+    std::vector<double> th(m);
+    for (int j = 0; j < m; ++j) {
+        th[j] = theta[ord[j]];
+        KF_CUDA(cudaMemcpyAsync(V.as<double>() + (int64_t)j * N, Xd + (int64_t)ord[j] * N, N * sizeof(double),
+                                cudaMemcpyDeviceToDevice, s));
+    }
+    launch_apply(op, false, V.as<double>(), HV.as<double>(), N, N, m, 1, 0, nullptr, 0, 0, s);
+    KF_CUDA(cudaMemcpyAsync(dth.p, th.data(), m * sizeof(double), cudaMemcpyHostToDevice, s));
+    residual_block<double>(V.as<double>(), HV.as<double>(), N, m, N, dth.as<double>(), HV.as<double>(), N, s);
+    colnorms2<double>(HV.as<double>(), N, m, N, dn.as<double>(), part.as<double>(), s);
+    std::vector<double> r2(m);
+    KF_CUDA(cudaMemcpyAsync(r2.data(), dn.p, m * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (V_out) KF_CUDA(cudaMemcpyAsync(V_out, V.p, (size_t)N * m * sizeof(double), cudaMemcpyDeviceToHost, s));
+    KF_CUDA(cudaStreamSynchronize(s));
+    resid_out.resize(m);
+    for (int j = 0; j < m; ++j) {
+        resid_out[j] = std::sqrt(r2[j]);
+        if (E_out) E_out[j] = th[j];
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// LOBPCG solve (src/lobpcg.jl:217-301)
+
+static void solve_lobpcg(kf_op *op, const kf_solver_opts &o, int m, const double *X0, const double *seed,
+                         double *E_out, double *V_out, kf_solve_stats &st) {
+    const int64_t N = op->N;
+    cudaStream_t s = op->stream;
+    KF_REQUIRE(m >= 1, KF_EINVAL, "LOBPCG requires m >= 1, got " + std::to_string(m));
+    KF_REQUIRE(N >= 3 * (int64_t)m + 5, KF_EINVAL,
+               "LOBPCG needs N ≥ 3m + 5, got N = " + std::to_string(N) + " for m = " + std::to_string(m) +
+                   "; the block eigensolver is unreliable on so small a problem, use Dense()");
+    KF_REQUIRE(o.tol > 0 && std::isfinite(o.tol), KF_EINVAL, "LOBPCG: tol must be positive and finite");
+    KF_REQUIRE(o.maxiter >= 1, KF_EINVAL, "LOBPCG: maxiter must be at least 1");
+    KF_REQUIRE(o.eta > 0 && std::isfinite(o.eta), KF_EINVAL, "eta must be positive and finite");
+    KF_REQUIRE(o.guard >= 0, KF_EINVAL, "LOBPCG: guard must be nonnegative");
+    if (X0) {
+        for (int j = 0; j < m; ++j) {
+            bool nz = false;
+            for (int64_t i = 0; i < N; ++i) {
+                const double v = X0[i + N * j];
+                KF_REQUIRE(std::isfinite(v), KF_EINVAL, "LOBPCG: X0 has non-finite entries");
+                nz = nz || v != 0.0;
+            }
+            KF_REQUIRE(nz, KF_EINVAL, "LOBPCG: column " + std::to_string(j + 1) + " of X0 is zero");
+        }
+    }
+    const int g = (int)std::min<int64_t>(o.guard, (N - 5) / 3 - m);
+    const int w = m + g;
+    const double hn = op->gershgorin;
+    st.hnorm = hn;
+    // the initial block on the host (FP64)
+    std::vector<double> X((size_t)N * w);
+    const double delta = std::sqrt(std::numeric_limits<double>::epsilon());
+    HostNormal rng(o.rng_seed);
+    bool guards_random = true;
+    if (X0) {
+        std::memcpy(X.data(), X0, sizeof(double) * (size_t)N * m);
+        perturb_columns(X.data(), N, m, delta, 0x4b46);
+        if (seed) {
+            std::memcpy(X.data() + (size_t)N * m, seed + (size_t)N * m, sizeof(double) * (size_t)N * g);
+            perturb_columns(X.data() + (size_t)N * m, N, g, delta, 0x4b46);
+            guards_random = false;
+        }
+        st.warm = 1;
+    } else if (seed) {
+        std::memcpy(X.data(), seed, sizeof(double) * (size_t)N * w);
+        perturb_columns(X.data(), N, w, delta, 0x4b46);
+        guards_random = false;
+    } else {
+        for (size_t i = 0; i < (size_t)N * m; ++i) X[i] = rng();
+    }
+    if (guards_random)
+        for (size_t i = (size_t)N * m; i < (size_t)N * w; ++i) X[i] = rng();
+
+    DevMem dD((size_t)N * sizeof(double));
+    KF_CUDA(cudaMemcpyAsync(dD.p, op->h_fulldiag.data(), N * sizeof(double), cudaMemcpyHostToDevice, s));
+    LobWork<double> W64(N, w);
+    auto load64 = [&](const std::vector<double> &Xh) {
+        KF_CUDA(cudaMemcpyAsync(W64.X.p, Xh.data(), sizeof(double) * (size_t)N * w, cudaMemcpyHostToDevice, s));
+    };
+    LobParams p64{o.tol, o.maxiter, o.preconditioner, o.eta, w, 1e-12, false, o.fallback_iters,
+                  o.fallback_resid > 0 ? o.fallback_resid * hn : 0.0};
+    std::vector<double> theta;
+    LobOut r;
+    const double t0 = now_s();
+    auto attempt = [&](bool allow_judge) {
+        LobParams q = p64;
+        if (!allow_judge) q.judge_resid = 0;
+        int iters32 = 0;
+        int64_t nmv32 = 0;
+        if (o.precision == KF_PREC_MIXED) {
+            LobWork<float> W32(N, w);
+            convert<double, float>(W64.X.as<double>(), N, W32.X.as<float>(), N, w, N, s);
+            LobParams p32 = q;
+            p32.lock_tol = std::max(o.tol, o.mixed_switch * hn);
+            p32.cutoff = 1e-6;
+            p32.stall_exit = true;
+            LobOut r32 = lobpcg_run<float>(op, W32, dD.as<double>(), p32, s, theta);
+            iters32 = r32.iters;
+            nmv32 = r32.nmv;
+            if (r32.judged_bad) {
+                r = r32;
+                return;
+            }
+            convert<float, double>(W32.X.as<float>(), N, W64.X.as<double>(), N, w, N, s);
+            q.judge_resid = 0;
+        }
+        const double tf = now_s();
+        r = lobpcg_run<double>(op, W64, dD.as<double>(), q, s, theta);
+        st.seconds_f64 = now_s() - tf;
+        st.iterations_f64 = r.iters;
+        r.iters += iters32;
+        r.nmv += nmv32;
+    };
+    load64(X);
+    bool failed = false;
+    try {
+        attempt(X0 != nullptr);
+    } catch (const Error &e) {
+        if (e.code != KF_EBREAKDOWN && e.code != KF_ENOTFINITE) throw;
+        if (!X0 && !seed) throw Error(KF_EBREAKDOWN, std::string("LOBPCG: the eigensolver failed (") + e.what() + ")");
+        failed = true;
+    }
+    if (failed || r.judged_bad) {
+        // one retry from a random block (src/lobpcg.jl:272-289); also the warm-start fallback
+        if (r.judged_bad) st.fell_back = 1;
+        std::vector<double> Xr((size_t)N * w);
+        HostNormal rr(o.rng_seed ^ 0x52455452ull);
+        for (auto &v : Xr) v = rr();
+        load64(Xr);
+        const int it0 = r.judged_bad ? r.iters : 0;
+        const int64_t nmv0 = r.judged_bad ? r.nmv : 0;
+        try {
+            attempt(false);
+        } catch (const Error &e) {
+            throw Error(e.code, std::string("LOBPCG: the eigensolver failed (") + e.what() +
+                                    "). An exactly zero residual block (an operator proportional to the identity on "
+                                    "the block, or exact eigenvectors) can break its orthogonalization; use Dense() "
+                                    "for such operators");
+        }
+        r.iters += it0;
+        r.nmv += nmv0;
+    }
+    st.iterations = r.iters;
+    st.n_matvec = r.nmv;
+    std::vector<double> resid;
+    accept_and_copy(op, W64.X.as<double>(), w, theta, m, E_out, V_out, resid, s);
+    st.seconds = now_s() - t0;
+    double worst = 0;
+    int bad = 0;
+    for (int j = 0; j < m; ++j) {
+        worst = std::max(worst, resid[j]);
+        if (!(resid[j] <= o.tol)) ++bad;
+    }
+    st.max_residual = worst;
+    st.converged = m - bad;
+    if (bad) {
+        char buf[256];
+        snprintf(buf, sizeof buf,
+                 "LOBPCG: %d of %d eigenpairs did not converge within %d iterations (only %d converged; maximum "
+                 "residual %.3e > tol = %.3e)",
+                 bad, m, o.maxiter, m - bad, worst, o.tol);
+        throw Error(KF_ENOCONV, buf);
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// Chebyshev-filtered subspace iteration (src/chebyshev.jl:310-406), FP64 or FP32 filter
+
+static constexpr double SVQB_CUTOFF = 1e-12;
+static constexpr double LOCK_FRACTION = 0.5;
+static constexpr double SEED_ADMIXTURE = 1e-2;
+static constexpr int CHEB_GUARDS = 4;
+static constexpr double GUARD_GAIN_FRACTION = 0.1;
+
+static double log_gain(double t, double lcut, double lmax) {
+    const double x = std::fabs((t - (lmax + lcut) / 2) / ((lmax - lcut) / 2));
+    return x > 1 ? std::acosh(x) : 0.0;
+}
+
+static double kth_smallest(std::vector<double> v, int k) {
+    std::nth_element(v.begin(), v.begin() + (k - 1), v.end());
+    return v[k - 1];
+}
+
+static void solve_chebyshev(kf_op *op, const kf_solver_opts &o, int m, const double *seed, double *E_out,
+                            double *V_out, kf_solve_stats &st) {
+    const int64_t N = op->N;
+    cudaStream_t s = op->stream;
+    KF_REQUIRE(m >= 1, KF_EINVAL, "ChebyshevFilter requires m >= 1, got " + std::to_string(m));
+    KF_REQUIRE(m <= N, KF_EINVAL, "ChebyshevFilter: m exceeds the operator dimension");
+    KF_REQUIRE(o.tol > 0 && std::isfinite(o.tol), KF_EINVAL, "ChebyshevFilter: tol must be positive and finite");
+    KF_REQUIRE(o.degree >= 1 && o.degree <= 200, KF_EINVAL, "ChebyshevFilter: degree must lie in 1:200");
+    KF_REQUIRE(o.extra >= 2, KF_EINVAL,
+               "ChebyshevFilter: extra must be at least 2 so at least one column serves as a convergence guard");
+    KF_REQUIRE(o.maxiter >= 1 && o.rescale_every >= 1, KF_EINVAL, "ChebyshevFilter: maxiter and rescale_every must be at least 1");
+    const int nb = (int)std::min<int64_t>(m + o.extra, N);
+    KF_REQUIRE(nb <= 110, KF_EINVAL, "ChebyshevFilter: this build supports blocks of at most 110 columns (m + extra)");
+    const double hb = op->gershgorin;
+    st.hnorm = hb;
+    const double lmax = std::isnan(o.bound) ? hb : o.bound;
+    const double eps = std::numeric_limits<double>::epsilon();
+    const int g = std::max(std::min(std::min(o.extra - 1, CHEB_GUARDS), nb - 1 - m), 0);
+    const double t0 = now_s();
+    // seed on the host: product seed + 1e-2 admixture, or random
+    std::vector<double> X0((size_t)N * nb);
+    if (seed) {
+        std::memcpy(X0.data(), seed, sizeof(double) * (size_t)N * nb);
+        perturb_columns(X0.data(), N, nb, SEED_ADMIXTURE, 0x4346);
+    } else {
+        HostNormal rng(o.rng_seed);
+        for (auto &v : X0) v = rng();
+    }
+    // buffers (FP64): X, HX, A, B, C, S
+    const size_t blk = (size_t)N * nb * sizeof(double);
+    DevMem dX(blk), dHX(blk), dA(blk), dB(blk), dC(blk), dS(blk), dG((size_t)nb * nb * 8), dM((size_t)nb * nb * 8),
+        dpart(gram_partials_size(nb, nb, N)), dv(2 * nb * 8);
+    HostMem hG((size_t)nb * nb * 8), hv(2 * nb * 8);
+    double *X = dX.as<double>(), *HX = dHX.as<double>();
+    double *bufs[3] = {dA.as<double>(), dB.as<double>(), dC.as<double>()};
+    double *S = dS.as<double>(), *G = dG.as<double>(), *M = dM.as<double>(), *part = dpart.as<double>();
+    uint64_t refill_stream = 1;
+    KF_CUDA(cudaMemcpyAsync(bufs[0], X0.data(), blk, cudaMemcpyHostToDevice, s));
+
+    auto colnorms_host = [&](const double *Z, int k, std::vector<double> &out) {
+        colnorms2<double>(Z, N, k, N, dv.as<double>(), part, s);
+        KF_CUDA(cudaMemcpyAsync(hv.p, dv.p, k * 8, cudaMemcpyDeviceToHost, s));
+        KF_CUDA(cudaStreamSynchronize(s));
+        out.resize(k);
+        for (int j = 0; j < k; ++j) out[j] = std::sqrt(hv.as<double>()[j]);
+    };
+    auto normalize = [&](double *Z, int k) {
+        std::vector<double> nrm;
+        colnorms_host(Z, k, nrm);
+        for (int j = 0; j < k; ++j) hv.as<double>()[j] = 1.0 / std::max(nrm[j], 1e-300);
+        KF_CUDA(cudaMemcpyAsync(dv.p, hv.p, k * 8, cudaMemcpyHostToDevice, s));
+        scale_columns<double>(Z, N, k, N, dv.as<double>(), s);
+    };
+    // Z <- Z - L (L' Z), twice
+    auto project_out = [&](double *Z, int k, const double *L, int nl) {
+        if (nl == 0 || k == 0) return;
+        for (int q = 0; q < 2; ++q) {
+            gram<double>(L, N, nl, Z, N, k, N, G, part, s);
+            update<double>(Z, N, k, L, N, nl, G, nl, -1.0, 1.0, N, s);
+        }
+    };
+    // one SVQB pass: dst[:, 0:r] = orthonormal basis of Z; returns r
+    auto svqb_pass = [&](double *dst, const double *Z, int k) -> int {
+        if (k == 0) return 0;
+        gram<double>(Z, N, k, Z, N, k, N, G, part, s);
+        KF_CUDA(cudaMemcpyAsync(hG.p, G, (size_t)k * k * 8, cudaMemcpyDeviceToHost, s));
+        KF_CUDA(cudaStreamSynchronize(s));
+        std::vector<double> T;
+        const int r = svqb_coeffs(k, hG.as<double>(), SVQB_CUTOFF, T);
+        if (r == 0) return 0;
+        KF_CUDA(cudaMemcpyAsync(M, T.data(), (size_t)k * r * 8, cudaMemcpyHostToDevice, s));
+        update<double>(dst, N, r, Z, N, k, M, k, 1.0, 0.0, N, s);
+        return r;
+    };
+    // orthonormalise Z (na columns) against the locked L into Wd; Z and Sd are scratch
+    auto orthonormalize = [&](double *Wd, double *Z, int na, const double *L, int nl, double *Sd) {
+        project_out(Z, na, L, nl);
+        if (o.ortho == KF_ORTHO_CHOLQR) {
+            const double *src = Z;
+            double *dsts[2] = {Sd, Wd};
+            for (int q = 0; q < 2; ++q) {
+                gram<double>(src, N, na, src, N, na, N, G, part, s);
+                KF_CUDA(cudaMemcpyAsync(hG.p, G, (size_t)na * na * 8, cudaMemcpyDeviceToHost, s));
+                KF_CUDA(cudaStreamSynchronize(s));
+                std::vector<double> U(hG.as<double>(), hG.as<double>() + (size_t)na * na), Ui((size_t)na * na);
+                for (int j = 0; j < na; ++j)
+                    for (int i = 0; i < j; ++i) U[j + (size_t)na * i] = U[i + (size_t)na * j] = 0.5 * (U[i + (size_t)na * j] + U[j + (size_t)na * i]);
+                if (!cholesky_upper(na, U.data(), na))
+                    throw Error(KF_EBREAKDOWN,
+                                "ChebyshevFilter: Cholesky-QR failed, the filtered block is numerically rank "
+                                "deficient; use ortho=:svqb (it drops and refills dependent directions)");
+                tri_upper_inverse(na, U.data(), na, Ui.data(), na);
+                KF_CUDA(cudaMemcpyAsync(M, Ui.data(), (size_t)na * na * 8, cudaMemcpyHostToDevice, s));
+                update<double>(dsts[q], N, na, src, N, na, M, na, 1.0, 0.0, N, s);
+                src = dsts[q];
+            }
+            project_out(Wd, na, L, nl);
+            return;
+        }
+        int k1 = svqb_pass(Sd, Z, na);
+        int k = svqb_pass(Wd, Sd, k1);
+        int refills = 0;
+        while (k < na) {
+            if (++refills > 10)
+                throw Error(KF_EBREAKDOWN,
+                            "ChebyshevFilter: SVQB could not refill " + std::to_string(na - k) +
+                                " dropped directions with random vectors; the block is wider than the space left "
+                                "beside the locked columns");
+            const int r = na - k;
+            double *Rr = Z;
+            fill_normal<double>(Rr, N, r, N, o.rng_seed, refill_stream++, s);
+            std::vector<double> before, after;
+            colnorms_host(Rr, r, before);
+            project_out(Rr, r, L, nl);
+            project_out(Rr, r, Wd, k);
+            colnorms_host(Rr, r, after);
+            for (int j = 0; j < r; ++j) {
+                const bool room = after[j] > std::sqrt(eps) * before[j];
+                hv.as<double>()[j] = room ? 1.0 / std::max(after[j], 1e-300) : 0.0;
+            }
+            KF_CUDA(cudaMemcpyAsync(dv.p, hv.p, r * 8, cudaMemcpyHostToDevice, s));
+            scale_columns<double>(Rr, N, r, N, dv.as<double>(), s);
+            const int j1 = svqb_pass(Sd, Rr, r);
+            if (j1 == 0) continue;
+            project_out(Sd, j1, Wd, k);
+            k += svqb_pass(Wd + (int64_t)k * N, Sd, j1);
+        }
+        project_out(Wd, na, L, nl);
+    };
+    // Rayleigh-Ritz on W with HW: Xa = W Q, HXa = HW Q, theta (host)
+    auto rayleigh_ritz = [&](double *Xa, double *HXa, const double *Wd, const double *HWd, int k,
+                             std::vector<double> &th) {
+        gram<double>(Wd, N, k, HWd, N, k, N, G, part, s);
+        KF_CUDA(cudaMemcpyAsync(hG.p, G, (size_t)k * k * 8, cudaMemcpyDeviceToHost, s));
+        KF_CUDA(cudaStreamSynchronize(s));
+        std::vector<double> V((size_t)k * k);
+        th.resize(k);
+        if (sym_eig(k, hG.as<double>(), k, th.data(), V.data(), k) != 0)
+            throw Error(KF_EBREAKDOWN, "ChebyshevFilter: Rayleigh-Ritz eigenproblem did not converge");
+        KF_CUDA(cudaMemcpyAsync(M, V.data(), (size_t)k * k * 8, cudaMemcpyHostToDevice, s));
+        update<double>(Xa, N, k, Wd, N, k, M, k, 1.0, 0.0, N, s);
+        update<double>(HXa, N, k, HWd, N, k, M, k, 1.0, 0.0, N, s);
+    };
+    auto check_bound = [&](const double *th, int k) {
+        const double slack = std::sqrt(eps) * std::max(std::fabs(lmax), 1.0);
+        double top = -INFINITY;
+        for (int j = 0; j < k; ++j) top = std::max(top, th[j]);
+        if (!(top <= lmax + slack)) {
+            char buf[320];
+            snprintf(buf, sizeof buf,
+                     "ChebyshevFilter: a Ritz value %.6g exceeds the upper end λ_max = %.6g of the filter interval, "
+                     "so the bound is below the true largest eigenvalue; use bound=:gershgorin",
+                     top, lmax);
+            throw Error(KF_ENOCONV, buf);
+        }
+    };
+
+    // the seed's Rayleigh-Ritz
+    normalize(bufs[0], nb);
+    orthonormalize(bufs[1], bufs[0], nb, nullptr, 0, bufs[2]);
+    launch_apply(op, false, bufs[1], bufs[0], N, N, nb, 1, 0, nullptr, 0, 0, s);
+    int64_t nmv = nb;
+    std::vector<double> theta;
+    rayleigh_ritz(X, HX, bufs[1], bufs[0], nb, theta);
+    check_bound(theta.data(), nb);
+    std::vector<double> res(nb, INFINITY);
+    int nlock = 0, it = 0, deg = 0;
+    double lcut = NAN;
+    const bool f32 = o.precision == KF_PREC_MIXED;
+    DevMem fA(f32 ? (size_t)N * nb * 4 : 0), fB(f32 ? (size_t)N * nb * 4 : 0), fC(f32 ? (size_t)N * nb * 4 : 0);
+    while (true) {
+        const int na = nb - nlock;
+        // residual norms of the active columns
+        KF_CUDA(cudaMemcpyAsync(dv.p, theta.data() + nlock, na * 8, cudaMemcpyHostToDevice, s));
+        residual_block<double>(X + (int64_t)nlock * N, HX + (int64_t)nlock * N, N, na, N, dv.as<double>(), bufs[0], N, s);
+        std::vector<double> rn;
+        colnorms_host(bufs[0], na, rn);
+        for (int j = 0; j < na; ++j) res[nlock + j] = rn[j];
+        const bool filtered = it >= 1 || nb == N;
+        const double tmin = *std::min_element(theta.begin(), theta.end());
+        const double floor_ = 10 * eps * std::max(std::fabs(hb), std::fabs(tmin));
+        while (filtered && nlock < nb && res[nlock] <= LOCK_FRACTION * std::max(o.tol, floor_)) ++nlock;
+        // counted guards
+        int counted = g;
+        if (deg > 0 && std::isfinite(lcut)) {
+            const double ref = log_gain(kth_smallest(theta, m), lcut, lmax);
+            if (ref > 0) {
+                counted = 0;
+                for (int j = m; j < m + g; ++j) {
+                    if (log_gain(theta[j], lcut, lmax) < GUARD_GAIN_FRACTION * ref) break;
+                    ++counted;
+                }
+            }
+        }
+        const int need = m + counted;
+        bool done = false;
+        if (nlock >= need) {
+            if (nlock == nb)
+                done = true;
+            else
+                done = theta[nlock] >= kth_smallest(std::vector<double>(theta.begin(), theta.begin() + nlock), m);
+        }
+        if (done) break;
+        if (it >= o.maxiter) {
+            char buf[256];
+            snprintf(buf, sizeof buf, "ChebyshevFilter: within maxiter = %d iterations only %d of %d eigenpairs converged",
+                     o.maxiter, std::min(nlock, need), need);
+            throw Error(KF_ENOCONV, buf);
+        }
+        ++it;
+        const int nact = nb - nlock;
+        lcut = theta[nb - 1];
+        if (!(lcut < lmax)) throw Error(KF_ENOCONV, "ChebyshevFilter: the block's largest Ritz value reaches the upper end λ_max of the filter interval; use Dense()");
+        // degree cap (src/chebyshev.jl:169-174)
+        deg = o.degree;
+        {
+            const double x = std::fabs((tmin - (lmax + lcut) / 2) / ((lmax - lcut) / 2));
+            if (x > 1) {
+                const double cap = std::acosh(1.0 / std::sqrt(eps)) / std::acosh(x);
+                if (cap < o.degree) deg = std::max((int)std::floor(cap), 1);
+            }
+        }
+        const double c = (lmax + lcut) / 2, e = (lmax - lcut) / 2;
+        const double *Xa = X + (int64_t)nlock * N;
+        double *Zres;
+        int zi;
+        if (!f32) {
+            double *A = bufs[0], *B = bufs[1], *Cc = bufs[2];
+            copy_block<double>(Xa, N, A, N, nact, N, s);
+            launch_apply(op, false, A, B, N, N, nact, 1.0 / e, -c / e, nullptr, N, 0.0, s);   // T1 = (H - c) X / e
+            for (int k = 2; k <= deg; ++k) {
+                launch_apply(op, false, B, Cc, N, N, nact, 2.0 / e, -2.0 * c / e, A, N, -1.0, s);
+                std::swap(A, B);
+                std::swap(B, Cc);   // (A, B, C) <- (B, C, A)
+                if (k % o.rescale_every == 0) {
+                    std::vector<double> nrm;
+                    colnorms_host(B, nact, nrm);
+                    for (int j = 0; j < nact; ++j) hv.as<double>()[j] = 1.0 / std::max(nrm[j], 1e-300);
+                    KF_CUDA(cudaMemcpyAsync(dv.p, hv.p, nact * 8, cudaMemcpyHostToDevice, s));
+                    scale_columns<double>(A, N, nact, N, dv.as<double>(), s);
+                    scale_columns<double>(B, N, nact, N, dv.as<double>(), s);
+                }
+            }
+            Zres = B;
+        } else {
+            // FP32 filter: the recurrence in FP32, result widened to FP64
+            float *A = fA.as<float>(), *B = fB.as<float>(), *Cc = fC.as<float>();
+            convert<double, float>(Xa, N, A, N, nact, N, s);
+            launch_apply(op, true, A, B, N, N, nact, 1.0 / e, -c / e, nullptr, N, 0.0, s);
+            for (int k = 2; k <= deg; ++k) {
+                launch_apply(op, true, B, Cc, N, N, nact, 2.0 / e, -2.0 * c / e, A, N, -1.0, s);
+                std::swap(A, B);
+                std::swap(B, Cc);
+                if (k % o.rescale_every == 0) {
+                    colnorms2<float>(B, N, nact, N, dv.as<double>(), part, s);
+                    KF_CUDA(cudaMemcpyAsync(hv.p, dv.p, nact * 8, cudaMemcpyDeviceToHost, s));
+                    KF_CUDA(cudaStreamSynchronize(s));
+                    for (int j = 0; j < nact; ++j) hv.as<double>()[j] = 1.0 / std::max(std::sqrt(hv.as<double>()[j]), 1e-300);
+                    KF_CUDA(cudaMemcpyAsync(dv.p, hv.p, nact * 8, cudaMemcpyHostToDevice, s));
+                    scale_columns<float>(A, N, nact, N, dv.as<double>(), s);
+                    scale_columns<float>(B, N, nact, N, dv.as<double>(), s);
+                }
+            }
+            convert<float, double>(B, N, bufs[0], N, nact, N, s);
+            Zres = bufs[0];
+        }
+        nmv += (int64_t)deg * nact;
+        zi = Zres == bufs[0] ? 0 : Zres == bufs[1] ? 1 : 2;
+        double *Wv = bufs[(zi + 1) % 3], *Sv = bufs[(zi + 2) % 3];
+        {
+            std::vector<double> nrm;
+            colnorms_host(Zres, nact, nrm);
+            for (int j = 0; j < nact; ++j)
+                if (!std::isfinite(nrm[j]))
+                    throw Error(KF_ENOTFINITE,
+                                "ChebyshevFilter: the filtered block is not finite: the upper end λ_max of the filter "
+                                "interval is below the true largest eigenvalue, so the filter amplifies the top of the "
+                                "spectrum; use bound=:gershgorin");
+        }
+        normalize(Zres, nact);
+        orthonormalize(Wv, Zres, nact, X, nlock, Sv);
+        launch_apply(op, false, Wv, Zres, N, N, nact, 1, 0, nullptr, 0, 0, s);
+        nmv += nact;
+        std::vector<double> th;
+        rayleigh_ritz(X + (int64_t)nlock * N, HX + (int64_t)nlock * N, Wv, Zres, nact, th);
+        for (int j = 0; j < nact; ++j) theta[nlock + j] = th[j];
+        check_bound(th.data(), nact);
+    }
+    st.iterations = it;
+    st.n_matvec = nmv;
+    // the lowest m locked pairs, accepted with a fresh application (src/chebyshev.jl:395-405)
+    std::vector<double> thl(theta.begin(), theta.begin() + nlock);
+    std::vector<double> resid;
+    accept_and_copy(op, X, nlock, thl, m, E_out, V_out, resid, s);
+    double worst = 0;
+    int jw = 0;
+    for (int j = 0; j < m; ++j)
+        if (resid[j] > worst) { worst = resid[j]; jw = j; }
+    std::vector<int> ord(nlock);
+    std::iota(ord.begin(), ord.end(), 0);
+    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return thl[a] < thl[b]; });
+    const double floor_ = 10 * eps * std::max(std::fabs(hb), std::fabs(thl[ord[0]]));
+    st.max_residual = worst;
+    st.converged = 0;
+    for (int j = 0; j < m; ++j) st.converged += resid[j] <= std::max(o.tol, floor_);
+    st.seconds = now_s() - t0;
+    if (!(worst <= std::max(o.tol, floor_))) {
+        char buf[256];
+        snprintf(buf, sizeof buf, "ChebyshevFilter: the true residual ‖H v − E v‖ = %.3e of pair %d exceeds %.3e on return",
+                 worst, jw + 1, std::max(o.tol, floor_));
+        throw Error(KF_ENOCONV, buf);
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// Lanczos (src/solvers.jl:85-106): thick-restart Lanczos with full reorthogonalisation in FP64
+// (KrylovKit's eigsolve is a Krylov-Schur method; both keep the Ritz vectors of the wanted end
+// at each restart).
+
+static void solve_lanczos(kf_op *op, const kf_solver_opts &o, int m, double *E_out, double *V_out,
+                          kf_solve_stats &st) {
+    const int64_t N = op->N;
+    cudaStream_t s = op->stream;
+    KF_REQUIRE(m >= 1, KF_EINVAL, "Lanczos requires m >= 1, got " + std::to_string(m));
+    KF_REQUIRE(m <= N, KF_EINVAL, "Lanczos: m = " + std::to_string(m) + " exceeds the operator dimension " + std::to_string(N));
+    const int kd = (int)std::min<int64_t>(std::max(2 * m + 10, o.krylovdim > 0 ? o.krylovdim : 40), N);
+    KF_REQUIRE(kd <= 128, KF_EINVAL, "Lanczos: this build supports krylovdim <= 128");
+    const double t0 = now_s();
+    DevMem dV((size_t)N * (kd + 1) * 8), dHV((size_t)N * 8), dW((size_t)N * kd * 8), dG((size_t)(kd + 1) * 8 * 2),
+        dC((size_t)(kd + 1) * (kd + 1) * 8), dpart(gram_partials_size(kd + 1, 1, N)), dn(8);
+    HostMem hG((size_t)(kd + 1) * (kd + 1) * 8);
+    double *V = dV.as<double>(), *G = dG.as<double>(), *part = dpart.as<double>();
+    // start vector
+    fill_normal<double>(V, N, 1, N, o.rng_seed, 7, s);
+    double nrm2;
+    colnorms2<double>(V, N, 1, N, dn.as<double>(), part, s);
+    KF_CUDA(cudaMemcpyAsync(&nrm2, dn.p, 8, cudaMemcpyDeviceToHost, s));
+    KF_CUDA(cudaStreamSynchronize(s));
+    double sc = 1.0 / std::sqrt(nrm2);
+    KF_CUDA(cudaMemcpyAsync(dn.p, &sc, 8, cudaMemcpyHostToDevice, s));
+    scale_columns<double>(V, N, 1, N, dn.as<double>(), s);
+    // T: the projected matrix in the current basis (k x k, symmetric, arrow + tridiagonal)
+    std::vector<double> T((size_t)(kd + 1) * (kd + 1), 0.0);
+    int k = 0;          // vectors kept from the last restart (T[0:k, 0:k] diagonal, row k the arrow)
+    int64_t nmv = 0;
+    int restarts = 0;
+    std::vector<double> theta, resid(m, INFINITY);
+    const double tol = o.tol;
+    while (true) {
+        // extend the basis from column j = k to kd
+        for (int j = k; j < kd; ++j) {
+            double *vj = V + (int64_t)j * N, *w = V + (int64_t)(j + 1) * N;
+            launch_apply(op, false, vj, w, N, N, 1, 1, 0, nullptr, 0, 0, s);
+            ++nmv;
+            // full reorthogonalisation, twice: h = V[:, 0:j+1]' w, w -= V h
+            std::vector<double> h(j + 1, 0.0);
+            for (int q = 0; q < 2; ++q) {
+                gram<double>(V, N, j + 1, w, N, 1, N, G, part, s);
+                KF_CUDA(cudaMemcpyAsync(hG.p, G, (j + 1) * 8, cudaMemcpyDeviceToHost, s));
+                update<double>(w, N, 1, V, N, j + 1, G, j + 1, -1.0, 1.0, N, s);
+                KF_CUDA(cudaStreamSynchronize(s));
+                for (int i = 0; i <= j; ++i) h[i] += hG.as<double>()[i];
+            }
+            colnorms2<double>(w, N, 1, N, dn.as<double>(), part, s);
+            KF_CUDA(cudaMemcpyAsync(&nrm2, dn.p, 8, cudaMemcpyDeviceToHost, s));
+            KF_CUDA(cudaStreamSynchronize(s));
+            const double beta = std::sqrt(nrm2);
+            for (int i = 0; i <= j; ++i) {
+                T[i + (size_t)(kd + 1) * j] = h[i];
+                T[j + (size_t)(kd + 1) * i] = h[i];
+            }
+            T[(j + 1) + (size_t)(kd + 1) * j] = beta;
+            T[j + (size_t)(kd + 1) * (j + 1)] = beta;
+            if (beta <= 1e-14 * std::max(1.0, std::fabs(op->gershgorin))) {
+                // invariant subspace: restart the new direction randomly, orthogonalised
+                fill_normal<double>(w, N, 1, N, o.rng_seed, 1000 + nmv, s);
+                for (int q = 0; q < 2; ++q) {
+                    gram<double>(V, N, j + 1, w, N, 1, N, G, part, s);
+                    update<double>(w, N, 1, V, N, j + 1, G, j + 1, -1.0, 1.0, N, s);
+                }
+                colnorms2<double>(w, N, 1, N, dn.as<double>(), part, s);
+                KF_CUDA(cudaMemcpyAsync(&nrm2, dn.p, 8, cudaMemcpyDeviceToHost, s));
+                KF_CUDA(cudaStreamSynchronize(s));
+                T[(j + 1) + (size_t)(kd + 1) * j] = 0;
+                T[j + (size_t)(kd + 1) * (j + 1)] = 0;
+                sc = 1.0 / std::sqrt(nrm2);
+            } else {
+                sc = 1.0 / beta;
+            }
+            KF_CUDA(cudaMemcpyAsync(dn.p, &sc, 8, cudaMemcpyHostToDevice, s));
+            scale_columns<double>(w, N, 1, N, dn.as<double>(), s);
+        }
+        // Ritz pairs of T[0:kd, 0:kd]; residual of pair i = |beta_kd * y[kd-1, i]|
+        std::vector<double> Ts((size_t)kd * kd), lam(kd), Y((size_t)kd * kd);
+        for (int j = 0; j < kd; ++j)
+            for (int i = 0; i < kd; ++i) Ts[i + (size_t)kd * j] = T[i + (size_t)(kd + 1) * j];
+        if (sym_eig(kd, Ts.data(), kd, lam.data(), Y.data(), kd) != 0)
+            throw Error(KF_EBREAKDOWN, "Lanczos: the projected eigenproblem did not converge");
+        const double bk = T[kd + (size_t)(kd + 1) * (kd - 1)];
+        int conv = 0;
+        for (int i = 0; i < m; ++i) {
+            resid[i] = std::fabs(bk * Y[(kd - 1) + (size_t)kd * i]);
+            if (resid[i] <= tol) ++conv;
+        }
+        theta.assign(lam.begin(), lam.begin() + m);
+        const int keep = std::min(kd - 1, std::max(m + (kd - m) / 2, m));
+        if (conv == m || restarts >= o.maxiter) {
+            // Ritz vectors of the lowest m into dW
+            KF_CUDA(cudaMemcpyAsync(dC.p, Y.data(), (size_t)kd * m * 8, cudaMemcpyHostToDevice, s));
+            update<double>(dW.as<double>(), N, m, V, N, kd, dC.as<double>(), kd, 1.0, 0.0, N, s);
+            break;
+        }
+        // thick restart: keep the lowest `keep` Ritz vectors and the residual direction
+        KF_CUDA(cudaMemcpyAsync(dC.p, Y.data(), (size_t)kd * keep * 8, cudaMemcpyHostToDevice, s));
+        update<double>(dW.as<double>(), N, keep, V, N, kd, dC.as<double>(), kd, 1.0, 0.0, N, s);
+        copy_block<double>(V + (int64_t)kd * N, N, V + (int64_t)keep * N, N, 1, N, s);
+        copy_block<double>(dW.as<double>(), N, V, N, keep, N, s);
+        std::fill(T.begin(), T.end(), 0.0);
+        for (int i = 0; i < keep; ++i) {
+            T[i + (size_t)(kd + 1) * i] = lam[i];
+            const double a = bk * Y[(kd - 1) + (size_t)kd * i];
+            T[keep + (size_t)(kd + 1) * i] = a;
+            T[i + (size_t)(kd + 1) * keep] = a;
+        }
+        k = keep;
+        ++restarts;
+    }
+    st.iterations = restarts;
+    st.n_matvec = nmv;
+    std::vector<double> r2;
+    accept_and_copy(op, dW.as<double>(), m, theta, m, E_out, V_out, r2, s);
+    double worst = 0;
+    int bad = 0;
+    for (int j = 0; j < m; ++j) {
+        worst = std::max(worst, r2[j]);
+        bad += !(r2[j] <= std::max(tol, 10 * std::numeric_limits<double>::epsilon() * std::fabs(op->gershgorin)));
+    }
+    st.max_residual = worst;
+    st.converged = m - bad;
+    st.seconds = now_s() - t0;
+    if (bad) {
+        char buf[200];
+        snprintf(buf, sizeof buf, "Lanczos: only %d of %d eigenpairs converged (normres = %.3e)", m - bad, m, worst);
+        throw Error(KF_ENOCONV, buf);
+    }
+}
+
+void solve_dispatch(kf_op *op, const kf_solver_opts &o, int m, const double *X0, const double *seed, double *E_out,
+                    double *V_out, kf_solve_stats &st) {
+    std::memset(&st, 0, sizeof(st));
+    switch (o.kind) {
+        case KF_SOLVER_LOBPCG: solve_lobpcg(op, o, m, X0, seed, E_out, V_out, st); break;
+        case KF_SOLVER_CHEBYSHEV: solve_chebyshev(op, o, m, seed, E_out, V_out, st); break;
+        case KF_SOLVER_LANCZOS: solve_lanczos(op, o, m, E_out, V_out, st); break;
+        default: throw Error(KF_EINVAL, "kf_solve: unknown solver kind " + std::to_string(o.kind));
+    }
+}
+
+}  // namespace kf

@@ -1,0 +1,78 @@
+"""The synthetic circuits of the measured workloads, built the reference's way (test infrastructure only).
+
+Each circuit is written as a kronfree-spec dictionary (the reference's input format, src/spec.jl)
+and expanded by `kfref.circuit_terms` + the real expansion, i.e. the route
+materialize -> _real_node_terms -> KronFreeOperator takes in the reference
+(src/materialize.jl:583-647).  The GPU side builds the same Hamiltonians from its own port
+operators; tests compare the two.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import kfref
+
+PI = np.pi
+
+
+def three_mode_spec():
+    """H = 4E_C1 n1^2 - E_C2 d2^2 - E_C3 d3^2 + E_L/2 (phi2^2 + phi3^2) - 2E_J cos phi1 cos phi2 - E_J' cos(phi2 - phi3).
+
+    -E_C d^2 is `n2port` with coefficient E_C, i.e. a spec diagonal E_C/4; -2E_J cos phi1 cos phi2 is
+    the pair of cosines E_J (phi1 + phi2) and E_J (phi1 - phi2).
+    """
+    return {
+        "format": "kronfree-spec", "version": 1,
+        "parameters": ["E_J", "E_C1", "E_C2", "E_C3", "E_L", "E_Jp"],
+        "modes": [{"name": "phi1", "type": "c"}, {"name": "phi2", "type": "e"}, {"name": "phi3", "type": "e"}],
+        "E_C": [["E_C1", "0", "0"], ["0", "E_C2/4", "0"], ["0", "0", "E_C3/4"]],
+        "E_L": [["0", "0", "0"], ["0", "E_L", "0"], ["0", "0", "E_L"]],
+        "flux_linear": ["0", "0", "0"],
+        "n_g": ["0", "0", "0"],
+        "cosines": [
+            {"energy": "E_J", "omega": [1, 1, 0], "offset": "0"},
+            {"energy": "E_J", "omega": [1, -1, 0], "offset": "0"},
+            {"energy": "E_Jp", "omega": [0, 1, -1], "offset": "0"},
+        ],
+    }
+
+
+def three_mode_theta(rng):
+    """theta ~ the uniform ranges of the three-mode leaf workload."""
+    return {"E_J": rng.uniform(5, 15), "E_C1": rng.uniform(0.02, 0.1), "E_C2": rng.uniform(0.5, 2),
+            "E_C3": rng.uniform(0.5, 2), "E_L": rng.uniform(0.02, 0.2), "E_Jp": rng.uniform(0.5, 2)}
+
+
+def three_mode_operator(theta, ncut=20, n2=256, n3=64):
+    bases = {"phi1": kfref.ChargeBasis(ncut), "phi2": kfref.PhaseGrid(-4 * PI, 4 * PI, n2, 4),
+             "phi3": kfref.PhaseGrid(-3 * PI, 3 * PI, n3, 4)}
+    terms = kfref.leaf_terms(three_mode_spec(), theta, bases, real=True)
+    return kfref.KronFreeOperator([b.dim for b in bases.values()], _merge(terms))
+
+
+def fluxonium_theta(rng):
+    """theta ~ U: E_J [3,10], E_C [0.5,1.5], E_L [0.2,1.2], phi_ext [0, 2 pi]."""
+    return {"E_J": rng.uniform(3, 10), "E_C": rng.uniform(0.5, 1.5), "E_L": rng.uniform(0.2, 1.2),
+            "phi_ext": rng.uniform(0, 2 * PI)}
+
+
+def fluxonium_spec():
+    """-E_C d^2 (5-point) + E_L/2 phi^2 - E_J cos(phi - phi_ext): E_C/4 on the spec diagonal."""
+    return {
+        "format": "kronfree-spec", "version": 1,
+        "parameters": ["E_J", "E_C", "E_L", "phi_ext"],
+        "modes": [{"name": "phi", "type": "e"}],
+        "E_C": [["E_C/4"]], "E_L": [["E_L"]], "flux_linear": ["0"], "n_g": ["0"],
+        "cosines": [{"energy": "E_J", "omega": [1], "offset": "-phi_ext"}],
+    }
+
+
+def fluxonium_operator(theta, npts):
+    bases = {"phi": kfref.PhaseGrid(-5 * PI, 5 * PI, npts, 4)}
+    terms = kfref.leaf_terms(fluxonium_spec(), theta, bases, real=True)
+    return kfref.KronFreeOperator([npts], _merge(terms))
+
+
+def _merge(terms):
+    """Sum real terms with identical factor objects (the reference merges equal keys, src/materialize.jl:616-647)."""
+    return terms
