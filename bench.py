@@ -1,0 +1,306 @@
+"""Benchmark: converged eigenpairs per second on the three-mode leaf (N = 671,744, m = 12, block 16).
+
+A step is one eigen-solve of the leaf Hamiltonian
+    H = 4E_C1 n1^2 - E_C2 d2^2 - E_C3 d3^2 + E_L/2 (phi2^2 + phi3^2) - 2E_J cos phi1 cos phi2 - E_J' cos(phi2 - phi3)
+on a 41 x 256 x 64 charge x grid x grid basis for one synthetic theta drawn from the stated
+uniform ranges (seeded; the draws cycle), lowest 12 eigenpairs with LOBPCG (block 16, product
+seed), every pair accepted at ||H x - lambda x|| <= 1e-8 ||H|| (||H|| = Gershgorin bound) by a
+fresh FP64 application.
+
+  value            converged pairs / s of the mixed-precision solver (FP32 bulk, FP64 Rayleigh-Ritz
+                   and refinement), operators already on the device when the timed region starts
+  plain_f64        the same for the plain FP64 solver (the metric's denominator)
+  e2e              the public API end to end with host buffers: kf_op_create from the host term
+                   list, host product seed in, host eigenpairs out, kf_op_destroy, every step
+  roofline         the fused stencil apply (FP32, 16 columns): algorithmic bytes 2 N b 4 per launch
+                   over its CUDA-event time, against the measured HBM copy bandwidth
+  cpu_baseline     the oracle's restatement of the reference CPU path (C/OpenMP mul! + NumPy LOBPCG)
+                   on the host cores, a bounded sample
+
+`--impl reference` times the reference's CPU path (the oracle port: the reference is Julia and
+cannot run here) on the same workload and metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "kronfreecircuits.jl_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+M_PAIRS = 12
+SEED = 20261205          # theta draws of the three-mode leaf workload
+NDRAWS = 64
+# ncu dram__bytes_read.sum + dram__bytes_write.sum of one FP32 16-column fused-apply launch at
+# N = 671,744 (profiles/apply_fused_three_mode.md); None until captured
+APPLY_TRAFFIC_BYTES = None
+
+
+def thetas():
+    from kfgpu import circuits
+    rng = np.random.default_rng(SEED)
+    return [circuits.three_mode_theta(rng) for _ in range(NDRAWS)]
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    def __init__(self):
+        self.rows, self._stop, self._t = [], threading.Event(), None
+
+    def start(self):
+        def run():
+            q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+            while not self._stop.is_set():
+                try:
+                    out = subprocess.run(["nvidia-smi", "-i", "0", f"--query-gpu={q}", "--format=csv,noheader,nounits"],
+                                         capture_output=True, text=True, timeout=5).stdout.strip()
+                    if out:
+                        self.rows.append([x.strip() for x in out.split(",")])
+                except Exception:
+                    pass
+                self._stop.wait(0.2)
+        self._t = threading.Thread(target=run, daemon=True)
+        self._t.start()
+        return self
+
+    def stop(self):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+        sm = [float(r[0]) for r in self.rows if r and r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if len(r) > 1 and r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if len(r) > 2 + i and r[2 + i] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def measure_apply(torch, H, f32, b=16, reps=20):
+    """CUDA-event time of one fused apply launch (inputs larger than L2 rotate between launches)."""
+    dt = torch.float32 if f32 else torch.float64
+    nbuf = 3
+    Xs = [torch.randn(b, H.N, dtype=dt, device="cuda") for _ in range(nbuf)]
+    Ys = [torch.empty_like(Xs[0]) for _ in range(nbuf)]
+    s = torch.cuda.Stream()
+    H.set_stream(s.cuda_stream)
+    for i in range(3):
+        H.apply_device(Xs[i % nbuf].data_ptr(), Ys[i % nbuf].data_ptr(), b, f32=f32)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for i in range(reps):
+        H.apply_device(Xs[i % nbuf].data_ptr(), Ys[i % nbuf].data_ptr(), b, f32=f32)
+    e1.record(s)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps / 1e3
+
+
+def run_ours(args):
+    import torch
+    from kfgpu import KronFreeOperator, LOBPCG, circuits, solve
+    from kfgpu._abi import launch_count
+    from kfgpu.build import build_library
+
+    assert torch.cuda.is_available(), "bench.py needs a CUDA device"
+    torch.cuda.set_device(0)
+    build_library()
+    ths = thetas()
+    K, W = args.steps, args.warmup
+    idx = [(W + k) % NDRAWS for k in range(K)]
+    # operators and host seeds prepared before the timed region (inputs resident)
+    ops = {}
+    for i in sorted(set(idx) | set(range(W))):
+        dims, terms = circuits.three_mode_leaf(ths[i])
+        H = KronFreeOperator(dims, terms)
+        ops[i] = (H, H.product_seed(M_PAIRS + 4))
+    stream = torch.cuda.Stream()
+    for H, _ in ops.values():
+        H.set_stream(stream.cuda_stream)
+
+    def one(i, precision):
+        H, seedb = ops[i]
+        tol = 1e-8 * H.gershgorin_bound()
+        E, V, st = solve(LOBPCG(tol=tol, precision=precision), H, M_PAIRS, seed_block=seedb)
+        return st["converged"], st
+
+    for w in range(W):
+        one(w, "mixed")
+    torch.cuda.synchronize()
+    n0 = launch_count()
+    clocks = Clocks().start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    conv, stats = 0, []
+    for i in idx:
+        c, st = one(i, "mixed")
+        conv += c
+        stats.append(st)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    t_mixed = e0.elapsed_time(e1) / 1e3
+    launches = launch_count() - n0
+    value = conv / t_mixed
+    # plain FP64 on a subset of the same draws (the metric's denominator)
+    kp = max(1, min(args.plain_steps, K))
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    conv64, st64 = 0, []
+    for i in idx[:kp]:
+        c, st = one(i, "f64")
+        conv64 += c
+        st64.append(st)
+    f1.record(stream)
+    torch.cuda.synchronize()
+    t64 = f0.elapsed_time(f1) / 1e3
+    plain = conv64 / t64
+    # end to end through the public API with host buffers
+    ke = max(1, min(args.e2e_steps, K))
+    h2d = d2h = 0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    conv_e = 0
+    for i in idx[:ke]:
+        dims, terms = circuits.three_mode_leaf(ths[i])
+        H = KronFreeOperator(dims, terms)
+        seedb = H.product_seed(M_PAIRS + 4)
+        tol = 1e-8 * H.gershgorin_bound()
+        E, V, st = solve(LOBPCG(tol=tol, precision="mixed"), H, M_PAIRS, seed_block=seedb)
+        conv_e += st["converged"]
+        h2d += H.N * 8 + seedb.nbytes + sum(op.n * 8 * 5 for _, fs in terms for _, op in fs)
+        d2h += V.nbytes + E.nbytes
+        H.close()
+    torch.cuda.synchronize()
+    te = time.perf_counter() - t0
+    # roofline of the dominant kernel: the FP32 fused stencil apply on a 16-column block
+    H0 = ops[idx[0]][0]
+    t_apply = measure_apply(torch, H0, True)
+    alg = 2 * H0.N * 16 * 4
+    peak, kind = peaks()
+    achieved = alg / t_apply / 1e9
+    line = {
+        "metric": "converged eigenpairs/s at 1e-8 resid: warm-start mixed vs plain FP64, 1 GB300",
+        "value": value, "unit": "eigenpairs/s", "n_gpus": 1, "steps": K, "warmup": W,
+        "ms_per_step": 1e3 * t_mixed / K, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 bulk + f64 refinement", "data": "synthetic",
+        "config": {"workload": "three-mode leaf 41x256x64 (N=671,744), LOBPCG m=12 block=16, product seed, "
+                               "tol 1e-8*||H||, theta ~ U(ranges) seed 20261205",
+                   "l2": "inputs larger than L2 (a 16-column FP32 block is 43 MB; a solve streams ~10 GB)"},
+        "plain_f64": {"value": plain, "steps": kp, "ms_per_step": 1e3 * t64 / kp,
+                      "iterations": [s["iterations"] for s in st64]},
+        "speedup_mixed_vs_f64": value / plain if plain > 0 else None,
+        "iterations": [s["iterations"] for s in stats], "iterations_f64_phase": [s["iterations_f64"] for s in stats],
+        "max_residual_rel": max(s["max_residual"] / s["hnorm"] for s in stats),
+        "e2e": {"value": conv_e / te, "unit": "eigenpairs/s", "h2d_bytes_per_step": int(h2d / ke),
+                "d2h_bytes_per_step": int(d2h / ke), "steps": ke},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": APPLY_TRAFFIC_BYTES, "kernel": "k_apply_fused<float> (16 columns)",
+                     "launch_us": t_apply * 1e6, "peak_kind": kind},
+        "clocks": clk, "gpu_launches": launches,
+    }
+    if not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(ths[idx[0]], bounded=True,
+                                            iters=int(round(np.mean([s["iterations"] for s in st64]))))
+    return line
+
+
+def cpu_baseline(theta, bounded=True, iters=None):
+    """The oracle's restatement of the reference CPU path on the host cores: a bounded sample of
+    LOBPCG iterations of the same solve (C/OpenMP mul! + NumPy LOBPCG), extrapolated to the
+    iteration count the same algorithm needs (measured here on the GPU's FP64 run when given,
+    else the sample's own count)."""
+    from oracle import capply, circuits as oc, solvers as osol
+    H = oc.three_mode_operator(theta)
+    CA = capply.CApply(H)
+
+    class Fast:
+        N, dtype = H.N, H.dtype
+
+        def matvec(self, X):
+            return CA.matvec(X)
+
+        def full_diagonal(self):
+            return H.full_diagonal()
+
+    tol = 1e-8 * H.gershgorin_bound()
+    X0 = osol.perturbed_seed(H.product_seed(M_PAIRS + 4))
+    D = H.full_diagonal()
+    n_it = 8 if bounded else 100000
+    t0 = time.perf_counter()
+    r = osol.lobpcg_core(Fast(), X0, D, tol, n_it, "ritz", 0.01)
+    dt = time.perf_counter() - t0
+    per_it = dt / max(r["iters"], 1)
+    need = iters if iters else r["iters"]
+    cores = os.cpu_count()
+    return {"value": M_PAIRS / (per_it * need), "unit": "eigenpairs/s", "cores": cores, "kind": "port",
+            "sample": f"{r['iters']} LOBPCG iterations of the N=671,744 solve in {dt:.1f} s "
+                      f"({per_it:.2f} s/iteration, OpenMP threads={cores}), extrapolated to {need} iterations"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return None
+    ths = thetas()
+    K, W = args.steps, args.warmup
+    vals = []
+    for k in range(W + K):
+        cb = cpu_baseline(ths[k % NDRAWS], bounded=True, iters=args.ref_iters)
+        if k >= W:
+            vals.append(cb)
+    v = float(np.mean([c["value"] for c in vals]))
+    return {"metric": "converged eigenpairs/s at 1e-8 resid: warm-start mixed vs plain FP64, 1 GB300",
+            "impl": "reference", "value": v, "unit": "eigenpairs/s", "n_gpus": 0, "steps": K, "warmup": W,
+            "higher_is_better": True, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "three-mode leaf 41x256x64 (N=671,744), LOBPCG m=12 block=16, product seed"},
+            "cpu_baseline": {"value": v, "unit": "eigenpairs/s", "cores": vals[0]["cores"], "kind": "port",
+                             "sample": vals[0]["sample"]},
+            "e2e": {"value": v, "unit": "eigenpairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=4)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--plain-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--ref-iters", type=int, default=570,
+                    help="LOBPCG iterations the FP64 solve of this workload takes (for the reference arm's extrapolation)")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        line = run_reference(args)
+    else:
+        rank = int(os.environ.get("RANK", "0"))
+        line = run_ours(args) if rank == 0 else None
+    if line is not None:
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -241,6 +241,9 @@ int kf_last_error(char *buf, size_t len);
 /* KFGPU_VERSION. */
 int kf_version(void);
 
+/* The number of CUDA kernels this library has launched in this process (all ops and solves). */
+int kf_launch_count(uint64_t *count);
+
 #ifdef __cplusplus
 }
 #endif

@@ -12,6 +12,7 @@ void free_op(kf_op *op);
 void solve_dispatch(kf_op *op, const kf_solver_opts &o, int m, const double *X0, const double *seed, double *E_out,
                     double *V_out, kf_solve_stats &st);
 
+std::atomic<uint64_t> g_launches{0};
 static thread_local std::string g_last_error;
 void set_last_error(const std::string &msg) { g_last_error = msg; }
 
@@ -38,6 +39,12 @@ using namespace kf;
 extern "C" {
 
 int kf_version(void) { return KFGPU_VERSION; }
+
+int kf_launch_count(uint64_t *count) {
+    if (!count) return KF_EINVAL;
+    *count = g_launches.load(std::memory_order_relaxed);
+    return KF_OK;
+}
 
 int kf_last_error(char *buf, size_t len) {
     if (!buf || len == 0) return KF_EINVAL;

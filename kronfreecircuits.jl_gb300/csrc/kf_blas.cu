@@ -9,8 +9,8 @@
 //
 // Blocks are column-major (N rows, k <= 128 columns, leading dimension ld).  Every reduction
 // over N is split across CTAs into FP64 partials and summed in a fixed order by a second
-// kernel, so results are deterministic run to run.  Within a CTA, FP32 blocks accumulate in
-// FP32 over that CTA's rows (at most GRAM_ROWS_PER_CTA) and FP64 blocks in FP64.
+// kernel, so results are deterministic run to run.  Within a CTA, FP32 Gram products accumulate
+// in FP32 over one 32-row tile and then in FP64; FP64 blocks accumulate in FP64 throughout.
 #include "kf_internal.h"
 
 namespace kf {
@@ -51,11 +51,17 @@ __global__ void __launch_bounds__(GRAM_THREADS) k_gram(const T *__restrict__ A, 
     T *Bs = As + GRAM_RT * ka;                          // [GRAM_RT][kb]
     const int ti_n = (ka + 3) / 4, tj_n = (kb + 3) / 4;
     const int ntiles = ti_n * tj_n;
+    // FP32 blocks: products accumulate in FP32 over one 32-row tile, then into FP64
     T acc[GRAM_MAXTILES][16];
+    double acc64[sizeof(T) == 4 ? GRAM_MAXTILES : 1][16];
 #pragma unroll
     for (int m = 0; m < GRAM_MAXTILES; ++m)
 #pragma unroll
         for (int q = 0; q < 16; ++q) acc[m][q] = T(0);
+#pragma unroll
+    for (int m = 0; m < (sizeof(T) == 4 ? GRAM_MAXTILES : 1); ++m)
+#pragma unroll
+        for (int q = 0; q < 16; ++q) acc64[m][q] = 0.0;
     const int64_t r0 = (int64_t)blockIdx.x * rows_per;
     const int64_t r1 = (r0 + rows_per < N) ? r0 + rows_per : N;
     for (int64_t rb = r0; rb < r1; rb += GRAM_RT) {
@@ -86,6 +92,13 @@ __global__ void __launch_bounds__(GRAM_THREADS) k_gram(const T *__restrict__ A, 
 #pragma unroll
                         for (int v = 0; v < 4; ++v) acc[m][u * 4 + v] += a[u] * bv[v];
                 }
+                if constexpr (sizeof(T) == 4) {
+#pragma unroll
+                    for (int q = 0; q < 16; ++q) {
+                        acc64[m][q] += (double)acc[m][q];
+                        acc[m][q] = T(0);
+                    }
+                }
             }
         }
         __syncthreads();
@@ -100,7 +113,9 @@ __global__ void __launch_bounds__(GRAM_THREADS) k_gram(const T *__restrict__ A, 
             for (int u = 0; u < 4; ++u)
 #pragma unroll
                 for (int v = 0; v < 4; ++v)
-                    if (i0 + u < ka && j0 + v < kb) P[(i0 + u) + (size_t)ka * (j0 + v)] = (double)acc[m][u * 4 + v];
+                    if (i0 + u < ka && j0 + v < kb)
+                        P[(i0 + u) + (size_t)ka * (j0 + v)] =
+                            (sizeof(T) == 4) ? acc64[sizeof(T) == 4 ? m : 0][u * 4 + v] : (double)acc[m][u * 4 + v];
         }
     }
 }
@@ -124,10 +139,10 @@ void gram(const T *A, int64_t lda, int ka, const T *B, int64_t ldb, int kb, int6
     const size_t sm = (size_t)GRAM_RT * (ka + kb) * sizeof(T);
     if (sm > 48 * 1024) KF_CUDA(cudaFuncSetAttribute(k_gram<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     k_gram<T><<<nc, GRAM_THREADS, sm, s>>>(A, lda, ka, B, ldb, kb, N, rp, partials);
-    KF_CUDA(cudaGetLastError());
+    KF_LAUNCH_CHECK();
     const int n = ka * kb;
     k_reduce_partials<<<(n + 255) / 256, 256, 0, s>>>(partials, nc, n, G);
-    KF_CUDA(cudaGetLastError());
+    KF_LAUNCH_CHECK();
 }
 
 // Y[r, j] = alpha * sum_i X[r, i] C[i, j] + beta * Y[r, j], one thread per row and a chunk of
@@ -189,7 +204,7 @@ void update(T *Y, int64_t ldy, int ky, const T *X, int64_t ldx, int kx, const do
         k_update<T, 8><<<grid, 256, sm, s>>>(Y, ldy, ky, X, ldx, kx, C, ldc, (T)alpha, (T)beta, N);
     else
         k_update<T, 16><<<grid, 256, sm, s>>>(Y, ldy, ky, X, ldx, kx, C, ldc, (T)alpha, (T)beta, N);
-    KF_CUDA(cudaGetLastError());
+    KF_LAUNCH_CHECK();
 }
 
 // ---- column reductions -------------------------------------------------------------------
@@ -248,9 +263,9 @@ void colnorms2(const T *X, int64_t ldx, int k, int64_t N, double *out, double *p
     const int nblk = (int)((N + rp - 1) / rp);
     dim3 grid(nblk, k);
     k_colnorm2<T><<<grid, RED_THREADS, 0, s>>>(X, ldx, N, rp, partials);
-    KF_CUDA(cudaGetLastError());
+    KF_LAUNCH_CHECK();
     k_reduce_cols<<<(k + 127) / 128, 128, 0, s>>>(partials, nblk, k, out);
-    KF_CUDA(cudaGetLastError());
+    KF_LAUNCH_CHECK();
 }
 
 // R[:, j] = HX[:, j] - theta_j X[:, j]; partial sums of R^2; then R[:, j] is preconditioned in
@@ -295,9 +310,9 @@ void residual_precond(const T *X, const T *HX, int64_t ld, int k, int64_t N, con
     const int nblk = (int)((N + rp - 1) / rp);
     dim3 grid(nblk, k);
     k_residual_precond<T><<<grid, RED_THREADS, 0, s>>>(X, HX, ld, N, rp, theta, thetap, D, eta, mode, R, ldr, partials);
-    KF_CUDA(cudaGetLastError());
+    KF_LAUNCH_CHECK();
     k_reduce_cols<<<(k + 127) / 128, 128, 0, s>>>(partials, nblk, k, norms2);
-    KF_CUDA(cudaGetLastError());
+    KF_LAUNCH_CHECK();
 }
 
 // theta_j = sum_i D_i X_ij^2 / sum_i X_ij^2 (ext/KronFreeCircuitsCUDAExt.jl:16-44): two
@@ -335,12 +350,12 @@ void diag_expectation(const double *D, const double *X, int64_t ld, int k, int64
     const int nblk = (int)((N + rp - 1) / rp);
     dim3 grid(nblk, k);
     k_diag_expect<<<grid, RED_THREADS, 0, s>>>(D, X, ld, N, rp, partials);
-    KF_CUDA(cudaGetLastError());
+    KF_LAUNCH_CHECK();
     // reduce 2k rows of partials in place into the head of `partials` region after them
     double *sums = partials + (size_t)2 * k * nblk;
     k_reduce_cols<<<(2 * k + 127) / 128, 128, 0, s>>>(partials, nblk, 2 * k, sums);
     k_expect_finish<<<(k + 127) / 128, 128, 0, s>>>(sums, k, theta);
-    KF_CUDA(cudaGetLastError());
+    KF_LAUNCH_CHECK();
 }
 
 // ---- elementwise ---------------------------------------------------------------------------
@@ -358,7 +373,7 @@ void scale_columns(T *X, int64_t ld, int k, int64_t N, const double *sc, cudaStr
     if (k <= 0) return;
     const int64_t tot = N * k;
     k_scale_cols<T><<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(X, ld, N, k, sc);
-    KF_CUDA(cudaGetLastError());
+    KF_LAUNCH_CHECK();
 }
 
 template <typename T>
@@ -376,7 +391,7 @@ void residual_block(const T *X, const T *HX, int64_t ld, int k, int64_t N, const
     if (k <= 0) return;
     const int64_t tot = N * k;
     k_residual_block<T><<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(X, HX, ld, N, k, theta, R, ldr);
-    KF_CUDA(cudaGetLastError());
+    KF_LAUNCH_CHECK();
 }
 
 // A counter-based normal generator: splitmix64 of (seed, stream, column, row) into two
@@ -405,7 +420,7 @@ void fill_normal(T *X, int64_t ld, int k, int64_t N, uint64_t seed, uint64_t sid
     if (k <= 0) return;
     const int64_t tot = N * k;
     k_fill_normal<T><<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(X, ld, N, k, seed, sid);
-    KF_CUDA(cudaGetLastError());
+    KF_LAUNCH_CHECK();
 }
 
 template <typename Ts, typename Td>
@@ -421,7 +436,7 @@ void convert(const Ts *X, int64_t ldx, Td *Y, int64_t ldy, int k, int64_t N, cud
     if (k <= 0) return;
     const int64_t tot = N * k;
     k_convert<Ts, Td><<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(X, ldx, Y, ldy, N, k);
-    KF_CUDA(cudaGetLastError());
+    KF_LAUNCH_CHECK();
 }
 
 template <typename T>

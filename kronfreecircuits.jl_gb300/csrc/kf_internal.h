@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <stdexcept>
@@ -31,41 +32,45 @@ void set_last_error(const std::string &msg);
                               std::string(#call) + ": " + cudaGetErrorString(e_));             \
     } while (0)
 
+// Every kernel launch of the library is followed by this: it counts the launch (kf_launch_count)
+// and turns a launch error into a kf::Error.
+extern std::atomic<uint64_t> g_launches;
+#define KF_LAUNCH_CHECK()                                                                      \
+    do {                                                                                       \
+        ::kf::g_launches.fetch_add(1, std::memory_order_relaxed);                              \
+        KF_CUDA(cudaGetLastError());                                                           \
+    } while (0)
+
 #define KF_REQUIRE(cond, code, msg)                                                            \
     do {                                                                                       \
         if (!(cond)) throw ::kf::Error((code), (msg));                                         \
     } while (0)
 
 constexpr int MAXDIMS = 8;     // axes of a state tensor
-constexpr int MAXF = 4;        // non-dense factors of one fused product term
 constexpr int MAXB = 24;       // bands of one banded factor (a periodic order-8 stencil has 16)
-constexpr int MAXT = 16;       // fused product terms of one operator
 constexpr int MAXE = 48;       // stencil entries (products of bands) over all fused terms
 
-// A banded factor in the form the fused kernel reads: per band an offset, and weights
-// w[i * nb + b] (row-major, the band index fastest), zero where i + off[b] leaves [0, n).
-struct BandFactorDev {
-    int axis;
-    int nb;
-    int off[MAXB];
-    int w_off;                 // offset of this factor's weights in the op's weight pool
+// The fused kernel's stencil entries.  Every term built only of diagonal, banded and shift
+// factors on at most two axes is a product of banded factors; the cartesian product of its
+// bands gives entries e with output  Y[p] += w_e(p) X[p + delta_e],  where
+// w_e(p) = W[w0_e + i_{a0}(p) nb0_e] (* W[w1_e + i_{a1}(p) nb1_e]) and the entry is skipped when
+// i_a + off_a leaves [0, n_a) on either axis.  The coefficient is folded into the weights.
+struct Entry {
+    int nf;            // 1 or 2 factors
+    int a0, o0, n0, nb0, w0;
+    int a1, o1, n1, nb1, w1;
+    int delta;         // sum of off * stride over the factors
 };
 
-// One fused product term: a product of banded factors on distinct axes, the coefficient
-// folded into the first factor's weights.
-struct FusedTerm {
-    int nf;
-    BandFactorDev f[MAXF];
-};
+constexpr int MAXDIMS_F = 6;   // axes the fused kernel decodes (more: the chain path)
 
 // Everything the fused apply kernel needs, passed by value as a kernel parameter.
 struct ApplyPlan {
     int ndims;
-    int64_t dims[MAXDIMS];
-    int64_t stride[MAXDIMS];
-    int64_t N;
-    int nterms;
-    FusedTerm t[MAXT];
+    int dims[MAXDIMS_F];
+    int N;
+    int ne;
+    Entry e[MAXE];
 };
 
 // A dense-containing term, applied as a chain of single-axis products through scratch.
@@ -92,6 +97,7 @@ struct kf_op {
     kf::ApplyPlan plan{};
     int64_t N = 0;
     std::vector<int64_t> dims;
+    std::vector<int64_t> strides;
     // fused diagonal on the device, FP64 and FP32
     double *d_diag64 = nullptr;
     float *d_diag32 = nullptr;

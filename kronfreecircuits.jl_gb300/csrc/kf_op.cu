@@ -28,84 +28,74 @@ namespace kf {
 // ------------------------------------------------------------------------------------------
 // kernels
 
-template <typename T, int CB>
+// The per-axis index of the state point p: idx[a] for a < ndims (static indexing only).
+__device__ __forceinline__ int pick(const int (&idx)[MAXDIMS_F], int a) {
+    int v = idx[0];
+#pragma unroll
+    for (int k = 1; k < MAXDIMS_F; ++k) v = (a == k) ? idx[k] : v;
+    return v;
+}
+
+// Y = D X + sum_entries w_e X[p + delta_e]  (then the epilogue Y = alpha Y + beta X + gamma Z).
+// One thread per state point p; the point's entry weights and offsets are evaluated once into
+// registers (ME >= ne, fully unrolled), then reused for every column of the block (the column
+// loop unrolled CB times), so each column's ne neighbour loads are independent and in flight
+// together.
+template <typename T, int CB, int ME>
 __global__ void __launch_bounds__(256) k_apply_fused(const ApplyPlan plan, const T *__restrict__ D,
                                                      const T *__restrict__ W, const T *__restrict__ X,
                                                      T *__restrict__ Y, int64_t ldx, int64_t ldy, int b,
                                                      T alpha, T beta, const T *__restrict__ Z, int64_t ldz,
                                                      T gamma, int epi) {
-    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= plan.N) return;
-    int idx[MAXDIMS];
+    int idx[MAXDIMS_F];
     {
-        int64_t rem = p;
+        int rem = p;
 #pragma unroll
-        for (int a = 0; a < MAXDIMS; ++a) {
+        for (int a = 0; a < MAXDIMS_F; ++a) {
             if (a < plan.ndims) {
-                idx[a] = (int)(rem % plan.dims[a]);
+                idx[a] = rem % plan.dims[a];
                 rem /= plan.dims[a];
+            } else {
+                idx[a] = 0;
             }
         }
     }
+    T w[ME];
+    int off[ME];
+#pragma unroll
+    for (int e = 0; e < ME; ++e) {
+        w[e] = T(0);
+        off[e] = 0;
+        if (e < plan.ne) {
+            const Entry &E = plan.e[e];
+            const int i0 = pick(idx, E.a0);
+            bool ok = (unsigned)(i0 + E.o0) < (unsigned)E.n0;
+            T wv = ok ? __ldg(W + E.w0 + i0 * E.nb0) : T(0);
+            if (E.nf == 2) {
+                const int i1 = pick(idx, E.a1);
+                const bool ok1 = (unsigned)(i1 + E.o1) < (unsigned)E.n1;
+                wv = ok1 ? wv * __ldg(W + E.w1 + i1 * E.nb1) : T(0);
+                ok = ok && ok1;
+            }
+            w[e] = ok ? wv : T(0);
+            off[e] = ok ? E.delta : 0;
+        }
+    }
     const T dv = D[p];
-    for (int c0 = 0; c0 < b; c0 += CB) {
-        T acc[CB];
-        const T *xb = X + (int64_t)c0 * ldx + p;
+#pragma unroll CB
+    for (int c = 0; c < b; ++c) {
+        const T *xc = X + (int64_t)c * ldx + p;
+        T v = dv * xc[0];
 #pragma unroll
-        for (int c = 0; c < CB; ++c) acc[c] = (c0 + c < b) ? dv * xb[(int64_t)c * ldx] : T(0);
-        for (int t = 0; t < plan.nterms; ++t) {
-            const FusedTerm &ft = plan.t[t];
-            if (ft.nf == 1) {
-                const BandFactorDev &f = ft.f[0];
-                const int a = f.axis;
-                const int i = idx[a];
-                const int n = (int)plan.dims[a];
-                const int64_t st = plan.stride[a];
-                const T *w = W + f.w_off + (int64_t)i * f.nb;
-                for (int bb = 0; bb < f.nb; ++bb) {
-                    const int o = f.off[bb];
-                    const int j = i + o;
-                    const T wv = w[bb];
-                    if (j < 0 || j >= n || wv == T(0)) continue;
-                    const T *xs = xb + (int64_t)o * st;
-#pragma unroll
-                    for (int c = 0; c < CB; ++c)
-                        if (c0 + c < b) acc[c] += wv * xs[(int64_t)c * ldx];
-                }
-            } else {  // nf == 2
-                const BandFactorDev &f1 = ft.f[0];
-                const BandFactorDev &f2 = ft.f[1];
-                const int i1 = idx[f1.axis], i2 = idx[f2.axis];
-                const int n1 = (int)plan.dims[f1.axis], n2 = (int)plan.dims[f2.axis];
-                const int64_t s1 = plan.stride[f1.axis], s2 = plan.stride[f2.axis];
-                const T *w1 = W + f1.w_off + (int64_t)i1 * f1.nb;
-                const T *w2 = W + f2.w_off + (int64_t)i2 * f2.nb;
-                for (int b1 = 0; b1 < f1.nb; ++b1) {
-                    const int j1 = i1 + f1.off[b1];
-                    const T wv1 = w1[b1];
-                    if (j1 < 0 || j1 >= n1 || wv1 == T(0)) continue;
-                    for (int b2 = 0; b2 < f2.nb; ++b2) {
-                        const int j2 = i2 + f2.off[b2];
-                        const T wv = wv1 * w2[b2];
-                        if (j2 < 0 || j2 >= n2 || wv == T(0)) continue;
-                        const T *xs = xb + (int64_t)f1.off[b1] * s1 + (int64_t)f2.off[b2] * s2;
-#pragma unroll
-                        for (int c = 0; c < CB; ++c)
-                            if (c0 + c < b) acc[c] += wv * xs[(int64_t)c * ldx];
-                    }
-                }
-            }
+        for (int e = 0; e < ME; ++e)
+            if (e < plan.ne) v += w[e] * ((w[e] != T(0)) ? xc[off[e]] : T(0));
+        if (epi) {
+            v = alpha * v + beta * xc[0];
+            if (Z != nullptr) v += gamma * Z[(int64_t)c * ldz + p];
         }
-#pragma unroll
-        for (int c = 0; c < CB; ++c) {
-            if (c0 + c >= b) break;
-            T v = acc[c];
-            if (epi) {
-                v = alpha * v + beta * xb[(int64_t)c * ldx];
-                if (Z != nullptr) v += gamma * Z[(int64_t)(c0 + c) * ldz + p];
-            }
-            Y[(int64_t)(c0 + c) * ldy + p] = v;
-        }
+        Y[(int64_t)c * ldy + p] = v;
     }
 }
 
@@ -185,13 +175,17 @@ static void apply_t(kf_op *op, const T *X, T *Y, int64_t ldx, int64_t ldy, int64
     const bool trivial_epi = alpha == 1.0 && beta == 0.0 && (Z == nullptr || gamma == 0.0);
     const int epi = (!chains && !trivial_epi) ? 1 : 0;
     const unsigned grid = (unsigned)((N + 255) / 256);
-    if (f32)
-        k_apply_fused<T, 16><<<grid, 256, 0, s>>>(op->plan, D, W, X, Y, ldx, ldy, (int)b, (T)alpha, (T)beta, Z, ldz,
-                                                  (T)gamma, epi);
-    else
-        k_apply_fused<T, 8><<<grid, 256, 0, s>>>(op->plan, D, W, X, Y, ldx, ldy, (int)b, (T)alpha, (T)beta, Z, ldz,
-                                                 (T)gamma, epi);
-    KF_CUDA(cudaGetLastError());
+    const int ne = op->plan.ne;
+#define KF_FUSED(CB, ME)                                                                                 \
+    k_apply_fused<T, CB, ME><<<grid, 256, 0, s>>>(op->plan, D, W, X, Y, ldx, ldy, (int)b, (T)alpha, (T)beta, \
+                                                  Z, ldz, (T)gamma, epi)
+    if (f32) {
+        if (ne <= 16) KF_FUSED(2, 16); else if (ne <= 32) KF_FUSED(2, 32); else KF_FUSED(1, 48);
+    } else {
+        if (ne <= 16) KF_FUSED(2, 16); else if (ne <= 32) KF_FUSED(1, 32); else KF_FUSED(1, 48);
+    }
+#undef KF_FUSED
+    KF_LAUNCH_CHECK();
     if (!chains) return;
     // dense-containing terms: chain through scratch, one contiguous (N x b) block per buffer
     const size_t need = (size_t)2 * N * b * sizeof(T);
@@ -217,7 +211,7 @@ static void apply_t(kf_op *op, const T *X, T *Y, int64_t ldx, int64_t ldy, int64
             const int64_t ldd = last ? ldy : N;
             const T a = last ? (T)ct.coeff : T(1);
             const int acc = last ? 1 : 0;
-            const int64_t stride = op->plan.stride[f.axis];
+            const int64_t stride = op->strides[f.axis];
             if (f.kind == KF_DENSE) {
                 const size_t sm = (size_t)f.n * f.n * sizeof(T) <= 48 * 1024 ? (size_t)f.n * f.n * sizeof(T) : 0;
                 k_axis_dense<T><<<g2, 256, sm, s>>>(dst, ldd, src, lds, cdata + f.data_off, f.n, stride, N, total, a,
@@ -225,14 +219,14 @@ static void apply_t(kf_op *op, const T *X, T *Y, int64_t ldx, int64_t ldy, int64
             } else {
                 k_axis_banded<T><<<g2, 256, 0, s>>>(dst, ldd, src, lds, cdata + f.data_off, f, stride, N, total, a, acc);
             }
-            KF_CUDA(cudaGetLastError());
+            KF_LAUNCH_CHECK();
             src = dst;
             lds = ldd;
         }
     }
     if (!trivial_epi) {
         k_axpby_cols<T><<<g2, 256, 0, s>>>(Y, ldy, X, ldx, Z, ldz, N, (int)b, (T)alpha, (T)beta, (T)gamma);
-        KF_CUDA(cudaGetLastError());
+        KF_LAUNCH_CHECK();
     }
 }
 
@@ -427,13 +421,15 @@ void build_op(const kf_op_desc *desc, kf_op *op) {
     ApplyPlan &P = op->plan;
     std::memset(&P, 0, sizeof(P));
     P.ndims = desc->ndims;
-    P.N = N;
+    P.N = (int)N;
     int64_t st = 1;
+    op->strides.assign(desc->ndims, 0);
     for (int a = 0; a < desc->ndims; ++a) {
-        P.dims[a] = op->dims[a];
-        P.stride[a] = st;
+        if (a < MAXDIMS_F) P.dims[a] = (int)op->dims[a];
+        op->strides[a] = st;
         st *= op->dims[a];
     }
+    const bool fusable_dims = desc->ndims <= MAXDIMS_F;
     // validate terms (src/apply.jl:226-231, src/apply.jl:160-163)
     for (int t = 0; t < desc->nterms; ++t) {
         const kf_term &T = desc->terms[t];
@@ -528,11 +524,15 @@ void build_op(const kf_op_desc *desc, kf_op *op) {
     }
     // merge single-axis and structurally equal fused terms
     merge_terms(fused);
-    // a fused term beyond the plan's capacity runs as a chain instead
-    int nterms = 0;
+    // fused terms become stencil entries (the cartesian product of their bands); a term that
+    // would overflow the entry table, or an operator with more axes than the fused kernel
+    // decodes, runs as a chain instead
+    int ne = 0;
     std::vector<double> pool;
     for (HTerm &h : fused) {
-        bool fits = nterms < MAXT && (int)h.f.size() >= 1 && (int)h.f.size() <= 2;
+        int cnt = 1;
+        for (auto &b : h.f) cnt *= std::max(b.nb(), 1);
+        bool fits = fusable_dims && (int)h.f.size() >= 1 && (int)h.f.size() <= 2 && ne + cnt <= MAXE;
         for (auto &b : h.f) fits = fits && b.nb() <= MAXB;
         if (!fits) {
             ChainTerm ct;
@@ -543,28 +543,43 @@ void build_op(const kf_op_desc *desc, kf_op *op) {
                 cf.n = b.n;
                 cf.kind = KF_BANDED;
                 cf.nb = b.nb();
-                for (int q = 0; q < cf.nb && q < MAXB; ++q) cf.off[q] = b.off[q];
                 KF_REQUIRE(cf.nb <= MAXB, KF_EINVAL, "KronFreeOperator: too many bands in one factor");
+                for (int q = 0; q < cf.nb; ++q) cf.off[q] = b.off[q];
                 chain_data.push_back(b.w);
                 ct.f.push_back(cf);
             }
             chains_h.push_back(ct);
             continue;
         }
-        FusedTerm &ft = P.t[nterms++];
-        ft.nf = (int)h.f.size();
-        for (int k = 0; k < ft.nf; ++k) {
-            HBand &b = h.f[k];
-            BandFactorDev &bf = ft.f[k];
-            bf.axis = b.axis;
-            bf.nb = b.nb();
-            for (int q = 0; q < bf.nb; ++q) bf.off[q] = b.off[q];
-            bf.w_off = (int)pool.size();
+        // weights of the term's factors in the pool, the coefficient folded into the first
+        std::vector<int> woff(h.f.size());
+        for (size_t k = 0; k < h.f.size(); ++k) {
+            woff[k] = (int)pool.size();
             const double c = (k == 0) ? h.coeff : 1.0;
-            for (double v : b.w) pool.push_back(c * v);
+            for (double v : h.f[k].w) pool.push_back(c * v);
+        }
+        const HBand &f0 = h.f[0];
+        for (int b0 = 0; b0 < f0.nb(); ++b0) {
+            if (h.f.size() == 1) {
+                Entry &E = P.e[ne++];
+                E = Entry{};
+                E.nf = 1;
+                E.a0 = f0.axis; E.o0 = f0.off[b0]; E.n0 = f0.n; E.nb0 = f0.nb(); E.w0 = woff[0] + b0;
+                E.delta = (int)(f0.off[b0] * op->strides[f0.axis]);
+                continue;
+            }
+            const HBand &f1 = h.f[1];
+            for (int b1 = 0; b1 < f1.nb(); ++b1) {
+                Entry &E = P.e[ne++];
+                E = Entry{};
+                E.nf = 2;
+                E.a0 = f0.axis; E.o0 = f0.off[b0]; E.n0 = f0.n; E.nb0 = f0.nb(); E.w0 = woff[0] + b0;
+                E.a1 = f1.axis; E.o1 = f1.off[b1]; E.n1 = f1.n; E.nb1 = f1.nb(); E.w1 = woff[1] + b1;
+                E.delta = (int)(f0.off[b0] * op->strides[f0.axis] + f1.off[b1] * op->strides[f1.axis]);
+            }
         }
     }
-    P.nterms = nterms;
+    P.ne = ne;
     // lay out chain data
     std::vector<double> cpool;
     {

@@ -262,11 +262,13 @@ static LobOut lobpcg_run(kf_op *op, LobWork<T> &Wk, const double *D, const LobPa
             break;
         }
         if (prm.stall_exit) {
-            if (worst < 0.7 * best) {
+            // FP32 has reached its floor when the largest active residual has not fallen by 10%
+            // over 40 iterations (LOBPCG's residuals stall for stretches before a column locks).
+            if (worst < 0.9 * best) {
                 best = worst;
                 since_best = 0;
-            } else if (++since_best >= 6) {
-                break;                                   // FP32 has reached its floor
+            } else if (++since_best >= 40) {
+                break;
             }
         }
         if (it >= prm.maxiter) break;

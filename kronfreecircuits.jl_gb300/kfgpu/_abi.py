@@ -90,6 +90,7 @@ def lib():
     P = C.c_void_p
     sig = {
         "kf_version": (C.c_int, []),
+        "kf_launch_count": (C.c_int, [C.POINTER(C.c_uint64)]),
         "kf_last_error": (C.c_int, [C.c_char_p, C.c_size_t]),
         "kf_op_create": (C.c_int, [C.POINTER(KfOpDesc), C.POINTER(P)]),
         "kf_op_destroy": (C.c_int, [P]),
@@ -122,6 +123,13 @@ def lib():
         fn.argtypes = args
     _lib = L
     return L
+
+
+def launch_count():
+    """Kernels libkfgpu has launched in this process."""
+    v = C.c_uint64()
+    lib().kf_launch_count(C.byref(v))
+    return v.value
 
 
 def last_error():

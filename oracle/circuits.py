@@ -73,6 +73,27 @@ def fluxonium_operator(theta, npts):
     return kfref.KronFreeOperator([npts], _merge(terms))
 
 
+def _same_op(a, b):
+    if type(a) is not type(b) or a.n != b.n:
+        return False
+    if isinstance(a, kfref.ShiftOp):
+        return a.s == b.s and a.factor == b.factor
+    if isinstance(a, kfref.BandedOp):
+        return a.offsets == b.offsets and all(np.array_equal(x, y) for x, y in zip(a.weights, b.weights))
+    if isinstance(a, kfref.DiagonalOp):
+        return np.array_equal(a.d, b.d)
+    return np.array_equal(a.M, b.M)
+
+
 def _merge(terms):
-    """Sum real terms with identical factor objects (the reference merges equal keys, src/materialize.jl:616-647)."""
-    return terms
+    """Sum real terms on equal factors, as the reference's `_real_node_terms` sums equal keys
+    (src/materialize.jl:616-647); terms whose coefficients cancel are dropped."""
+    out = []
+    for c, fs in terms:
+        for k, (c2, fs2) in enumerate(out):
+            if len(fs) == len(fs2) and all(a == a2 and _same_op(o, o2) for (a, o), (a2, o2) in zip(fs, fs2)):
+                out[k] = (c2 + c, fs2)
+                break
+        else:
+            out.append((c, fs))
+    return [(c, fs) for c, fs in out if c != 0]
