@@ -130,6 +130,9 @@ int kf_op_sync(kf_op *op);
 #define KF_PRECOND_RITZ    0
 #define KF_PRECOND_JACOBI  1
 #define KF_PRECOND_NONE    2
+#define KF_PRECOND_SEPARABLE 3   /* U diag(1/hypot(S - theta_j, eta_s)) U' from the per-axis
+                                    eigenbases of the single-axis terms (separable_eigenbases,
+                                    src/apply.jl:606-642); eta_s = max(eta, 1e-3 ||H||)  */
 
 #define KF_ORTHO_SVQB    0
 #define KF_ORTHO_CHOLQR  1

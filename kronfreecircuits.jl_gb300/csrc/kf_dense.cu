@@ -1,0 +1,152 @@
+// Mode-k products with a dense d x d matrix, Y[l, i, r] = alpha sum_j A[i, j] X[l, j, r] (+ beta Y),
+// for blocks of columns (the column index folds into r), as one shared-memory-tiled GEMM:
+//   rows m = (l, r) (l fastest, left = stride of axis k), columns i, reduction over j.
+// Reference: the dense factor application of src/apply.jl:37-53 and 301-340 (which permutes a
+// middle axis to the front through scratch; here the strided rows are gathered by the tile
+// loader instead, so no permute passes).
+//
+// Tile: 64 rows x 64 columns x 16 reduction per step, 256 threads, a 4 x 4 register tile per
+// thread.  The X tile loader walks l fastest when the axis stride is > 1 (coalesced along l) and
+// j fastest when the axis is the leading one (coalesced along j).
+#include "kf_internal.h"
+
+namespace kf {
+
+constexpr int DM = 64, DN = 64, DK = 16;
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_mode_product(T *__restrict__ Y, int64_t ldy, const T *__restrict__ X,
+                                                      int64_t ldx, const T *__restrict__ A, int d, int64_t left,
+                                                      int64_t rows_per_col, int64_t M, int64_t N, T alpha, T beta) {
+    __shared__ T Xs[DK][DM + 1];
+    __shared__ T As[DK][DN + 1];
+    const int tid = threadIdx.x;
+    const int64_t m0 = (int64_t)blockIdx.x * DM;
+    const int i0 = blockIdx.y * DN;
+    const int tr = (tid % 16) * 4, tc = (tid / 16) * 4;
+    T acc[4][4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) acc[u][v] = T(0);
+    // base offset of row m: column c = m / rows_per_col of the block, within it (l, r) with
+    // l = q % left, r = q / left, element (l, j, r) at l + left * (j + d * r)
+    for (int j0 = 0; j0 < d; j0 += DK) {
+        if (left == 1) {
+            // j fastest: X[j + d * q] per column
+            for (int e = tid; e < DM * DK; e += 256) {
+                const int jj = e % DK, mm = e / DK;
+                const int64_t m = m0 + mm;
+                const int j = j0 + jj;
+                T v = T(0);
+                if (m < M && j < d) {
+                    const int64_t c = m / rows_per_col, q = m % rows_per_col;
+                    v = X[c * ldx + (int64_t)j + (int64_t)d * q];
+                }
+                Xs[jj][mm] = v;
+            }
+        } else {
+            for (int e = tid; e < DM * DK; e += 256) {
+                const int mm = e % DM, jj = e / DM;
+                const int64_t m = m0 + mm;
+                const int j = j0 + jj;
+                T v = T(0);
+                if (m < M && j < d) {
+                    const int64_t c = m / rows_per_col, q = m % rows_per_col;
+                    const int64_t l = q % left, r = q / left;
+                    v = X[c * ldx + l + left * ((int64_t)j + (int64_t)d * r)];
+                }
+                Xs[jj][mm] = v;
+            }
+        }
+        // A tile: As[jj][ii] = A[i, j] (A column-major, A[i + d * j])
+        for (int e = tid; e < DN * DK; e += 256) {
+            const int ii = e % DN, jj = e / DN;
+            const int i = i0 + ii, j = j0 + jj;
+            As[jj][ii] = (i < d && j < d) ? A[(int64_t)i + (int64_t)d * j] : T(0);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int jj = 0; jj < DK; ++jj) {
+            T a[4], x[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) x[u] = Xs[jj][tr + u];
+#pragma unroll
+            for (int v = 0; v < 4; ++v) a[v] = As[jj][tc + v];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int v = 0; v < 4; ++v) acc[u][v] += x[u] * a[v];
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        const int64_t m = m0 + tr + u;
+        if (m >= M) continue;
+        const int64_t c = m / rows_per_col, q = m % rows_per_col;
+        const int64_t l = q % left, r = q / left;
+        T *yrow = Y + c * ldy + l + left * ((int64_t)d * r);
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            const int i = i0 + tc + v;
+            if (i >= d) continue;
+            T *yp = yrow + left * (int64_t)i;
+            *yp = (beta == T(0)) ? alpha * acc[u][v] : alpha * acc[u][v] + beta * *yp;
+        }
+    }
+}
+
+// Y = alpha (A along `axis` of X) + beta Y for a block of b columns of length N, the axis of
+// length d with stride `left`.  A is d x d column-major on the device.
+template <typename T>
+void mode_product(T *Y, int64_t ldy, const T *X, int64_t ldx, const T *A, int d, int64_t left, int64_t N, int64_t b,
+                  double alpha, double beta, cudaStream_t s) {
+    if (b <= 0 || N <= 0) return;
+    const int64_t rows_per_col = N / d;          // (l, r) pairs per column
+    const int64_t M = rows_per_col * b;
+    dim3 grid((unsigned)((M + DM - 1) / DM), (unsigned)((d + DN - 1) / DN));
+    k_mode_product<T><<<grid, 256, 0, s>>>(Y, ldy, X, ldx, A, d, left, rows_per_col, M, N, (T)alpha, (T)beta);
+    KF_LAUNCH_CHECK();
+}
+
+template void mode_product<float>(float *, int64_t, const float *, int64_t, const float *, int, int64_t, int64_t,
+                                  int64_t, double, double, cudaStream_t);
+template void mode_product<double>(double *, int64_t, const double *, int64_t, const double *, int, int64_t, int64_t,
+                                   int64_t, double, double, cudaStream_t);
+
+// W[:, j] <- W[:, j] / hypot(S(p) - theta_j, eta) with S(p) = sum_a lam_a[i_a(p)] (the separable
+// spectrum evaluated from per-axis eigenvalues, no N-sized table).
+template <typename T>
+__global__ void k_sep_scale(T *__restrict__ W, int64_t ld, int64_t N, int k, int ndims, const int *__restrict__ dims,
+                            const double *__restrict__ lam, const int *__restrict__ lam_off,
+                            const double *__restrict__ theta, double eta) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= N * k) return;
+    const int64_t c = t / N, p = t % N;
+    int64_t rem = p;
+    double S = 0;
+    for (int a = 0; a < ndims; ++a) {
+        const int i = (int)(rem % dims[a]);
+        rem /= dims[a];
+        S += lam[lam_off[a] + i];
+    }
+    const double f = 1.0 / hypot(S - theta[c], eta);
+    W[c * ld + p] = (T)((double)W[c * ld + p] * f);
+}
+
+template <typename T>
+void sep_scale(T *W, int64_t ld, int64_t N, int k, int ndims, const int *dims, const double *lam, const int *lam_off,
+               const double *theta, double eta, cudaStream_t s) {
+    if (k <= 0) return;
+    const int64_t tot = N * k;
+    k_sep_scale<T><<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(W, ld, N, k, ndims, dims, lam, lam_off, theta, eta);
+    KF_LAUNCH_CHECK();
+}
+
+template void sep_scale<float>(float *, int64_t, int64_t, int, int, const int *, const double *, const int *,
+                               const double *, double, cudaStream_t);
+template void sep_scale<double>(double *, int64_t, int64_t, int, int, const int *, const double *, const int *,
+                                const double *, double, cudaStream_t);
+
+}  // namespace kf

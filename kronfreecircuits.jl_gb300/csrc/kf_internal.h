@@ -120,6 +120,17 @@ struct kf_op {
     struct HostFactor { int axis; int kind; int64_t n; std::vector<double> data; std::vector<int64_t> offs; int64_t shift; double factor; };
     struct HostTerm { double coeff; std::vector<HostFactor> f; };
     std::vector<HostTerm> kept;
+    // separable part for the preconditioner: per axis the sum of the single-axis terms
+    // (src/apply.jl:606-642), its eigendecomposition made on first use
+    struct Separable {
+        std::vector<std::vector<double>> M;   // host d_a x d_a sums (column-major)
+        bool ready = false;
+        std::vector<int> ident;               // axis whose sum is diagonal (U = I)
+        std::vector<double> lam;              // concatenated per-axis eigenvalues
+        std::vector<float *> dU, dUt;         // FP32 U and U' per axis (nullptr when ident)
+        double *d_lam = nullptr;
+        int *d_lam_off = nullptr, *d_dims = nullptr;
+    } sep;
 };
 
 namespace kf {
@@ -156,6 +167,18 @@ void residual_block(const T *X, const T *HX, int64_t ld, int k, int64_t N, const
                     int64_t ldr, cudaStream_t s);    // R = HX - X diag(theta)
 void diag_expectation(const double *D, const double *X, int64_t ld, int k, int64_t N, double *theta_dev,
                       double *partials, cudaStream_t s);
+
+// dense mode products and the separable preconditioner (kf_dense.cu, kf_precond.cu)
+template <typename T>
+void mode_product(T *Y, int64_t ldy, const T *X, int64_t ldx, const T *A, int d, int64_t left, int64_t N, int64_t b,
+                  double alpha, double beta, cudaStream_t s);
+template <typename T>
+void sep_scale(T *W, int64_t ld, int64_t N, int k, int ndims, const int *dims, const double *lam, const int *lam_off,
+               const double *theta, double eta, cudaStream_t s);
+void sep_prepare(kf_op *op);
+// W (N x k, FP32, leading dimension N) <- U diag(1 / hypot(S - theta_j, eta)) U' W; s1 is an
+// N x k FP32 scratch.  Returns the block holding the result (W or s1).
+float *sep_apply(kf_op *op, float *W, float *s1, int k, const double *theta_dev, double eta, cudaStream_t s);
 
 // small dense FP64 routines on the host (kf_small.cpp); column-major.
 int sym_eig(int n, const double *A, int lda, double *w, double *V, int ldv);   // ascending

@@ -42,7 +42,7 @@ __device__ __forceinline__ int pick(const int (&idx)[MAXDIMS_F], int a) {
 // loop unrolled CB times), so each column's ne neighbour loads are independent and in flight
 // together.
 template <typename T, int CB, int ME>
-__global__ void __launch_bounds__(256) k_apply_fused(const ApplyPlan plan, const T *__restrict__ D,
+__global__ void __launch_bounds__(256, 2) k_apply_fused(const ApplyPlan plan, const T *__restrict__ D,
                                                      const T *__restrict__ W, const T *__restrict__ X,
                                                      T *__restrict__ Y, int64_t ldx, int64_t ldy, int b,
                                                      T alpha, T beta, const T *__restrict__ Z, int64_t ldz,
@@ -88,9 +88,11 @@ __global__ void __launch_bounds__(256) k_apply_fused(const ApplyPlan plan, const
     for (int c = 0; c < b; ++c) {
         const T *xc = X + (int64_t)c * ldx + p;
         T v = dv * xc[0];
+        // unconditional loads (an invalid entry has weight 0 and offset 0, a valid address), so
+        // all ne loads of the column issue back to back
 #pragma unroll
         for (int e = 0; e < ME; ++e)
-            if (e < plan.ne) v += w[e] * ((w[e] != T(0)) ? xc[off[e]] : T(0));
+            if (e < plan.ne) v += w[e] * __ldg(xc + off[e]);
         if (epi) {
             v = alpha * v + beta * xc[0];
             if (Z != nullptr) v += gamma * Z[(int64_t)c * ldz + p];
@@ -180,9 +182,9 @@ static void apply_t(kf_op *op, const T *X, T *Y, int64_t ldx, int64_t ldy, int64
     k_apply_fused<T, CB, ME><<<grid, 256, 0, s>>>(op->plan, D, W, X, Y, ldx, ldy, (int)b, (T)alpha, (T)beta, \
                                                   Z, ldz, (T)gamma, epi)
     if (f32) {
-        if (ne <= 16) KF_FUSED(2, 16); else if (ne <= 32) KF_FUSED(2, 32); else KF_FUSED(1, 48);
+        if (ne <= 16) KF_FUSED(1, 16); else if (ne <= 32) KF_FUSED(1, 32); else KF_FUSED(1, 48);
     } else {
-        if (ne <= 16) KF_FUSED(2, 16); else if (ne <= 32) KF_FUSED(1, 32); else KF_FUSED(1, 48);
+        if (ne <= 16) KF_FUSED(1, 16); else if (ne <= 32) KF_FUSED(1, 32); else KF_FUSED(1, 48);
     }
 #undef KF_FUSED
     KF_LAUNCH_CHECK();
@@ -457,6 +459,45 @@ void build_op(const kf_op_desc *desc, kf_op *op) {
         }
         KF_REQUIRE(std::isfinite(T.coeff), KF_EINVAL, "KronFreeOperator: a coefficient is not finite");
     }
+    // per-axis sums of the single-axis terms, for the separable preconditioner (the matrices of
+    // src/apply.jl:606-622: kept and fused single-factor terms, the constant on axis 1)
+    {
+        size_t tot = 0;
+        for (int64_t d : op->dims) tot += (size_t)d * d;
+        op->sep.M.clear();
+        if (tot <= ((size_t)1 << 26)) {
+            op->sep.M.resize(desc->ndims);
+            for (int a = 0; a < desc->ndims; ++a) op->sep.M[a].assign((size_t)op->dims[a] * op->dims[a], 0.0);
+            const int64_t d0 = op->dims[0];
+            for (int64_t i = 0; i < d0; ++i) op->sep.M[0][i + d0 * i] += desc->constant;
+            for (int t = 0; t < desc->nterms; ++t) {
+                const kf_term &T = desc->terms[t];
+                if (T.nfactors == 0) {
+                    for (int64_t i = 0; i < d0; ++i) op->sep.M[0][i + d0 * i] += T.coeff;
+                    continue;
+                }
+                if (T.nfactors != 1) continue;
+                const kf_factor &f = T.factors[0];
+                std::vector<double> &M = op->sep.M[f.axis];
+                const int64_t n = f.n;
+                const double c = T.coeff;
+                if (f.kind == KF_DIAG) {
+                    for (int64_t i = 0; i < n; ++i) M[i + n * i] += c * f.data[i];
+                } else if (f.kind == KF_SHIFT) {
+                    for (int64_t i = 0; i < n; ++i)
+                        if (i + f.shift >= 0 && i + f.shift < n) M[(i + f.shift) + n * i] += c * f.factor;
+                } else if (f.kind == KF_BANDED) {
+                    for (int bb = 0; bb < f.nbands; ++bb)
+                        for (int64_t i = 0; i < n; ++i) {
+                            const int64_t j = i + f.offsets[bb];
+                            if (j >= 0 && j < n) M[i + n * j] += c * f.data[(size_t)bb * n + i];
+                        }
+                } else {
+                    for (int64_t k = 0; k < n * n; ++k) M[k] += c * f.data[k];
+                }
+            }
+        }
+    }
     // fused diagonal (src/apply.jl:234-241, 438-447)
     std::vector<double> D(N, desc->constant);
     if (desc->diag) for (int64_t p = 0; p < N; ++p) D[p] += desc->diag[p];
@@ -634,6 +675,11 @@ void free_op(kf_op *op) {
     cudaFree(op->d_chain64);
     cudaFree(op->d_chain32);
     cudaFree(op->d_scratch);
+    for (float *p : op->sep.dU) cudaFree(p);
+    for (float *p : op->sep.dUt) cudaFree(p);
+    cudaFree(op->sep.d_lam);
+    cudaFree(op->sep.d_lam_off);
+    cudaFree(op->sep.d_dims);
     if (op->own_stream && op->stream) cudaStreamDestroy(op->stream);
 }
 

@@ -121,13 +121,14 @@ template <typename T>
 struct LobWork {
     int64_t N;
     int w;
-    DevMem X, HX, Xn, HXn, Z, HZ, Zt, Pn, dG, dC, dpart, dth, dthp, dnorm, dD;
+    DevMem X, HX, Xn, HXn, Z, HZ, Zt, Pn, F1, F2, dG, dC, dpart, dth, dthp, dnorm, dD;
     HostMem hG, hC, hv;
     LobWork(int64_t N_, int w_)
         : N(N_), w(w_),
           X((size_t)N_ * w_ * sizeof(T)), HX((size_t)N_ * w_ * sizeof(T)), Xn((size_t)N_ * w_ * sizeof(T)),
           HXn((size_t)N_ * w_ * sizeof(T)), Z((size_t)N_ * 2 * w_ * sizeof(T)), HZ((size_t)N_ * 2 * w_ * sizeof(T)),
           Zt((size_t)N_ * 2 * w_ * sizeof(T)), Pn((size_t)N_ * w_ * sizeof(T)),
+          F1((size_t)N_ * w_ * sizeof(float)), F2((size_t)N_ * w_ * sizeof(float)),
           dG((size_t)9 * w_ * w_ * sizeof(double)), dC((size_t)9 * w_ * w_ * sizeof(double)),
           dpart(gram_partials_size(3 * w_, 3 * w_, N_)), dth(w_ * sizeof(double)), dthp(w_ * sizeof(double)),
           dnorm(2 * w_ * sizeof(double)), dD(0),
@@ -236,7 +237,7 @@ static LobOut lobpcg_run(kf_op *op, LobWork<T> &Wk, const double *D, const LobPa
             double sig = dmin - 1.0;
             h2d(dthp, &sig, 1, s);
         }
-        const int mode = prm.precond == KF_PRECOND_RITZ ? 0 : prm.precond == KF_PRECOND_JACOBI ? 1 : 2;
+        const int mode = prm.precond == KF_PRECOND_RITZ ? 0 : prm.precond == KF_PRECOND_JACOBI ? 1 : 2;  // separable: 2, then below
         residual_precond<T>(X + (int64_t)nl * N, HX + (int64_t)nl * N, N, na, N, dth, dthp, D, prm.eta, mode, Z, N,
                             dnorm, part, s);
         d2h_sync<T>(hv + w, dnorm, na, s);
@@ -275,6 +276,21 @@ static LobOut lobpcg_run(kf_op *op, LobWork<T> &Wk, const double *D, const LobPa
         // W = Z[:, newly : na] (na2 columns), P = previous Pn[:, newly : na] placed right after it
         const int na2 = na - newly;
         T *Wb = Z + (int64_t)newly * N;
+        if (prm.precond == KF_PRECOND_SEPARABLE && na2 > 0) {
+            // the separable preconditioner always runs in FP32: it only steers the search
+            // directions, the FP64 orthogonalisation and Rayleigh-Ritz keep the accuracy
+            const double eta_s = std::max(prm.eta, 1e-3 * std::fabs(op->gershgorin));
+            float *f1 = Wk.F1.template as<float>(), *f2 = Wk.F2.template as<float>();
+            float *in = f2;
+            if constexpr (sizeof(T) == 4) in = (float *)Wb;
+            else convert<double, float>((const double *)Wb, N, f2, N, na2, N, s);
+            float *outp = sep_apply(op, in, f1, na2, dth + newly, eta_s, s);
+            if constexpr (sizeof(T) == 4) {
+                if (outp != (float *)Wb) copy_block<float>(outp, N, (float *)Wb, N, na2, N, s);
+            } else {
+                convert<float, double>(outp, N, (double *)Wb, N, na2, N, s);
+            }
+        }
         int nz = na2;
         if (np > 0) {
             const int np2 = np - newly;
@@ -431,6 +447,9 @@ static void solve_lobpcg(kf_op *op, const kf_solver_opts &o, int m, const double
     KF_REQUIRE(o.tol > 0 && std::isfinite(o.tol), KF_EINVAL, "LOBPCG: tol must be positive and finite");
     KF_REQUIRE(o.maxiter >= 1, KF_EINVAL, "LOBPCG: maxiter must be at least 1");
     KF_REQUIRE(o.eta > 0 && std::isfinite(o.eta), KF_EINVAL, "eta must be positive and finite");
+    KF_REQUIRE(o.preconditioner >= KF_PRECOND_RITZ && o.preconditioner <= KF_PRECOND_SEPARABLE, KF_EINVAL,
+               "LOBPCG: preconditioner must be :ritz, :jacobi, :none or :separable");
+    KF_REQUIRE(o.precision == KF_PREC_F64 || o.precision == KF_PREC_MIXED, KF_EINVAL, "LOBPCG: unknown precision mode");
     KF_REQUIRE(o.guard >= 0, KF_EINVAL, "LOBPCG: guard must be nonnegative");
     if (X0) {
         for (int j = 0; j < m; ++j) {

@@ -18,7 +18,7 @@ KF_DEVICE = 0x0
 KF_DIAG, KF_BANDED, KF_SHIFT, KF_DENSE = range(4)
 KF_SOLVER_LOBPCG, KF_SOLVER_CHEBYSHEV, KF_SOLVER_LANCZOS = range(3)
 KF_PREC_F64, KF_PREC_MIXED = 0, 1
-KF_PRECOND_RITZ, KF_PRECOND_JACOBI, KF_PRECOND_NONE = range(3)
+KF_PRECOND_RITZ, KF_PRECOND_JACOBI, KF_PRECOND_NONE, KF_PRECOND_SEPARABLE = range(4)
 KF_ORTHO_SVQB, KF_ORTHO_CHOLQR = 0, 1
 
 

@@ -32,8 +32,8 @@ class LOBPCG:
                  precision="f64", mixed_switch=2e-6, fallback_iters=3, fallback_resid=0.0, rng_seed=0x4B46):
         _arg(tol > 0 and math.isfinite(tol), f"LOBPCG: tol must be positive and finite, got {tol}")
         _arg(maxiter >= 1, f"LOBPCG: maxiter must be at least 1, got {maxiter}")
-        _arg(preconditioner in ("ritz", "jacobi", "none"),
-             f"LOBPCG: preconditioner must be :ritz, :jacobi or :none, got :{preconditioner}")
+        _arg(preconditioner in ("ritz", "jacobi", "none", "separable"),
+             f"LOBPCG: preconditioner must be :ritz, :jacobi, :none or :separable, got :{preconditioner}")
         _arg(eta > 0 and math.isfinite(eta), f"LOBPCG: eta must be positive and finite, got {eta}")
         _arg(guard >= 0, f"LOBPCG: guard must be nonnegative, got {guard}")
         _arg(seed in ("product", "random"), f"LOBPCG: seed must be :product or :random, got {seed!r}")
@@ -47,7 +47,7 @@ class LOBPCG:
         o = _abi.KfSolverOpts()
         lib().kf_solver_opts_default(C.byref(o), _abi.KF_SOLVER_LOBPCG)
         o.precision, o.tol, o.maxiter = _PREC[self.precision], self.tol, self.maxiter
-        o.preconditioner = {"ritz": 0, "jacobi": 1, "none": 2}[self.preconditioner]
+        o.preconditioner = {"ritz": 0, "jacobi": 1, "none": 2, "separable": 3}[self.preconditioner]
         o.eta, o.guard, o.mixed_switch = self.eta, self.guard, self.mixed_switch
         o.fallback_iters, o.fallback_resid, o.rng_seed = self.fallback_iters, self.fallback_resid, self.rng_seed
         return o

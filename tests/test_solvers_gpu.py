@@ -49,8 +49,30 @@ def test_chebyshev_matches_dense(cuda, small_leaf, precision):
     from kfgpu import ChebyshevFilter, solve
     H, Ho, Eref = small_leaf
     tol = 1e-8 * H.gershgorin_bound()
-    E, V, st = solve(ChebyshevFilter(tol=tol, degree=20, extra=4, precision=precision), H, 12)
+    E, V, st = solve(ChebyshevFilter(tol=tol, degree=20, extra=8, precision=precision), H, 12)
     _check_pairs(Ho, E, V, Eref[:12], tol * 1.0001)
+
+
+def test_chebyshev_weak_filter_raises_like_the_oracle(cuda, small_leaf):
+    """degree 20 with extra 4 is a weak filter on this leaf: the oracle runs out of maxiter = 50
+    (14 of 15 locked), and so must the GPU solver, with the reference's maxiter error."""
+    from kfgpu import ChebyshevFilter, ConvergenceError, solve
+    H, Ho, Eref = small_leaf
+    with pytest.raises(ConvergenceError, match="within maxiter = 50"):
+        solve(ChebyshevFilter(tol=1e-8 * H.gershgorin_bound(), degree=20, extra=4), H, 12)
+
+
+@pytest.mark.parametrize("precision", ["f64", "mixed"])
+def test_lobpcg_separable_preconditioner(cuda, small_leaf, precision):
+    """The separable preconditioner (per-axis eigenbases of the single-axis terms) converges to
+    the same pairs in fewer iterations than the per-Ritz Jacobi default."""
+    from kfgpu import LOBPCG, solve
+    H, Ho, Eref = small_leaf
+    tol = 1e-8 * H.gershgorin_bound()
+    E, V, st = solve(LOBPCG(tol=tol, precision=precision, preconditioner="separable"), H, 12)
+    _check_pairs(Ho, E, V, Eref[:12], tol)
+    E2, V2, st2 = solve(LOBPCG(tol=tol, precision=precision), H, 12)
+    assert st["iterations"] < st2["iterations"]
 
 
 def test_chebyshev_defaults_and_cholqr(cuda, small_leaf):
