@@ -234,6 +234,24 @@ def run_ours(args):
     return line
 
 
+def profile_one(args):
+    """One mixed-precision solve (the timed step's work) for a profiler's launch list."""
+    import torch
+    from kfgpu import KronFreeOperator, LOBPCG, circuits, solve
+    from kfgpu._abi import launch_count
+    ths = thetas()
+    dims, terms = circuits.three_mode_leaf(ths[args.warmup])
+    H = KronFreeOperator(dims, terms)
+    seedb = H.product_seed(M_PAIRS + 4)
+    n0 = launch_count()
+    t0 = time.perf_counter()
+    E, V, st = solve(LOBPCG(tol=1e-8 * H.gershgorin_bound(), precision="mixed", preconditioner="separable"), H,
+                     M_PAIRS, seed_block=seedb)
+    torch.cuda.synchronize()
+    return {"seconds": time.perf_counter() - t0, "launches": launch_count() - n0, "iterations": st["iterations"],
+            "iterations_f64": st["iterations_f64"], "seconds_f64": st["seconds_f64"]}
+
+
 def cpu_baseline(theta, bounded=True, iters=None):
     """The oracle's restatement of the reference CPU path on the host cores: a bounded sample of
     LOBPCG iterations of the same solve (C/OpenMP mul! + NumPy LOBPCG), extrapolated to the
@@ -299,7 +317,12 @@ def main():
     ap.add_argument("--ref-iters", type=int, default=570,
                     help="LOBPCG iterations the FP64 solve of this workload takes (for the reference arm's extrapolation)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="one mixed-precision solve of the first timed draw, no warm-up (for the ncu launch list)")
     args = ap.parse_args()
+    if args.profile:
+        print(json.dumps(profile_one(args)), flush=True)
+        return
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

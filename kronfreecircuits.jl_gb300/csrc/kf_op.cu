@@ -37,10 +37,9 @@ __device__ __forceinline__ int pick(const int (&idx)[MAXDIMS_F], int a) {
 }
 
 // Y = D X + sum_entries w_e X[p + delta_e]  (then the epilogue Y = alpha Y + beta X + gamma Z).
-// One thread per state point p; the point's entry weights and offsets are evaluated once into
-// registers (ME >= ne, fully unrolled), then reused for every column of the block (the column
-// loop unrolled CB times), so each column's ne neighbour loads are independent and in flight
-// together.
+// One thread per state point p and group of CB columns (blockIdx.y); the point's entry weights
+// and offsets are evaluated into registers (ME >= ne, fully unrolled) and used for its columns,
+// whose ne neighbour loads are independent and in flight together.
 template <typename T, int CB, int ME>
 __global__ void __launch_bounds__(256, 2) k_apply_fused(const ApplyPlan plan, const T *__restrict__ D,
                                                      const T *__restrict__ W, const T *__restrict__ X,
@@ -84,8 +83,11 @@ __global__ void __launch_bounds__(256, 2) k_apply_fused(const ApplyPlan plan, co
         }
     }
     const T dv = D[p];
-#pragma unroll CB
-    for (int c = 0; c < b; ++c) {
+    // this thread's columns: [blockIdx.y * CB, blockIdx.y * CB + CB)
+#pragma unroll
+    for (int cc = 0; cc < CB; ++cc) {
+        const int c = blockIdx.y * CB + cc;
+        if (c >= b) break;
         const T *xc = X + (int64_t)c * ldx + p;
         T v = dv * xc[0];
         // unconditional loads (an invalid entry has weight 0 and offset 0, a valid address), so
@@ -176,10 +178,10 @@ static void apply_t(kf_op *op, const T *X, T *Y, int64_t ldx, int64_t ldy, int64
     const bool chains = !op->chains.empty();
     const bool trivial_epi = alpha == 1.0 && beta == 0.0 && (Z == nullptr || gamma == 0.0);
     const int epi = (!chains && !trivial_epi) ? 1 : 0;
-    const unsigned grid = (unsigned)((N + 255) / 256);
     const int ne = op->plan.ne;
 #define KF_FUSED(CB, ME)                                                                                 \
-    k_apply_fused<T, CB, ME><<<grid, 256, 0, s>>>(op->plan, D, W, X, Y, ldx, ldy, (int)b, (T)alpha, (T)beta, \
+    k_apply_fused<T, CB, ME><<<dim3((unsigned)((N + 255) / 256), (unsigned)((b + CB - 1) / CB)), 256, 0, s>>>(   \
+        op->plan, D, W, X, Y, ldx, ldy, (int)b, (T)alpha, (T)beta,                                               \
                                                   Z, ldz, (T)gamma, epi)
     if (f32) {
         if (ne <= 16) KF_FUSED(1, 16); else if (ne <= 32) KF_FUSED(1, 32); else KF_FUSED(1, 48);
@@ -235,6 +237,7 @@ static void apply_t(kf_op *op, const T *X, T *Y, int64_t ldx, int64_t ldy, int64
 void launch_apply(kf_op *op, bool f32, const void *X, void *Y, int64_t ldx, int64_t ldy, int64_t b, double alpha,
                   double beta, const void *Z, int64_t ldz, double gamma, cudaStream_t s) {
     if (b <= 0 || op->N == 0) return;
+    KF_REQUIRE(b <= 65535, KF_EINVAL, "mul!: at most 65535 columns per call");
     if (f32)
         apply_t<float>(op, (const float *)X, (float *)Y, ldx, ldy, b, alpha, beta, (const float *)Z, ldz, gamma, s);
     else

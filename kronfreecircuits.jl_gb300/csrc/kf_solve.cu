@@ -769,8 +769,13 @@ static void solve_chebyshev(kf_op *op, const kf_solver_opts &o, int m, const dou
     std::vector<double> res(nb, INFINITY);
     int nlock = 0, it = 0, deg = 0;
     double lcut = NAN;
-    const bool f32 = o.precision == KF_PREC_MIXED;
-    DevMem fA(f32 ? (size_t)N * nb * 4 : 0), fB(f32 ? (size_t)N * nb * 4 : 0), fC(f32 ? (size_t)N * nb * 4 : 0);
+    // mixed precision: the filter runs in FP32 until the smallest unlocked residual reaches the
+    // FP32 floor region (1e-4 ||H||) or stops halving, then in FP64 (the FP32 filter cannot
+    // resolve residuals below ~1e-6 ||H||, so the last iterations must be FP64)
+    const bool mixed = o.precision == KF_PREC_MIXED;
+    bool f32 = mixed;
+    double prev_best = INFINITY;
+    DevMem fA(mixed ? (size_t)N * nb * 4 : 0), fB(mixed ? (size_t)N * nb * 4 : 0), fC(mixed ? (size_t)N * nb * 4 : 0);
     while (true) {
         const int na = nb - nlock;
         // residual norms of the active columns
@@ -779,6 +784,12 @@ static void solve_chebyshev(kf_op *op, const kf_solver_opts &o, int m, const dou
         std::vector<double> rn;
         colnorms_host(bufs[0], na, rn);
         for (int j = 0; j < na; ++j) res[nlock + j] = rn[j];
+        if (f32 && it >= 1) {
+            double best = INFINITY;
+            for (int j = nlock; j < nb; ++j) best = std::min(best, res[j]);
+            if (best <= 1e-4 * std::fabs(hb) || best > 0.5 * prev_best) f32 = false;
+            prev_best = std::min(prev_best, best);
+        }
         const bool filtered = it >= 1 || nb == N;
         const double tmin = *std::min_element(theta.begin(), theta.end());
         const double floor_ = 10 * eps * std::max(std::fabs(hb), std::fabs(tmin));
