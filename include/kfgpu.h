@@ -104,6 +104,20 @@ int kf_op_apply(kf_op *op, const void *X, void *Y, int64_t ldx, int64_t ldy, int
 int kf_op_apply_axpby(kf_op *op, const void *X, void *Y, const void *Z, int64_t ld, int64_t b,
                       double alpha, double beta, double gamma, int32_t flags);
 
+/* kf_op_apply for callers that must not allocate device memory (no counterpart in the
+ * reference).  kf_op_apply allocates two N x b scratch blocks with cudaMalloc the first time it
+ * applies a term with dense factors to a block that wide; a caller whose device memory is owned
+ * by its own pool or arena (a Julia or PyTorch caching allocator, a fixed-size arena) must not
+ * have memory allocated behind its back, and a tight solver loop cannot take the device
+ * synchronisation of a cudaMalloc.  This entry point computes the same Y = H X (device pointers
+ * only; KF_F64 or KF_F32) and allocates nothing: its scratch is a static device array of
+ * KF_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until exit.  Blocks whose
+ * dense-factor chains need more than that (2 N b elements) are rejected with KF_EINVAL.  All calls
+ * on a device share the array, so calls that overlap on the GPU race; the first call on each
+ * device looks up the array's address and should come before any stream capture. */
+#define KF_NOALLOC_SCRATCH_BYTES (8u << 20)
+int kf_op_apply_noalloc(kf_op *op, const void *X, void *Y, int64_t ldx, int64_t ldy, int64_t b, int32_t flags);
+
 /* diagonal(H) real part (src/apply.jl:455-478, _full_diagonal), N values into host memory. */
 int kf_op_diagonal(kf_op *op, double *out);
 

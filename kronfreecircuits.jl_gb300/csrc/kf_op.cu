@@ -234,6 +234,61 @@ static void apply_t(kf_op *op, const T *X, T *Y, int64_t ldx, int64_t ldy, int64
     }
 }
 
+// Y = H X with the chain scratch supplied by the caller (2 N b elements of T) instead of the op's
+// lazily allocated buffer; the same kernels as apply_t, no epilogue.  Used by the allocation-free
+// entry point (kf_noalloc.cu).
+template <typename T>
+void apply_given_scratch(kf_op *op, const T *X, T *Y, int64_t ldx, int64_t ldy, int64_t b, T *scratch,
+                         cudaStream_t s) {
+    const int64_t N = op->N;
+    if (b <= 0 || N == 0) return;
+    const bool f32 = sizeof(T) == 4;
+    const T *D = f32 ? (const T *)op->d_diag32 : (const T *)op->d_diag64;
+    const T *W = f32 ? (const T *)op->d_w32 : (const T *)op->d_w64;
+    const dim3 grid((unsigned)((N + 255) / 256), (unsigned)b);
+    const int ne = op->plan.ne;
+#define KF_FUSED2(ME)                                                                                     \
+    k_apply_fused<T, 1, ME><<<grid, 256, 0, s>>>(op->plan, D, W, X, Y, ldx, ldy, (int)b, T(1), T(0), nullptr, \
+                                                 (int64_t)0, T(0), 0)
+    if (ne <= 16) KF_FUSED2(16); else if (ne <= 32) KF_FUSED2(32); else KF_FUSED2(48);
+#undef KF_FUSED2
+    KF_LAUNCH_CHECK();
+    if (op->chains.empty()) return;
+    T *buf[2] = {scratch, scratch + N * b};
+    const T *cdata = f32 ? (const T *)op->d_chain32 : (const T *)op->d_chain64;
+    const int64_t total = N * b;
+    const unsigned g2 = (unsigned)((total + 255) / 256);
+    for (const ChainTerm &ct : op->chains) {
+        const T *src = X;
+        int64_t lds = ldx;
+        const int nf = (int)ct.f.size();
+        for (int k = 0; k < nf; ++k) {
+            const ChainFactor &f = ct.f[k];
+            const bool last = k == nf - 1;
+            T *dst = last ? Y : buf[k & 1];
+            const int64_t ldd = last ? ldy : N;
+            const T a = last ? (T)ct.coeff : T(1);
+            const int acc = last ? 1 : 0;
+            const int64_t stride = op->strides[f.axis];
+            if (f.kind == KF_DENSE) {
+                const size_t sm = (size_t)f.n * f.n * sizeof(T) <= 48 * 1024 ? (size_t)f.n * f.n * sizeof(T) : 0;
+                k_axis_dense<T><<<g2, 256, sm, s>>>(dst, ldd, src, lds, cdata + f.data_off, f.n, stride, N, total, a,
+                                                    acc);
+            } else {
+                k_axis_banded<T><<<g2, 256, 0, s>>>(dst, ldd, src, lds, cdata + f.data_off, f, stride, N, total, a, acc);
+            }
+            KF_LAUNCH_CHECK();
+            src = dst;
+            lds = ldd;
+        }
+    }
+}
+
+template void apply_given_scratch<float>(kf_op *, const float *, float *, int64_t, int64_t, int64_t, float *,
+                                         cudaStream_t);
+template void apply_given_scratch<double>(kf_op *, const double *, double *, int64_t, int64_t, int64_t, double *,
+                                          cudaStream_t);
+
 void launch_apply(kf_op *op, bool f32, const void *X, void *Y, int64_t ldx, int64_t ldy, int64_t b, double alpha,
                   double beta, const void *Z, int64_t ldz, double gamma, cudaStream_t s) {
     if (b <= 0 || op->N == 0) return;

@@ -96,6 +96,7 @@ def lib():
         "kf_op_destroy": (C.c_int, [P]),
         "kf_op_size": (C.c_int, [P, C.POINTER(C.c_int64)]),
         "kf_op_apply": (C.c_int, [P, P, P, C.c_int64, C.c_int64, C.c_int64, C.c_int32]),
+        "kf_op_apply_noalloc": (C.c_int, [P, P, P, C.c_int64, C.c_int64, C.c_int64, C.c_int32]),
         "kf_op_apply_axpby": (C.c_int, [P, P, P, P, C.c_int64, C.c_int64, C.c_double, C.c_double, C.c_double,
                                         C.c_int32]),
         "kf_op_diagonal": (C.c_int, [P, C.POINTER(C.c_double)]),
