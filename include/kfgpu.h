@@ -172,8 +172,9 @@ typedef struct {
     double mixed_switch;       /* MIXED: FP32 phase stops when every active residual is below
                                   mixed_switch * ||H|| (||H|| = gershgorin bound)              */
     int32_t fallback_iters;    /* warm start judge: after this many iterations ...             */
-    double fallback_resid;     /* ... a largest residual above this times ||H|| restarts the
-                                  solve from a random block (0 disables)                       */
+    double fallback_resid;     /* ... a largest residual above this (absolute, energy units)
+                                  restarts a warm-started solve from a random block (0
+                                  disables); the judge of a learned warm start                 */
 } kf_solver_opts;
 
 typedef struct {

@@ -10,7 +10,7 @@
 // Blocks are column-major (N rows, k <= 128 columns, leading dimension ld).  Every reduction
 // over N is split across CTAs into FP64 partials and summed in a fixed order by a second
 // kernel, so results are deterministic run to run.  Within a CTA, FP32 Gram products accumulate
-// in FP32 over one 32-row tile and then in FP64; FP64 blocks accumulate in FP64 throughout.
+// in FP32 over 256 rows and then in FP64; FP64 blocks accumulate in FP64 throughout.
 #include "kf_internal.h"
 
 namespace kf {
@@ -41,7 +41,11 @@ size_t gram_partials_size(int ka, int kb, int64_t N) {
     return (a > b ? a : b) * sizeof(double);
 }
 
-// partial[cta][i + ka*j] = sum over this CTA's rows of A[r,i] B[r,j]
+// partial[cta][i + ka*j] = sum over this CTA's rows of A[r,i] B[r,j].
+// The output is cut into 4x4 register tiles; when there are fewer tiles than threads, the
+// threads form `ng` groups that split the rows of each smem tile (row r goes to group r % ng)
+// and are summed in a fixed order at the end, so narrow Gram matrices keep every thread busy.
+// FP32 products accumulate in FP32 over 256 rows at a time, then in FP64.
 template <typename T>
 __global__ void __launch_bounds__(GRAM_THREADS) k_gram(const T *__restrict__ A, int64_t lda, int ka,
                                                        const T *__restrict__ B, int64_t ldb, int kb, int64_t N,
@@ -49,21 +53,23 @@ __global__ void __launch_bounds__(GRAM_THREADS) k_gram(const T *__restrict__ A, 
     extern __shared__ unsigned char smem_raw[];
     T *As = reinterpret_cast<T *>(smem_raw);            // [GRAM_RT][ka]
     T *Bs = As + GRAM_RT * ka;                          // [GRAM_RT][kb]
+    double *red = reinterpret_cast<double *>(smem_raw); // reused after the row loop
     const int ti_n = (ka + 3) / 4, tj_n = (kb + 3) / 4;
     const int ntiles = ti_n * tj_n;
-    // FP32 blocks: products accumulate in FP32 over one 32-row tile, then into FP64
+    const int ng = ntiles >= GRAM_THREADS ? 1 : GRAM_THREADS / ntiles;   // row groups
+    const int grp = threadIdx.x / (ntiles < GRAM_THREADS ? ntiles : GRAM_THREADS);
     T acc[GRAM_MAXTILES][16];
-    double acc64[sizeof(T) == 4 ? GRAM_MAXTILES : 1][16];
+    double acc64[GRAM_MAXTILES][16];
 #pragma unroll
     for (int m = 0; m < GRAM_MAXTILES; ++m)
 #pragma unroll
-        for (int q = 0; q < 16; ++q) acc[m][q] = T(0);
-#pragma unroll
-    for (int m = 0; m < (sizeof(T) == 4 ? GRAM_MAXTILES : 1); ++m)
-#pragma unroll
-        for (int q = 0; q < 16; ++q) acc64[m][q] = 0.0;
+        for (int q = 0; q < 16; ++q) {
+            acc[m][q] = T(0);
+            acc64[m][q] = 0.0;
+        }
     const int64_t r0 = (int64_t)blockIdx.x * rows_per;
     const int64_t r1 = (r0 + rows_per < N) ? r0 + rows_per : N;
+    int tiles_since_flush = 0;
     for (int64_t rb = r0; rb < r1; rb += GRAM_RT) {
         const int nr = (int)((r1 - rb) < GRAM_RT ? (r1 - rb) : GRAM_RT);
         for (int e = threadIdx.x; e < GRAM_RT * ka; e += blockDim.x) {
@@ -75,12 +81,13 @@ __global__ void __launch_bounds__(GRAM_THREADS) k_gram(const T *__restrict__ A, 
             Bs[r * kb + j] = (r < nr) ? B[rb + r + (int64_t)j * ldb] : T(0);
         }
         __syncthreads();
+        if (grp < ng) {
 #pragma unroll
-        for (int m = 0; m < GRAM_MAXTILES; ++m) {
-            const int tile = threadIdx.x + m * GRAM_THREADS;
-            if (tile < ntiles) {
+            for (int m = 0; m < GRAM_MAXTILES; ++m) {
+                const int tile = (ng > 1 ? threadIdx.x % ntiles : threadIdx.x) + m * GRAM_THREADS;
+                if ((ng > 1 && m > 0) || tile >= ntiles) continue;
                 const int i0 = (tile % ti_n) * 4, j0 = (tile / ti_n) * 4;
-                for (int r = 0; r < GRAM_RT; ++r) {
+                for (int r = grp; r < GRAM_RT; r += ng) {
                     T a[4], bv[4];
 #pragma unroll
                     for (int u = 0; u < 4; ++u) {
@@ -92,32 +99,53 @@ __global__ void __launch_bounds__(GRAM_THREADS) k_gram(const T *__restrict__ A, 
 #pragma unroll
                         for (int v = 0; v < 4; ++v) acc[m][u * 4 + v] += a[u] * bv[v];
                 }
-                if constexpr (sizeof(T) == 4) {
-#pragma unroll
-                    for (int q = 0; q < 16; ++q) {
-                        acc64[m][q] += (double)acc[m][q];
-                        acc[m][q] = T(0);
-                    }
-                }
             }
         }
         __syncthreads();
+        if (++tiles_since_flush == 8 || rb + GRAM_RT >= r1) {
+            tiles_since_flush = 0;
+#pragma unroll
+            for (int m = 0; m < GRAM_MAXTILES; ++m)
+#pragma unroll
+                for (int q = 0; q < 16; ++q) {
+                    acc64[m][q] += (double)acc[m][q];
+                    acc[m][q] = T(0);
+                }
+        }
     }
     double *P = partials + (size_t)blockIdx.x * ka * kb;
+    if (ng == 1) {
 #pragma unroll
-    for (int m = 0; m < GRAM_MAXTILES; ++m) {
-        const int tile = threadIdx.x + m * GRAM_THREADS;
-        if (tile < ntiles) {
+        for (int m = 0; m < GRAM_MAXTILES; ++m) {
+            const int tile = threadIdx.x + m * GRAM_THREADS;
+            if (tile < ntiles) {
+                const int i0 = (tile % ti_n) * 4, j0 = (tile / ti_n) * 4;
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+#pragma unroll
+                    for (int v = 0; v < 4; ++v)
+                        if (i0 + u < ka && j0 + v < kb) P[(i0 + u) + (size_t)ka * (j0 + v)] = acc64[m][u * 4 + v];
+            }
+        }
+        return;
+    }
+    // several row groups: sum their tiles in shared memory in group order
+    const int ntot = ka * kb;
+    for (int e = threadIdx.x; e < ntot; e += blockDim.x) red[e] = 0.0;
+    __syncthreads();
+    for (int g = 0; g < ng; ++g) {
+        if (grp == g) {
+            const int tile = threadIdx.x % ntiles;
             const int i0 = (tile % ti_n) * 4, j0 = (tile / ti_n) * 4;
 #pragma unroll
             for (int u = 0; u < 4; ++u)
 #pragma unroll
                 for (int v = 0; v < 4; ++v)
-                    if (i0 + u < ka && j0 + v < kb)
-                        P[(i0 + u) + (size_t)ka * (j0 + v)] =
-                            (sizeof(T) == 4) ? acc64[sizeof(T) == 4 ? m : 0][u * 4 + v] : (double)acc[m][u * 4 + v];
+                    if (i0 + u < ka && j0 + v < kb) red[(i0 + u) + ka * (j0 + v)] += acc64[0][u * 4 + v];
         }
+        __syncthreads();
     }
+    for (int e = threadIdx.x; e < ntot; e += blockDim.x) P[e] = red[e];
 }
 
 // out[e] = sum_c partials[c][e], e < n, in a fixed order
@@ -136,7 +164,8 @@ void gram(const T *A, int64_t lda, int ka, const T *B, int64_t ldb, int kb, int6
                KF_EINVAL, "gram: block widths out of range");
     const int64_t rp = gram_rows_per_cta(N);
     const int nc = num_ctas_for(N, rp);
-    const size_t sm = (size_t)GRAM_RT * (ka + kb) * sizeof(T);
+    size_t sm = (size_t)GRAM_RT * (ka + kb) * sizeof(T);
+    if (sm < (size_t)ka * kb * sizeof(double)) sm = (size_t)ka * kb * sizeof(double);   // the group reduction
     if (sm > 48 * 1024) KF_CUDA(cudaFuncSetAttribute(k_gram<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     k_gram<T><<<nc, GRAM_THREADS, sm, s>>>(A, lda, ka, B, ldb, kb, N, rp, partials);
     KF_LAUNCH_CHECK();

@@ -184,9 +184,9 @@ static void apply_t(kf_op *op, const T *X, T *Y, int64_t ldx, int64_t ldy, int64
         op->plan, D, W, X, Y, ldx, ldy, (int)b, (T)alpha, (T)beta,                                               \
                                                   Z, ldz, (T)gamma, epi)
     if (f32) {
-        if (ne <= 16) KF_FUSED(1, 16); else if (ne <= 32) KF_FUSED(1, 32); else KF_FUSED(1, 48);
+        if (ne <= 16) KF_FUSED(4, 16); else if (ne <= 32) KF_FUSED(2, 32); else KF_FUSED(1, 48);
     } else {
-        if (ne <= 16) KF_FUSED(1, 16); else if (ne <= 32) KF_FUSED(1, 32); else KF_FUSED(1, 48);
+        if (ne <= 16) KF_FUSED(4, 16); else if (ne <= 32) KF_FUSED(2, 32); else KF_FUSED(1, 48);
     }
 #undef KF_FUSED
     KF_LAUNCH_CHECK();

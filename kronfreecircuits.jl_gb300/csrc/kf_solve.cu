@@ -263,12 +263,16 @@ static LobOut lobpcg_run(kf_op *op, LobWork<T> &Wk, const double *D, const LobPa
             break;
         }
         if (prm.stall_exit) {
-            // FP32 has reached its floor when the largest active residual has not fallen by 10%
-            // over 40 iterations (LOBPCG's residuals stall for stretches before a column locks).
-            if (worst < 0.9 * best) {
-                best = worst;
+            // FP32 has reached its floor when, for 30 iterations, no column has locked and the
+            // geometric mean of the active residuals has not halved (single columns stall for
+            // stretches while the block as a whole still converges)
+            double lg = 0;
+            for (int j = nl; j < w; ++j) lg += std::log(std::max(res[j], 1e-300));
+            lg /= std::max(w - nl, 1);
+            if (newly > 0 || lg < best - std::log(2.0)) {
+                best = std::min(best, lg);
                 since_best = 0;
-            } else if (++since_best >= 40) {
+            } else if (++since_best >= 30) {
                 break;
             }
         }
@@ -497,7 +501,7 @@ static void solve_lobpcg(kf_op *op, const kf_solver_opts &o, int m, const double
         KF_CUDA(cudaMemcpyAsync(W64.X.p, Xh.data(), sizeof(double) * (size_t)N * w, cudaMemcpyHostToDevice, s));
     };
     LobParams p64{o.tol, o.maxiter, o.preconditioner, o.eta, w, 1e-12, false, o.fallback_iters,
-                  o.fallback_resid > 0 ? o.fallback_resid * hn : 0.0};
+                  o.fallback_resid > 0 ? o.fallback_resid : 0.0};
     std::vector<double> theta;
     LobOut r;
     const double t0 = now_s();
