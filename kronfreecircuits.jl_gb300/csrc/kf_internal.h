@@ -48,6 +48,7 @@ extern std::atomic<uint64_t> g_launches;
 
 constexpr int MAXDIMS = 8;     // axes of a state tensor
 constexpr int MAXB = 24;       // bands of one banded factor (a periodic order-8 stencil has 16)
+constexpr int KF_APPLY_VARIANTS = 5;   // (columns per thread, columns at once) candidates
 constexpr int MAXE = 48;       // stencil entries (products of bands) over all fused terms
 
 // The fused kernel's stencil entries.  Every term built only of diagonal, banded and shift
@@ -95,6 +96,8 @@ struct kf_op {
     cudaStream_t stream = nullptr;
     bool own_stream = true;
     kf::ApplyPlan plan{};
+    int apply_variant[16] = {-1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1};
+    float apply_variant_ms[16] = {};
     int64_t N = 0;
     std::vector<int64_t> dims;
     std::vector<int64_t> strides;

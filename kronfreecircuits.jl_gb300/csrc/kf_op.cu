@@ -37,10 +37,10 @@ __device__ __forceinline__ int pick(const int (&idx)[MAXDIMS_F], int a) {
 }
 
 // Y = D X + sum_entries w_e X[p + delta_e]  (then the epilogue Y = alpha Y + beta X + gamma Z).
-// One thread per state point p and group of CB columns (blockIdx.y); the point's entry weights
-// and offsets are evaluated into registers (ME >= ne, fully unrolled) and used for its columns,
-// whose ne neighbour loads are independent and in flight together.
-template <typename T, int CB, int ME>
+// One thread per state point p and group of CPT columns (blockIdx.y); the point's entry weights
+// and offsets are evaluated once into registers (ME >= ne, fully unrolled) and reused for its
+// columns.  (CPT, U) is chosen per operator by timing the candidates on its first apply.
+template <typename T, int CPT, int U, int ME>
 __global__ void __launch_bounds__(256, 2) k_apply_fused(const ApplyPlan plan, const T *__restrict__ D,
                                                      const T *__restrict__ W, const T *__restrict__ X,
                                                      T *__restrict__ Y, int64_t ldx, int64_t ldy, int b,
@@ -83,23 +83,38 @@ __global__ void __launch_bounds__(256, 2) k_apply_fused(const ApplyPlan plan, co
         }
     }
     const T dv = D[p];
-    // this thread's columns: [blockIdx.y * CB, blockIdx.y * CB + CB)
+    // this thread's columns [blockIdx.y * CPT, ... + CPT), U of them at a time: the U columns'
+    // ne neighbour loads are independent and all in flight together
+    const int cbeg = blockIdx.y * CPT;
+    const int cend = min(b, cbeg + CPT);
+    for (int c0 = cbeg; c0 < cend; c0 += U) {
+        T v[U];
+        const T *xc[U];
 #pragma unroll
-    for (int cc = 0; cc < CB; ++cc) {
-        const int c = blockIdx.y * CB + cc;
-        if (c >= b) break;
-        const T *xc = X + (int64_t)c * ldx + p;
-        T v = dv * xc[0];
-        // unconditional loads (an invalid entry has weight 0 and offset 0, a valid address), so
-        // all ne loads of the column issue back to back
-#pragma unroll
-        for (int e = 0; e < ME; ++e)
-            if (e < plan.ne) v += w[e] * __ldg(xc + off[e]);
-        if (epi) {
-            v = alpha * v + beta * xc[0];
-            if (Z != nullptr) v += gamma * Z[(int64_t)c * ldz + p];
+        for (int u = 0; u < U; ++u) {
+            const int c = (c0 + u < cend) ? c0 + u : c0;
+            xc[u] = X + (int64_t)c * ldx + p;
+            v[u] = dv * xc[u][0];
         }
-        Y[(int64_t)c * ldy + p] = v;
+        // unconditional loads: an invalid entry has weight 0 and offset 0 (a valid address)
+#pragma unroll
+        for (int e = 0; e < ME; ++e) {
+            if (e < plan.ne) {
+#pragma unroll
+                for (int u = 0; u < U; ++u) v[u] += w[e] * __ldg(xc[u] + off[e]);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int c = c0 + u;
+            if (c >= cend) break;
+            T r = v[u];
+            if (epi) {
+                r = alpha * r + beta * xc[u][0];
+                if (Z != nullptr) r += gamma * Z[(int64_t)c * ldz + p];
+            }
+            Y[(int64_t)c * ldy + p] = r;
+        }
     }
 }
 
@@ -179,17 +194,48 @@ static void apply_t(kf_op *op, const T *X, T *Y, int64_t ldx, int64_t ldy, int64
     const bool trivial_epi = alpha == 1.0 && beta == 0.0 && (Z == nullptr || gamma == 0.0);
     const int epi = (!chains && !trivial_epi) ? 1 : 0;
     const int ne = op->plan.ne;
-#define KF_FUSED(CB, ME)                                                                                 \
-    k_apply_fused<T, CB, ME><<<dim3((unsigned)((N + 255) / 256), (unsigned)((b + CB - 1) / CB)), 256, 0, s>>>(   \
-        op->plan, D, W, X, Y, ldx, ldy, (int)b, (T)alpha, (T)beta,                                               \
-                                                  Z, ldz, (T)gamma, epi)
-    if (f32) {
-        if (ne <= 16) KF_FUSED(4, 16); else if (ne <= 32) KF_FUSED(2, 32); else KF_FUSED(1, 48);
-    } else {
-        if (ne <= 16) KF_FUSED(4, 16); else if (ne <= 32) KF_FUSED(2, 32); else KF_FUSED(1, 48);
+    auto run = [&](int variant) {
+#define KF_FUSED(CPT, U, ME)                                                                                  \
+    k_apply_fused<T, CPT, U, ME><<<dim3((unsigned)((N + 255) / 256), (unsigned)((b + CPT - 1) / CPT)), 256, 0, s>>>( \
+        op->plan, D, W, X, Y, ldx, ldy, (int)b, (T)alpha, (T)beta, Z, ldz, (T)gamma, epi)
+#define KF_VARIANTS(ME)                                  \
+    switch (variant) {                                   \
+        case 0: KF_FUSED(16, 1, ME); break;              \
+        case 1: KF_FUSED(16, 2, ME); break;              \
+        case 2: KF_FUSED(8, 2, ME); break;               \
+        case 3: KF_FUSED(4, 4, ME); break;               \
+        default: KF_FUSED(32, 1, ME); break;             \
     }
+        if (ne <= 16) { KF_VARIANTS(16) } else if (ne <= 32) { KF_VARIANTS(32) } else { KF_VARIANTS(48) }
+#undef KF_VARIANTS
 #undef KF_FUSED
-    KF_LAUNCH_CHECK();
+        KF_LAUNCH_CHECK();
+    };
+    // autotune: on the first apply of a block this wide (per precision), time every variant on the
+    // caller's own buffers (each overwrites Y completely with the same result) and keep the fastest
+    const int slot = (f32 ? 1 : 0) * 8 + (b >= 32 ? 3 : b >= 16 ? 2 : b >= 4 ? 1 : 0);
+    if (op->apply_variant[slot] < 0) {
+        cudaEvent_t e0, e1;
+        KF_CUDA(cudaEventCreate(&e0));
+        KF_CUDA(cudaEventCreate(&e1));
+        float best = 1e30f;
+        int bestv = 0;
+        for (int v = 0; v < KF_APPLY_VARIANTS; ++v) {
+            run(v);                                   // warm
+            KF_CUDA(cudaEventRecord(e0, s));
+            for (int r = 0; r < 3; ++r) run(v);
+            KF_CUDA(cudaEventRecord(e1, s));
+            KF_CUDA(cudaEventSynchronize(e1));
+            float ms = 0;
+            KF_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            if (ms < best) { best = ms; bestv = v; }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        op->apply_variant[slot] = bestv;
+        op->apply_variant_ms[slot] = best / 3;
+    }
+    run(op->apply_variant[slot]);
     if (!chains) return;
     // dense-containing terms: chain through scratch, one contiguous (N x b) block per buffer
     const size_t need = (size_t)2 * N * b * sizeof(T);
@@ -217,9 +263,12 @@ static void apply_t(kf_op *op, const T *X, T *Y, int64_t ldx, int64_t ldy, int64
             const int acc = last ? 1 : 0;
             const int64_t stride = op->strides[f.axis];
             if (f.kind == KF_DENSE) {
-                const size_t sm = (size_t)f.n * f.n * sizeof(T) <= 48 * 1024 ? (size_t)f.n * f.n * sizeof(T) : 0;
-                k_axis_dense<T><<<g2, 256, sm, s>>>(dst, ldd, src, lds, cdata + f.data_off, f.n, stride, N, total, a,
-                                                    acc);
+                // the mode-k product as a tiled GEMM (accumulating into Y for the last factor)
+                mode_product<T>(dst, ldd, src, lds, cdata + f.data_off, f.n, stride, N, b, (double)a, acc ? 1.0 : 0.0,
+                                s);
+                src = dst;
+                lds = ldd;
+                continue;
             } else {
                 k_axis_banded<T><<<g2, 256, 0, s>>>(dst, ldd, src, lds, cdata + f.data_off, f, stride, N, total, a, acc);
             }
@@ -245,10 +294,10 @@ void apply_given_scratch(kf_op *op, const T *X, T *Y, int64_t ldx, int64_t ldy, 
     const bool f32 = sizeof(T) == 4;
     const T *D = f32 ? (const T *)op->d_diag32 : (const T *)op->d_diag64;
     const T *W = f32 ? (const T *)op->d_w32 : (const T *)op->d_w64;
-    const dim3 grid((unsigned)((N + 255) / 256), (unsigned)b);
+    const dim3 grid((unsigned)((N + 255) / 256), (unsigned)((b + 15) / 16));
     const int ne = op->plan.ne;
 #define KF_FUSED2(ME)                                                                                     \
-    k_apply_fused<T, 1, ME><<<grid, 256, 0, s>>>(op->plan, D, W, X, Y, ldx, ldy, (int)b, T(1), T(0), nullptr, \
+    k_apply_fused<T, 16, 1, ME><<<grid, 256, 0, s>>>(op->plan, D, W, X, Y, ldx, ldy, (int)b, T(1), T(0), nullptr, \
                                                  (int64_t)0, T(0), 0)
     if (ne <= 16) KF_FUSED2(16); else if (ne <= 32) KF_FUSED2(32); else KF_FUSED2(48);
 #undef KF_FUSED2
@@ -271,9 +320,12 @@ void apply_given_scratch(kf_op *op, const T *X, T *Y, int64_t ldx, int64_t ldy, 
             const int acc = last ? 1 : 0;
             const int64_t stride = op->strides[f.axis];
             if (f.kind == KF_DENSE) {
-                const size_t sm = (size_t)f.n * f.n * sizeof(T) <= 48 * 1024 ? (size_t)f.n * f.n * sizeof(T) : 0;
-                k_axis_dense<T><<<g2, 256, sm, s>>>(dst, ldd, src, lds, cdata + f.data_off, f.n, stride, N, total, a,
-                                                    acc);
+                // the mode-k product as a tiled GEMM (accumulating into Y for the last factor)
+                mode_product<T>(dst, ldd, src, lds, cdata + f.data_off, f.n, stride, N, b, (double)a, acc ? 1.0 : 0.0,
+                                s);
+                src = dst;
+                lds = ldd;
+                continue;
             } else {
                 k_axis_banded<T><<<g2, 256, 0, s>>>(dst, ldd, src, lds, cdata + f.data_off, f, stride, N, total, a, acc);
             }

@@ -25,6 +25,7 @@
 // the last sweep being the FP64 refinement that the acceptance test measures.
 #include <algorithm>
 #include <chrono>
+#include <cstdlib>
 #include <cstring>
 #include <numeric>
 #include <random>
@@ -62,6 +63,17 @@ struct HostMem {
     template <typename T>
     T *as() const { return (T *)p; }
 };
+
+// KF_TRACE=1 in the environment prints one line per LOBPCG iteration to stderr (phase,
+// iteration, locked columns, smallest / largest active residual, SVQB rank) -- the per-iteration
+// information the reference hands to its solver callbacks (src/tree.jl:55-56).
+static bool trace_on() {
+    static const bool on = [] {
+        const char *e = std::getenv("KF_TRACE");
+        return e && e[0] && e[0] != '0';
+    }();
+    return on;
+}
 
 static double now_s() {
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
@@ -255,8 +267,14 @@ static LobOut lobpcg_run(kf_op *op, LobWork<T> &Wk, const double *D, const LobPa
             out.converged = true;
             break;
         }
-        double worst = 0;
-        for (int j = nl; j < w; ++j) worst = std::max(worst, res[j]);
+        double worst = 0, bestr = INFINITY;
+        for (int j = nl; j < w; ++j) {
+            worst = std::max(worst, res[j]);
+            bestr = std::min(bestr, res[j]);
+        }
+        if (trace_on())
+            std::fprintf(stderr, "kf lobpcg %s it=%d locked=%d(+%d) active_resid=[%.3e, %.3e]\n", sizeof(T) == 4 ? "f32" : "f64",
+                         it, nl, newly, bestr, worst);
         if (!std::isfinite(worst)) throw Error(KF_ENOTFINITE, "LOBPCG: the residual block is not finite");
         if (prm.judge_resid > 0 && it == prm.judge_iters && worst > prm.judge_resid) {
             out.judged_bad = true;
