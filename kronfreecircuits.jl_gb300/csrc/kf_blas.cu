@@ -9,15 +9,13 @@
 //
 // Blocks are column-major (N rows, k <= 128 columns, leading dimension ld).  Every reduction
 // over N is split across CTAs into FP64 partials and summed in a fixed order by a second
-// kernel, so results are deterministic run to run.  Within a CTA, FP32 Gram products accumulate
-// in FP32 over 256 rows and then in FP64; FP64 blocks accumulate in FP64 throughout.
+// kernel, so results are deterministic run to run.  In a Gram product each thread accumulates its
+// few rows in the block's precision, and the cross-thread sums are FP64.
 #include "kf_internal.h"
 
 namespace kf {
 
-constexpr int GRAM_RT = 32;               // rows per shared-memory tile
 constexpr int GRAM_THREADS = 256;
-constexpr int GRAM_MAXTILES = 3;          // 4x4 register tiles per thread
 constexpr int RED_THREADS = 256;
 
 static int num_ctas_for(int64_t N, int64_t rows_per) {
@@ -27,125 +25,73 @@ static int num_ctas_for(int64_t N, int64_t rows_per) {
     return (int)c;
 }
 
-static int64_t gram_rows_per_cta(int64_t N) {
-    // about two waves of CTAs on 152 SMs, at least one tile each
-    int64_t r = (N + 303) / 304;
-    r = ((r + GRAM_RT - 1) / GRAM_RT) * GRAM_RT;
-    return r < GRAM_RT ? GRAM_RT : r;
+// rows per CTA so that all chunks together fill about four waves of 152 SMs, at least 256 rows
+static int64_t gram_rows_per_cta(int64_t N, int chunks) {
+    int64_t target = (608 + chunks - 1) / chunks;
+    if (target < 1) target = 1;
+    int64_t r = (N + target - 1) / target;
+    if (r < 256) r = 256;
+    return r;
 }
 
 size_t gram_partials_size(int ka, int kb, int64_t N) {
-    const int nc = num_ctas_for(N, gram_rows_per_cta(N));
+    // the largest CTA count over the chunkings used: one chunk gives the most row blocks
+    const int nc = num_ctas_for(N, gram_rows_per_cta(N, 1));
     const size_t a = (size_t)nc * ka * kb;
     const size_t b = (size_t)1216 * 128;  // also enough for the column reductions
     return (a > b ? a : b) * sizeof(double);
 }
 
-// partial[cta][i + ka*j] = sum over this CTA's rows of A[r,i] B[r,j].
-// The output is cut into 4x4 register tiles; when there are fewer tiles than threads, the
-// threads form `ng` groups that split the rows of each smem tile (row r goes to group r % ng)
-// and are summed in a fixed order at the end, so narrow Gram matrices keep every thread busy.
-// FP32 products accumulate in FP32 over 256 rows at a time, then in FP64.
-template <typename T>
+// partial[cta][i + ka*j] = sum over this CTA's rows of A[r,i] B[r,j], for one RI x RJ chunk of
+// the output (blockIdx.y).  Rows stream through the threads (consecutive threads read
+// consecutive rows of a column: coalesced), each thread keeps its chunk's products in registers
+// (FP32 blocks: FP32 over its few rows), and the CTA sums them in FP64 -- warp shuffles, then the
+// warps in a fixed order through shared memory.
+template <typename T, int RI, int RJ>
 __global__ void __launch_bounds__(GRAM_THREADS) k_gram(const T *__restrict__ A, int64_t lda, int ka,
                                                        const T *__restrict__ B, int64_t ldb, int kb, int64_t N,
                                                        int64_t rows_per, double *__restrict__ partials) {
-    extern __shared__ unsigned char smem_raw[];
-    T *As = reinterpret_cast<T *>(smem_raw);            // [GRAM_RT][ka]
-    T *Bs = As + GRAM_RT * ka;                          // [GRAM_RT][kb]
-    double *red = reinterpret_cast<double *>(smem_raw); // reused after the row loop
-    const int ti_n = (ka + 3) / 4, tj_n = (kb + 3) / 4;
-    const int ntiles = ti_n * tj_n;
-    const int ng = ntiles >= GRAM_THREADS ? 1 : GRAM_THREADS / ntiles;   // row groups
-    const int grp = threadIdx.x / (ntiles < GRAM_THREADS ? ntiles : GRAM_THREADS);
-    T acc[GRAM_MAXTILES][16];
-    double acc64[GRAM_MAXTILES][16];
+    __shared__ double red[GRAM_THREADS / 32][RI * RJ];
+    const int cj_n = (kb + RJ - 1) / RJ;
+    const int i0 = (blockIdx.y / cj_n) * RI, j0 = (blockIdx.y % cj_n) * RJ;
+    const int ni = min(RI, ka - i0), nj = min(RJ, kb - j0);
+    T acc[RI][RJ];
 #pragma unroll
-    for (int m = 0; m < GRAM_MAXTILES; ++m)
+    for (int u = 0; u < RI; ++u)
 #pragma unroll
-        for (int q = 0; q < 16; ++q) {
-            acc[m][q] = T(0);
-            acc64[m][q] = 0.0;
-        }
+        for (int v = 0; v < RJ; ++v) acc[u][v] = T(0);
     const int64_t r0 = (int64_t)blockIdx.x * rows_per;
     const int64_t r1 = (r0 + rows_per < N) ? r0 + rows_per : N;
-    int tiles_since_flush = 0;
-    for (int64_t rb = r0; rb < r1; rb += GRAM_RT) {
-        const int nr = (int)((r1 - rb) < GRAM_RT ? (r1 - rb) : GRAM_RT);
-        for (int e = threadIdx.x; e < GRAM_RT * ka; e += blockDim.x) {
-            const int r = e % GRAM_RT, i = e / GRAM_RT;
-            As[r * ka + i] = (r < nr) ? A[rb + r + (int64_t)i * lda] : T(0);
-        }
-        for (int e = threadIdx.x; e < GRAM_RT * kb; e += blockDim.x) {
-            const int r = e % GRAM_RT, j = e / GRAM_RT;
-            Bs[r * kb + j] = (r < nr) ? B[rb + r + (int64_t)j * ldb] : T(0);
-        }
-        __syncthreads();
-        if (grp < ng) {
+    for (int64_t r = r0 + threadIdx.x; r < r1; r += GRAM_THREADS) {
+        T a[RI], bv[RJ];
 #pragma unroll
-            for (int m = 0; m < GRAM_MAXTILES; ++m) {
-                const int tile = (ng > 1 ? threadIdx.x % ntiles : threadIdx.x) + m * GRAM_THREADS;
-                if ((ng > 1 && m > 0) || tile >= ntiles) continue;
-                const int i0 = (tile % ti_n) * 4, j0 = (tile / ti_n) * 4;
-                for (int r = grp; r < GRAM_RT; r += ng) {
-                    T a[4], bv[4];
+        for (int u = 0; u < RI; ++u) a[u] = (u < ni) ? A[r + (int64_t)(i0 + u) * lda] : T(0);
 #pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        a[u] = (i0 + u < ka) ? As[r * ka + i0 + u] : T(0);
-                        bv[u] = (j0 + u < kb) ? Bs[r * kb + j0 + u] : T(0);
-                    }
+        for (int v = 0; v < RJ; ++v) bv[v] = (v < nj) ? B[r + (int64_t)(j0 + v) * ldb] : T(0);
 #pragma unroll
-                    for (int u = 0; u < 4; ++u)
+        for (int u = 0; u < RI; ++u)
 #pragma unroll
-                        for (int v = 0; v < 4; ++v) acc[m][u * 4 + v] += a[u] * bv[v];
-                }
-            }
-        }
-        __syncthreads();
-        if (++tiles_since_flush == 8 || rb + GRAM_RT >= r1) {
-            tiles_since_flush = 0;
-#pragma unroll
-            for (int m = 0; m < GRAM_MAXTILES; ++m)
-#pragma unroll
-                for (int q = 0; q < 16; ++q) {
-                    acc64[m][q] += (double)acc[m][q];
-                    acc[m][q] = T(0);
-                }
-        }
+            for (int v = 0; v < RJ; ++v) acc[u][v] += a[u] * bv[v];
     }
-    double *P = partials + (size_t)blockIdx.x * ka * kb;
-    if (ng == 1) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
-        for (int m = 0; m < GRAM_MAXTILES; ++m) {
-            const int tile = threadIdx.x + m * GRAM_THREADS;
-            if (tile < ntiles) {
-                const int i0 = (tile % ti_n) * 4, j0 = (tile / ti_n) * 4;
+    for (int u = 0; u < RI; ++u)
 #pragma unroll
-                for (int u = 0; u < 4; ++u)
+        for (int v = 0; v < RJ; ++v) {
+            double x = (double)acc[u][v];
 #pragma unroll
-                    for (int v = 0; v < 4; ++v)
-                        if (i0 + u < ka && j0 + v < kb) P[(i0 + u) + (size_t)ka * (j0 + v)] = acc64[m][u * 4 + v];
-            }
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+            if (lane == 0) red[warp][u * RJ + v] = x;
         }
-        return;
-    }
-    // several row groups: sum their tiles in shared memory in group order
-    const int ntot = ka * kb;
-    for (int e = threadIdx.x; e < ntot; e += blockDim.x) red[e] = 0.0;
     __syncthreads();
-    for (int g = 0; g < ng; ++g) {
-        if (grp == g) {
-            const int tile = threadIdx.x % ntiles;
-            const int i0 = (tile % ti_n) * 4, j0 = (tile / ti_n) * 4;
-#pragma unroll
-            for (int u = 0; u < 4; ++u)
-#pragma unroll
-                for (int v = 0; v < 4; ++v)
-                    if (i0 + u < ka && j0 + v < kb) red[(i0 + u) + ka * (j0 + v)] += acc64[0][u * 4 + v];
-        }
-        __syncthreads();
+    double *P = partials + (size_t)blockIdx.x * ka * kb;
+    for (int e = threadIdx.x; e < RI * RJ; e += GRAM_THREADS) {
+        const int u = e / RJ, v = e % RJ;
+        if (u >= ni || v >= nj) continue;
+        double s = 0;
+        for (int w = 0; w < GRAM_THREADS / 32; ++w) s += red[w][e];
+        P[(i0 + u) + (size_t)ka * (j0 + v)] = s;
     }
-    for (int e = threadIdx.x; e < ntot; e += blockDim.x) P[e] = red[e];
 }
 
 // out[e] = sum_c partials[c][e], e < n, in a fixed order
@@ -160,14 +106,13 @@ __global__ void k_reduce_partials(const double *__restrict__ partials, int npart
 template <typename T>
 void gram(const T *A, int64_t lda, int ka, const T *B, int64_t ldb, int kb, int64_t N, double *G, double *partials,
           cudaStream_t s) {
-    KF_REQUIRE(ka >= 1 && kb >= 1 && ka <= 128 && kb <= 128 && ((ka + 3) / 4) * ((kb + 3) / 4) <= GRAM_THREADS * GRAM_MAXTILES,
-               KF_EINVAL, "gram: block widths out of range");
-    const int64_t rp = gram_rows_per_cta(N);
+    KF_REQUIRE(ka >= 1 && kb >= 1 && ka <= 128 && kb <= 128, KF_EINVAL, "gram: block widths out of range");
+    // output chunks of RI x RJ (FP64: 4 x 8, FP32: 8 x 8 accumulators per thread)
+    constexpr int RI = sizeof(T) == 8 ? 4 : 8, RJ = 8;
+    const int chunks = ((ka + RI - 1) / RI) * ((kb + RJ - 1) / RJ);
+    const int64_t rp = gram_rows_per_cta(N, chunks);
     const int nc = num_ctas_for(N, rp);
-    size_t sm = (size_t)GRAM_RT * (ka + kb) * sizeof(T);
-    if (sm < (size_t)ka * kb * sizeof(double)) sm = (size_t)ka * kb * sizeof(double);   // the group reduction
-    if (sm > 48 * 1024) KF_CUDA(cudaFuncSetAttribute(k_gram<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_gram<T><<<nc, GRAM_THREADS, sm, s>>>(A, lda, ka, B, ldb, kb, N, rp, partials);
+    k_gram<T, RI, RJ><<<dim3(nc, chunks), GRAM_THREADS, 0, s>>>(A, lda, ka, B, ldb, kb, N, rp, partials);
     KF_LAUNCH_CHECK();
     const int n = ka * kb;
     k_reduce_partials<<<(n + 255) / 256, 256, 0, s>>>(partials, nc, n, G);
