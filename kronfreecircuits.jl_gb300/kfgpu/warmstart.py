@@ -118,8 +118,9 @@ def evaluate(ws, thetas, m=12, ncut=30, fallback_resid=1e-2, fallback_iters=3, p
         row = {"random_iters": sr["iterations"], "random_s": tr, "E": Er}
         if X0 is not None:
             t0 = time.perf_counter()
-            Ew, _, sw = solve(LOBPCG(tol=tol, seed="random", preconditioner=preconditioner, fallback_iters=fallback_iters,
-                                     fallback_resid=fallback_resid), H, m, X0=X0)
+            # guards from the product seed, as the reference's warm starts take them (src/lobpcg.jl:182-190)
+            Ew, _, sw = solve(LOBPCG(tol=tol, seed="product", preconditioner=preconditioner,
+                                     fallback_iters=fallback_iters, fallback_resid=fallback_resid), H, m, X0=X0)
             tw = time.perf_counter() - t0
             row.update({"warm_iters": sw["iterations"], "warm_s": tw, "fell_back": sw["fell_back"],
                         "max_dE": float(np.max(np.abs(Ew - Er)))})

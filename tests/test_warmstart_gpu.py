@@ -15,11 +15,11 @@ pytestmark = pytest.mark.gpu
 @pytest.fixture(scope="module")
 def trained(cuda):
     from kfgpu import warmstart as W
-    train = W.sample_thetas(384, seed=11)
+    train = W.sample_thetas(512, seed=11)
     Vs, _ = W.label(train)
-    POD = W.pod_basis(Vs, k=96)
+    POD = W.pod_basis(Vs, k=128)
     ws = W.WarmStart(POD, 12, hidden=256, seed=1)
-    losses = ws.fit(train, W.targets(Vs, POD), epochs=150, batch=128, lr=1e-3)
+    losses = ws.fit(train, W.targets(Vs, POD), epochs=300, batch=128, lr=1e-3)
     return W, ws, losses
 
 
@@ -42,9 +42,9 @@ def test_untrained_network_is_judged_and_replaced(cuda):
     from kfgpu import warmstart as W
     th = W.sample_thetas(4, seed=5)
     rng = np.random.default_rng(0)
-    POD = np.linalg.qr(rng.standard_normal((3721, 96)))[0]
+    POD = np.linalg.qr(rng.standard_normal((3721, 128)))[0]
     ws = W.WarmStart(POD, 12, seed=3)                       # random weights: a poor block
-    ws.net.set_scaling(np.zeros(7), np.ones(7), np.zeros(96 * 12), np.ones(96 * 12))
+    ws.net.set_scaling(np.zeros(7), np.ones(7), np.zeros(128 * 12), np.ones(128 * 12))
     rows = W.evaluate(ws, th, fallback_resid=1e-6)
     assert all(r["fell_back"] == 1 for r in rows)
     for r in rows:
