@@ -252,6 +252,121 @@ def profile_one(args):
             "iterations_f64": st["iterations_f64"], "seconds_f64": st["seconds_f64"]}
 
 
+def run_batch_workload(args):
+    """Batched theta sweep: 512 fluxonium leaves (n ~ U{200..1600} on [-5 pi, 5 pi], 5-point stencil,
+    keep 10) plus 64 chains of 2-4 leaves (g ~ U[0.01, 0.1] n_i n_{i+1}, parents keep 20), all leaves
+    in one persistent graph-captured launch (CTA size from the autotuner), then the parents."""
+    import torch
+    from kfgpu import KronFreeOperator, LOBPCG, circuits, ops as P, solve
+    from kfgpu.batch import autotune, batch_solve
+    from kfgpu.ops import PhaseGrid, localop
+    rng = np.random.default_rng(SEED + 2)
+    leaves = []
+    for _ in range(512):
+        th = circuits.fluxonium_theta(rng)
+        leaves.append((th, int(rng.integers(200, 1601))))
+    chains = []
+    for _ in range(64):
+        k = int(rng.integers(2, 5))
+        chains.append(([(circuits.fluxonium_theta(rng), int(rng.integers(200, 1601))) for _ in range(k)],
+                       [rng.uniform(0.01, 0.1) for _ in range(k - 1)]))
+    all_leaves = leaves + [lf for c, _ in chains for lf in c]
+    ops = []
+    for th, n in all_leaves:
+        dims, terms = circuits.fluxonium_leaf(th, n)
+        ops.append((dims, terms, 0.0))
+    m = [10] * len(ops)
+    tol = 1e-8 * 2e3            # 1e-8 ||H|| for the coarsest leaves' Gershgorin bound scale
+    tile = autotune(ops[:64], m[:64], tol)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    Es, Vs, iters, resid = batch_solve(ops, m, tol)
+    t_leaves = time.perf_counter() - t0
+    # parents of the chains
+    t1 = time.perf_counter()
+    k0 = len(leaves)
+    nparent_pairs = 0
+    for c, gs in chains:
+        idx = list(range(k0, k0 + len(c)))
+        k0 += len(c)
+        dims = [10] * len(c)
+        terms = [(1.0, [(a, P.DiagonalOp(Es[i]))]) for a, i in enumerate(idx)]
+        ports = []
+        for i in idx:
+            n = all_leaves[i][1]
+            A = localop(PhaseGrid(-5 * np.pi, 5 * np.pi, n, 4), "n", part="im").dense()
+            ports.append(Vs[i].T @ A @ Vs[i])
+        for a in range(len(c) - 1):
+            terms.append((-gs[a], [(a, P.DenseOp(ports[a])), (a + 1, P.DenseOp(ports[a + 1]))]))
+        H = KronFreeOperator(dims, terms, block_capacity=24)
+        Ep, Vp, st = solve(LOBPCG(tol=1e-8 * H.gershgorin_bound(), precision="mixed"), H, 20)
+        nparent_pairs += 20
+        H.close()
+    t_parents = time.perf_counter() - t1
+    return {"workload": "batched theta sweep: 512 fluxonium leaves + 64 chains of 2-4 (704 leaves in one launch)",
+            "leaves": len(ops), "leaf_pairs_per_s": 10 * len(ops) / t_leaves, "leaf_seconds": t_leaves,
+            "parents": len(chains), "parent_seconds": t_parents,
+            "pairs_per_s_total": (10 * len(ops) + nparent_pairs) / (t_leaves + t_parents),
+            "tuned_threads_per_cta": tile, "max_leaf_iterations": int(iters.max()),
+            "mean_leaf_iterations": float(iters.mean()), "max_residual": float(resid.max())}
+
+
+def run_warmstart_workload(args):
+    """Learned warm start on the two-transmon circuit (flat 61 x 61): label n_train theta with the
+    plain solver, POD 128, train 7 -> 256 -> 256 -> 1536 with the library's kernels, then LOBPCG on
+    n_test held-out theta: warm-started vs random start."""
+    from kfgpu import warmstart as W
+    t0 = time.perf_counter()
+    train = W.sample_thetas(args.n_train, seed=SEED + 3)
+    Vs, _ = W.label(train)
+    t_label = time.perf_counter() - t0
+    POD = W.pod_basis(Vs, k=128)
+    ws = W.WarmStart(POD, 12, hidden=256, seed=1)
+    t1 = time.perf_counter()
+    losses = ws.fit(train, W.targets(Vs, POD), epochs=args.epochs, batch=256, lr=1e-3)
+    t_train = time.perf_counter() - t1
+    rows = W.evaluate(ws, W.sample_thetas(args.n_test, seed=SEED + 4))
+    wi = np.array([r["warm_iters"] for r in rows]); ri = np.array([r["random_iters"] for r in rows])
+    wt = np.array([r["warm_s"] for r in rows]); rt = np.array([r["random_s"] for r in rows])
+    return {"workload": "learned warm start, two transmons flat 61x61 (N=3,721), m=12",
+            "n_train": args.n_train, "n_test": args.n_test, "label_seconds": t_label, "train_seconds": t_train,
+            "loss_first_last": [float(losses[0]), float(losses[-1])],
+            "warm_mean_iterations": float(wi.mean()), "random_mean_iterations": float(ri.mean()),
+            "warm_mean_seconds": float(wt.mean()), "random_mean_seconds": float(rt.mean()),
+            "warm_pairs_per_s": 12 / float(wt.mean()), "random_pairs_per_s": 12 / float(rt.mean()),
+            "fell_back": int(sum(r["fell_back"] for r in rows)),
+            "max_abs_dE": float(max(r["max_dE"] for r in rows))}
+
+
+def run_dense_workload(args):
+    """Three children of 48 kept states (N = 110,592) with dense pairwise port couplings; the lowest
+    30 pairs, mixed vs FP64 (eigenvalue differences and FP64 residuals)."""
+    import torch
+    from kfgpu import KronFreeOperator, LOBPCG, circuits, solve
+    out = {"workload": "dense parent 48^3 (N=110,592), 3 dense pair couplings, m=30 block 32"}
+    rng = np.random.default_rng(SEED + 5)
+    dims, terms = circuits.dense_parent(rng, d=48)
+    H = KronFreeOperator(dims, terms, block_capacity=32)
+    tol = 1e-8 * H.gershgorin_bound()
+    res = {}
+    for prec in ("mixed", "f64"):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        E, V, st = solve(LOBPCG(tol=tol, precision=prec, guard=2), H, 30)
+        res[prec] = (E, time.perf_counter() - t0, st)
+    out.update({"mixed_pairs_per_s": 30 / res["mixed"][1], "f64_pairs_per_s": 30 / res["f64"][1],
+                "mixed_iterations": res["mixed"][2]["iterations"], "f64_iterations": res["f64"][2]["iterations"],
+                "max_rel_dE_mixed_vs_f64": float(np.max(np.abs(res["mixed"][0] - res["f64"][0]) / np.abs(res["f64"][0]))),
+                "max_residual_rel": float(res["mixed"][2]["max_residual"] / H.gershgorin_bound())})
+    # the dense apply alone (32 columns, FP32 and FP64): flops counted as 6 mode products per column
+    for f32 in (True, False):
+        t = measure_apply(torch, H, f32, b=32)
+        flops = 6 * 2 * 48 * H.N * 32
+        out["apply_%s_us" % ("f32" if f32 else "f64")] = t * 1e6
+        out["apply_%s_tflops" % ("f32" if f32 else "f64")] = flops / t / 1e12
+    return out
+
+
 def cpu_baseline(theta, bounded=True, iters=None):
     """The oracle's restatement of the reference CPU path on the host cores: a bounded sample of
     LOBPCG iterations of the same solve (C/OpenMP mul! + NumPy LOBPCG), extrapolated to the
@@ -317,11 +432,20 @@ def main():
     ap.add_argument("--ref-iters", type=int, default=570,
                     help="LOBPCG iterations the FP64 solve of this workload takes (for the reference arm's extrapolation)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="leaf3", choices=["leaf3", "batch", "warmstart", "dense"],
+                    help="leaf3 (the benchmarked workload) or one of the other measured configurations")
+    ap.add_argument("--n-train", type=int, default=4096)
+    ap.add_argument("--n-test", type=int, default=1024)
+    ap.add_argument("--epochs", type=int, default=200)
     ap.add_argument("--profile", action="store_true",
                     help="one mixed-precision solve of the first timed draw, no warm-up (for the ncu launch list)")
     args = ap.parse_args()
     if args.profile:
         print(json.dumps(profile_one(args)), flush=True)
+        return
+    if args.workload != "leaf3":
+        fn = {"batch": run_batch_workload, "warmstart": run_warmstart_workload, "dense": run_dense_workload}
+        print(json.dumps(fn[args.workload](args)), flush=True)
         return
     if args.warmup < 3:
         args.warmup = 3
