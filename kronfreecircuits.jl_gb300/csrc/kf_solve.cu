@@ -14,8 +14,8 @@
 // The block LOBPCG iteration (the reference calls the unvendored LOBPCGEigensolver 0.1.4): X
 // holds the Ritz vectors (a converged prefix is hard-locked), W the preconditioned residuals of
 // the active columns, P the previous update directions.  Per iteration [W P] is orthogonalised
-// against all of X (classical Gram-Schmidt, twice) and against itself by SVQB (drop directions
-// below a relative cutoff), H is applied to that basis, and Rayleigh-Ritz on
+// against all of X and against itself, twice: a classical Gram-Schmidt projection followed by
+// SVQB (directions below a relative cutoff dropped); H is applied to that basis, and Rayleigh-Ritz on
 // [X_active, W, P] gives the new active Ritz pairs; P is the [W P] part of the update.
 //
 // Precision (KF_PREC_MIXED): the bulk of the iterations run with FP32 blocks (FP32 applies,
@@ -170,10 +170,10 @@ static int ortho_against(kf_op *op, LobWork<T> &W, T *Zb, int k, const T *X, int
     int r = k;
     for (int pass = 0; pass < 2; ++pass) {
         if (wx > 0) {
-            for (int cgs = 0; cgs < 2; ++cgs) {
-                gram<T>(X, N, wx, cur, N, r, N, G, part, s);
-                update<T>(cur, N, r, X, N, wx, G, wx, -1.0, 1.0, N, s);
-            }
+            // one classical Gram-Schmidt projection per pass; with the SVQB between the two passes
+            // this is "twice is enough" against X
+            gram<T>(X, N, wx, cur, N, r, N, G, part, s);
+            update<T>(cur, N, r, X, N, wx, G, wx, -1.0, 1.0, N, s);
         }
         gram<T>(cur, N, r, cur, N, r, N, G, part, s);
         double *hG = W.hG.template as<double>();

@@ -128,10 +128,9 @@ def lobpcg_core(H, X, D, tol, maxiter, precond="ritz", eta=0.01, n_conv_check=No
             P = P[:, newly:]
         nl += newly
         na = w - nl
-        # orthogonalize [W P] against every column of X, then against itself (SVQB), twice
+        # orthogonalize [W P] against every column of X (one projection), then against itself (SVQB), twice
         Z = np.hstack([W, P])
         for _ in range(2):
-            Z = Z - X @ (X.T @ Z)
             Z = Z - X @ (X.T @ Z)
             Z = svqb(Z, cutoff)
         if Z.shape[1] == 0:
