@@ -252,6 +252,23 @@ def profile_one(args):
             "iterations_f64": st["iterations_f64"], "seconds_f64": st["seconds_f64"]}
 
 
+def run_apply_workload(args):
+    """The fused stencil apply alone on the three-mode leaf: 3 launches per precision after the
+    autotuner's first call (16 columns, inputs rotating over three blocks larger than L2)."""
+    import torch
+    from kfgpu import KronFreeOperator, circuits
+    ths = thetas()
+    dims, terms = circuits.three_mode_leaf(ths[args.warmup])
+    H = KronFreeOperator(dims, terms)
+    out = {"workload": "fused apply, three-mode leaf 41x256x64 (N=671,744), 16 columns"}
+    for f32 in (True, False):
+        t = measure_apply(torch, H, f32, b=16, reps=3)
+        by = 2 * H.N * 16 * (4 if f32 else 8)
+        out["apply_%s_us" % ("f32" if f32 else "f64")] = t * 1e6
+        out["apply_%s_gbs" % ("f32" if f32 else "f64")] = by / t / 1e9
+    return out
+
+
 def run_batch_workload(args):
     """Batched theta sweep: 512 fluxonium leaves (n ~ U{200..1600} on [-5 pi, 5 pi], 5-point stencil,
     keep 10) plus 64 chains of 2-4 leaves (g ~ U[0.01, 0.1] n_i n_{i+1}, parents keep 20), all leaves
@@ -432,7 +449,7 @@ def main():
     ap.add_argument("--ref-iters", type=int, default=570,
                     help="LOBPCG iterations the FP64 solve of this workload takes (for the reference arm's extrapolation)")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="leaf3", choices=["leaf3", "batch", "warmstart", "dense"],
+    ap.add_argument("--workload", default="leaf3", choices=["leaf3", "batch", "warmstart", "dense", "apply"],
                     help="leaf3 (the benchmarked workload) or one of the other measured configurations")
     ap.add_argument("--n-train", type=int, default=4096)
     ap.add_argument("--n-test", type=int, default=1024)
@@ -444,7 +461,8 @@ def main():
         print(json.dumps(profile_one(args)), flush=True)
         return
     if args.workload != "leaf3":
-        fn = {"batch": run_batch_workload, "warmstart": run_warmstart_workload, "dense": run_dense_workload}
+        fn = {"batch": run_batch_workload, "warmstart": run_warmstart_workload, "dense": run_dense_workload,
+              "apply": run_apply_workload}
         print(json.dumps(fn[args.workload](args)), flush=True)
         return
     if args.warmup < 3:

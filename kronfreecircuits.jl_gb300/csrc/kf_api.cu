@@ -5,6 +5,7 @@
 #include <limits>
 
 #include "kf_internal.h"
+#include "../../include/kfgpu_testing.h"
 
 namespace kf {
 void build_op(const kf_op_desc *desc, kf_op *op);
@@ -209,6 +210,36 @@ int kf_solve(kf_op *op, const kf_solver_opts *opts, int32_t m, const double *X0,
             throw;
         }
         if (stats) *stats = st;
+    });
+}
+
+// ---- test-only entry points (include/kfgpu_testing.h) ----------------------------------
+
+int kf_test_mode_product(int path, const float *X, float *Y, const double *A, int d, int64_t left, int64_t N,
+                         int64_t b, double alpha, double beta, void *stream) {
+    return guarded([&] {
+        KF_REQUIRE(X && Y && A, KF_EINVAL, "kf_test_mode_product: NULL argument");
+        KF_REQUIRE(d >= 1 && left >= 1 && N % d == 0 && (N / d) % left == 0, KF_EDIM,
+                   "kf_test_mode_product: N must be a multiple of d * left");
+        cudaStream_t s = (cudaStream_t)stream;
+        if (path == 1) {
+            kf::TcMatrix m = kf::tc_matrix_create(A, d, false);
+            kf::tc_mode_product(Y, N, X, N, m, left, N, b, alpha, beta, s);
+            const cudaError_t e = cudaStreamSynchronize(s);
+            kf::tc_matrix_free(m);
+            KF_CUDA(e);
+            if (const int t = kf::tc_take_error()) throw kf::Error(t, "tensor-core mode product: device wait timed out");
+        } else {
+            std::vector<float> a32((size_t)d * d);
+            for (size_t i = 0; i < a32.size(); ++i) a32[i] = (float)A[i];
+            float *dA = nullptr;
+            KF_CUDA(cudaMalloc(&dA, a32.size() * 4));
+            KF_CUDA(cudaMemcpy(dA, a32.data(), a32.size() * 4, cudaMemcpyHostToDevice));
+            kf::mode_product<float>(Y, N, X, N, dA, d, left, N, b, alpha, beta, s);
+            const cudaError_t e = cudaStreamSynchronize(s);
+            cudaFree(dA);
+            KF_CUDA(e);
+        }
     });
 }
 

@@ -94,29 +94,263 @@ __global__ void __launch_bounds__(GRAM_THREADS) k_gram(const T *__restrict__ A, 
     }
 }
 
-// out[e] = sum_c partials[c][e], e < n, in a fixed order
+// out[e] = sum_c partials[c][e], e < n, in a fixed order: one warp per entry, lane l summing
+// c = l, l + 32, ... , then a fixed shuffle tree
 __global__ void k_reduce_partials(const double *__restrict__ partials, int nparts, int n, double *__restrict__ out) {
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    const int e = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
     if (e >= n) return;
     double s = 0;
-    for (int c = 0; c < nparts; ++c) s += partials[(size_t)c * n + e];
-    out[e] = s;
+    for (int c = lane; c < nparts; c += 32) s += partials[(size_t)c * n + e];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) out[e] = s;
+}
+
+static void reduce_partials(const double *partials, int nparts, int n, double *out, cudaStream_t s) {
+    k_reduce_partials<<<(n + 7) / 8, 256, 0, s>>>(partials, nparts, n, out);
+    KF_LAUNCH_CHECK();
+}
+
+// ---- FP32 Gram: rows staged through shared memory, one 8 x 8 output tile per warp ----------
+//
+// A CTA owns a contiguous range of rows and one "group" of output tiles (at most 8 tiles of
+// 8 x 8, a rectangle gti x gtj of them).  Rows arrive in batches of `tr` (a multiple of 64, larger
+// for narrow blocks so that about 24 KB per stage is in flight) through a three-stage cp.async
+// pipeline, one column-major slab per operand in shared memory, so each element of A and B is
+// read from memory once per group.  Warp w works on tile w / wpt over the batch rows congruent to
+// its sub-index (wpt = warps per tile, when the group has fewer than 8 tiles); lane l takes every
+// 32nd of those rows.  Per row a lane loads 8 + 8 operands from shared memory (consecutive lanes,
+// consecutive rows: conflict-free) for 64 FMAs.  The lanes' FP32 sums meet in a butterfly
+// reduce-scatter (62 shuffles for 64 values; lane l ends with entries 2l and 2l + 1), the
+// sub-warps of a tile in FP64 in a fixed order, and the CTA's partial lands in
+// partials[cta][i + ka j] for the final fixed-order FP64 reduction.
+constexpr int G32_PAD = 4;          // column stride tr + G32_PAD floats (16-byte multiple)
+constexpr int G32_STAGES = 3;
+constexpr int G32_SMEM = 96 * 1024; // dynamic shared memory ceiling (two CTAs per SM)
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem, int src_bytes) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(sa), "l"(gmem), "r"(src_bytes));
+}
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem, int src_bytes) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(sa), "l"(gmem), "r"(src_bytes));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
+
+struct Gram32Shape {
+    int nti, ntj, gti, gtj, ngi, ngj;   // tiles per axis, group size in tiles, groups per axis
+    int tr;                             // rows per batch
+};
+
+static Gram32Shape gram32_shape(int ka, int kb) {
+    Gram32Shape g;
+    g.nti = (ka + 7) / 8;
+    g.ntj = (kb + 7) / 8;
+    g.gtj = g.ntj < 8 ? g.ntj : 8;
+    g.gti = 8 / g.gtj;
+    if (g.gti > g.nti) g.gti = g.nti;
+    g.ngi = (g.nti + g.gti - 1) / g.gti;
+    g.ngj = (g.ntj + g.gtj - 1) / g.gtj;
+    // ~24 KB of loads per stage, at most 512 rows, within the shared-memory ceiling
+    const int cols = 8 * (g.gti + g.gtj);
+    int tr = (24 * 1024 / (4 * cols)) / 64 * 64;
+    if (tr < 64) tr = 64;
+    if (tr > 512) tr = 512;
+    while (tr > 64 && (size_t)G32_STAGES * cols * (tr + G32_PAD) * 4 > (size_t)G32_SMEM) tr -= 64;
+    g.tr = tr;
+    return g;
+}
+
+static size_t gram32_smem(const Gram32Shape &g) {
+    return (size_t)G32_STAGES * 8 * (g.gti + g.gtj) * (g.tr + G32_PAD) * sizeof(float);
+}
+
+// stage rows [row0, row0 + tr) of `nc` columns (column c at src + c * ld) into dst (column
+// stride tr + G32_PAD); rows at or past `rend` are zero-filled
+template <bool VEC>
+__device__ __forceinline__ void g32_stage(float *dst, const float *src, int64_t ld, int nc, int tr, int64_t row0,
+                                          int64_t rend) {
+    const int S = tr + G32_PAD;
+    if (VEC) {
+        const int per = tr / 4;
+        for (int e = threadIdx.x; e < nc * per; e += blockDim.x) {
+            const int c = e / per, q = e % per;
+            const int64_t r = row0 + 4 * q;
+            const int64_t left = rend - r;
+            const int bytes = left >= 4 ? 16 : left > 0 ? (int)left * 4 : 0;
+            const float *g = src + (int64_t)c * ld + (bytes > 0 ? r : 0);
+            cp_async16(dst + c * S + 4 * q, g, bytes);
+        }
+    } else {
+        for (int e = threadIdx.x; e < nc * tr; e += blockDim.x) {
+            const int c = e / tr, q = e % tr;
+            const int64_t r = row0 + q;
+            const bool ok = r < rend;
+            cp_async4(dst + c * S + q, src + (int64_t)c * ld + (ok ? r : 0), ok ? 4 : 0);
+        }
+    }
+}
+
+// one reduce-scatter step: the lanes differing in bit O exchange halves of their first L values
+template <int O, int L>
+__device__ __forceinline__ void g32_butterfly(float *f, int lane) {
+    const bool upper = (lane & O) != 0;
+#pragma unroll
+    for (int k = 0; k < L / 2; ++k) {
+        const float send = upper ? f[k] : f[k + L / 2];
+        const float keep = upper ? f[k + L / 2] : f[k];
+        f[k] = keep + __shfl_xor_sync(0xffffffffu, send, O);
+    }
+}
+
+template <bool VEC>
+__global__ void __launch_bounds__(256, 2) k_gram32(const float *__restrict__ A, int64_t lda, int ka,
+                                                   const float *__restrict__ B, int64_t ldb, int kb, int64_t N,
+                                                   int64_t rows_per, Gram32Shape sh, double *__restrict__ partials) {
+    extern __shared__ __align__(16) unsigned char g32_smem[];
+    const int tr = sh.tr, S = tr + G32_PAD;
+    const int gi = blockIdx.y / sh.ngj, gj = blockIdx.y % sh.ngj;
+    const int ti0 = gi * sh.gti, tj0 = gj * sh.gtj;
+    const int gti = min(sh.gti, sh.nti - ti0), gtj = min(sh.gtj, sh.ntj - tj0);
+    const int ca0 = ti0 * 8, cb0 = tj0 * 8;
+    const int nca = min(gti * 8, ka - ca0), ncb = min(gtj * 8, kb - cb0);   // valid columns staged
+    const int sa = gti * 8, sb = gtj * 8;                                     // slab widths (padded)
+    float *const buf0 = reinterpret_cast<float *>(g32_smem);
+    const int bstride = (sa + sb) * S;   // stage t starts at buf0 + t * bstride
+    // padding columns stay zero in every stage
+    for (int e = threadIdx.x; e < G32_STAGES * bstride; e += blockDim.x) {
+        const int c = (e % bstride) / S;
+        if ((c < sa && c >= nca) || (c >= sa && c - sa >= ncb)) buf0[e] = 0.f;
+    }
+    const int ntile = gti * gtj;
+    const int wpt = 8 / ntile;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int tile = warp / wpt, sub = warp % wpt;
+    const bool active = tile < ntile;
+    const int ta = active ? (tile / gtj) * 8 : 0, tb = active ? (tile % gtj) * 8 : 0;
+
+    const int64_t r0 = (int64_t)blockIdx.x * rows_per;
+    const int64_t r1 = (r0 + rows_per < N) ? r0 + rows_per : N;
+    const int nb = (int)((r1 - r0 + tr - 1) / tr);
+    float acc[8][8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+#pragma unroll
+        for (int v = 0; v < 8; ++v) acc[u][v] = 0.f;
+
+    // prologue: stages 0 and 1 in flight (an empty commit group keeps the group count uniform)
+    for (int t = 0; t < G32_STAGES - 1; ++t) {
+        if (t < nb) {
+            float *st = buf0 + t * bstride;
+            const int64_t rn = r0 + (int64_t)t * tr;
+            g32_stage<VEC>(st, A + ca0 * lda, lda, nca, tr, rn, r1);
+            g32_stage<VEC>(st + sa * S, B + cb0 * ldb, ldb, ncb, tr, rn, r1);
+        }
+        cp_async_commit();
+    }
+    for (int b = 0; b < nb; ++b) {
+        // issue batch b + 2 into the stage batch b - 1 used (freed by the barrier ending b - 1)
+        const int bn = b + G32_STAGES - 1;
+        if (bn < nb) {
+            float *st = buf0 + (bn % G32_STAGES) * bstride;
+            const int64_t rn = r0 + (int64_t)bn * tr;
+            g32_stage<VEC>(st, A + ca0 * lda, lda, nca, tr, rn, r1);
+            g32_stage<VEC>(st + sa * S, B + cb0 * ldb, ldb, ncb, tr, rn, r1);
+        }
+        cp_async_commit();
+        cp_async_wait<G32_STAGES - 1>();   // batch b has landed (this thread's copies)
+        __syncthreads();                    // ... and everyone's
+        if (active) {
+            const float *cur = buf0 + (b % G32_STAGES) * bstride;
+            const float *As = cur + ta * S, *Bs = cur + (sa + tb) * S;
+            for (int q = sub * 32 + lane; q < tr; q += 32 * wpt) {
+                float a[8], bv[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) a[u] = As[u * S + q];
+#pragma unroll
+                for (int v = 0; v < 8; ++v) bv[v] = Bs[v * S + q];
+#pragma unroll
+                for (int u = 0; u < 8; ++u)
+#pragma unroll
+                    for (int v = 0; v < 8; ++v) acc[u][v] = fmaf(a[u], bv[v], acc[u][v]);
+            }
+        }
+        __syncthreads();
+    }
+    cp_async_wait<0>();
+    // butterfly reduce-scatter over the 32 lanes: lane l ends with flattened entries 2l, 2l + 1
+    float *f = &acc[0][0];
+    g32_butterfly<16, 64>(f, lane);
+    g32_butterfly<8, 32>(f, lane);
+    g32_butterfly<4, 16>(f, lane);
+    g32_butterfly<2, 8>(f, lane);
+    g32_butterfly<1, 4>(f, lane);
+    double *red = reinterpret_cast<double *>(g32_smem);   // [warp][64], staging no longer needed
+    if (active) {
+        red[warp * 64 + 2 * lane] = (double)f[0];
+        red[warp * 64 + 2 * lane + 1] = (double)f[1];
+    }
+    __syncthreads();
+    double *P = partials + (size_t)blockIdx.x * ka * kb;
+    for (int e = threadIdx.x; e < ntile * 64; e += blockDim.x) {
+        const int t = e / 64, idx = e % 64, u = idx / 8, v = idx % 8;
+        const int i = ca0 + (t / gtj) * 8 + u, j = cb0 + (t % gtj) * 8 + v;
+        if (i >= ka || j >= kb) continue;
+        double s = 0;
+        for (int w = 0; w < wpt; ++w) s += red[(t * wpt + w) * 64 + idx];
+        P[i + (size_t)ka * j] = s;
+    }
 }
 
 template <typename T>
 void gram(const T *A, int64_t lda, int ka, const T *B, int64_t ldb, int kb, int64_t N, double *G, double *partials,
           cudaStream_t s) {
     KF_REQUIRE(ka >= 1 && kb >= 1 && ka <= 128 && kb <= 128, KF_EINVAL, "gram: block widths out of range");
-    // output chunks of RI x RJ (FP64: 4 x 8, FP32: 8 x 8 accumulators per thread)
-    constexpr int RI = sizeof(T) == 8 ? 4 : 8, RJ = 8;
+    if constexpr (sizeof(T) == 4) {
+        const Gram32Shape sh = gram32_shape(ka, kb);
+        const int groups = sh.ngi * sh.ngj;
+        // about 2 CTAs per SM over all groups, whole batches per CTA, never more row blocks than
+        // gram_partials_size provides for
+        int64_t target = (304 + groups - 1) / groups;
+        int64_t rp = (N + target - 1) / target;
+        if (rp < 256) rp = 256;
+        rp = (rp + sh.tr - 1) / sh.tr * sh.tr;
+        const int nc = (int)((N + rp - 1) / rp);
+        const size_t smem = gram32_smem(sh);
+        const bool vec = (lda % 4 == 0) && (ldb % 4 == 0) && ((uintptr_t)A % 16 == 0) && ((uintptr_t)B % 16 == 0);
+        static int attr_dev_mask[2] = {0, 0};   // devices whose kernel attribute is set, per variant
+        int dev = 0;
+        KF_CUDA(cudaGetDevice(&dev));
+        if (dev < 31 && !(attr_dev_mask[vec] & (1 << dev))) {
+            if (vec)
+                KF_CUDA(cudaFuncSetAttribute(k_gram32<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, G32_SMEM));
+            else
+                KF_CUDA(cudaFuncSetAttribute(k_gram32<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, G32_SMEM));
+            attr_dev_mask[vec] |= 1 << dev;
+        }
+        if (vec)
+            k_gram32<true><<<dim3(nc, groups), 256, smem, s>>>((const float *)A, lda, ka, (const float *)B, ldb, kb, N,
+                                                               rp, sh, partials);
+        else
+            k_gram32<false><<<dim3(nc, groups), 256, smem, s>>>((const float *)A, lda, ka, (const float *)B, ldb, kb,
+                                                                N, rp, sh, partials);
+        KF_LAUNCH_CHECK();
+        reduce_partials(partials, nc, ka * kb, G, s);
+        return;
+    }
+    // FP64: output chunks of 4 x 8 accumulators per thread
+    constexpr int RI = 4, RJ = 8;
     const int chunks = ((ka + RI - 1) / RI) * ((kb + RJ - 1) / RJ);
     const int64_t rp = gram_rows_per_cta(N, chunks);
     const int nc = num_ctas_for(N, rp);
     k_gram<T, RI, RJ><<<dim3(nc, chunks), GRAM_THREADS, 0, s>>>(A, lda, ka, B, ldb, kb, N, rp, partials);
     KF_LAUNCH_CHECK();
     const int n = ka * kb;
-    k_reduce_partials<<<(n + 255) / 256, 256, 0, s>>>(partials, nc, n, G);
-    KF_LAUNCH_CHECK();
+    reduce_partials(partials, nc, n, G, s);
 }
 
 // Y[r, j] = alpha * sum_i X[r, i] C[i, j] + beta * Y[r, j], one thread per row and a chunk of
@@ -154,6 +388,48 @@ __global__ void k_update(T *__restrict__ Y, int64_t ldy, int ky, const T *__rest
     }
 }
 
+// The same product with the row's kx operands loaded into registers first (all loads in flight
+// together) and C read from shared memory as UC-wide vectors (broadcast across the warp); C is
+// padded to a multiple of UC columns with zeros.  For kx <= KX.
+template <typename T, int KX, int UC>
+__global__ void __launch_bounds__(256) k_update_reg(T *__restrict__ Y, int64_t ldy, int ky, const T *__restrict__ X,
+                                                    int64_t ldx, int kx, const double *__restrict__ C, int ldc,
+                                                    T alpha, T beta, int64_t N) {
+    extern __shared__ __align__(16) unsigned char smem_raw_reg[];
+    T *Cs = reinterpret_cast<T *>(smem_raw_reg);   // [kx][kyp]
+    const int kyp = (ky + UC - 1) / UC * UC;
+    for (int e = threadIdx.x; e < kx * kyp; e += blockDim.x) {
+        const int i = e / kyp, j = e % kyp;
+        Cs[e] = j < ky ? (T)C[i + (size_t)ldc * j] : T(0);
+    }
+    __syncthreads();
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= N) return;
+    T x[KX];
+#pragma unroll
+    for (int i = 0; i < KX; ++i) x[i] = (i < kx) ? X[r + (int64_t)i * ldx] : T(0);
+    for (int j0 = 0; j0 < ky; j0 += UC) {
+        T acc[UC];
+#pragma unroll
+        for (int v = 0; v < UC; ++v) acc[v] = T(0);
+#pragma unroll
+        for (int i = 0; i < KX; ++i) {
+            if (i < kx) {
+                const T *cr = Cs + i * kyp + j0;
+#pragma unroll
+                for (int v = 0; v < UC; ++v) acc[v] = fma(x[i], cr[v], acc[v]);
+            }
+        }
+#pragma unroll
+        for (int v = 0; v < UC; ++v) {
+            if (j0 + v < ky) {
+                T *yp = Y + r + (int64_t)(j0 + v) * ldy;
+                *yp = (beta == T(0)) ? alpha * acc[v] : alpha * acc[v] + beta * *yp;
+            }
+        }
+    }
+}
+
 template <typename T>
 void update(T *Y, int64_t ldy, int ky, const T *X, int64_t ldx, int kx, const double *C, int ldc, double alpha,
             double beta, int64_t N, cudaStream_t s) {
@@ -165,9 +441,27 @@ void update(T *Y, int64_t ldy, int ky, const T *X, int64_t ldx, int kx, const do
             for (int j = 0; j < ky; ++j) KF_CUDA(cudaMemsetAsync(Y + (int64_t)j * ldy, 0, N * sizeof(T), s));
         return;
     }
+    const unsigned grid = (unsigned)((N + 255) / 256);
+    constexpr int UC = sizeof(T) == 8 ? 4 : 8;
+    const int kyp = (ky + UC - 1) / UC * UC;
+    const size_t smr = (size_t)kx * kyp * sizeof(T);
+    const int kxmax = sizeof(T) == 8 ? 32 : 64;
+    if (kx <= kxmax && smr <= 48 * 1024) {
+        const T a = (T)alpha, b = (T)beta;
+        if (kx <= 8)
+            k_update_reg<T, 8, UC><<<grid, 256, smr, s>>>(Y, ldy, ky, X, ldx, kx, C, ldc, a, b, N);
+        else if (kx <= 16)
+            k_update_reg<T, 16, UC><<<grid, 256, smr, s>>>(Y, ldy, ky, X, ldx, kx, C, ldc, a, b, N);
+        else if (kx <= 32)
+            k_update_reg<T, 32, UC><<<grid, 256, smr, s>>>(Y, ldy, ky, X, ldx, kx, C, ldc, a, b, N);
+        else
+            k_update_reg<T, (sizeof(T) == 8 ? 32 : 64), UC><<<grid, 256, smr, s>>>(Y, ldy, ky, X, ldx, kx, C, ldc, a,
+                                                                                   b, N);
+        KF_LAUNCH_CHECK();
+        return;
+    }
     const size_t sm = (size_t)kx * ky * sizeof(T);
     KF_REQUIRE(sm <= 200 * 1024, KF_EINVAL, "update: coefficient matrix too large");
-    const unsigned grid = (unsigned)((N + 255) / 256);
     if (sm > 48 * 1024) {
         if (sizeof(T) == 8)
             KF_CUDA(cudaFuncSetAttribute(k_update<T, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
@@ -286,6 +580,73 @@ void residual_precond(const T *X, const T *HX, int64_t ld, int k, int64_t N, con
     k_residual_precond<T><<<grid, RED_THREADS, 0, s>>>(X, HX, ld, N, rp, theta, thetap, D, eta, mode, R, ldr, partials);
     KF_LAUNCH_CHECK();
     k_reduce_cols<<<(k + 127) / 128, 128, 0, s>>>(partials, nblk, k, norms2);
+    KF_LAUNCH_CHECK();
+}
+
+// Refinement-phase residual: R = HX - X theta from the FP64 iterate, its FP64 squared norms,
+// and two FP32 blocks: R itself (for the Rayleigh-Ritz blocks) and, unless Wout is null, the
+// preconditioned direction (mode 0: / hypot(D - theta, eta), mode 1: / (D - sigma)) computed in
+// FP32 -- the preconditioner only steers the search directions.
+__global__ void k_residual_mixed(const double *__restrict__ X, const double *__restrict__ HX, int64_t ld, int64_t N,
+                                 int64_t rows_per, const double *__restrict__ theta,
+                                 const double *__restrict__ thetap, const double *__restrict__ D, double eta, int mode,
+                                 float *__restrict__ R, int64_t ldr, float *__restrict__ Wout, int64_t ldw,
+                                 double *__restrict__ partials) {
+    __shared__ double red[32];
+    const int col = blockIdx.y;
+    const int64_t r0 = (int64_t)blockIdx.x * rows_per;
+    const int64_t r1 = (r0 + rows_per < N) ? r0 + rows_per : N;
+    const double th = theta[col];
+    const float tp = (float)((mode == 0) ? thetap[col] : (mode == 1 ? thetap[0] : 0.0));
+    const float et = (float)eta;
+    const double *x = X + (int64_t)col * ld;
+    const double *hx = HX + (int64_t)col * ld;
+    float *rr = R + (int64_t)col * ldr;
+    float *ww = Wout ? Wout + (int64_t)col * ldw : nullptr;
+    double s = 0;
+    for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+        const double v = hx[r] - th * x[r];
+        s += v * v;
+        const float vf = (float)v;
+        rr[r] = vf;
+        if (ww) {
+            const float d = (float)D[r] - tp;
+            ww[r] = mode == 0 ? vf / hypotf(d, et) : mode == 1 ? vf / d : vf;
+        }
+    }
+    const double t = block_sum(s, red);
+    if (threadIdx.x == 0) partials[(size_t)col * gridDim.x + blockIdx.x] = t;
+}
+
+void residual_mixed(const double *X, const double *HX, int64_t ld, int k, int64_t N, const double *theta,
+                    const double *thetap, const double *D, double eta, int mode, float *R, int64_t ldr, float *W,
+                    int64_t ldw, double *norms2, double *partials, cudaStream_t s) {
+    if (k <= 0) return;
+    const int64_t rp = red_rows_per(N, k);
+    const int nblk = (int)((N + rp - 1) / rp);
+    k_residual_mixed<<<dim3(nblk, k), RED_THREADS, 0, s>>>(X, HX, ld, N, rp, theta, thetap, D, eta, mode, R, ldr, W,
+                                                           ldw, partials);
+    KF_LAUNCH_CHECK();
+    k_reduce_cols<<<(k + 127) / 128, 128, 0, s>>>(partials, nblk, k, norms2);
+    KF_LAUNCH_CHECK();
+}
+
+// Y64 += (double) P32 column by column; Y32 (optional) receives the FP32 rounding of the sum
+__global__ void k_add_f32_into_f64(double *__restrict__ Y, int64_t ldy, const float *__restrict__ P, int64_t ldp,
+                                   float *__restrict__ Y32, int64_t ld32, int64_t N, int64_t total) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= total) return;
+    const int64_t c = t / N, r = t % N;
+    const double v = Y[r + c * ldy] + (double)P[r + c * ldp];
+    Y[r + c * ldy] = v;
+    if (Y32) Y32[r + c * ld32] = (float)v;
+}
+
+void add_f32_into_f64(double *Y, int64_t ldy, const float *P, int64_t ldp, float *Y32, int64_t ld32, int k, int64_t N,
+                      cudaStream_t s) {
+    if (k <= 0 || N <= 0) return;
+    const int64_t total = N * k;
+    k_add_f32_into_f64<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(Y, ldy, P, ldp, Y32, ld32, N, total);
     KF_LAUNCH_CHECK();
 }
 

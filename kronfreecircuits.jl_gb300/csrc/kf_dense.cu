@@ -116,7 +116,9 @@ template void mode_product<double>(double *, int64_t, const double *, int64_t, c
                                    int64_t, double, double, cudaStream_t);
 
 // W[:, j] <- W[:, j] / hypot(S(p) - theta_j, eta) with S(p) = sum_a lam_a[i_a(p)] (the separable
-// spectrum evaluated from per-axis eigenvalues, no N-sized table).
+// spectrum evaluated from per-axis eigenvalues, no N-sized table).  The sum is FP64 (S and theta
+// are close where it matters); the scale is FP32 -- it only steers the search directions, and
+// GB300's FP64 hypot / divide rate would make this pass FP64-bound.
 template <typename T>
 __global__ void k_sep_scale(T *__restrict__ W, int64_t ld, int64_t N, int k, int ndims, const int *__restrict__ dims,
                             const double *__restrict__ lam, const int *__restrict__ lam_off,
@@ -125,14 +127,14 @@ __global__ void k_sep_scale(T *__restrict__ W, int64_t ld, int64_t N, int k, int
     if (t >= N * k) return;
     const int64_t c = t / N, p = t % N;
     int64_t rem = p;
-    double S = 0;
+    double S = -theta[c];
     for (int a = 0; a < ndims; ++a) {
         const int i = (int)(rem % dims[a]);
         rem /= dims[a];
         S += lam[lam_off[a] + i];
     }
-    const double f = 1.0 / hypot(S - theta[c], eta);
-    W[c * ld + p] = (T)((double)W[c * ld + p] * f);
+    const float f = 1.0f / hypotf((float)S, (float)eta);
+    W[c * ld + p] = W[c * ld + p] * (T)f;
 }
 
 template <typename T>

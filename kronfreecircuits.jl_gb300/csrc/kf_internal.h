@@ -88,6 +88,20 @@ struct ChainTerm {
     std::vector<ChainFactor> f;
 };
 
+// tensor-core mode products (kf_tc.cu): a d x d operator (d <= 256) as a BF16 image in the
+// tcgen05 K-major shared-memory layout, rows padded to Mp (128 or 256), columns to Kp
+struct TcMatrix {
+    void *img = nullptr;
+    int d = 0, Mp = 0, Kp = 0;
+};
+int tc_mode_layout_ok(int d);
+TcMatrix tc_matrix_create(const double *A, int d, bool transpose);
+void tc_matrix_free(TcMatrix &m);
+size_t tc_mode_smem(const TcMatrix &m);
+void tc_mode_product(float *Y, int64_t ldy, const float *X, int64_t ldx, const TcMatrix &A, int64_t left, int64_t N,
+                     int64_t b, double alpha, double beta, cudaStream_t s);
+int tc_take_error();   // a pending device-side timeout (KF_ETIMEOUT) of a tensor-core launch, cleared
+
 }  // namespace kf
 
 // The operator handle.
@@ -131,6 +145,7 @@ struct kf_op {
         std::vector<int> ident;               // axis whose sum is diagonal (U = I)
         std::vector<double> lam;              // concatenated per-axis eigenvalues
         std::vector<float *> dU, dUt;         // FP32 U and U' per axis (nullptr when ident)
+        std::vector<kf::TcMatrix> tU, tUt;    // the same as tensor-core BF16 images (d <= 256)
         double *d_lam = nullptr;
         int *d_lam_off = nullptr, *d_dims = nullptr;
     } sep;
@@ -147,6 +162,12 @@ void launch_apply(kf_op *op, bool f32, const void *X, void *Y, int64_t ldx, int6
 template <typename T>
 void gram(const T *A, int64_t lda, int ka, const T *B, int64_t ldb, int kb, int64_t N, double *G_dev,
           double *partials, cudaStream_t s);                 // G = A' B (ka x kb, column-major, FP64)
+// refinement phase: FP64 iterate, FP32 residual / directions
+void residual_mixed(const double *X, const double *HX, int64_t ld, int k, int64_t N, const double *theta,
+                    const double *thetap, const double *D, double eta, int mode, float *R, int64_t ldr, float *W,
+                    int64_t ldw, double *norms2, double *partials, cudaStream_t s);
+void add_f32_into_f64(double *Y, int64_t ldy, const float *P, int64_t ldp, float *Y32, int64_t ld32, int k, int64_t N,
+                      cudaStream_t s);
 size_t gram_partials_size(int ka, int kb, int64_t N);
 template <typename T>
 void update(T *Y, int64_t ldy, int ky, const T *X, int64_t ldx, int kx, const double *C_dev, int ldc,

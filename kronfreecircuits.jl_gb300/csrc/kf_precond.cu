@@ -5,7 +5,8 @@
 // for LOBPCG.  The coupling terms (products over two or more axes) are left out, so P inverts the
 // stiff single-axis kinetic parts exactly (the 1/Delta^2 finite-difference stencils that make
 // ||H|| large) and the coupling only shifts the spectrum.  Each application costs 2 mode products
-// per non-diagonal axis (tiled GEMMs, FP32) and one scaling pass.
+// per non-diagonal axis (tcgen05 tensor-core GEMMs with BF16 operands for axes up to 256 long,
+// SIMT FP32 beyond) and one scaling pass.
 #include <cstring>
 
 #include "kf_internal.h"
@@ -20,6 +21,8 @@ void sep_prepare(kf_op *op) {
     S.ident.assign(nd, 0);
     S.dU.assign(nd, nullptr);
     S.dUt.assign(nd, nullptr);
+    S.tU.assign(nd, TcMatrix());
+    S.tUt.assign(nd, TcMatrix());
     std::vector<int> off(nd), dims(nd);
     S.lam.clear();
     for (int a = 0; a < nd; ++a) {
@@ -50,6 +53,10 @@ void sep_prepare(kf_op *op) {
         KF_CUDA(cudaMalloc(&S.dUt[a], ut32.size() * 4));
         KF_CUDA(cudaMemcpy(S.dU[a], u32.data(), u32.size() * 4, cudaMemcpyHostToDevice));
         KF_CUDA(cudaMemcpy(S.dUt[a], ut32.data(), ut32.size() * 4, cudaMemcpyHostToDevice));
+        if (tc_mode_layout_ok(d)) {
+            S.tU[a] = tc_matrix_create(U.data(), d, false);
+            S.tUt[a] = tc_matrix_create(U.data(), d, true);
+        }
     }
     KF_CUDA(cudaMalloc(&S.d_lam, S.lam.size() * 8));
     KF_CUDA(cudaMalloc(&S.d_lam_off, nd * sizeof(int)));
@@ -66,17 +73,21 @@ float *sep_apply(kf_op *op, float *W, float *s1, int k, const double *theta_dev,
     const int nd = (int)op->dims.size();
     const int64_t N = op->N;
     float *cur = W, *other = s1;
-    for (int a = 0; a < nd; ++a) {
-        if (S.ident[a]) continue;
-        mode_product<float>(other, N, cur, N, S.dUt[a], (int)op->dims[a], op->strides[a], N, k, 1.0, 0.0, s);
+    // tensor cores (BF16 operands, FP32 sums) where the axis fits the tcgen05 image, else SIMT FP32
+    auto product = [&](int a, bool forward) {
+        const TcMatrix &t = forward ? S.tUt[a] : S.tU[a];
+        if (t.img)
+            tc_mode_product(other, N, cur, N, t, op->strides[a], N, k, 1.0, 0.0, s);
+        else
+            mode_product<float>(other, N, cur, N, forward ? S.dUt[a] : S.dU[a], (int)op->dims[a], op->strides[a], N,
+                                k, 1.0, 0.0, s);
         std::swap(cur, other);
-    }
+    };
+    for (int a = 0; a < nd; ++a)
+        if (!S.ident[a]) product(a, true);
     sep_scale<float>(cur, N, N, k, nd, S.d_dims, S.d_lam, S.d_lam_off, theta_dev, eta, s);
-    for (int a = nd - 1; a >= 0; --a) {
-        if (S.ident[a]) continue;
-        mode_product<float>(other, N, cur, N, S.dU[a], (int)op->dims[a], op->strides[a], N, k, 1.0, 0.0, s);
-        std::swap(cur, other);
-    }
+    for (int a = nd - 1; a >= 0; --a)
+        if (!S.ident[a]) product(a, false);
     return cur;
 }
 

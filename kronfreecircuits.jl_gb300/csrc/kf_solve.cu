@@ -152,6 +152,7 @@ template <typename T>
 static void d2h_sync(double *h, const double *d, size_t n, cudaStream_t s) {
     KF_CUDA(cudaMemcpyAsync(h, d, n * sizeof(double), cudaMemcpyDeviceToHost, s));
     KF_CUDA(cudaStreamSynchronize(s));
+    if (const int e = tc_take_error()) throw Error(e, "a tensor-core mode product timed out on the device");
 }
 
 static void h2d(double *d, const double *h, size_t n, cudaStream_t s) {
@@ -382,6 +383,200 @@ static LobOut lobpcg_run(kf_op *op, LobWork<T> &Wk, const double *D, const LobPa
 }
 
 // ------------------------------------------------------------------------------------------
+// Mixed-precision refinement: the FP64 phase of precision = mixed.
+//
+// GB300 runs FP64 arithmetic at about 1/64 of its FP32 rate, so FP64 is kept to what sets the
+// final accuracy: the iterate X and HX (FP64), the residual R = HX - X theta and its norms (FP64),
+// and the X-part of each update (X C_x, HX C_x).  The search block Z = [W P], its orthogonalisation
+// against X (through an FP32 copy of X), H Z, and the Rayleigh-Ritz blocks are FP32.  Every FP32
+// rounding then enters the next iterate multiplied by the correction coefficients C_z, which
+// shrink with the residual, so the iteration converges to FP64 accuracy (mixed-precision
+// iterative refinement):
+//   A_xx = X_a' H X_a = theta + X_a' R          (X' X = I in FP64; X_a' R from FP32 blocks)
+//   A_xz = X_a' H Z   = theta X_a' Z + R' Z  ~  R' Z
+// Dropping theta X_a' Z (FP32-small, since Z is orthogonalised against X) is the exact
+// Rayleigh-Ritz for the basis [X_a, Z - X_a (X_a' Z)], whose X-part differs from the update
+// actually formed by X_a (X_a' Z) C_z -- again proportional to C_z.
+// Locking, guards, the convergence count and the final FP64 acceptance are those of the FP64
+// phase (src/lobpcg.jl:217-301).
+struct RefineWork {
+    int64_t N;
+    int w;
+    DevMem X, HX, Xn, HXn, R32, T32;
+    RefineWork(int64_t N_, int w_)
+        : N(N_), w(w_), X((size_t)N_ * w_ * sizeof(double)), HX((size_t)N_ * w_ * sizeof(double)),
+          Xn((size_t)N_ * w_ * sizeof(double)), HXn((size_t)N_ * w_ * sizeof(double)),
+          R32((size_t)N_ * w_ * sizeof(float)), T32((size_t)N_ * w_ * sizeof(float)) {}
+};
+
+// X64 (in R.X) on entry: orthonormalise it in FP64, H X64 with a fresh FP64 apply, Rayleigh-Ritz
+// in FP64; leaves X, HX, theta and the FP32 copy W32.X consistent.
+static void refine_start(kf_op *op, RefineWork &R, LobWork<float> &W32, double cutoff, cudaStream_t s,
+                         std::vector<double> &theta, int64_t &nmv) {
+    const int64_t N = R.N;
+    const int w = R.w;
+    double *X = R.X.as<double>(), *HX = R.HX.as<double>(), *Xn = R.Xn.as<double>(), *HXn = R.HXn.as<double>();
+    double *G = W32.dG.as<double>(), *C = W32.dC.as<double>(), *part = W32.dpart.as<double>();
+    double *hG = W32.hG.as<double>(), *hC = W32.hC.as<double>();
+    gram<double>(X, N, w, X, N, w, N, G, part, s);
+    d2h_sync<double>(hG, G, (size_t)w * w, s);
+    std::vector<double> Tc;
+    const int r = svqb_coeffs(w, hG, cutoff, Tc);
+    if (r < w) throw Error(KF_EBREAKDOWN, "LOBPCG: the refinement block is numerically rank deficient");
+    std::memcpy(hC, Tc.data(), sizeof(double) * (size_t)w * w);
+    h2d(C, hC, (size_t)w * w, s);
+    update<double>(Xn, N, w, X, N, w, C, w, 1.0, 0.0, N, s);
+    launch_apply(op, false, Xn, HXn, N, N, w, 1, 0, nullptr, 0, 0, s);
+    nmv += w;
+    gram<double>(Xn, N, w, HXn, N, w, N, G, part, s);
+    d2h_sync<double>(hG, G, (size_t)w * w, s);
+    theta.assign(w, 0.0);
+    std::vector<double> V((size_t)w * w);
+    if (sym_eig(w, hG, w, theta.data(), V.data(), w) != 0)
+        throw Error(KF_EBREAKDOWN, "LOBPCG: Rayleigh-Ritz eigenproblem did not converge");
+    std::memcpy(hC, V.data(), sizeof(double) * w * w);
+    h2d(C, hC, (size_t)w * w, s);
+    update<double>(X, N, w, Xn, N, w, C, w, 1.0, 0.0, N, s);
+    update<double>(HX, N, w, HXn, N, w, C, w, 1.0, 0.0, N, s);
+    convert<double, float>(X, N, W32.X.as<float>(), N, w, N, s);
+}
+
+static LobOut lobpcg_refine(kf_op *op, RefineWork &Rw, LobWork<float> &Wk, const double *D, const LobParams &prm,
+                            cudaStream_t s, std::vector<double> &theta) {
+    const int64_t N = Wk.N;
+    const int w = Wk.w;
+    LobOut out;
+    refine_start(op, Rw, Wk, 1e-12, s, theta, out.nmv);
+    double *X = Rw.X.as<double>(), *HX = Rw.HX.as<double>();
+    double *Xn = Rw.Xn.as<double>(), *HXn = Rw.HXn.as<double>();
+    float *X32 = Wk.X.as<float>();
+    float *R32 = Rw.R32.as<float>(), *T32 = Rw.T32.as<float>();
+    float *Z = Wk.Z.as<float>(), *HZ = Wk.HZ.as<float>(), *Zt = Wk.Zt.as<float>(), *Pn = Wk.Pn.as<float>();
+    double *G = Wk.dG.as<double>(), *C = Wk.dC.as<double>();
+    double *part = Wk.dpart.as<double>();
+    double *hG = Wk.hG.as<double>(), *hC = Wk.hC.as<double>();
+    double *dth = Wk.dth.as<double>(), *dthp = Wk.dthp.as<double>();
+    double *dnorm = Wk.dnorm.as<double>();
+    double *hv = Wk.hv.as<double>();
+
+    std::vector<double> res(w, INFINITY);
+    int nl = 0, np = 0;
+    for (int it = 0;; ++it) {
+        const int na = w - nl;
+        std::memcpy(hv, theta.data() + nl, sizeof(double) * na);
+        h2d(dth, hv, na, s);
+        h2d(dthp, hv, na, s);
+        if (prm.precond == KF_PRECOND_JACOBI) {
+            double dmin = op->h_fulldiag.empty() ? 0.0
+                                                 : *std::min_element(op->h_fulldiag.begin(), op->h_fulldiag.end());
+            double sig = dmin - 1.0;
+            h2d(dthp, &sig, 1, s);
+        }
+        const int mode = prm.precond == KF_PRECOND_RITZ ? 0 : prm.precond == KF_PRECOND_JACOBI ? 1 : 2;
+        residual_mixed(X + (int64_t)nl * N, HX + (int64_t)nl * N, N, na, N, dth, dthp, D, prm.eta, mode, R32, N, Z, N,
+                       dnorm, part, s);
+        d2h_sync<double>(hv + w, dnorm, na, s);
+        for (int j = 0; j < na; ++j) res[nl + j] = std::sqrt(hv[w + j]);
+        int newly = 0;
+        while (nl + newly < w && res[nl + newly] <= prm.lock_tol) ++newly;
+        if (newly > 0) {
+            copy_block<double>(X + (int64_t)nl * N, N, Xn + (int64_t)nl * N, N, newly, N, s);
+            copy_block<double>(HX + (int64_t)nl * N, N, HXn + (int64_t)nl * N, N, newly, N, s);
+        }
+        out.iters = it;
+        if (nl + newly >= prm.n_conv_check) {
+            nl += newly;
+            out.converged = true;
+            break;
+        }
+        double worst = 0, bestr = INFINITY;
+        for (int j = nl; j < w; ++j) {
+            worst = std::max(worst, res[j]);
+            bestr = std::min(bestr, res[j]);
+        }
+        if (trace_on())
+            std::fprintf(stderr, "kf lobpcg refine it=%d locked=%d(+%d) active_resid=[%.3e, %.3e]\n", it, nl, newly,
+                         bestr, worst);
+        if (!std::isfinite(worst)) throw Error(KF_ENOTFINITE, "LOBPCG: the residual block is not finite");
+        if (it >= prm.maxiter) break;
+        const int na2 = na - newly;
+        float *Wb = Z + (int64_t)newly * N;
+        if (prm.precond == KF_PRECOND_SEPARABLE && na2 > 0) {
+            const double eta_s = std::max(prm.eta, 1e-3 * std::fabs(op->gershgorin));
+            float *f1 = Wk.F1.as<float>();
+            float *outp = sep_apply(op, Wb, f1, na2, dth + newly, eta_s, s);
+            if (outp != Wb) copy_block<float>(outp, N, Wb, N, na2, N, s);
+        }
+        int nz = na2;
+        if (np > 0) {
+            const int np2 = np - newly;
+            if (np2 > 0) {
+                copy_block<float>(Pn + (int64_t)newly * N, N, Wb + (int64_t)na2 * N, N, np2, N, s);
+                nz += np2;
+            }
+        }
+        nl += newly;
+        float *Q = nullptr;
+        // the FP32 blocks' Gram eigenvalues below 1e-6 of the largest are rounding noise
+        const int k = ortho_against<float>(op, Wk, Wb, nz, X32, w, Zt, Q, 1e-6, s);
+        if (k == 0) throw Error(KF_EBREAKDOWN, "LOBPCG: the search directions vanished");
+        launch_apply(op, true, Q, HZ, N, N, k, 1, 0, nullptr, 0, 0, s);
+        out.nmv += k;
+        // Rayleigh-Ritz on [X_a, Q]: X_a' R, R' Q and Q' H Q, one transfer
+        const int na3 = w - nl;
+        const int ns = na3 + k;
+        const float *Ra = R32 + (int64_t)newly * N;
+        const float *Xa32 = X32 + (int64_t)nl * N;
+        double *G1 = G, *G2 = G + (size_t)na3 * na3, *G3 = G2 + (size_t)na3 * k;
+        gram<float>(Xa32, N, na3, Ra, N, na3, N, G1, part, s);
+        gram<float>(Ra, N, na3, Q, N, k, N, G2, part, s);
+        gram<float>(Q, N, k, HZ, N, k, N, G3, part, s);
+        d2h_sync<double>(hG, G, (size_t)na3 * na3 + (size_t)na3 * k + (size_t)k * k, s);
+        const double *h1 = hG, *h2 = hG + (size_t)na3 * na3, *h3 = h2 + (size_t)na3 * k;
+        std::vector<double> A((size_t)ns * ns);
+        for (int j = 0; j < na3; ++j)
+            for (int i = 0; i < na3; ++i)
+                A[i + (size_t)ns * j] = 0.5 * (h1[i + (size_t)na3 * j] + h1[j + (size_t)na3 * i]) +
+                                        (i == j ? theta[nl + i] : 0.0);
+        for (int j = 0; j < k; ++j)
+            for (int i = 0; i < na3; ++i) {
+                A[i + (size_t)ns * (na3 + j)] = h2[i + (size_t)na3 * j];
+                A[(na3 + j) + (size_t)ns * i] = h2[i + (size_t)na3 * j];
+            }
+        for (int j = 0; j < k; ++j)
+            for (int i = 0; i < k; ++i)
+                A[(na3 + i) + (size_t)ns * (na3 + j)] = 0.5 * (h3[i + (size_t)k * j] + h3[j + (size_t)k * i]);
+        std::vector<double> lam(ns), V((size_t)ns * ns);
+        if (sym_eig(ns, A.data(), ns, lam.data(), V.data(), ns) != 0)
+            throw Error(KF_EBREAKDOWN, "LOBPCG: Rayleigh-Ritz eigenproblem did not converge");
+        std::memcpy(hC, V.data(), sizeof(double) * (size_t)ns * na3);
+        h2d(C, hC, (size_t)ns * na3, s);
+        // X_a <- X_a C_x (FP64) + Q C_z (FP32); HX_a likewise with H Q; P <- Q C_z
+        double *Xa = X + (int64_t)nl * N, *HXa = HX + (int64_t)nl * N;
+        double *Xna = Xn + (int64_t)nl * N, *HXna = HXn + (int64_t)nl * N;
+        update<double>(Xna, N, na3, Xa, N, na3, C, ns, 1.0, 0.0, N, s);
+        update<float>(Pn, N, na3, Q, N, k, C + na3, ns, 1.0, 0.0, N, s);
+        add_f32_into_f64(Xna, N, Pn, N, X32 + (int64_t)nl * N, N, na3, N, s);
+        update<double>(HXna, N, na3, HXa, N, na3, C, ns, 1.0, 0.0, N, s);
+        update<float>(T32, N, na3, HZ, N, k, C + na3, ns, 1.0, 0.0, N, s);
+        add_f32_into_f64(HXna, N, T32, N, nullptr, 0, na3, N, s);
+        np = na3;
+        std::swap(X, Xn);
+        std::swap(HX, HXn);
+        for (int j = 0; j < na3; ++j) theta[nl + j] = lam[j];
+    }
+    if (X != Rw.X.as<double>()) {
+        copy_block<double>(X, N, Rw.X.as<double>(), N, w, N, s);
+        copy_block<double>(HX, N, Rw.HX.as<double>(), N, w, N, s);
+    }
+    KF_CUDA(cudaStreamSynchronize(s));
+    out.nlocked = nl;
+    out.theta = theta;
+    out.resid = res;
+    return out;
+}
+
+// ------------------------------------------------------------------------------------------
 // host-side seed construction (src/lobpcg.jl:167-190)
 
 // splitmix64-based normal stream on the host, keyed like the reference's MersenneTwister seeds
@@ -542,8 +737,18 @@ static void solve_lobpcg(kf_op *op, const kf_solver_opts &o, int m, const double
                 r = r32;
                 return;
             }
-            convert<float, double>(W32.X.as<float>(), N, W64.X.as<double>(), N, w, N, s);
             q.judge_resid = 0;
+            // FP64 refinement with FP32 search directions
+            RefineWork RW(N, w);
+            convert<float, double>(W32.X.as<float>(), N, RW.X.as<double>(), N, w, N, s);
+            const double tf = now_s();
+            r = lobpcg_refine(op, RW, W32, dD.as<double>(), q, s, theta);
+            KF_CUDA(cudaMemcpyAsync(W64.X.p, RW.X.p, sizeof(double) * (size_t)N * w, cudaMemcpyDeviceToDevice, s));
+            st.seconds_f64 = now_s() - tf;
+            st.iterations_f64 = r.iters;
+            r.iters += iters32;
+            r.nmv += nmv32;
+            return;
         }
         const double tf = now_s();
         r = lobpcg_run<double>(op, W64, dD.as<double>(), q, s, theta);

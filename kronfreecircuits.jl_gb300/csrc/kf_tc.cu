@@ -1,0 +1,389 @@
+// Mode-k products on the 5th-generation tensor cores (tcgen05, sm_103a):
+//   Y[l, i, r] = alpha sum_j A[i, j] X[l, j, r] + beta Y[l, i, r]
+// for a block of FP32 columns, A a d x d matrix held as a BF16 image in the tensor core's
+// K-major shared-memory layout, FP32 accumulation in tensor memory (TMEM).
+//
+// Reference: the dense factor application of src/apply.jl:37-53 and 301-340 -- the same product
+// the SIMT kernel of kf_dense.cu forms; here for the separable preconditioner's axis bases
+// (src/apply.jl:606-642), which only steer LOBPCG's search directions, so BF16 operands (8-bit
+// mantissa, FP32 sums) are accurate enough.
+//
+// GEMM view: D[i, q] = sum_j A[i, j] B[j, q], with q enumerating the (column, l, r) triples of the
+// block.  One CTA (persistent, 256 threads) keeps A in shared memory and walks tiles of 128 q:
+//   1. the 256 threads gather the tile's X[:, j] values (coalesced along l when the axis stride
+//      is > 1, along j for the leading axis), round them to BF16 and store them as the B operand
+//      (K-major core matrices: 8 rows x 16 bytes, LBO = 128 B between K-neighbours);
+//   2. one thread issues the tcgen05.mma chain (M = 128 per A tile, N = 128, K = 16 per
+//      instruction) and commits it to an mbarrier;
+//   3. the first warpgroup waits (bounded), reads its TMEM lanes with tcgen05.ld, and writes Y
+//      through a shared-memory transpose so that the global stores are coalesced.
+// A wait that exceeds its cycle budget records KF_ETIMEOUT in host-mapped memory and the CTA
+// leaves its loop; TMEM is always released.
+#include <cuda_bf16.h>
+
+#include <cstring>
+#include <mutex>
+
+#include "kf_internal.h"
+
+namespace kf {
+
+namespace {
+
+constexpr int TC_THREADS = 256;
+constexpr int TC_NT = 128;                        // q per tile (MMA N)
+constexpr int TC_EP_STRIDE = 33;                  // epilogue transpose row stride (floats)
+constexpr long long TC_WAIT_CYCLES = 4000000000LL;  // ~2 s at 2 GHz
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// shared-memory matrix descriptor: no swizzle, K-major, version 1 (tcgen05)
+__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;
+}
+
+// instruction descriptor, kind::f16: D FP32, A and B BF16, both K-major, M x N
+__host__ __device__ constexpr uint32_t tc_idesc_bf16(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+
+__device__ __forceinline__ void tc_mma(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ void tc_commit(uint64_t *bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.b32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(done)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+
+// bounded wait on one mbarrier phase; false when the cycle budget ran out
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
+    const long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity))
+        if (clock64() - t0 > TC_WAIT_CYCLES) return false;
+    return true;
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15}, [%16];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+    for (int t = 0; t < 16; ++t) v[t] = __uint_as_float(r[t]);
+}
+
+__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
+    __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);   // .x = lo (lower address)
+    return *reinterpret_cast<uint32_t *>(&h);
+}
+
+struct TcArgs {
+    float *Y;
+    const float *X;
+    const uint4 *Aimg;      // BF16 image, Mp x Kp, K-major core matrices
+    int *err;               // host-mapped error word
+    int64_t ldy, ldx, left, rows_per_col, Q;
+    int d, Mp, Kp, ntiles;
+    float alpha, beta;
+};
+
+__global__ void __launch_bounds__(TC_THREADS, 1) k_mode_tc(const TcArgs a) {
+    extern __shared__ __align__(16) unsigned char tc_smem[];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int Kp = a.Kp, Mp = a.Mp;
+    // shared layout: A image | B tile | epilogue transpose | q bases | barrier, TMEM slot
+    unsigned char *Asm = tc_smem;
+    unsigned char *Bsm = Asm + (size_t)Mp * Kp * 2;
+    float *Ep = reinterpret_cast<float *>(Bsm + (size_t)TC_NT * Kp * 2);
+    int64_t *xbase = reinterpret_cast<int64_t *>(Ep + 128 * TC_EP_STRIDE);
+    int64_t *ybase = xbase + TC_NT;
+    uint64_t *bar = reinterpret_cast<uint64_t *>(ybase + TC_NT);
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(bar + 1);
+    __shared__ int s_abort;
+
+    const uint32_t ncols = (uint32_t)(Mp / 128) * TC_NT;   // 128 or 256 FP32 columns
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        s_abort = 0;
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(tslot)),
+                     "r"(ncols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    {
+        const int n16 = Mp * Kp * 2 / 16;
+        uint4 *dst = reinterpret_cast<uint4 *>(Asm);
+        for (int e = tid; e < n16; e += TC_THREADS) dst[e] = a.Aimg[e];
+    }
+    fence_proxy_async();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tslot;
+    const uint32_t sbo_a = (uint32_t)(Kp / 8) * 128, sbo_b = sbo_a;   // 8-row groups along M / N
+    const uint32_t idesc = tc_idesc_bf16(128, TC_NT);
+    const int kg_n = Kp / 8;
+    uint32_t phase = 0;
+
+    for (int tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x) {
+        const int64_t q0 = (int64_t)tile * TC_NT;
+        if (tid < TC_NT) {
+            const int64_t q = q0 + tid;
+            if (q < a.Q) {
+                const int64_t c = q / a.rows_per_col, qq = q % a.rows_per_col;
+                const int64_t l = qq % a.left, r = qq / a.left;
+                const int64_t off = l + a.left * ((int64_t)a.d * r);
+                xbase[tid] = c * a.ldx + off;
+                ybase[tid] = c * a.ldy + off;
+            } else {
+                xbase[tid] = -1;
+                ybase[tid] = -1;
+            }
+        }
+        __syncthreads();
+        // 1. gather + round to BF16 into the K-major B tile: item (n, kg) = 8 consecutive j of row n
+        const int items = TC_NT * kg_n;
+        for (int e = tid; e < items; e += TC_THREADS) {
+            int n, kg;
+            if (a.left > 1) { n = e % TC_NT; kg = e / TC_NT; }   // consecutive threads: consecutive l
+            else { kg = e % kg_n; n = e / kg_n; }                // leading axis: consecutive j
+            const int64_t xb = xbase[n];
+            float v[8];
+#pragma unroll
+            for (int t = 0; t < 8; ++t) {
+                const int j = kg * 8 + t;
+                v[t] = (xb >= 0 && j < a.d) ? __ldg(a.X + xb + a.left * (int64_t)j) : 0.f;
+            }
+            uint4 pk;
+            pk.x = pack_bf16x2(v[0], v[1]);
+            pk.y = pack_bf16x2(v[2], v[3]);
+            pk.z = pack_bf16x2(v[4], v[5]);
+            pk.w = pack_bf16x2(v[6], v[7]);
+            *reinterpret_cast<uint4 *>(Bsm + (size_t)(n >> 3) * sbo_b + (size_t)kg * 128 + (n & 7) * 16) = pk;
+        }
+        fence_proxy_async();
+        tc_fence_before();
+        __syncthreads();
+        // 2. one thread issues the MMA chain for every 128-row tile of A, commits it to the
+        //    mbarrier and waits for it (bounded)
+        if (tid == 0) {
+            tc_fence_after();
+            const uint32_t a0 = smem_u32(Asm), b0 = smem_u32(Bsm);
+            for (int mt = 0; mt < Mp / 128; ++mt) {
+                for (int ks = 0; ks < Kp / 16; ++ks) {
+                    const uint64_t ad = tc_desc(a0 + (uint32_t)mt * 16 * sbo_a + (uint32_t)ks * 256, 128, sbo_a);
+                    const uint64_t bd = tc_desc(b0 + (uint32_t)ks * 256, 128, sbo_b);
+                    tc_mma(tmem + (uint32_t)mt * TC_NT, ad, bd, idesc, ks > 0 ? 1u : 0u);
+                }
+            }
+            tc_commit(bar);
+            if (!mbar_wait_bounded(bar, phase)) {
+                *(volatile int *)a.err = KF_ETIMEOUT;
+                __threadfence_system();
+                s_abort = 1;
+            }
+        }
+        __syncthreads();
+        if (s_abort) break;
+        tc_fence_after();
+        // 3. epilogue by warps 0-3 (TMEM lanes 32 w .. 32 w + 31 = rows i of each A tile)
+        if (warp < 4) {
+            for (int mt = 0; mt < Mp / 128; ++mt) {
+                const int i = mt * 128 + warp * 32 + lane;   // output row of this thread
+                for (int n0 = 0; n0 < TC_NT; n0 += 32) {
+                    float v[32];
+                    const uint32_t ta = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(mt * TC_NT + n0);
+                    tmem_ld16(ta, v);
+                    tmem_ld16(ta + 16, v + 16);
+                    if (a.left == 1) {
+                        // leading axis: consecutive lanes = consecutive i = consecutive addresses
+                        if (i < a.d) {
+#pragma unroll
+                            for (int t = 0; t < 32; ++t) {
+                                const int64_t yb = ybase[n0 + t];
+                                if (yb >= 0) {
+                                    float *yp = a.Y + yb + i;
+                                    *yp = (a.beta == 0.f) ? a.alpha * v[t] : a.alpha * v[t] + a.beta * *yp;
+                                }
+                            }
+                        }
+                    } else {
+                        // transpose 128 rows x 32 q through shared memory, then store along q
+                        float *row = Ep + (warp * 32 + lane) * TC_EP_STRIDE;
+#pragma unroll
+                        for (int t = 0; t < 32; ++t) row[t] = v[t];
+                        asm volatile("bar.sync 1, 128;\n" ::: "memory");
+                        for (int rr = warp; rr < 128; rr += 4) {
+                            const int ii = mt * 128 + rr;
+                            const int64_t yb = ybase[n0 + lane];
+                            if (ii < a.d && yb >= 0) {
+                                float *yp = a.Y + yb + a.left * (int64_t)ii;
+                                const float val = Ep[rr * TC_EP_STRIDE + lane];
+                                *yp = (a.beta == 0.f) ? a.alpha * val : a.alpha * val + a.beta * *yp;
+                            }
+                        }
+                        asm volatile("bar.sync 1, 128;\n" ::: "memory");
+                    }
+                }
+            }
+        }
+        phase ^= 1u;
+        tc_fence_before();
+        __syncthreads();
+    }
+    // after a timeout: one more bounded wait for the MMAs still in flight before TMEM is freed
+    if (s_abort && tid == 0) (void)mbar_wait_bounded(bar, phase);
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(ncols));
+}
+
+// host-mapped error word shared by every tensor-core launch
+std::mutex g_tc_mu;
+int *g_tc_err_host = nullptr;
+int *g_tc_err_dev = nullptr;
+bool g_tc_attr = false;
+
+int *tc_err_word() {
+    std::lock_guard<std::mutex> lk(g_tc_mu);
+    if (!g_tc_err_host) {
+        KF_CUDA(cudaHostAlloc(&g_tc_err_host, sizeof(int), cudaHostAllocMapped));
+        *g_tc_err_host = 0;
+        KF_CUDA(cudaHostGetDevicePointer(&g_tc_err_dev, g_tc_err_host, 0));
+    }
+    return g_tc_err_dev;
+}
+
+// round-to-nearest-even FP32 -> BF16 bits (finite inputs)
+uint16_t bf16_bits(float f) {
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    const uint32_t lsb = (u >> 16) & 1u;
+    u += 0x7FFFu + lsb;
+    return (uint16_t)(u >> 16);
+}
+
+}  // namespace
+
+int tc_mode_layout_ok(int d) { return d >= 1 && d <= 256; }
+
+TcMatrix tc_matrix_create(const double *A, int d, bool transpose) {
+    KF_REQUIRE(tc_mode_layout_ok(d), KF_EINVAL, "tensor-core mode product: axis length must be 1..256");
+    TcMatrix m;
+    m.d = d;
+    m.Mp = d <= 128 ? 128 : 256;
+    m.Kp = (d + 15) / 16 * 16;
+    const size_t sbo = (size_t)(m.Kp / 8) * 128;
+    std::vector<uint16_t> img((size_t)m.Mp * m.Kp, 0);
+    for (int i = 0; i < d; ++i)
+        for (int j = 0; j < d; ++j) {
+            // operator entry (i, j): A[i + d j], or A[j + d i] when transposed
+            const double v = transpose ? A[j + (size_t)d * i] : A[i + (size_t)d * j];
+            const size_t byte = (size_t)(i >> 3) * sbo + (size_t)(j >> 3) * 128 + (size_t)(i & 7) * 16 + (size_t)(j & 7) * 2;
+            img[byte / 2] = bf16_bits((float)v);
+        }
+    KF_CUDA(cudaMalloc(&m.img, img.size() * 2));
+    KF_CUDA(cudaMemcpy(m.img, img.data(), img.size() * 2, cudaMemcpyHostToDevice));
+    return m;
+}
+
+void tc_matrix_free(TcMatrix &m) {
+    if (m.img) cudaFree(m.img);
+    m.img = nullptr;
+}
+
+size_t tc_mode_smem(const TcMatrix &m) {
+    return (size_t)m.Mp * m.Kp * 2 + (size_t)TC_NT * m.Kp * 2 + (size_t)128 * TC_EP_STRIDE * 4 +
+           (size_t)2 * TC_NT * 8 + 16;
+}
+
+void tc_mode_product(float *Y, int64_t ldy, const float *X, int64_t ldx, const TcMatrix &A, int64_t left, int64_t N,
+                     int64_t b, double alpha, double beta, cudaStream_t s) {
+    if (b <= 0 || N <= 0) return;
+    const int64_t rows_per_col = N / A.d;
+    TcArgs a;
+    a.Y = Y;
+    a.X = X;
+    a.Aimg = reinterpret_cast<const uint4 *>(A.img);
+    a.err = tc_err_word();
+    a.ldy = ldy;
+    a.ldx = ldx;
+    a.left = left;
+    a.rows_per_col = rows_per_col;
+    a.Q = rows_per_col * b;
+    a.d = A.d;
+    a.Mp = A.Mp;
+    a.Kp = A.Kp;
+    a.ntiles = (int)((a.Q + TC_NT - 1) / TC_NT);
+    a.alpha = (float)alpha;
+    a.beta = (float)beta;
+    const size_t smem = tc_mode_smem(A);
+    int sms = 152, optin = 0, dev = 0;
+    KF_CUDA(cudaGetDevice(&dev));
+    KF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    KF_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    cudaFuncAttributes fa;
+    KF_CUDA(cudaFuncGetAttributes(&fa, k_mode_tc));
+    const size_t dyn_max = (size_t)optin - fa.sharedSizeBytes;
+    KF_REQUIRE(smem <= dyn_max, KF_EINVAL, "tensor-core mode product: shared-memory image too large");
+    {
+        std::lock_guard<std::mutex> lk(g_tc_mu);
+        if (!g_tc_attr) {
+            KF_CUDA(cudaFuncSetAttribute(k_mode_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn_max));
+            g_tc_attr = true;
+        }
+    }
+    // resident CTAs per SM: by shared memory and by TMEM columns (512 per SM), at most 4
+    int per_sm = (int)(dyn_max / smem);
+    const int by_tmem = 512 / ((A.Mp / 128) * TC_NT);
+    if (per_sm > by_tmem) per_sm = by_tmem;
+    if (per_sm > 4) per_sm = 4;
+    if (per_sm < 1) per_sm = 1;
+    const int grid = a.ntiles < sms * per_sm ? a.ntiles : sms * per_sm;
+    k_mode_tc<<<grid, TC_THREADS, smem, s>>>(a);
+    KF_LAUNCH_CHECK();
+}
+
+int tc_take_error() {
+    std::lock_guard<std::mutex> lk(g_tc_mu);
+    if (!g_tc_err_host) return 0;
+    const int e = *(volatile int *)g_tc_err_host;
+    if (e) *(volatile int *)g_tc_err_host = 0;
+    return e;
+}
+
+}  // namespace kf

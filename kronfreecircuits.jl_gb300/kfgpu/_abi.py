@@ -117,6 +117,9 @@ def lib():
         "kf_mlp_forward": (C.c_int, [P, P, P, C.c_int64]),
         "kf_mlp_gradients": (C.c_int, [P, P, P, C.c_int64, P, P]),
         "kf_mlp_get_params": (C.c_int, [P, P, C.POINTER(C.c_int64)]),
+        # test-only (include/kfgpu_testing.h)
+        "kf_test_mode_product": (C.c_int, [C.c_int32, P, P, P, C.c_int32, C.c_int64, C.c_int64, C.c_int64,
+                                           C.c_double, C.c_double, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

@@ -6,6 +6,7 @@ kfgpu/libkfgpu.so.  A source newer than the library (or `force=True`) triggers a
 from __future__ import annotations
 
 import concurrent.futures as cf
+import glob
 import os
 import shutil
 import subprocess
@@ -35,7 +36,7 @@ def _stale():
         return True
     t = os.path.getmtime(LIB)
     deps = sources() + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
-    deps.append(os.path.join(os.path.dirname(ROOT), "include", "kfgpu.h"))
+    deps += glob.glob(os.path.join(os.path.dirname(ROOT), "include", "*.h"))
     return any(os.path.getmtime(p) > t for p in deps if os.path.exists(p))
 
 

@@ -2,6 +2,7 @@
 include/kfgpu.h declares, option structs validate like the reference's constructors, and the
 host-built term lists equal the oracle's spec-built Hamiltonians (no GPU calls)."""
 import ctypes
+import glob
 import os
 import re
 
@@ -15,10 +16,13 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def _declared_symbols():
-    with open(os.path.join(ROOT, "include", "kfgpu.h")) as f:
-        src = f.read()
-    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    return sorted(set(re.findall(r"\b(kf_[a-z0-9_]+)\s*\(", src)))
+    syms = set()
+    for h in sorted(glob.glob(os.path.join(ROOT, "include", "*.h"))):
+        with open(h) as f:
+            src = f.read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        syms |= set(re.findall(r"\b(kf_[a-z0-9_]+)\s*\(", src))
+    return sorted(syms)
 
 
 def test_library_builds_and_exports_every_declared_symbol():
