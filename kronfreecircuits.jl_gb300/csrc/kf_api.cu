@@ -63,6 +63,10 @@ int kf_op_create(const kf_op_desc *desc, kf_op **out) {
             KF_CUDA(cudaGetDevice(&op->device));
             KF_CUDA(cudaStreamCreateWithFlags(&op->stream, cudaStreamNonBlocking));
             build_op(desc, op);
+            // the separable preconditioner's per-axis eigendecompositions (host only) start now,
+            // on their own thread; the first solve that needs them waits for the result
+            if (!op->sep.M.empty())
+                op->sep.host_job = std::async(std::launch::async, [op] { kf::sep_host_prepare(op); });
         } catch (...) {
             free_op(op);
             delete op;
@@ -240,6 +244,46 @@ int kf_test_mode_product(int path, const float *X, float *Y, const double *A, in
             cudaFree(dA);
             KF_CUDA(e);
         }
+    });
+}
+
+int kf_test_time_mode_product(int path, const float *X, float *Y, const double *A, int d, int64_t left, int64_t N,
+                              int64_t b, int reps, void *stream, float *ms_per_launch) {
+    return guarded([&] {
+        KF_REQUIRE(X && Y && A && ms_per_launch && reps >= 1, KF_EINVAL, "kf_test_time_mode_product: bad argument");
+        KF_REQUIRE(d >= 1 && left >= 1 && N % d == 0 && (N / d) % left == 0, KF_EDIM,
+                   "kf_test_time_mode_product: N must be a multiple of d * left");
+        cudaStream_t s = (cudaStream_t)stream;
+        kf::TcMatrix m;
+        float *dA = nullptr;
+        if (path == 1) {
+            m = kf::tc_matrix_create(A, d, false);
+        } else {
+            std::vector<float> a32((size_t)d * d);
+            for (size_t i = 0; i < a32.size(); ++i) a32[i] = (float)A[i];
+            KF_CUDA(cudaMalloc(&dA, a32.size() * 4));
+            KF_CUDA(cudaMemcpy(dA, a32.data(), a32.size() * 4, cudaMemcpyHostToDevice));
+        }
+        auto launch = [&] {
+            if (path == 1) kf::tc_mode_product(Y, N, X, N, m, left, N, b, 1.0, 0.0, s);
+            else kf::mode_product<float>(Y, N, X, N, dA, d, left, N, b, 1.0, 0.0, s);
+        };
+        cudaEvent_t e0, e1;
+        KF_CUDA(cudaEventCreate(&e0));
+        KF_CUDA(cudaEventCreate(&e1));
+        launch();   // warm
+        KF_CUDA(cudaEventRecord(e0, s));
+        for (int r = 0; r < reps; ++r) launch();
+        KF_CUDA(cudaEventRecord(e1, s));
+        KF_CUDA(cudaEventSynchronize(e1));
+        float ms = 0;
+        KF_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        if (path == 1) kf::tc_matrix_free(m);
+        else cudaFree(dA);
+        if (const int t = kf::tc_take_error()) throw kf::Error(t, "tensor-core mode product: device wait timed out");
+        *ms_per_launch = ms / reps;
     });
 }
 

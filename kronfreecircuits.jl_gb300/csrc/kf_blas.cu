@@ -758,6 +758,30 @@ void fill_normal(T *X, int64_t ld, int k, int64_t N, uint64_t seed, uint64_t sid
     KF_LAUNCH_CHECK();
 }
 
+// X[:, j] += delta * (||X_j|| / ||R_j||) R_j, the norms' squares in nrm[0..k) (X) and nrm[k..2k) (R)
+__global__ void k_perturb_add(double *__restrict__ X, const double *__restrict__ R, int64_t N, int k,
+                              const double *__restrict__ nrm, double delta) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= N * k) return;
+    const int64_t c = t / N, r = t % N;
+    const double f = delta * sqrt(nrm[c]) / sqrt(nrm[k + c]);
+    X[c * N + r] += f * R[c * N + r];
+}
+
+// Each column of X (N x k, leading dimension N) plus a vector of norm delta * ||column|| along a
+// pseudo-random normal direction (keyed by `key`): the sqrt(eps) perturbation of the initial
+// block (src/lobpcg.jl:182-190), drawn on the device.  R: N x k scratch; nrm: 2k doubles.
+void perturb_block(double *X, int64_t N, int k, double delta, uint64_t key, double *R, double *nrm, double *partials,
+                   cudaStream_t s) {
+    if (k <= 0) return;
+    fill_normal<double>(R, N, k, N, key, 0x50455254ull, s);
+    colnorms2<double>(X, N, k, N, nrm, partials, s);
+    colnorms2<double>(R, N, k, N, nrm + k, partials, s);
+    const int64_t tot = N * k;
+    k_perturb_add<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(X, R, N, k, nrm, delta);
+    KF_LAUNCH_CHECK();
+}
+
 template <typename Ts, typename Td>
 __global__ void k_convert(const Ts *__restrict__ X, int64_t ldx, Td *__restrict__ Y, int64_t ldy, int64_t N, int k) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;

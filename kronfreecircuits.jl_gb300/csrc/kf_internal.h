@@ -9,6 +9,7 @@
 #include <cstdio>
 #include <stdexcept>
 #include <string>
+#include <future>
 #include <vector>
 
 #include "../../include/kfgpu.h"
@@ -146,6 +147,9 @@ struct kf_op {
         std::vector<double> lam;              // concatenated per-axis eigenvalues
         std::vector<float *> dU, dUt;         // FP32 U and U' per axis (nullptr when ident)
         std::vector<kf::TcMatrix> tU, tUt;    // the same as tensor-core BF16 images (d <= 256)
+        std::vector<std::vector<double>> Uh;  // host eigenbases per axis (empty when ident)
+        bool host_ready = false;
+        std::future<void> host_job;           // the host eigendecompositions, started at creation
         double *d_lam = nullptr;
         int *d_lam_off = nullptr, *d_dims = nullptr;
     } sep;
@@ -162,6 +166,8 @@ void launch_apply(kf_op *op, bool f32, const void *X, void *Y, int64_t ldx, int6
 template <typename T>
 void gram(const T *A, int64_t lda, int ka, const T *B, int64_t ldb, int kb, int64_t N, double *G_dev,
           double *partials, cudaStream_t s);                 // G = A' B (ka x kb, column-major, FP64)
+void perturb_block(double *X, int64_t N, int k, double delta, uint64_t key, double *R, double *nrm, double *partials,
+                   cudaStream_t s);
 // refinement phase: FP64 iterate, FP32 residual / directions
 void residual_mixed(const double *X, const double *HX, int64_t ld, int k, int64_t N, const double *theta,
                     const double *thetap, const double *D, double eta, int mode, float *R, int64_t ldr, float *W,
@@ -199,6 +205,8 @@ void mode_product(T *Y, int64_t ldy, const T *X, int64_t ldx, const T *A, int d,
 template <typename T>
 void sep_scale(T *W, int64_t ld, int64_t N, int k, int ndims, const int *dims, const double *lam, const int *lam_off,
                const double *theta, double eta, cudaStream_t s);
+void sep_host_prepare(kf_op *op);   // host part only (no CUDA calls)
+void sep_host_prepare(kf_op *op);   // host part only (no CUDA calls)
 void sep_prepare(kf_op *op);
 // W (N x k, FP32, leading dimension N) <- U diag(1 / hypot(S - theta_j, eta)) U' W; s1 is an
 // N x k FP32 scratch.  Returns the block holding the result (W or s1).

@@ -778,6 +778,7 @@ void build_op(const kf_op_desc *desc, kf_op *op) {
 }
 
 void free_op(kf_op *op) {
+    if (op->sep.host_job.valid()) op->sep.host_job.wait();
     cudaFree(op->d_diag64);
     cudaFree(op->d_diag32);
     cudaFree(op->d_w64);

@@ -13,22 +13,17 @@
 
 namespace kf {
 
-void sep_prepare(kf_op *op) {
+// The per-axis eigendecompositions (host FP64), no CUDA calls: run on a host thread started by
+// kf_op_create, so that by the first solve they are usually done.
+void sep_host_prepare(kf_op *op) {
     auto &S = op->sep;
-    if (S.ready) return;
     const int nd = (int)op->dims.size();
     KF_REQUIRE((int)S.M.size() == nd, KF_EINVAL, "separable preconditioner: the operator has no per-axis sums");
     S.ident.assign(nd, 0);
-    S.dU.assign(nd, nullptr);
-    S.dUt.assign(nd, nullptr);
-    S.tU.assign(nd, TcMatrix());
-    S.tUt.assign(nd, TcMatrix());
-    std::vector<int> off(nd), dims(nd);
+    S.Uh.assign(nd, std::vector<double>());
     S.lam.clear();
     for (int a = 0; a < nd; ++a) {
         const int d = (int)op->dims[a];
-        dims[a] = d;
-        off[a] = (int)S.lam.size();
         const std::vector<double> &M = S.M[a];
         bool diag = true;
         for (int j = 0; j < d && diag; ++j)
@@ -43,6 +38,30 @@ void sep_prepare(kf_op *op) {
         if (sym_eig(d, M.data(), d, w.data(), U.data(), d) != 0)
             throw Error(KF_EBREAKDOWN, "separable preconditioner: an axis eigenproblem did not converge");
         S.lam.insert(S.lam.end(), w.begin(), w.end());
+        S.Uh[a] = std::move(U);
+    }
+    S.host_ready = true;
+}
+
+void sep_prepare(kf_op *op) {
+    auto &S = op->sep;
+    if (S.ready) return;
+    if (S.host_job.valid()) S.host_job.get();   // rethrows the host job's error, if any
+    if (!S.host_ready) sep_host_prepare(op);
+    const int nd = (int)op->dims.size();
+    S.dU.assign(nd, nullptr);
+    S.dUt.assign(nd, nullptr);
+    S.tU.assign(nd, TcMatrix());
+    S.tUt.assign(nd, TcMatrix());
+    std::vector<int> off(nd), dims(nd);
+    int acc = 0;
+    for (int a = 0; a < nd; ++a) {
+        const int d = (int)op->dims[a];
+        dims[a] = d;
+        off[a] = acc;
+        acc += d;
+        if (S.ident[a]) continue;
+        const std::vector<double> &U = S.Uh[a];
         std::vector<float> u32((size_t)d * d), ut32((size_t)d * d);
         for (int j = 0; j < d; ++j)
             for (int i = 0; i < d; ++i) {

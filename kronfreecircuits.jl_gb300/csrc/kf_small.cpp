@@ -56,8 +56,10 @@ int sym_eig(int n, const double *A, int lda, double *w, double *V, int ldv) {
         // p = A22 v, K = v'p, q = 2 (p - K v), A22 -= v q' + q v'
         double K = 0;
         for (int i = 0; i < m; ++i) {
+            // A22 is symmetric: row i read down column i (contiguous)
+            const double *col = &a[(size_t)(k + 1) + (size_t)n * (k + 1 + i)];
             double s = 0;
-            for (int j = 0; j < m; ++j) s += at(k + 1 + i, k + 1 + j) * v[j];
+            for (int j = 0; j < m; ++j) s += col[j] * v[j];
             p[i] = s;
             K += v[i] * s;
         }

@@ -27,6 +27,7 @@
 #include <chrono>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <numeric>
 #include <random>
 
@@ -36,15 +37,64 @@ namespace kf {
 
 // ------------------------------------------------------------------------------------------
 // device / pinned memory helpers
+//
+// Inside a solve (AllocScope), device work blocks come from the device's default stream-ordered
+// memory pool on the solve's stream (cudaMallocAsync / cudaFreeAsync); the pool keeps freed
+// memory for the next solve (release threshold raised once per device), so back-to-back solves
+// do not pay cudaMalloc / cudaFree (and cudaFree's device-wide synchronisation) for their
+// gigabyte-sized workspaces.  Pinned host staging buffers are recycled the same way.
+
+static thread_local cudaStream_t g_alloc_stream = nullptr;
+static thread_local bool g_alloc_async = false;
+
+struct AllocScope {
+    cudaStream_t prev_s;
+    bool prev_a;
+    explicit AllocScope(cudaStream_t s) : prev_s(g_alloc_stream), prev_a(g_alloc_async) {
+        static std::mutex mu;
+        static uint64_t done_mask = 0;
+        int dev = 0;
+        KF_CUDA(cudaGetDevice(&dev));
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            if (dev < 64 && !(done_mask & (1ull << dev))) {
+                cudaMemPool_t pool;
+                KF_CUDA(cudaDeviceGetDefaultMemPool(&pool, dev));
+                uint64_t thr = UINT64_MAX;
+                KF_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
+                done_mask |= 1ull << dev;
+            }
+        }
+        g_alloc_stream = s;
+        g_alloc_async = true;
+    }
+    ~AllocScope() {
+        g_alloc_stream = prev_s;
+        g_alloc_async = prev_a;
+    }
+    AllocScope(const AllocScope &) = delete;
+    AllocScope &operator=(const AllocScope &) = delete;
+};
 
 struct DevMem {
     void *p = nullptr;
+    cudaStream_t s = nullptr;
+    bool async = false;
     DevMem() = default;
     explicit DevMem(size_t bytes) {
-        if (bytes) KF_CUDA(cudaMalloc(&p, bytes));
+        if (!bytes) return;
+        if (g_alloc_async) {
+            KF_CUDA(cudaMallocAsync(&p, bytes, g_alloc_stream));
+            s = g_alloc_stream;
+            async = true;
+        } else {
+            KF_CUDA(cudaMalloc(&p, bytes));
+        }
     }
     ~DevMem() {
-        if (p) cudaFree(p);
+        if (!p) return;
+        if (async) cudaFreeAsync(p, s);
+        else cudaFree(p);
     }
     DevMem(const DevMem &) = delete;
     DevMem &operator=(const DevMem &) = delete;
@@ -52,11 +102,25 @@ struct DevMem {
     T *as() const { return (T *)p; }
 };
 
+// pinned host blocks, recycled per thread by size
+static thread_local std::vector<std::pair<size_t, void *>> g_pinned_free;
+
 struct HostMem {
     void *p = nullptr;
-    explicit HostMem(size_t bytes) { KF_CUDA(cudaMallocHost(&p, bytes ? bytes : 8)); }
+    size_t n = 0;
+    explicit HostMem(size_t bytes) : n(bytes ? bytes : 8) {
+        for (size_t i = 0; i < g_pinned_free.size(); ++i)
+            if (g_pinned_free[i].first == n) {
+                p = g_pinned_free[i].second;
+                g_pinned_free.erase(g_pinned_free.begin() + (long)i);
+                return;
+            }
+        KF_CUDA(cudaMallocHost(&p, n));
+    }
     ~HostMem() {
-        if (p) cudaFreeHost(p);
+        if (!p) return;
+        if (g_pinned_free.size() < 64) g_pinned_free.emplace_back(n, p);
+        else cudaFreeHost(p);
     }
     HostMem(const HostMem &) = delete;
     HostMem &operator=(const HostMem &) = delete;
@@ -79,6 +143,21 @@ static double now_s() {
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
+// KF_TRACE: host time spent blocked on the stream (waiting for the GPU) and in the small host
+// eigenproblems, per LOBPCG phase
+struct TraceTimes {
+    double sync = 0, eig = 0;
+    int nsync = 0;
+};
+static thread_local TraceTimes g_tt;
+
+static int timed_sym_eig(int n, const double *A, int lda, double *w, double *V, int ldv) {
+    const double t0 = now_s();
+    const int r = sym_eig(n, A, lda, w, V, ldv);
+    g_tt.eig += now_s() - t0;
+    return r;
+}
+
 // ------------------------------------------------------------------------------------------
 // SVQB coefficients on the host: for the Gram matrix G (k x k) of a block Z, T (k x r) with
 // Z T orthonormal, dropping directions whose unit-diagonal Gram eigenvalue is below
@@ -88,7 +167,7 @@ static int svqb_coeffs(int k, const double *G, double cutoff, std::vector<double
     for (int i = 0; i < k; ++i) d[i] = 1.0 / std::sqrt(std::max(G[i + (size_t)k * i], 1e-300));
     for (int j = 0; j < k; ++j)
         for (int i = 0; i < k; ++i) Gs[i + (size_t)k * j] = d[i] * G[i + (size_t)k * j] * d[j];
-    if (sym_eig(k, Gs.data(), k, w.data(), U.data(), k) != 0)
+    if (timed_sym_eig(k, Gs.data(), k, w.data(), U.data(), k) != 0)
         throw Error(KF_EBREAKDOWN, "SVQB: the Gram eigenproblem did not converge");
     const double top = w[k - 1];
     std::vector<int> keep;
@@ -151,7 +230,10 @@ struct LobWork {
 template <typename T>
 static void d2h_sync(double *h, const double *d, size_t n, cudaStream_t s) {
     KF_CUDA(cudaMemcpyAsync(h, d, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    const double t0 = now_s();
     KF_CUDA(cudaStreamSynchronize(s));
+    g_tt.sync += now_s() - t0;
+    ++g_tt.nsync;
     if (const int e = tc_take_error()) throw Error(e, "a tensor-core mode product timed out on the device");
 }
 
@@ -235,6 +317,8 @@ static LobOut lobpcg_run(kf_op *op, LobWork<T> &Wk, const double *D, const LobPa
     }
     std::vector<double> res(w, INFINITY);
     int nl = 0, np = 0, na_prev = w;
+    const TraceTimes tt0 = g_tt;
+    const double tw0 = now_s();
     double best = INFINITY;
     int since_best = 0;
     for (int it = 0;; ++it) {
@@ -335,23 +419,23 @@ static LobOut lobpcg_run(kf_op *op, LobWork<T> &Wk, const double *D, const LobPa
         const int ns = na3 + k;
         T *Xa = X + (int64_t)nl * N, *HXa = HX + (int64_t)nl * N;
         std::vector<double> A((size_t)ns * ns);
-        gram<T>(Xa, N, na3, HXa, N, na3, N, G, part, s);
-        d2h_sync<T>(hG, G, (size_t)na3 * na3, s);
+        double *G1 = G, *G2 = G + (size_t)na3 * na3, *G3 = G2 + (size_t)na3 * k;
+        gram<T>(Xa, N, na3, HXa, N, na3, N, G1, part, s);
+        gram<T>(Xa, N, na3, HZ, N, k, N, G2, part, s);
+        gram<T>(Qc, N, k, HZ, N, k, N, G3, part, s);
+        d2h_sync<T>(hG, G, (size_t)na3 * na3 + (size_t)na3 * k + (size_t)k * k, s);
+        const double *h1 = hG, *h2 = hG + (size_t)na3 * na3, *h3 = h2 + (size_t)na3 * k;
         for (int j = 0; j < na3; ++j)
-            for (int i = 0; i < na3; ++i) A[i + (size_t)ns * j] = hG[i + (size_t)na3 * j];
-        gram<T>(Xa, N, na3, HZ, N, k, N, G, part, s);
-        d2h_sync<T>(hG, G, (size_t)na3 * k, s);
+            for (int i = 0; i < na3; ++i) A[i + (size_t)ns * j] = h1[i + (size_t)na3 * j];
         for (int j = 0; j < k; ++j)
             for (int i = 0; i < na3; ++i) {
-                A[i + (size_t)ns * (na3 + j)] = hG[i + (size_t)na3 * j];
-                A[(na3 + j) + (size_t)ns * i] = hG[i + (size_t)na3 * j];
+                A[i + (size_t)ns * (na3 + j)] = h2[i + (size_t)na3 * j];
+                A[(na3 + j) + (size_t)ns * i] = h2[i + (size_t)na3 * j];
             }
-        gram<T>(Qc, N, k, HZ, N, k, N, G, part, s);
-        d2h_sync<T>(hG, G, (size_t)k * k, s);
         for (int j = 0; j < k; ++j)
-            for (int i = 0; i < k; ++i) A[(na3 + i) + (size_t)ns * (na3 + j)] = hG[i + (size_t)k * j];
+            for (int i = 0; i < k; ++i) A[(na3 + i) + (size_t)ns * (na3 + j)] = h3[i + (size_t)k * j];
         std::vector<double> lam(ns), V((size_t)ns * ns);
-        if (sym_eig(ns, A.data(), ns, lam.data(), V.data(), ns) != 0)
+        if (timed_sym_eig(ns, A.data(), ns, lam.data(), V.data(), ns) != 0)
             throw Error(KF_EBREAKDOWN, "LOBPCG: Rayleigh-Ritz eigenproblem did not converge");
         // C = V[:, 0:na3]  (ns x na3)
         std::memcpy(hC, V.data(), sizeof(double) * (size_t)ns * na3);
@@ -370,6 +454,10 @@ static LobOut lobpcg_run(kf_op *op, LobWork<T> &Wk, const double *D, const LobPa
         na_prev = na3;
     }
     (void)na_prev;
+    if (trace_on())
+        std::fprintf(stderr, "kf lobpcg %s: %d iterations, %.4f s; blocked on the stream %.4f s (%d syncs), host eig %.4f s\n",
+                     f32 ? "f32" : "f64", out.iters, now_s() - tw0, g_tt.sync - tt0.sync, g_tt.nsync - tt0.nsync,
+                     g_tt.eig - tt0.eig);
     // make sure the final block sits in Wk.X / Wk.HX
     if (X != Wk.X.template as<T>()) {
         copy_block<T>(X, N, Wk.X.template as<T>(), N, w, N, s);
@@ -461,6 +549,8 @@ static LobOut lobpcg_refine(kf_op *op, RefineWork &Rw, LobWork<float> &Wk, const
 
     std::vector<double> res(w, INFINITY);
     int nl = 0, np = 0;
+    const TraceTimes tt0 = g_tt;
+    const double tw0 = now_s();
     for (int it = 0;; ++it) {
         const int na = w - nl;
         std::memcpy(hv, theta.data() + nl, sizeof(double) * na);
@@ -547,7 +637,7 @@ static LobOut lobpcg_refine(kf_op *op, RefineWork &Rw, LobWork<float> &Wk, const
             for (int i = 0; i < k; ++i)
                 A[(na3 + i) + (size_t)ns * (na3 + j)] = 0.5 * (h3[i + (size_t)k * j] + h3[j + (size_t)k * i]);
         std::vector<double> lam(ns), V((size_t)ns * ns);
-        if (sym_eig(ns, A.data(), ns, lam.data(), V.data(), ns) != 0)
+        if (timed_sym_eig(ns, A.data(), ns, lam.data(), V.data(), ns) != 0)
             throw Error(KF_EBREAKDOWN, "LOBPCG: Rayleigh-Ritz eigenproblem did not converge");
         std::memcpy(hC, V.data(), sizeof(double) * (size_t)ns * na3);
         h2d(C, hC, (size_t)ns * na3, s);
@@ -565,6 +655,9 @@ static LobOut lobpcg_refine(kf_op *op, RefineWork &Rw, LobWork<float> &Wk, const
         std::swap(HX, HXn);
         for (int j = 0; j < na3; ++j) theta[nl + j] = lam[j];
     }
+    if (trace_on())
+        std::fprintf(stderr, "kf lobpcg refine: %d iterations, %.4f s; blocked on the stream %.4f s (%d syncs), host eig %.4f s\n",
+                     out.iters, now_s() - tw0, g_tt.sync - tt0.sync, g_tt.nsync - tt0.nsync, g_tt.eig - tt0.eig);
     if (X != Rw.X.as<double>()) {
         copy_block<double>(X, N, Rw.X.as<double>(), N, w, N, s);
         copy_block<double>(HX, N, Rw.HX.as<double>(), N, w, N, s);
@@ -574,48 +667,6 @@ static LobOut lobpcg_refine(kf_op *op, RefineWork &Rw, LobWork<float> &Wk, const
     out.theta = theta;
     out.resid = res;
     return out;
-}
-
-// ------------------------------------------------------------------------------------------
-// host-side seed construction (src/lobpcg.jl:167-190)
-
-// splitmix64-based normal stream on the host, keyed like the reference's MersenneTwister seeds
-struct HostNormal {
-    uint64_t state;
-    bool have = false;
-    double spare = 0;
-    explicit HostNormal(uint64_t seed) : state(seed * 0x9e3779b97f4a7c15ull + 0x4b46) {}
-    uint64_t next() {
-        uint64_t z = (state += 0x9e3779b97f4a7c15ull);
-        z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
-        z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
-        return z ^ (z >> 31);
-    }
-    double operator()() {
-        if (have) { have = false; return spare; }
-        double u1 = ((next() >> 11) + 1) * (1.0 / 9007199254740993.0);
-        double u2 = (next() >> 11) * (1.0 / 9007199254740992.0);
-        double r = std::sqrt(-2.0 * std::log(u1));
-        spare = r * std::sin(2 * M_PI * u2);
-        have = true;
-        return r * std::cos(2 * M_PI * u2);
-    }
-};
-
-// Each column plus a vector of norm delta * ||column|| along a fixed pseudo-random direction.
-static void perturb_columns(double *X, int64_t N, int k, double delta, uint64_t key) {
-    HostNormal rng(key);
-    std::vector<double> r(N);
-    for (int j = 0; j < k; ++j) {
-        double nc = 0, nr = 0;
-        for (int64_t i = 0; i < N; ++i) {
-            r[i] = rng();
-            nr += r[i] * r[i];
-            nc += X[i + N * j] * X[i + N * j];
-        }
-        const double f = delta * std::sqrt(nc) / std::sqrt(nr);
-        for (int64_t i = 0; i < N; ++i) X[i + N * j] += f * r[i];
-    }
 }
 
 // ------------------------------------------------------------------------------------------
@@ -683,36 +734,37 @@ static void solve_lobpcg(kf_op *op, const kf_solver_opts &o, int m, const double
     const int w = m + g;
     const double hn = op->gershgorin;
     st.hnorm = hn;
-    // the initial block on the host (FP64)
-    std::vector<double> X((size_t)N * w);
-    const double delta = std::sqrt(std::numeric_limits<double>::epsilon());
-    HostNormal rng(o.rng_seed);
-    bool guards_random = true;
-    if (X0) {
-        std::memcpy(X.data(), X0, sizeof(double) * (size_t)N * m);
-        perturb_columns(X.data(), N, m, delta, 0x4b46);
-        if (seed) {
-            std::memcpy(X.data() + (size_t)N * m, seed + (size_t)N * m, sizeof(double) * (size_t)N * g);
-            perturb_columns(X.data() + (size_t)N * m, N, g, delta, 0x4b46);
-            guards_random = false;
-        }
-        st.warm = 1;
-    } else if (seed) {
-        std::memcpy(X.data(), seed, sizeof(double) * (size_t)N * w);
-        perturb_columns(X.data(), N, w, delta, 0x4b46);
-        guards_random = false;
-    } else {
-        for (size_t i = 0; i < (size_t)N * m; ++i) X[i] = rng();
-    }
-    if (guards_random)
-        for (size_t i = (size_t)N * m; i < (size_t)N * w; ++i) X[i] = rng();
-
     DevMem dD((size_t)N * sizeof(double));
     KF_CUDA(cudaMemcpyAsync(dD.p, op->h_fulldiag.data(), N * sizeof(double), cudaMemcpyHostToDevice, s));
     LobWork<double> W64(N, w);
-    auto load64 = [&](const std::vector<double> &Xh) {
-        KF_CUDA(cudaMemcpyAsync(W64.X.p, Xh.data(), sizeof(double) * (size_t)N * w, cudaMemcpyHostToDevice, s));
+    // the initial block, built on the device (src/lobpcg.jl:179-190): the warm start's / the
+    // product seed's columns with the sqrt(eps) perturbation, random normal columns otherwise
+    const double delta = std::sqrt(std::numeric_limits<double>::epsilon());
+    auto build_block = [&](bool use_inputs, uint64_t rkey) {
+        double *Xd = W64.X.as<double>();
+        double *R = W64.Z.as<double>();   // scratch, 2 N w
+        double *nrm = W64.dnorm.as<double>();
+        double *part = W64.dpart.as<double>();
+        bool guards_random = true;
+        if (use_inputs && X0) {
+            KF_CUDA(cudaMemcpyAsync(Xd, X0, sizeof(double) * (size_t)N * m, cudaMemcpyHostToDevice, s));
+            perturb_block(Xd, N, m, delta, 0x4b46, R, nrm, part, s);
+            if (seed) {
+                KF_CUDA(cudaMemcpyAsync(Xd + (size_t)N * m, seed + (size_t)N * m, sizeof(double) * (size_t)N * g,
+                                        cudaMemcpyHostToDevice, s));
+                perturb_block(Xd + (size_t)N * m, N, g, delta, 0x4b47, R, nrm, part, s);
+                guards_random = false;
+            }
+        } else if (use_inputs && seed) {
+            KF_CUDA(cudaMemcpyAsync(Xd, seed, sizeof(double) * (size_t)N * w, cudaMemcpyHostToDevice, s));
+            perturb_block(Xd, N, w, delta, 0x4b46, R, nrm, part, s);
+            guards_random = false;
+        } else {
+            fill_normal<double>(Xd, N, m, N, rkey, 1, s);
+        }
+        if (guards_random) fill_normal<double>(Xd + (size_t)N * m, N, g, N, rkey, 2, s);
     };
+    if (X0) st.warm = 1;
     LobParams p64{o.tol, o.maxiter, o.preconditioner, o.eta, w, 1e-12, false, o.fallback_iters,
                   o.fallback_resid > 0 ? o.fallback_resid : 0.0};
     std::vector<double> theta;
@@ -757,7 +809,7 @@ static void solve_lobpcg(kf_op *op, const kf_solver_opts &o, int m, const double
         r.iters += iters32;
         r.nmv += nmv32;
     };
-    load64(X);
+    build_block(true, o.rng_seed);
     bool failed = false;
     try {
         attempt(X0 != nullptr);
@@ -769,10 +821,7 @@ static void solve_lobpcg(kf_op *op, const kf_solver_opts &o, int m, const double
     if (failed || r.judged_bad) {
         // one retry from a random block (src/lobpcg.jl:272-289); also the warm-start fallback
         if (r.judged_bad) st.fell_back = 1;
-        std::vector<double> Xr((size_t)N * w);
-        HostNormal rr(o.rng_seed ^ 0x52455452ull);
-        for (auto &v : Xr) v = rr();
-        load64(Xr);
+        build_block(false, o.rng_seed ^ 0x52455452ull);
         const int it0 = r.judged_bad ? r.iters : 0;
         const int64_t nmv0 = r.judged_bad ? r.nmv : 0;
         try {
@@ -847,15 +896,6 @@ static void solve_chebyshev(kf_op *op, const kf_solver_opts &o, int m, const dou
     const double eps = std::numeric_limits<double>::epsilon();
     const int g = std::max(std::min(std::min(o.extra - 1, CHEB_GUARDS), nb - 1 - m), 0);
     const double t0 = now_s();
-    // seed on the host: product seed + 1e-2 admixture, or random
-    std::vector<double> X0((size_t)N * nb);
-    if (seed) {
-        std::memcpy(X0.data(), seed, sizeof(double) * (size_t)N * nb);
-        perturb_columns(X0.data(), N, nb, SEED_ADMIXTURE, 0x4346);
-    } else {
-        HostNormal rng(o.rng_seed);
-        for (auto &v : X0) v = rng();
-    }
     // buffers (FP64): X, HX, A, B, C, S
     const size_t blk = (size_t)N * nb * sizeof(double);
     DevMem dX(blk), dHX(blk), dA(blk), dB(blk), dC(blk), dS(blk), dG((size_t)nb * nb * 8), dM((size_t)nb * nb * 8),
@@ -865,7 +905,13 @@ static void solve_chebyshev(kf_op *op, const kf_solver_opts &o, int m, const dou
     double *bufs[3] = {dA.as<double>(), dB.as<double>(), dC.as<double>()};
     double *S = dS.as<double>(), *G = dG.as<double>(), *M = dM.as<double>(), *part = dpart.as<double>();
     uint64_t refill_stream = 1;
-    KF_CUDA(cudaMemcpyAsync(bufs[0], X0.data(), blk, cudaMemcpyHostToDevice, s));
+    // the starting block on the device: product seed + 1e-2 admixture (src/chebyshev.jl), or random
+    if (seed) {
+        KF_CUDA(cudaMemcpyAsync(bufs[0], seed, blk, cudaMemcpyHostToDevice, s));
+        perturb_block(bufs[0], N, nb, SEED_ADMIXTURE, 0x4346, bufs[1], dv.as<double>(), part, s);
+    } else {
+        fill_normal<double>(bufs[0], N, nb, N, o.rng_seed, 3, s);
+    }
 
     auto colnorms_host = [&](const double *Z, int k, std::vector<double> &out) {
         colnorms2<double>(Z, N, k, N, dv.as<double>(), part, s);
@@ -1289,6 +1335,7 @@ static void solve_lanczos(kf_op *op, const kf_solver_opts &o, int m, double *E_o
 void solve_dispatch(kf_op *op, const kf_solver_opts &o, int m, const double *X0, const double *seed, double *E_out,
                     double *V_out, kf_solve_stats &st) {
     std::memset(&st, 0, sizeof(st));
+    AllocScope scope(op->stream);
     switch (o.kind) {
         case KF_SOLVER_LOBPCG: solve_lobpcg(op, o, m, X0, seed, E_out, V_out, st); break;
         case KF_SOLVER_CHEBYSHEV: solve_chebyshev(op, o, m, seed, E_out, V_out, st); break;

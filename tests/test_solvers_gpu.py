@@ -96,7 +96,9 @@ def test_lobpcg_warm_start_and_random_seed(cuda, small_leaf):
     E, V, st = solve(LOBPCG(tol=tol), H, 8)
     E2, V2, st2 = solve(LOBPCG(tol=tol), H, 8, X0=V)
     _check_pairs(Ho, E2, V2, Eref[:8], tol)
-    assert st2["warm"] == 1 and st2["iterations"] <= st["iterations"]
+    # work in H columns, as the reference measures it (test/test_solvers.jl:798): the guards
+    # converge alike on warm and cold starts, but the seeded columns lock at once
+    assert st2["warm"] == 1 and st2["n_matvec"] < st["n_matvec"]
     E3, V3, _ = solve(LOBPCG(tol=tol, seed="random", preconditioner="jacobi"), H, 8)
     _check_pairs(Ho, E3, V3, Eref[:8], tol)
 
