@@ -41,9 +41,11 @@ for _p in (ROOT, PKG):
 M_PAIRS = 12
 SEED = 20261205          # theta draws of the three-mode leaf workload
 NDRAWS = 64
-# ncu dram__bytes_read.sum + dram__bytes_write.sum of one FP32 16-column fused-apply launch at
-# N = 671,744 (profiles/apply_fused_three_mode.md); None until captured
-APPLY_TRAFFIC_BYTES = None
+# ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch (profiles/*.md): the FP32 16-column
+# fused apply at N = 671,744 (written Y stays in L2: reads 45.7 MB, writes 9.9 MB); the 16 x 32 FP32
+# Gram (None until captured)
+APPLY_TRAFFIC_BYTES = 55641088
+GRAM_TRAFFIC_BYTES = None
 
 
 def thetas():
@@ -201,11 +203,14 @@ def run_ours(args):
         H.close()
     torch.cuda.synchronize()
     te = time.perf_counter() - t0
-    # roofline of the dominant kernel: the FP32 fused stencil apply on a 16-column block
+    # roofline of the dominant kernel of a solve (the FP32 Gram product, by the ncu launch list):
+    # the orthogonalisation's X' [W P] at 16 x 32 columns; and of the fused stencil apply
     H0 = ops[idx[0]][0]
+    peak, kind = peaks()
+    t_gram = time_gram(torch, 16, 32, H0.N)
+    alg_gram = (16 + 32) * H0.N * 4
     t_apply = measure_apply(torch, H0, True)
     alg = 2 * H0.N * 16 * 4
-    peak, kind = peaks()
     achieved = alg / t_apply / 1e9
     line = {
         "metric": "converged eigenpairs/s at 1e-8 resid: warm-start mixed vs plain FP64, 1 GB300",
@@ -223,9 +228,13 @@ def run_ours(args):
         "max_residual_rel": max(s["max_residual"] / s["hnorm"] for s in stats),
         "e2e": {"value": conv_e / te, "unit": "eigenpairs/s", "h2d_bytes_per_step": int(h2d / ke),
                 "d2h_bytes_per_step": int(d2h / ke), "steps": ke},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": APPLY_TRAFFIC_BYTES, "kernel": "k_apply_fused<float> (16 columns)",
-                     "launch_us": t_apply * 1e6, "peak_kind": kind},
+        "roofline": {"bound": "hbm", "achieved": alg_gram / t_gram / 1e9, "peak": peak, "unit": "GB/s",
+                     "frac": alg_gram / t_gram / 1e9 / peak, "traffic": GRAM_TRAFFIC_BYTES,
+                     "kernel": "k_gram32 + k_reduce_partials (FP32 Gram, 16 x 32 columns, N=671,744)",
+                     "algorithmic_bytes": alg_gram, "launch_us": t_gram * 1e6, "peak_kind": kind},
+        "roofline_apply": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                           "traffic": APPLY_TRAFFIC_BYTES, "kernel": "k_apply_fused<float> (16 columns)",
+                           "algorithmic_bytes": alg, "launch_us": t_apply * 1e6, "peak_kind": kind},
         "clocks": clk, "gpu_launches": launches,
     }
     if not args.no_cpu:
@@ -266,6 +275,76 @@ def run_apply_workload(args):
         by = 2 * H.N * 16 * (4 if f32 else 8)
         out["apply_%s_us" % ("f32" if f32 else "f64")] = t * 1e6
         out["apply_%s_gbs" % ("f32" if f32 else "f64")] = by / t / 1e9
+    return out
+
+
+def time_mode_product(torch, path, dims, axis, b=16, reps=10):
+    """Mean device time of one mode product launch (the library's test-only timing entry point:
+    operator image built once, CUDA events around `reps` launches); X and Y are b-column FP32
+    blocks of the given grid (the 16-column three-mode block is 43 MB, so X and Y together exceed
+    L2 only partly; the launches read the same X)."""
+    import ctypes as C
+    from kfgpu import _abi
+    N = int(np.prod(dims))
+    d = dims[axis]
+    left = int(np.prod(dims[:axis])) if axis > 0 else 1
+    rng = np.random.default_rng(1)
+    A = np.ascontiguousarray(np.linalg.qr(rng.standard_normal((d, d)))[0].T)
+    X = torch.randn(b, N, dtype=torch.float32, device="cuda")
+    Y = torch.empty_like(X)
+    ms = C.c_float(0)
+    _abi.check(_abi.lib().kf_test_time_mode_product(path, C.c_void_p(X.data_ptr()), C.c_void_p(Y.data_ptr()),
+                                                    A.ctypes.data_as(C.c_void_p), d, left, N, b, reps, None,
+                                                    C.byref(ms)))
+    return ms.value / 1e3
+
+
+def time_gram(torch, ka, kb, N, reps=10):
+    """Mean device time of one FP32 Gram product A'B (A: N x ka, B: N x kb; the Gram kernel with its
+    fixed-order partial reduction), through the library's test-only timing entry point."""
+    import ctypes as C
+    from kfgpu import _abi
+    A = torch.randn(ka, N, dtype=torch.float32, device="cuda")
+    B = torch.randn(kb, N, dtype=torch.float32, device="cuda")
+    ms = C.c_float(0)
+    _abi.check(_abi.lib().kf_test_time_gram(C.c_void_p(A.data_ptr()), N, ka, C.c_void_p(B.data_ptr()), N, kb, N, reps,
+                                            None, C.byref(ms), None))
+    return ms.value / 1e3
+
+
+GRAM_SHAPES = ((16, 32), (32, 32), (16, 16), (16, 2), (2, 4))
+
+
+def run_gram_workload(args):
+    """The FP32 Gram products of LOBPCG's orthogonalisation and Rayleigh-Ritz on N = 671,744 rows."""
+    import torch
+    N = 671744
+    peak, kind = peaks()
+    out = {"workload": "FP32 Gram A'B, N=671,744 rows", "hbm_peak_gbs": peak, "peak_kind": kind}
+    for ka, kb in GRAM_SHAPES:
+        t = time_gram(torch, ka, kb, N)
+        out[f"gram_{ka}x{kb}_us"] = t * 1e6
+        out[f"gram_{ka}x{kb}_gbs"] = (ka + kb) * N * 4 / t / 1e9
+    return out
+
+
+def run_mode_workload(args):
+    """The separable preconditioner's mode products on the three-mode leaf grid (16 FP32 columns):
+    tensor cores (tcgen05, BF16 operands) and the SIMT FP32 kernel, per non-diagonal axis."""
+    import torch
+    dims = (41, 256, 64)
+    N = int(np.prod(dims))
+    peak, kind = peaks()
+    out = {"workload": "mode products, three-mode grid 41x256x64 (N=671,744), 16 FP32 columns"}
+    for axis in (1, 2):
+        for path, name in ((1, "tc"), (0, "simt")):
+            t = time_mode_product(torch, path, dims, axis)
+            by = 2 * N * 16 * 4
+            out[f"axis{axis}_{name}_us"] = t * 1e6
+            out[f"axis{axis}_{name}_gbs"] = by / t / 1e9
+            out[f"axis{axis}_{name}_tflops"] = 2 * N * dims[axis] * 16 / t / 1e12
+    out["hbm_peak_gbs"] = peak
+    out["peak_kind"] = kind
     return out
 
 
@@ -446,10 +525,12 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--plain-steps", type=int, default=2)
     ap.add_argument("--e2e-steps", type=int, default=2)
-    ap.add_argument("--ref-iters", type=int, default=570,
-                    help="LOBPCG iterations the FP64 solve of this workload takes (for the reference arm's extrapolation)")
+    ap.add_argument("--ref-iters", type=int, default=868,
+                    help="LOBPCG iterations the plain FP64 solve of this workload takes, for the reference arm's "
+                         "extrapolation (868: the mean over the first two timed draws measured on GB300)")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="leaf3", choices=["leaf3", "batch", "warmstart", "dense", "apply"],
+    ap.add_argument("--workload", default="leaf3",
+                    choices=["leaf3", "batch", "warmstart", "dense", "apply", "mode", "gram"],
                     help="leaf3 (the benchmarked workload) or one of the other measured configurations")
     ap.add_argument("--n-train", type=int, default=4096)
     ap.add_argument("--n-test", type=int, default=1024)
@@ -462,7 +543,7 @@ def main():
         return
     if args.workload != "leaf3":
         fn = {"batch": run_batch_workload, "warmstart": run_warmstart_workload, "dense": run_dense_workload,
-              "apply": run_apply_workload}
+              "apply": run_apply_workload, "mode": run_mode_workload, "gram": run_gram_workload}
         print(json.dumps(fn[args.workload](args)), flush=True)
         return
     if args.warmup < 3:

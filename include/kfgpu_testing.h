@@ -21,6 +21,24 @@ extern "C" {
 int kf_test_mode_product(int path, const float *X, float *Y, const double *A, int d, int64_t left, int64_t N,
                          int64_t b, double alpha, double beta, void *stream);
 
+/*
+ * The same product launched `reps` times on `stream` (the operator image built once, outside the
+ * timed region; X and Y as above), timed with CUDA events around the launches: *ms_per_launch
+ * receives the mean device time of one launch.  Returns a KF_* status.
+ */
+int kf_test_time_mode_product(int path, const float *X, float *Y, const double *A, int d, int64_t left, int64_t N,
+                              int64_t b, int reps, void *stream, float *ms_per_launch);
+
+/*
+ * The FP32 Gram product G = A' B (A: N x ka, B: N x kb, device, column-major with leading
+ * dimensions lda, ldb; ka, kb <= 128) launched `reps` times on `stream` and timed with CUDA events
+ * around the launches (the Gram kernel and its fixed-order partial reduction together);
+ * *ms_per_launch receives the mean device time of one product, G_out (host, ka x kb column-major,
+ * may be NULL) the last result.  Returns a KF_* status.
+ */
+int kf_test_time_gram(const float *A, int64_t lda, int ka, const float *B, int64_t ldb, int kb, int64_t N, int reps,
+                      void *stream, float *ms_per_launch, double *G_out);
+
 #ifdef __cplusplus
 }
 #endif

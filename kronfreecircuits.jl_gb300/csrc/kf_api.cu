@@ -287,4 +287,32 @@ int kf_test_time_mode_product(int path, const float *X, float *Y, const double *
     });
 }
 
+int kf_test_time_gram(const float *A, int64_t lda, int ka, const float *B, int64_t ldb, int kb, int64_t N, int reps,
+                      void *stream, float *ms_per_launch, double *G_out) {
+    return guarded([&] {
+        KF_REQUIRE(A && B && ms_per_launch && reps >= 1 && N >= 1, KF_EINVAL, "kf_test_time_gram: bad argument");
+        KF_REQUIRE(lda >= N && ldb >= N, KF_EDIM, "kf_test_time_gram: leading dimensions must be >= N");
+        cudaStream_t s = (cudaStream_t)stream;
+        double *G = nullptr, *part = nullptr;
+        KF_CUDA(cudaMalloc(&G, (size_t)ka * kb * sizeof(double)));
+        KF_CUDA(cudaMalloc(&part, kf::gram_partials_size(ka, kb, N)));
+        cudaEvent_t e0, e1;
+        KF_CUDA(cudaEventCreate(&e0));
+        KF_CUDA(cudaEventCreate(&e1));
+        kf::gram<float>(A, lda, ka, B, ldb, kb, N, G, part, s);   // warm
+        KF_CUDA(cudaEventRecord(e0, s));
+        for (int r = 0; r < reps; ++r) kf::gram<float>(A, lda, ka, B, ldb, kb, N, G, part, s);
+        KF_CUDA(cudaEventRecord(e1, s));
+        KF_CUDA(cudaEventSynchronize(e1));
+        float ms = 0;
+        KF_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (G_out) KF_CUDA(cudaMemcpy(G_out, G, (size_t)ka * kb * sizeof(double), cudaMemcpyDeviceToHost));
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        cudaFree(G);
+        cudaFree(part);
+        *ms_per_launch = ms / reps;
+    });
+}
+
 }  // extern "C"

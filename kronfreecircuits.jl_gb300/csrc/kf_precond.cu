@@ -7,6 +7,8 @@
 // ||H|| large) and the coupling only shifts the spectrum.  Each application costs 2 mode products
 // per non-diagonal axis (tcgen05 tensor-core GEMMs with BF16 operands for axes up to 256 long,
 // SIMT FP32 beyond) and one scaling pass.
+#include <chrono>
+#include <cstdlib>
 #include <cstring>
 
 #include "kf_internal.h"
@@ -46,6 +48,7 @@ void sep_host_prepare(kf_op *op) {
 void sep_prepare(kf_op *op) {
     auto &S = op->sep;
     if (S.ready) return;
+    const auto t0 = std::chrono::steady_clock::now();
     if (S.host_job.valid()) S.host_job.get();   // rethrows the host job's error, if any
     if (!S.host_ready) sep_host_prepare(op);
     const int nd = (int)op->dims.size();
@@ -84,6 +87,10 @@ void sep_prepare(kf_op *op) {
     KF_CUDA(cudaMemcpy(S.d_lam_off, off.data(), nd * sizeof(int), cudaMemcpyHostToDevice));
     KF_CUDA(cudaMemcpy(S.d_dims, dims.data(), nd * sizeof(int), cudaMemcpyHostToDevice));
     S.ready = true;
+    const char *tr = std::getenv("KF_TRACE");
+    if (tr && tr[0] && tr[0] != '0')
+        std::fprintf(stderr, "kf separable preconditioner set-up (wait for the host job + uploads) %.4f s\n",
+                     std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count());
 }
 
 float *sep_apply(kf_op *op, float *W, float *s1, int k, const double *theta_dev, double eta, cudaStream_t s) {

@@ -534,7 +534,12 @@ static LobOut lobpcg_refine(kf_op *op, RefineWork &Rw, LobWork<float> &Wk, const
     const int64_t N = Wk.N;
     const int w = Wk.w;
     LobOut out;
+    const double ts0 = now_s();
     refine_start(op, Rw, Wk, 1e-12, s, theta, out.nmv);
+    if (trace_on()) {
+        KF_CUDA(cudaStreamSynchronize(s));
+        std::fprintf(stderr, "kf lobpcg refine start (FP64 SVQB, apply, Rayleigh-Ritz) %.4f s\n", now_s() - ts0);
+    }
     double *X = Rw.X.as<double>(), *HX = Rw.HX.as<double>();
     double *Xn = Rw.Xn.as<double>(), *HXn = Rw.HXn.as<double>();
     float *X32 = Wk.X.as<float>();
@@ -809,7 +814,12 @@ static void solve_lobpcg(kf_op *op, const kf_solver_opts &o, int m, const double
         r.iters += iters32;
         r.nmv += nmv32;
     };
+    const double tb0 = now_s();
     build_block(true, o.rng_seed);
+    if (trace_on()) {
+        KF_CUDA(cudaStreamSynchronize(s));
+        std::fprintf(stderr, "kf lobpcg setup: initial block (upload + perturbation) %.4f s\n", now_s() - tb0);
+    }
     bool failed = false;
     try {
         attempt(X0 != nullptr);
@@ -838,7 +848,9 @@ static void solve_lobpcg(kf_op *op, const kf_solver_opts &o, int m, const double
     st.iterations = r.iters;
     st.n_matvec = r.nmv;
     std::vector<double> resid;
+    const double ta0 = now_s();
     accept_and_copy(op, W64.X.as<double>(), w, theta, m, E_out, V_out, resid, s);
+    if (trace_on()) std::fprintf(stderr, "kf lobpcg acceptance (FP64 residuals + V to the host) %.4f s\n", now_s() - ta0);
     st.seconds = now_s() - t0;
     double worst = 0;
     int bad = 0;

@@ -120,6 +120,10 @@ def lib():
         # test-only (include/kfgpu_testing.h)
         "kf_test_mode_product": (C.c_int, [C.c_int32, P, P, P, C.c_int32, C.c_int64, C.c_int64, C.c_int64,
                                            C.c_double, C.c_double, P]),
+        "kf_test_time_mode_product": (C.c_int, [C.c_int32, P, P, P, C.c_int32, C.c_int64, C.c_int64, C.c_int64,
+                                                C.c_int32, P, C.POINTER(C.c_float)]),
+        "kf_test_time_gram": (C.c_int, [P, C.c_int64, C.c_int32, P, C.c_int64, C.c_int32, C.c_int64, C.c_int32, P,
+                                        C.POINTER(C.c_float), P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
