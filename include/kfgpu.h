@@ -131,6 +131,14 @@ int kf_op_set_stream(kf_op *op, void *stream);
 /* Blocks until the op's stream is idle. */
 int kf_op_sync(kf_op *op);
 
+/* product_seed(H, k) (src/apply.jl:655-685): the k lowest product states of the single-axis part
+ * of H (the Kronecker products of the per-axis eigenbases of separable_eigenbases,
+ * src/apply.jl:606-642, ordered by their separable energy, ties by column-major index), or, when
+ * every axis' single-axis sum is diagonal, the unit vectors of the k smallest entries of the
+ * diagonal.  X: N x k, column-major, leading dimension N; flags KF_HOST / KF_DEVICE for where X
+ * lives (device: asynchronous on the op's stream).  KF_EINVAL unless 1 <= k <= N. */
+int kf_op_product_seed(kf_op *op, int32_t k, double *X, int32_t flags);
+
 /* ---- eigensolvers (src/solvers.jl:6-31 custom-solver contract) ---------------------- */
 #define KF_SOLVER_LOBPCG     0   /* src/lobpcg.jl:217-301                                  */
 #define KF_SOLVER_CHEBYSHEV  1   /* src/chebyshev.jl:310-406                               */
@@ -175,7 +183,13 @@ typedef struct {
     double fallback_resid;     /* ... a largest residual above this (absolute, energy units)
                                   restarts a warm-started solve from a random block (0
                                   disables); the judge of a learned warm start                 */
+    int32_t seed_kind;         /* LOBPCG / Chebyshev `seed` (src/tree.jl:66-87, 293-321):
+                                  KF_SEED_PRODUCT (default) or KF_SEED_RANDOM; used when
+                                  kf_solve's seed argument is NULL                             */
 } kf_solver_opts;
+
+#define KF_SEED_PRODUCT 0   /* seed=:product, product_seed(H, w) built by the library         */
+#define KF_SEED_RANDOM  1   /* seed=:random                                                    */
 
 typedef struct {
     int32_t iterations;        /* total iterations (FP32 + FP64)                               */
@@ -197,9 +211,10 @@ void kf_solver_opts_default(kf_solver_opts *opts, int32_t kind);
  * and V (N x m, column-major, orthonormal), both caller-owned HOST memory, like the reference
  * returning host arrays (src/lobpcg.jl:298-299).
  *   X0:   NULL or an N x m warm-start block (LOBPCG only; src/lobpcg.jl:226-233 checks).
- *   seed: NULL or the caller's product_seed(H, w) block, N x w with w = m + guard (LOBPCG) or
- *         m + extra (Chebyshev), the reference's seed=:product (src/apply.jl:655-685 runs on the
- *         caller's side); NULL means seed=:random.
+ *   seed: NULL or a caller's seed block, N x w with w = m + guard (LOBPCG) or m + extra
+ *         (Chebyshev).  NULL: opts->seed_kind decides -- KF_SEED_PRODUCT builds product_seed(H, w)
+ *         on the device, as lobpcg_solve does for seed=:product (src/lobpcg.jl:247,
+ *         src/apply.jl:655-685); KF_SEED_RANDOM draws a random block.
  * Every returned pair is checked with a fresh FP64 application of H (src/solvers.jl:65-69).
  * KF_ENOCONV when a pair is above tol, with the reference's message. */
 int kf_solve(kf_op *op, const kf_solver_opts *opts, int32_t m, const double *X0, const double *seed,

@@ -76,6 +76,31 @@ int kf_op_create(const kf_op_desc *desc, kf_op **out) {
     });
 }
 
+int kf_op_product_seed(kf_op *op, int32_t k, double *X, int32_t flags) {
+    return guarded([&] {
+        KF_REQUIRE(op && X, KF_EINVAL, "kf_op_product_seed: NULL argument");
+        if (flags & KF_HOST) {
+            const size_t bytes = sizeof(double) * (size_t)op->N * (size_t)std::max(k, 0);
+            KF_REQUIRE(k >= 1 && k <= op->N, KF_EINVAL,
+                       "product_seed: k must lie in 1:" + std::to_string(op->N) + " (the operator's dimension), got " +
+                           std::to_string(k));
+            double *d = nullptr;
+            KF_CUDA(cudaMallocAsync((void **)&d, bytes, op->stream));
+            try {
+                kf::product_seed_device(op, k, d, op->stream);
+                KF_CUDA(cudaMemcpyAsync(X, d, bytes, cudaMemcpyDeviceToHost, op->stream));
+                KF_CUDA(cudaStreamSynchronize(op->stream));
+            } catch (...) {
+                cudaFreeAsync(d, op->stream);
+                throw;
+            }
+            KF_CUDA(cudaFreeAsync(d, op->stream));
+        } else {
+            kf::product_seed_device(op, k, X, op->stream);
+        }
+    });
+}
+
 int kf_op_destroy(kf_op *op) {
     return guarded([&] {
         if (!op) return;
@@ -200,6 +225,7 @@ void kf_solver_opts_default(kf_solver_opts *o, int32_t kind) {
     o->mixed_switch = 2e-6;
     o->fallback_iters = 3;
     o->fallback_resid = 0.0;
+    o->seed_kind = KF_SEED_PRODUCT;
 }
 
 int kf_solve(kf_op *op, const kf_solver_opts *opts, int32_t m, const double *X0, const double *seed, double *E_out,

@@ -146,6 +146,7 @@ struct kf_op {
         std::vector<int> ident;               // axis whose sum is diagonal (U = I)
         std::vector<double> lam;              // concatenated per-axis eigenvalues
         std::vector<float *> dU, dUt;         // FP32 U and U' per axis (nullptr when ident)
+        std::vector<double *> dU64;           // FP64 U per axis (nullptr when ident), for product_seed
         std::vector<kf::TcMatrix> tU, tUt;    // the same as tensor-core BF16 images (d <= 256)
         std::vector<std::vector<double>> Uh;  // host eigenbases per axis (empty when ident)
         bool host_ready = false;
@@ -208,6 +209,8 @@ void sep_scale(T *W, int64_t ld, int64_t N, int k, int ndims, const int *dims, c
 void sep_host_prepare(kf_op *op);   // host part only (no CUDA calls)
 void sep_host_prepare(kf_op *op);   // host part only (no CUDA calls)
 void sep_prepare(kf_op *op);
+// product_seed(H, k) into the device block X (N x k, leading dimension N), on stream s
+void product_seed_device(kf_op *op, int k, double *X, cudaStream_t s);
 // W (N x k, FP32, leading dimension N) <- U diag(1 / hypot(S - theta_j, eta)) U' W; s1 is an
 // N x k FP32 scratch.  Returns the block holding the result (W or s1).
 float *sep_apply(kf_op *op, float *W, float *s1, int k, const double *theta_dev, double eta, cudaStream_t s);

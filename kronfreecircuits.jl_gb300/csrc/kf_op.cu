@@ -788,6 +788,7 @@ void free_op(kf_op *op) {
     cudaFree(op->d_scratch);
     for (float *p : op->sep.dU) cudaFree(p);
     for (float *p : op->sep.dUt) cudaFree(p);
+    for (double *p : op->sep.dU64) cudaFree(p);
     for (auto &m : op->sep.tU) kf::tc_matrix_free(m);
     for (auto &m : op->sep.tUt) kf::tc_matrix_free(m);
     cudaFree(op->sep.d_lam);

@@ -10,6 +10,10 @@
 #include <chrono>
 #include <cstdlib>
 #include <cstring>
+#include <algorithm>
+#include <set>
+#include <queue>
+#include <numeric>
 
 #include "kf_internal.h"
 
@@ -27,6 +31,21 @@ void sep_host_prepare(kf_op *op) {
     for (int a = 0; a < nd; ++a) {
         const int d = (int)op->dims[a];
         const std::vector<double> &M = S.M[a];
+        {
+            // src/apply.jl:627-630: a non-Hermitian single-axis sum means H is not Hermitian
+            double asym = 0, nrm = 0;
+            for (int j = 0; j < d; ++j)
+                for (int i = 0; i < d; ++i) {
+                    const double x = M[i + (size_t)d * j], y = M[j + (size_t)d * i];
+                    asym += (x - y) * (x - y);
+                    nrm += x * x;
+                }
+            asym = std::sqrt(asym);
+            nrm = std::sqrt(nrm);
+            if (!(asym <= std::sqrt(2.220446049250313e-16) * nrm))
+                throw Error(KF_EINVAL, "separable_eigenbases: the single-axis terms on axis " + std::to_string(a + 1) +
+                                           " sum to a non-Hermitian matrix, so the operator is not Hermitian");
+        }
         bool diag = true;
         for (int j = 0; j < d && diag; ++j)
             for (int i = 0; i < d; ++i)
@@ -54,6 +73,7 @@ void sep_prepare(kf_op *op) {
     const int nd = (int)op->dims.size();
     S.dU.assign(nd, nullptr);
     S.dUt.assign(nd, nullptr);
+    S.dU64.assign(nd, nullptr);
     S.tU.assign(nd, TcMatrix());
     S.tUt.assign(nd, TcMatrix());
     std::vector<int> off(nd), dims(nd);
@@ -65,6 +85,8 @@ void sep_prepare(kf_op *op) {
         acc += d;
         if (S.ident[a]) continue;
         const std::vector<double> &U = S.Uh[a];
+        KF_CUDA(cudaMalloc(&S.dU64[a], U.size() * 8));
+        KF_CUDA(cudaMemcpy(S.dU64[a], U.data(), U.size() * 8, cudaMemcpyHostToDevice));
         std::vector<float> u32((size_t)d * d), ut32((size_t)d * d);
         for (int j = 0; j < d; ++j)
             for (int i = 0; i < d; ++i) {
@@ -91,6 +113,145 @@ void sep_prepare(kf_op *op) {
     if (tr && tr[0] && tr[0] != '0')
         std::fprintf(stderr, "kf separable preconditioner set-up (wait for the host job + uploads) %.4f s\n",
                      std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count());
+}
+
+// ---- product_seed (src/apply.jl:655-685) ---------------------------------------------------
+
+namespace {
+
+struct SeedArgs {
+    int nd;
+    int dims[MAXDIMS];
+    const double *U[MAXDIMS];   // FP64 eigenbasis of each axis (nullptr: identity)
+};
+
+// X[p, c] = prod_a U_a[i_a(p), idx[c, a]] (axis 1 fastest), the product taken in the order
+// U_{K-1} (... (U_1 U_0)) of the reference's kron chain
+__global__ void k_product_seed(double *__restrict__ X, int64_t N, int k, SeedArgs a, const int *__restrict__ idx) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= N * k) return;
+    const int64_t c = t / N, p = t % N;
+    int64_t rem = p;
+    double v = 1.0;
+    for (int ax = 0; ax < a.nd; ++ax) {
+        const int i = (int)(rem % a.dims[ax]);
+        rem /= a.dims[ax];
+        const int j = idx[c * a.nd + ax];
+        const double u = a.U[ax] ? a.U[ax][i + (int64_t)a.dims[ax] * j] : (i == j ? 1.0 : 0.0);
+        v = u * v;
+    }
+    X[c * N + p] = v;
+}
+
+struct Cand {
+    double sum;
+    int64_t flat;
+    std::vector<int> rank;
+};
+
+}  // namespace
+
+// The k lowest product states' per-axis indices (k x nd, row c = state c), ordered by
+// (separable energy, column-major index).  Best-first search over the lattice of per-axis
+// ranks: every state's lattice predecessors have energies <= its own, so popping until the
+// heap's smallest energy exceeds the k-th popped one visits every state that can rank <= k.
+static std::vector<int> lowest_product_states(kf_op *op, int k) {
+    auto &S = op->sep;
+    const int nd = (int)op->dims.size();
+    std::vector<std::vector<int>> ord(nd);
+    std::vector<int> off(nd);
+    int acc = 0;
+    for (int a = 0; a < nd; ++a) {
+        const int d = (int)op->dims[a];
+        off[a] = acc;
+        acc += d;
+        ord[a].resize(d);
+        std::iota(ord[a].begin(), ord[a].end(), 0);
+        const double *lam = S.lam.data() + off[a];
+        std::stable_sort(ord[a].begin(), ord[a].end(), [&](int x, int y) { return lam[x] < lam[y]; });
+    }
+    auto make = [&](const std::vector<int> &rank) {
+        Cand c;
+        c.rank = rank;
+        c.sum = 0;
+        c.flat = 0;
+        int64_t stride = 1;
+        for (int a = 0; a < nd; ++a) {
+            const int i = ord[a][rank[a]];
+            c.sum = (a == 0) ? S.lam[off[a] + i] : c.sum + S.lam[off[a] + i];
+            c.flat += stride * i;
+            stride *= op->dims[a];
+        }
+        return c;
+    };
+    auto worse = [](const Cand &x, const Cand &y) { return x.sum > y.sum || (x.sum == y.sum && x.flat > y.flat); };
+    std::priority_queue<Cand, std::vector<Cand>, decltype(worse)> heap(worse);
+    std::set<std::vector<int>> seen;
+    std::vector<int> r0(nd, 0);
+    heap.push(make(r0));
+    seen.insert(r0);
+    std::vector<Cand> got;
+    double kth = INFINITY;
+    while (!heap.empty()) {
+        if ((int)got.size() >= k && heap.top().sum > kth) break;
+        Cand c = heap.top();
+        heap.pop();
+        got.push_back(c);
+        if ((int)got.size() == k) kth = c.sum;
+        for (int a = 0; a < nd; ++a) {
+            if (c.rank[a] + 1 >= (int)op->dims[a]) continue;
+            std::vector<int> r = c.rank;
+            ++r[a];
+            if (seen.insert(r).second) heap.push(make(r));
+        }
+    }
+    std::sort(got.begin(), got.end(), [&](const Cand &x, const Cand &y) { return worse(y, x); });
+    std::vector<int> idx((size_t)k * nd);
+    for (int c = 0; c < k; ++c)
+        for (int a = 0; a < nd; ++a) idx[(size_t)c * nd + a] = ord[a][got[c].rank[a]];
+    return idx;
+}
+
+void product_seed_device(kf_op *op, int k, double *X, cudaStream_t s) {
+    const int64_t N = op->N;
+    KF_REQUIRE(k >= 1 && k <= N, KF_EINVAL,
+               "product_seed: k must lie in 1:" + std::to_string(N) + " (the operator's dimension), got " +
+                   std::to_string(k));
+    KF_REQUIRE(!op->sep.M.empty(), KF_EINVAL, "product_seed: the per-axis sums of this operator are too large");
+    sep_prepare(op);
+    auto &S = op->sep;
+    const int nd = (int)op->dims.size();
+    KF_CUDA(cudaMemsetAsync(X, 0, sizeof(double) * (size_t)N * k, s));
+    bool all_ident = true;
+    for (int a = 0; a < nd; ++a) all_ident = all_ident && S.ident[a];
+    if (all_ident) {
+        // unit vectors of the k smallest entries of the full diagonal (ties by index)
+        std::vector<int64_t> ix(N);
+        std::iota(ix.begin(), ix.end(), 0);
+        const double *D = op->h_fulldiag.data();
+        std::partial_sort(ix.begin(), ix.begin() + k, ix.end(),
+                          [&](int64_t x, int64_t y) { return D[x] < D[y] || (D[x] == D[y] && x < y); });
+        const double one = 1.0;
+        for (int j = 0; j < k; ++j)
+            KF_CUDA(cudaMemcpyAsync(X + (size_t)N * j + ix[j], &one, sizeof(double), cudaMemcpyHostToDevice, s));
+        KF_CUDA(cudaStreamSynchronize(s));   // `one` is on this stack frame
+        return;
+    }
+    const std::vector<int> idx = lowest_product_states(op, k);
+    int *didx = nullptr;
+    KF_CUDA(cudaMallocAsync((void **)&didx, idx.size() * sizeof(int), s));
+    KF_CUDA(cudaMemcpyAsync(didx, idx.data(), idx.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+    SeedArgs a;
+    a.nd = nd;
+    for (int ax = 0; ax < MAXDIMS; ++ax) {
+        a.dims[ax] = ax < nd ? (int)op->dims[ax] : 1;
+        a.U[ax] = (ax < nd && !S.ident[ax]) ? S.dU64[ax] : nullptr;
+    }
+    const int64_t tot = N * k;
+    k_product_seed<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(X, N, k, a, didx);
+    KF_LAUNCH_CHECK();
+    KF_CUDA(cudaFreeAsync(didx, s));
+    KF_CUDA(cudaStreamSynchronize(s));   // idx (host) stays valid until the copy is done
 }
 
 float *sep_apply(kf_op *op, float *W, float *s1, int k, const double *theta_dev, double eta, cudaStream_t s) {

@@ -752,6 +752,12 @@ static void solve_lobpcg(kf_op *op, const kf_solver_opts &o, int m, const double
         double *part = W64.dpart.as<double>();
         bool guards_random = true;
         if (use_inputs && X0) {
+            if (!seed && o.seed_kind == KF_SEED_PRODUCT && g > 0) {
+                // the guards of a warm start are the product seed's columns m+1:w (src/lobpcg.jl:182-190)
+                product_seed_device(op, w, Xd, s);
+                perturb_block(Xd + (size_t)N * m, N, g, delta, 0x4b47, R, nrm, part, s);
+                guards_random = false;
+            }
             KF_CUDA(cudaMemcpyAsync(Xd, X0, sizeof(double) * (size_t)N * m, cudaMemcpyHostToDevice, s));
             perturb_block(Xd, N, m, delta, 0x4b46, R, nrm, part, s);
             if (seed) {
@@ -762,6 +768,10 @@ static void solve_lobpcg(kf_op *op, const kf_solver_opts &o, int m, const double
             }
         } else if (use_inputs && seed) {
             KF_CUDA(cudaMemcpyAsync(Xd, seed, sizeof(double) * (size_t)N * w, cudaMemcpyHostToDevice, s));
+            perturb_block(Xd, N, w, delta, 0x4b46, R, nrm, part, s);
+            guards_random = false;
+        } else if (use_inputs && o.seed_kind == KF_SEED_PRODUCT) {
+            product_seed_device(op, w, Xd, s);
             perturb_block(Xd, N, w, delta, 0x4b46, R, nrm, part, s);
             guards_random = false;
         } else {
@@ -920,6 +930,9 @@ static void solve_chebyshev(kf_op *op, const kf_solver_opts &o, int m, const dou
     // the starting block on the device: product seed + 1e-2 admixture (src/chebyshev.jl), or random
     if (seed) {
         KF_CUDA(cudaMemcpyAsync(bufs[0], seed, blk, cudaMemcpyHostToDevice, s));
+        perturb_block(bufs[0], N, nb, SEED_ADMIXTURE, 0x4346, bufs[1], dv.as<double>(), part, s);
+    } else if (o.seed_kind == KF_SEED_PRODUCT) {
+        product_seed_device(op, nb, bufs[0], s);
         perturb_block(bufs[0], N, nb, SEED_ADMIXTURE, 0x4346, bufs[1], dv.as<double>(), part, s);
     } else {
         fill_normal<double>(bufs[0], N, nb, N, o.rng_seed, 3, s);

@@ -12,7 +12,7 @@
 module KronFreeGB300
 
 using KronFreeCircuits
-using KronFreeCircuits: KronFreeOperator, DenseOp, DiagonalOp, BandedOp, ShiftOp, product_seed
+using KronFreeCircuits: KronFreeOperator, DenseOp, DiagonalOp, BandedOp, ShiftOp
 import KronFreeCircuits: solve, storage
 
 const LIB = Ref{String}("libkfgpu.so")
@@ -35,6 +35,7 @@ mutable struct KfSolverOpts
     kind::Int32; precision::Int32; tol::Float64; maxiter::Int32; preconditioner::Int32; eta::Float64
     guard::Int32; degree::Int32; extra::Int32; rescale_every::Int32; ortho::Int32; bound::Float64
     krylovdim::Int32; rng_seed::UInt64; mixed_switch::Float64; fallback_iters::Int32; fallback_resid::Float64
+    seed_kind::Int32
     KfSolverOpts() = new()
 end
 mutable struct KfSolveStats
@@ -131,8 +132,9 @@ function solve(s::GB300Solver, H::KronFreeOperator, m::Int; X0=nothing)
         o.preconditioner = Dict(:ritz => 0, :jacobi => 1, :none => 2, :separable => 3)[s.preconditioner]
         o.degree, o.extra, o.krylovdim = s.degree, s.extra, s.krylovdim
         N = size(H, 1)
-        w = kind == 0 ? m + min(s.guard, (N - 5) ÷ 3 - m) : min(m + s.extra, N)
-        seed = (kind != 2 && s.seed === :product) ? Matrix{Float64}(product_seed(H, w)) : nothing
+        # seed=:product: the library builds product_seed(H, w) on the device (kf_op_product_seed)
+        o.seed_kind = s.seed === :product ? 0 : 1
+        seed = nothing
         x0 = X0 === nothing ? nothing : Matrix{Float64}(X0)
         E = Vector{Float64}(undef, m); V = Matrix{Float64}(undef, N, m); st = KfSolveStats()
         _check(ccall((:kf_solve, LIB[]), Cint,

@@ -38,12 +38,15 @@ class KfOpDesc(C.Structure):
                 ("block_capacity", C.c_int64)]
 
 
+KF_SEED_PRODUCT, KF_SEED_RANDOM = 0, 1
+
+
 class KfSolverOpts(C.Structure):
     _fields_ = [("kind", C.c_int32), ("precision", C.c_int32), ("tol", C.c_double), ("maxiter", C.c_int32),
                 ("preconditioner", C.c_int32), ("eta", C.c_double), ("guard", C.c_int32), ("degree", C.c_int32),
                 ("extra", C.c_int32), ("rescale_every", C.c_int32), ("ortho", C.c_int32), ("bound", C.c_double),
                 ("krylovdim", C.c_int32), ("rng_seed", C.c_uint64), ("mixed_switch", C.c_double),
-                ("fallback_iters", C.c_int32), ("fallback_resid", C.c_double)]
+                ("fallback_iters", C.c_int32), ("fallback_resid", C.c_double), ("seed_kind", C.c_int32)]
 
 
 class KfSolveStats(C.Structure):
@@ -104,6 +107,7 @@ def lib():
         "kf_op_get_stream": (C.c_int, [P, C.POINTER(P)]),
         "kf_op_set_stream": (C.c_int, [P, P]),
         "kf_op_sync": (C.c_int, [P]),
+        "kf_op_product_seed": (C.c_int, [P, C.c_int32, P, C.c_int32]),
         "kf_solver_opts_default": (None, [C.POINTER(KfSolverOpts), C.c_int32]),
         "kf_solve": (C.c_int, [P, C.POINTER(KfSolverOpts), C.c_int32, P, P, P, P, C.POINTER(KfSolveStats)]),
         "kf_batch_solve": (C.c_int, [C.POINTER(KfOpDesc), C.c_int32, C.POINTER(C.c_int32), C.c_double, C.c_int32,

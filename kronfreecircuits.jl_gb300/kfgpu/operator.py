@@ -170,6 +170,12 @@ class KronFreeOperator:
                 lam.append(w)
         return U, lam
 
+    def product_seed_device(self, k):
+        """product_seed(H, k) built by the library on the device (kf_op_product_seed), host N x k."""
+        X = np.empty((self.N, k), order="F")
+        check(lib().kf_op_product_seed(self._h, int(k), X.ctypes.data, _abi.KF_HOST))
+        return X
+
     def product_seed(self, k):
         """k orthonormal lowest product states (src/apply.jl:655-685), host N x k."""
         if not 1 <= k <= self.N:

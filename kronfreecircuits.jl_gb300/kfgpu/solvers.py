@@ -50,6 +50,7 @@ class LOBPCG:
         o.preconditioner = {"ritz": 0, "jacobi": 1, "none": 2, "separable": 3}[self.preconditioner]
         o.eta, o.guard, o.mixed_switch = self.eta, self.guard, self.mixed_switch
         o.fallback_iters, o.fallback_resid, o.rng_seed = self.fallback_iters, self.fallback_resid, self.rng_seed
+        o.seed_kind = _abi.KF_SEED_PRODUCT if self.seed == "product" else _abi.KF_SEED_RANDOM
         return o
 
     def width(self, N, m):
@@ -81,6 +82,7 @@ class ChebyshevFilter:
         o.degree, o.extra, o.rescale_every = self.degree, self.extra, self.rescale_every
         o.ortho = 0 if self.ortho == "svqb" else 1
         o.bound = float("nan") if self.bound == "gershgorin" else float(self.bound)
+        o.seed_kind = _abi.KF_SEED_PRODUCT if self.seed == "product" else _abi.KF_SEED_RANDOM
         o.rng_seed = self.rng_seed
         return o
 
@@ -105,16 +107,14 @@ class Lanczos:
 def solve(s, H, m, X0=None, seed_block=None):
     """The lowest m eigenpairs of H: (E ascending, V N x m host, stats dict).
 
-    With `s.seed == "product"` the product seed is built here on the host (the reference builds
-    it on the host too, src/lobpcg.jl:247) unless `seed_block` is given.
+    With `s.seed == "product"` the library builds product_seed(H, w) on the device, as the
+    reference's solve does (src/lobpcg.jl:247); `seed_block` (N x w, host) replaces it.
     """
     N = H.N
     o = s.opts()
     seed_arr = None
-    if not isinstance(s, Lanczos) and s.seed == "product":
-        w = s.width(N, m)
-        if w >= 1:
-            seed_arr = np.asfortranarray(seed_block if seed_block is not None else H.product_seed(w), dtype=np.float64)
+    if not isinstance(s, Lanczos) and seed_block is not None:
+        seed_arr = np.asfortranarray(seed_block, dtype=np.float64)
     x0 = None
     if X0 is not None:
         x0 = np.asfortranarray(X0, dtype=np.float64)

@@ -206,3 +206,24 @@ def test_three_mode_leaf_full_size_mixed_vs_f64(cuda):
     for E, V in ((E64, V64), (Em, Vm)):
         R = Ho.matvec(V) - V * E[None, :]
         assert np.max(np.sqrt(np.sum(R ** 2, axis=0))) <= tol
+
+
+def test_device_product_seed_matches_host(cuda):
+    """kf_op_product_seed (product_seed, src/apply.jl:655-685, built on the device) spans the same
+    states as the host mirror: orthonormal columns, the same product states up to sign (the
+    per-axis eigenvectors' signs are free)."""
+    from kfgpu import KronFreeOperator, ArgumentError, circuits, ops as P
+    th = circuits.three_mode_theta(np.random.default_rng(8))
+    dims, terms = circuits.three_mode_leaf(th, ncut=6, n2=48, n3=20)
+    H = KronFreeOperator(dims, terms)
+    for k in (1, 16, 40):
+        Xd = H.product_seed_device(k)
+        Xh = H.product_seed(k)
+        assert np.allclose(Xd.T @ Xd, np.eye(k), atol=1e-12)
+        assert np.allclose(np.abs(np.sum(Xd * Xh, axis=0)), 1.0, atol=1e-9)
+    with pytest.raises(ArgumentError, match="product_seed: k must lie in"):
+        H.product_seed_device(H.N + 1)
+    # every axis diagonal: unit vectors at the smallest entries of the full diagonal
+    D = KronFreeOperator([7, 5], [(1.0, [(0, P.DiagonalOp(np.arange(7.0)[::-1]))]),
+                                  (0.5, [(1, P.DiagonalOp(np.arange(5.0)))])])
+    assert np.array_equal(D.product_seed_device(4), D.product_seed(4))
