@@ -141,6 +141,17 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
 
+// A set of FP32 columns in up to two blocks: columns [0, n0) at p0 + c ld0, the rest at
+// p1 + (c - n0) ld1 (so [X Z] needs no copy)
+struct Cols2 {
+    const float *p0, *p1;
+    int64_t ld0, ld1;
+    int n0;
+    __device__ __forceinline__ const float *col(int c) const {
+        return c < n0 ? p0 + (int64_t)c * ld0 : p1 + (int64_t)(c - n0) * ld1;
+    }
+};
+
 struct Gram32Shape {
     int nti, ntj, gti, gtj, ngi, ngj;   // tiles per axis, group size in tiles, groups per axis
     int tr;                             // rows per batch
@@ -169,10 +180,10 @@ static size_t gram32_smem(const Gram32Shape &g) {
     return (size_t)G32_STAGES * 8 * (g.gti + g.gtj) * (g.tr + G32_PAD) * sizeof(float);
 }
 
-// stage rows [row0, row0 + tr) of `nc` columns (column c at src + c * ld) into dst (column
-// stride tr + G32_PAD); rows at or past `rend` are zero-filled
+// stage rows [row0, row0 + tr) of columns c0 .. c0 + nc - 1 of the column set `src` into dst
+// (column stride tr + G32_PAD); rows at or past `rend` are zero-filled
 template <bool VEC>
-__device__ __forceinline__ void g32_stage(float *dst, const float *src, int64_t ld, int nc, int tr, int64_t row0,
+__device__ __forceinline__ void g32_stage(float *dst, const Cols2 &src, int c0, int nc, int tr, int64_t row0,
                                           int64_t rend) {
     const int S = tr + G32_PAD;
     if (VEC) {
@@ -182,7 +193,7 @@ __device__ __forceinline__ void g32_stage(float *dst, const float *src, int64_t 
             const int64_t r = row0 + 4 * q;
             const int64_t left = rend - r;
             const int bytes = left >= 4 ? 16 : left > 0 ? (int)left * 4 : 0;
-            const float *g = src + (int64_t)c * ld + (bytes > 0 ? r : 0);
+            const float *g = src.col(c0 + c) + (bytes > 0 ? r : 0);
             cp_async16(dst + c * S + 4 * q, g, bytes);
         }
     } else {
@@ -190,7 +201,7 @@ __device__ __forceinline__ void g32_stage(float *dst, const float *src, int64_t 
             const int c = e / tr, q = e % tr;
             const int64_t r = row0 + q;
             const bool ok = r < rend;
-            cp_async4(dst + c * S + q, src + (int64_t)c * ld + (ok ? r : 0), ok ? 4 : 0);
+            cp_async4(dst + c * S + q, src.col(c0 + c) + (ok ? r : 0), ok ? 4 : 0);
         }
     }
 }
@@ -208,8 +219,7 @@ __device__ __forceinline__ void g32_butterfly(float *f, int lane) {
 }
 
 template <bool VEC>
-__global__ void __launch_bounds__(256, 2) k_gram32(const float *__restrict__ A, int64_t lda, int ka,
-                                                   const float *__restrict__ B, int64_t ldb, int kb, int64_t N,
+__global__ void __launch_bounds__(256, 2) k_gram32(const Cols2 A, int ka, const Cols2 B, int kb, int64_t N,
                                                    int64_t rows_per, Gram32Shape sh, double *__restrict__ partials) {
     extern __shared__ __align__(16) unsigned char g32_smem[];
     const int tr = sh.tr, S = tr + G32_PAD;
@@ -247,8 +257,8 @@ __global__ void __launch_bounds__(256, 2) k_gram32(const float *__restrict__ A, 
         if (t < nb) {
             float *st = buf0 + t * bstride;
             const int64_t rn = r0 + (int64_t)t * tr;
-            g32_stage<VEC>(st, A + ca0 * lda, lda, nca, tr, rn, r1);
-            g32_stage<VEC>(st + sa * S, B + cb0 * ldb, ldb, ncb, tr, rn, r1);
+            g32_stage<VEC>(st, A, ca0, nca, tr, rn, r1);
+            g32_stage<VEC>(st + sa * S, B, cb0, ncb, tr, rn, r1);
         }
         cp_async_commit();
     }
@@ -258,8 +268,8 @@ __global__ void __launch_bounds__(256, 2) k_gram32(const float *__restrict__ A, 
         if (bn < nb) {
             float *st = buf0 + (bn % G32_STAGES) * bstride;
             const int64_t rn = r0 + (int64_t)bn * tr;
-            g32_stage<VEC>(st, A + ca0 * lda, lda, nca, tr, rn, r1);
-            g32_stage<VEC>(st + sa * S, B + cb0 * ldb, ldb, ncb, tr, rn, r1);
+            g32_stage<VEC>(st, A, ca0, nca, tr, rn, r1);
+            g32_stage<VEC>(st + sa * S, B, cb0, ncb, tr, rn, r1);
         }
         cp_async_commit();
         cp_async_wait<G32_STAGES - 1>();   // batch b has landed (this thread's copies)
@@ -306,40 +316,51 @@ __global__ void __launch_bounds__(256, 2) k_gram32(const float *__restrict__ A, 
     }
 }
 
+// G ((ka0 + ka1) x (kb0 + kb1), column-major, FP64) = [A0 A1]' [B0 B1] for FP32 column blocks
+void gram32_sets(const float *A0, int64_t lda0, int ka0, const float *A1, int64_t lda1, int ka1, const float *B0,
+                 int64_t ldb0, int kb0, const float *B1, int64_t ldb1, int kb1, int64_t N, double *G, double *partials,
+                 cudaStream_t s) {
+    const int ka = ka0 + ka1, kb = kb0 + kb1;
+    KF_REQUIRE(ka >= 1 && kb >= 1 && ka <= 128 && kb <= 128, KF_EINVAL, "gram: block widths out of range");
+    const Cols2 A{A0, ka1 > 0 ? A1 : A0, lda0, ka1 > 0 ? lda1 : lda0, ka0};
+    const Cols2 B{B0, kb1 > 0 ? B1 : B0, ldb0, kb1 > 0 ? ldb1 : ldb0, kb0};
+    const Gram32Shape sh = gram32_shape(ka, kb);
+    const int groups = sh.ngi * sh.ngj;
+    // about 2 CTAs per SM over all groups, whole batches per CTA, never more row blocks than
+    // gram_partials_size provides for
+    int64_t target = (304 + groups - 1) / groups;
+    int64_t rp = (N + target - 1) / target;
+    if (rp < 256) rp = 256;
+    rp = (rp + sh.tr - 1) / sh.tr * sh.tr;
+    const int nc = (int)((N + rp - 1) / rp);
+    const size_t smem = gram32_smem(sh);
+    auto al = [](const float *p, int64_t ld) { return ld % 4 == 0 && (uintptr_t)p % 16 == 0; };
+    const bool vec = al(A.p0, A.ld0) && al(A.p1, A.ld1) && al(B.p0, B.ld0) && al(B.p1, B.ld1);
+    static int attr_dev_mask[2] = {0, 0};   // devices whose kernel attribute is set, per variant
+    int dev = 0;
+    KF_CUDA(cudaGetDevice(&dev));
+    if (dev < 31 && !(attr_dev_mask[vec] & (1 << dev))) {
+        if (vec)
+            KF_CUDA(cudaFuncSetAttribute(k_gram32<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, G32_SMEM));
+        else
+            KF_CUDA(cudaFuncSetAttribute(k_gram32<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, G32_SMEM));
+        attr_dev_mask[vec] |= 1 << dev;
+    }
+    if (vec)
+        k_gram32<true><<<dim3(nc, groups), 256, smem, s>>>(A, ka, B, kb, N, rp, sh, partials);
+    else
+        k_gram32<false><<<dim3(nc, groups), 256, smem, s>>>(A, ka, B, kb, N, rp, sh, partials);
+    KF_LAUNCH_CHECK();
+    reduce_partials(partials, nc, ka * kb, G, s);
+}
+
 template <typename T>
 void gram(const T *A, int64_t lda, int ka, const T *B, int64_t ldb, int kb, int64_t N, double *G, double *partials,
           cudaStream_t s) {
     KF_REQUIRE(ka >= 1 && kb >= 1 && ka <= 128 && kb <= 128, KF_EINVAL, "gram: block widths out of range");
     if constexpr (sizeof(T) == 4) {
-        const Gram32Shape sh = gram32_shape(ka, kb);
-        const int groups = sh.ngi * sh.ngj;
-        // about 2 CTAs per SM over all groups, whole batches per CTA, never more row blocks than
-        // gram_partials_size provides for
-        int64_t target = (304 + groups - 1) / groups;
-        int64_t rp = (N + target - 1) / target;
-        if (rp < 256) rp = 256;
-        rp = (rp + sh.tr - 1) / sh.tr * sh.tr;
-        const int nc = (int)((N + rp - 1) / rp);
-        const size_t smem = gram32_smem(sh);
-        const bool vec = (lda % 4 == 0) && (ldb % 4 == 0) && ((uintptr_t)A % 16 == 0) && ((uintptr_t)B % 16 == 0);
-        static int attr_dev_mask[2] = {0, 0};   // devices whose kernel attribute is set, per variant
-        int dev = 0;
-        KF_CUDA(cudaGetDevice(&dev));
-        if (dev < 31 && !(attr_dev_mask[vec] & (1 << dev))) {
-            if (vec)
-                KF_CUDA(cudaFuncSetAttribute(k_gram32<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, G32_SMEM));
-            else
-                KF_CUDA(cudaFuncSetAttribute(k_gram32<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, G32_SMEM));
-            attr_dev_mask[vec] |= 1 << dev;
-        }
-        if (vec)
-            k_gram32<true><<<dim3(nc, groups), 256, smem, s>>>((const float *)A, lda, ka, (const float *)B, ldb, kb, N,
-                                                               rp, sh, partials);
-        else
-            k_gram32<false><<<dim3(nc, groups), 256, smem, s>>>((const float *)A, lda, ka, (const float *)B, ldb, kb,
-                                                                N, rp, sh, partials);
-        KF_LAUNCH_CHECK();
-        reduce_partials(partials, nc, ka * kb, G, s);
+        gram32_sets((const float *)A, lda, ka, nullptr, 0, 0, (const float *)B, ldb, kb, nullptr, 0, 0, N, G, partials,
+                    s);
         return;
     }
     // FP64: output chunks of 4 x 8 accumulators per thread
@@ -393,8 +414,9 @@ __global__ void k_update(T *__restrict__ Y, int64_t ldy, int ky, const T *__rest
 // padded to a multiple of UC columns with zeros.  For kx <= KX.
 template <typename T, int KX, int UC>
 __global__ void __launch_bounds__(256) k_update_reg(T *__restrict__ Y, int64_t ldy, int ky, const T *__restrict__ X,
-                                                    int64_t ldx, int kx, const double *__restrict__ C, int ldc,
-                                                    T alpha, T beta, int64_t N) {
+                                                    int64_t ldx, int kx0, const T *__restrict__ X1, int64_t ldx1,
+                                                    int kx, const double *__restrict__ C, int ldc, T alpha, T beta,
+                                                    int64_t N) {
     extern __shared__ __align__(16) unsigned char smem_raw_reg[];
     T *Cs = reinterpret_cast<T *>(smem_raw_reg);   // [kx][kyp]
     const int kyp = (ky + UC - 1) / UC * UC;
@@ -405,9 +427,11 @@ __global__ void __launch_bounds__(256) k_update_reg(T *__restrict__ Y, int64_t l
     __syncthreads();
     const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= N) return;
+    // operand i of the row: X[:, i] for i < kx0, X1[:, i - kx0] after
     T x[KX];
 #pragma unroll
-    for (int i = 0; i < KX; ++i) x[i] = (i < kx) ? X[r + (int64_t)i * ldx] : T(0);
+    for (int i = 0; i < KX; ++i)
+        x[i] = (i < kx0) ? X[r + (int64_t)i * ldx] : (i < kx) ? X1[r + (int64_t)(i - kx0) * ldx1] : T(0);
     for (int j0 = 0; j0 < ky; j0 += UC) {
         T acc[UC];
 #pragma unroll
@@ -431,6 +455,29 @@ __global__ void __launch_bounds__(256) k_update_reg(T *__restrict__ Y, int64_t l
 }
 
 template <typename T>
+static void update_reg_launch(T *Y, int64_t ldy, int ky, const T *X0, int64_t ldx0, int kx0, const T *X1,
+                              int64_t ldx1, int kx1, const double *C, int ldc, double alpha, double beta, int64_t N,
+                              cudaStream_t s) {
+    constexpr int UC = sizeof(T) == 8 ? 4 : 8;
+    const int kx = kx0 + kx1;
+    const int kyp = (ky + UC - 1) / UC * UC;
+    const size_t smr = (size_t)kx * kyp * sizeof(T);
+    const unsigned grid = (unsigned)((N + 255) / 256);
+    const T a = (T)alpha, b = (T)beta;
+    if (!X1) X1 = X0;
+    if (kx <= 8)
+        k_update_reg<T, 8, UC><<<grid, 256, smr, s>>>(Y, ldy, ky, X0, ldx0, kx0, X1, ldx1, kx, C, ldc, a, b, N);
+    else if (kx <= 16)
+        k_update_reg<T, 16, UC><<<grid, 256, smr, s>>>(Y, ldy, ky, X0, ldx0, kx0, X1, ldx1, kx, C, ldc, a, b, N);
+    else if (kx <= 32)
+        k_update_reg<T, 32, UC><<<grid, 256, smr, s>>>(Y, ldy, ky, X0, ldx0, kx0, X1, ldx1, kx, C, ldc, a, b, N);
+    else
+        k_update_reg<T, (sizeof(T) == 8 ? 32 : 64), UC><<<grid, 256, smr, s>>>(Y, ldy, ky, X0, ldx0, kx0, X1, ldx1, kx,
+                                                                               C, ldc, a, b, N);
+    KF_LAUNCH_CHECK();
+}
+
+template <typename T>
 void update(T *Y, int64_t ldy, int ky, const T *X, int64_t ldx, int kx, const double *C, int ldc, double alpha,
             double beta, int64_t N, cudaStream_t s) {
     if (ky <= 0 || N <= 0) return;
@@ -447,17 +494,7 @@ void update(T *Y, int64_t ldy, int ky, const T *X, int64_t ldx, int kx, const do
     const size_t smr = (size_t)kx * kyp * sizeof(T);
     const int kxmax = sizeof(T) == 8 ? 32 : 64;
     if (kx <= kxmax && smr <= 48 * 1024) {
-        const T a = (T)alpha, b = (T)beta;
-        if (kx <= 8)
-            k_update_reg<T, 8, UC><<<grid, 256, smr, s>>>(Y, ldy, ky, X, ldx, kx, C, ldc, a, b, N);
-        else if (kx <= 16)
-            k_update_reg<T, 16, UC><<<grid, 256, smr, s>>>(Y, ldy, ky, X, ldx, kx, C, ldc, a, b, N);
-        else if (kx <= 32)
-            k_update_reg<T, 32, UC><<<grid, 256, smr, s>>>(Y, ldy, ky, X, ldx, kx, C, ldc, a, b, N);
-        else
-            k_update_reg<T, (sizeof(T) == 8 ? 32 : 64), UC><<<grid, 256, smr, s>>>(Y, ldy, ky, X, ldx, kx, C, ldc, a,
-                                                                                   b, N);
-        KF_LAUNCH_CHECK();
+        update_reg_launch<T>(Y, ldy, ky, X, ldx, kx, nullptr, 0, 0, C, ldc, alpha, beta, N, s);
         return;
     }
     const size_t sm = (size_t)kx * ky * sizeof(T);
@@ -473,6 +510,24 @@ void update(T *Y, int64_t ldy, int ky, const T *X, int64_t ldx, int kx, const do
     else
         k_update<T, 16><<<grid, 256, sm, s>>>(Y, ldy, ky, X, ldx, kx, C, ldc, (T)alpha, (T)beta, N);
     KF_LAUNCH_CHECK();
+}
+
+// Y = alpha [X0 X1] C + beta Y: the operands of each row from two blocks (kx0 + kx1 columns), C
+// ((kx0 + kx1) x ky, FP64, leading dimension ldc)
+template <typename T>
+void update2(T *Y, int64_t ldy, int ky, const T *X0, int64_t ldx0, int kx0, const T *X1, int64_t ldx1, int kx1,
+             const double *C, int ldc, double alpha, double beta, int64_t N, cudaStream_t s) {
+    if (ky <= 0 || N <= 0) return;
+    constexpr int UC = sizeof(T) == 8 ? 4 : 8;
+    const int kx = kx0 + kx1;
+    const int kyp = (ky + UC - 1) / UC * UC;
+    const int kxmax = sizeof(T) == 8 ? 32 : 64;
+    if (kx0 > 0 && kx1 > 0 && kx <= kxmax && (size_t)kx * kyp * sizeof(T) <= 48 * 1024) {
+        update_reg_launch<T>(Y, ldy, ky, X0, ldx0, kx0, X1, ldx1, kx1, C, ldc, alpha, beta, N, s);
+        return;
+    }
+    update<T>(Y, ldy, ky, X0, ldx0, kx0, C, ldc, alpha, beta, N, s);
+    update<T>(Y, ldy, ky, X1, ldx1, kx1, C + kx0, ldc, alpha, kx0 > 0 ? 1.0 : beta, N, s);
 }
 
 // ---- column reductions -------------------------------------------------------------------
@@ -807,6 +862,8 @@ void copy_block(const T *X, int64_t ldx, T *Y, int64_t ldy, int k, int64_t N, cu
 // explicit instantiations
 #define KF_INST(T)                                                                                                   \
     template void gram<T>(const T *, int64_t, int, const T *, int64_t, int, int64_t, double *, double *, cudaStream_t); \
+    template void update2<T>(T *, int64_t, int, const T *, int64_t, int, const T *, int64_t, int, const double *, int,   \
+                             double, double, int64_t, cudaStream_t);                                                \
     template void update<T>(T *, int64_t, int, const T *, int64_t, int, const double *, int, double, double, int64_t, \
                             cudaStream_t);                                                                           \
     template void colnorms2<T>(const T *, int64_t, int, int64_t, double *, double *, cudaStream_t);                  \

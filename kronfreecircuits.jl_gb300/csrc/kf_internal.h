@@ -175,6 +175,14 @@ void residual_mixed(const double *X, const double *HX, int64_t ld, int k, int64_
                     int64_t ldw, double *norms2, double *partials, cudaStream_t s);
 void add_f32_into_f64(double *Y, int64_t ldy, const float *P, int64_t ldp, float *Y32, int64_t ld32, int k, int64_t N,
                       cudaStream_t s);
+// G = [A0 A1]' [B0 B1] for FP32 column blocks (a block with 0 columns is skipped)
+void gram32_sets(const float *A0, int64_t lda0, int ka0, const float *A1, int64_t lda1, int ka1, const float *B0,
+                 int64_t ldb0, int kb0, const float *B1, int64_t ldb1, int kb1, int64_t N, double *G, double *partials,
+                 cudaStream_t s);
+// Y = alpha [X0 X1] C + beta Y
+template <typename T>
+void update2(T *Y, int64_t ldy, int ky, const T *X0, int64_t ldx0, int kx0, const T *X1, int64_t ldx1, int kx1,
+             const double *C, int ldc, double alpha, double beta, int64_t N, cudaStream_t s);
 size_t gram_partials_size(int ka, int kb, int64_t N);
 template <typename T>
 void update(T *Y, int64_t ldy, int ky, const T *X, int64_t ldx, int kx, const double *C_dev, int ldc,

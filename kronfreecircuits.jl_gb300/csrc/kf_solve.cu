@@ -243,15 +243,58 @@ static void h2d(double *d, const double *h, size_t n, cudaStream_t s) {
 
 // Orthonormalise Zb (N x k, leading dimension N) against X (N x w) and itself, twice; the
 // result lands in `out` (N x r, may be Zt or Z).  Returns r.  `tmp` is an N x k scratch.
+//
+// FP32 blocks take one Gram launch and one update per pass: G = X'Z and S = Z'Z come from one
+// pass over [X Z]' Z; the Gram of the projected block (I - XX')Z is S - G'G (X orthonormal), its
+// SVQB transform T is computed on the host, and the projection and T are applied together,
+// Z_new = Z T - X (G T).  The second pass absorbs what the first lost to cancellation in S - G'G.
+// FP64 blocks project with one classical Gram-Schmidt step and then run SVQB, per pass.
 template <typename T>
 static int ortho_against(kf_op *op, LobWork<T> &W, T *Zb, int k, const T *X, int wx, T *tmp, T *&result,
                          double cutoff, cudaStream_t s) {
     const int64_t N = W.N;
     double *G = W.dG.template as<double>();
     double *part = W.dpart.template as<double>();
+    double *hG = W.hG.template as<double>();
+    double *hC = W.hC.template as<double>();
+    double *C = W.dC.template as<double>();
     T *cur = Zb, *other = tmp;
     int r = k;
     for (int pass = 0; pass < 2; ++pass) {
+        if constexpr (sizeof(T) == 4) {
+            if (wx > 0) {
+                // [X Z]' Z: rows 0..wx-1 = G = X'Z, rows wx.. = S = Z'Z ((wx + r) x r, column-major)
+                gram32_sets((const float *)X, N, wx, (const float *)cur, N, r, (const float *)cur, N, r, nullptr, 0, 0,
+                            N, G, part, s);
+                const int ld = wx + r;
+                d2h_sync<T>(hG, G, (size_t)ld * r, s);
+                std::vector<double> Sp((size_t)r * r);
+                for (int j = 0; j < r; ++j)
+                    for (int i = 0; i < r; ++i) {
+                        double v = hG[wx + i + (size_t)ld * j];
+                        for (int q = 0; q < wx; ++q) v -= hG[q + (size_t)ld * i] * hG[q + (size_t)ld * j];
+                        Sp[i + (size_t)r * j] = v;
+                    }
+                std::vector<double> Tc;
+                const int r2 = svqb_coeffs(r, Sp.data(), cutoff, Tc);
+                if (r2 == 0) { result = cur; return 0; }
+                // coefficients of [Z X]: T on top, -G T below ((r + wx) x r2)
+                const int lc = r + wx;
+                for (int j = 0; j < r2; ++j) {
+                    for (int i = 0; i < r; ++i) hC[i + (size_t)lc * j] = Tc[i + (size_t)r * j];
+                    for (int q = 0; q < wx; ++q) {
+                        double v = 0;
+                        for (int i = 0; i < r; ++i) v += hG[q + (size_t)ld * i] * Tc[i + (size_t)r * j];
+                        hC[r + q + (size_t)lc * j] = -v;
+                    }
+                }
+                h2d(C, hC, (size_t)lc * r2, s);
+                update2<T>(other, N, r2, cur, N, r, X, N, wx, C, lc, 1.0, 0.0, N, s);
+                std::swap(cur, other);
+                r = r2;
+                continue;
+            }
+        }
         if (wx > 0) {
             // one classical Gram-Schmidt projection per pass; with the SVQB between the two passes
             // this is "twice is enough" against X
@@ -259,14 +302,11 @@ static int ortho_against(kf_op *op, LobWork<T> &W, T *Zb, int k, const T *X, int
             update<T>(cur, N, r, X, N, wx, G, wx, -1.0, 1.0, N, s);
         }
         gram<T>(cur, N, r, cur, N, r, N, G, part, s);
-        double *hG = W.hG.template as<double>();
         d2h_sync<T>(hG, G, (size_t)r * r, s);
         std::vector<double> Tc;
         const int r2 = svqb_coeffs(r, hG, cutoff, Tc);
         if (r2 == 0) { result = cur; return 0; }
-        double *hC = W.hC.template as<double>();
         std::memcpy(hC, Tc.data(), sizeof(double) * (size_t)r * r2);
-        double *C = W.dC.template as<double>();
         h2d(C, hC, (size_t)r * r2, s);
         update<T>(other, N, r2, cur, N, r, C, r, 1.0, 0.0, N, s);
         std::swap(cur, other);
