@@ -252,8 +252,8 @@ int kf_test_mode_product(int path, const float *X, float *Y, const double *A, in
         KF_REQUIRE(d >= 1 && left >= 1 && N % d == 0 && (N / d) % left == 0, KF_EDIM,
                    "kf_test_mode_product: N must be a multiple of d * left");
         cudaStream_t s = (cudaStream_t)stream;
-        if (path == 1) {
-            kf::TcMatrix m = kf::tc_matrix_create(A, d, false);
+        if (path == 1 || path == 2) {
+            kf::TcMatrix m = kf::tc_matrix_create(A, d, false, path == 2);
             kf::tc_mode_product(Y, N, X, N, m, left, N, b, alpha, beta, s);
             const cudaError_t e = cudaStreamSynchronize(s);
             kf::tc_matrix_free(m);
@@ -282,8 +282,8 @@ int kf_test_time_mode_product(int path, const float *X, float *Y, const double *
         cudaStream_t s = (cudaStream_t)stream;
         kf::TcMatrix m;
         float *dA = nullptr;
-        if (path == 1) {
-            m = kf::tc_matrix_create(A, d, false);
+        if (path == 1 || path == 2) {
+            m = kf::tc_matrix_create(A, d, false, path == 2);
         } else {
             std::vector<float> a32((size_t)d * d);
             for (size_t i = 0; i < a32.size(); ++i) a32[i] = (float)A[i];
@@ -291,7 +291,7 @@ int kf_test_time_mode_product(int path, const float *X, float *Y, const double *
             KF_CUDA(cudaMemcpy(dA, a32.data(), a32.size() * 4, cudaMemcpyHostToDevice));
         }
         auto launch = [&] {
-            if (path == 1) kf::tc_mode_product(Y, N, X, N, m, left, N, b, 1.0, 0.0, s);
+            if (path == 1 || path == 2) kf::tc_mode_product(Y, N, X, N, m, left, N, b, 1.0, 0.0, s);
             else kf::mode_product<float>(Y, N, X, N, dA, d, left, N, b, 1.0, 0.0, s);
         };
         cudaEvent_t e0, e1;
@@ -306,7 +306,7 @@ int kf_test_time_mode_product(int path, const float *X, float *Y, const double *
         KF_CUDA(cudaEventElapsedTime(&ms, e0, e1));
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
-        if (path == 1) kf::tc_matrix_free(m);
+        if (path == 1 || path == 2) kf::tc_matrix_free(m);
         else cudaFree(dA);
         if (const int t = kf::tc_take_error()) throw kf::Error(t, "tensor-core mode product: device wait timed out");
         *ms_per_launch = ms / reps;

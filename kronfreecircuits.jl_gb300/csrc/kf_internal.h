@@ -83,6 +83,7 @@ struct ChainFactor {
     int nb;
     int off[MAXB];
     size_t data_off;           // dense: n*n matrix (column-major); banded: n*nb weights
+    int tc = -1;               // dense: index of its TF32-split tensor-core image in kf_op::chain_tc
 };
 struct ChainTerm {
     double coeff;
@@ -94,11 +95,13 @@ struct ChainTerm {
 struct TcMatrix {
     void *img = nullptr;
     int d = 0, Mp = 0, Kp = 0;
+    int split = 0;   // 0: BF16 operands; 1: TF32 hi / lo operands (three MMAs, FP32-accurate products)
 };
 int tc_mode_layout_ok(int d);
-TcMatrix tc_matrix_create(const double *A, int d, bool transpose);
+TcMatrix tc_matrix_create(const double *A, int d, bool transpose, bool split = false);
 void tc_matrix_free(TcMatrix &m);
 size_t tc_mode_smem(const TcMatrix &m);
+bool tc_mode_fits(int d, bool split);
 void tc_mode_product(float *Y, int64_t ldy, const float *X, int64_t ldx, const TcMatrix &A, int64_t left, int64_t N,
                      int64_t b, double alpha, double beta, cudaStream_t s);
 int tc_take_error();   // a pending device-side timeout (KF_ETIMEOUT) of a tensor-core launch, cleared
@@ -124,6 +127,7 @@ struct kf_op {
     float *d_w32 = nullptr;
     // dense-chain terms and their data (FP64 and FP32 copies)
     std::vector<kf::ChainTerm> chains;
+    std::vector<kf::TcMatrix> chain_tc;   // tensor-core images of dense chain factors (FP32 applies)
     double *d_chain64 = nullptr;
     float *d_chain32 = nullptr;
     // scratch for chains: two buffers of N * cap doubles

@@ -21,6 +21,8 @@
 #include <cstring>
 #include <map>
 
+#include <mutex>
+#include <string>
 #include "kf_internal.h"
 
 namespace kf {
@@ -183,6 +185,23 @@ __global__ void k_axpby_cols(T *__restrict__ Y, int64_t ldy, const T *__restrict
 // ------------------------------------------------------------------------------------------
 // host launch
 
+// fused-apply variant chosen per (device, stencil shape, precision and width class)
+static std::mutex g_tune_mu;
+static std::map<std::string, int> g_tune;
+
+static std::string tune_key(const kf_op *op, int slot) {
+    const ApplyPlan &P = op->plan;
+    std::string k = std::to_string(op->device) + ":" + std::to_string(slot) + ":" + std::to_string(P.N) + ":" +
+                    std::to_string(P.ne);
+    for (int a = 0; a < P.ndims; ++a) k += "," + std::to_string(P.dims[a]);
+    for (int e = 0; e < P.ne; ++e) {
+        const Entry &E = P.e[e];
+        k += ";" + std::to_string(E.nf) + "/" + std::to_string(E.a0) + "/" + std::to_string(E.o0) + "/" +
+             std::to_string(E.a1) + "/" + std::to_string(E.o1);
+    }
+    return k;
+}
+
 template <typename T>
 static void apply_t(kf_op *op, const T *X, T *Y, int64_t ldx, int64_t ldy, int64_t b, double alpha, double beta,
                     const T *Z, int64_t ldz, double gamma, cudaStream_t s) {
@@ -214,6 +233,14 @@ static void apply_t(kf_op *op, const T *X, T *Y, int64_t ldx, int64_t ldy, int64
     // autotune: on the first apply of a block this wide (per precision), time every variant on the
     // caller's own buffers (each overwrites Y completely with the same result) and keep the fastest
     const int slot = (f32 ? 1 : 0) * 8 + (b >= 32 ? 3 : b >= 16 ? 2 : b >= 4 ? 1 : 0);
+    // operators of the same stencil shape (a parameter sweep rebuilds the same structure with new
+    // coefficients) share one tuning per process and device
+    const std::string key = tune_key(op, slot);
+    if (op->apply_variant[slot] < 0) {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune.find(key);
+        if (it != g_tune.end()) op->apply_variant[slot] = it->second;
+    }
     if (op->apply_variant[slot] < 0) {
         cudaEvent_t e0, e1;
         KF_CUDA(cudaEventCreate(&e0));
@@ -234,6 +261,8 @@ static void apply_t(kf_op *op, const T *X, T *Y, int64_t ldx, int64_t ldy, int64
         cudaEventDestroy(e1);
         op->apply_variant[slot] = bestv;
         op->apply_variant_ms[slot] = best / 3;
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune[key] = bestv;
     }
     run(op->apply_variant[slot]);
     if (!chains) return;
@@ -263,7 +292,17 @@ static void apply_t(kf_op *op, const T *X, T *Y, int64_t ldx, int64_t ldy, int64
             const int acc = last ? 1 : 0;
             const int64_t stride = op->strides[f.axis];
             if (f.kind == KF_DENSE) {
-                // the mode-k product as a tiled GEMM (accumulating into Y for the last factor)
+                // the mode-k product (accumulating into Y for the last factor): on the tensor cores
+                // for FP32 blocks when the factor has an image, else a SIMT tiled GEMM
+                if constexpr (sizeof(T) == 4) {
+                    if (f.tc >= 0) {
+                        tc_mode_product((float *)dst, ldd, (const float *)src, lds, op->chain_tc[f.tc], stride, N, b,
+                                        (double)a, acc ? 1.0 : 0.0, s);
+                        src = dst;
+                        lds = ldd;
+                        continue;
+                    }
+                }
                 mode_product<T>(dst, ldd, src, lds, cdata + f.data_off, f.n, stride, N, b, (double)a, acc ? 1.0 : 0.0,
                                 s);
                 src = dst;
@@ -743,6 +782,19 @@ void build_op(const kf_op_desc *desc, kf_op *op) {
             }
     }
     op->chains = chains_h;
+    // dense chain factors short enough for the tensor-core kernel's TF32-split image: FP32 applies
+    // run them on tcgen05 (three MMAs per K step, FP32-accurate products)
+    {
+        size_t q = 0;
+        for (ChainTerm &ct : op->chains)
+            for (ChainFactor &cf : ct.f) {
+                if (cf.kind == KF_DENSE && tc_mode_fits(cf.n, true)) {
+                    op->chain_tc.push_back(tc_matrix_create(chain_data[q].data(), cf.n, false, true));
+                    cf.tc = (int)op->chain_tc.size() - 1;
+                }
+                ++q;
+            }
+    }
     // host-side derived quantities
     op->h_diag = D;
     double dmax = -INFINITY;
@@ -789,6 +841,7 @@ void free_op(kf_op *op) {
     for (float *p : op->sep.dU) cudaFree(p);
     for (float *p : op->sep.dUt) cudaFree(p);
     for (double *p : op->sep.dU64) cudaFree(p);
+    for (auto &m : op->chain_tc) kf::tc_matrix_free(m);
     for (auto &m : op->sep.tU) kf::tc_matrix_free(m);
     for (auto &m : op->sep.tUt) kf::tc_matrix_free(m);
     cudaFree(op->sep.d_lam);

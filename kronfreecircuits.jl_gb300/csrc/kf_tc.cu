@@ -47,20 +47,35 @@ __device__ __forceinline__ uint64_t tc_desc(uint32_t saddr, uint32_t lbo, uint32
     return d;
 }
 
-// instruction descriptor, kind::f16: D FP32, A and B BF16, both K-major, M x N
-__host__ __device__ constexpr uint32_t tc_idesc_bf16(int M, int N) {
-    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+// instruction descriptor: D FP32, A and B both K-major, M x N; A/B type 1 = BF16 (kind::f16),
+// 2 = TF32 (kind::tf32)
+__host__ __device__ constexpr uint32_t tc_idesc(int M, int N, uint32_t ab) {
+    return (1u << 4) | (ab << 7) | (ab << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
 
+template <bool TF32>
 __device__ __forceinline__ void tc_mma(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
-        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc));
+    if constexpr (TF32)
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+            "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+            "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc));
+    else
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+            "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc));
+}
+
+// TF32 split of an FP32 value: hi keeps the TF32 bits (10 explicit mantissa bits), lo = x - hi
+// (exact in FP32); hi*hi + hi*lo + lo*hi carries ~21 bits
+__device__ __forceinline__ void tf32_split(float x, uint32_t &hi, uint32_t &lo) {
+    hi = __float_as_uint(x) & 0xFFFFE000u;
+    lo = __float_as_uint(x - __uint_as_float(hi));
 }
 
 __device__ __forceinline__ void tc_commit(uint64_t *bar) {
@@ -119,14 +134,21 @@ struct TcArgs {
     float alpha, beta;
 };
 
+// SPLIT = false: BF16 operands, one MMA per K step; true: TF32 hi/lo operands, three MMAs per K
+// step (FP32-accurate products for the operator apply)
+template <bool SPLIT>
 __global__ void __launch_bounds__(TC_THREADS, 1) k_mode_tc(const TcArgs a) {
+    constexpr int EB = SPLIT ? 4 : 2;        // operand bytes
+    constexpr int EPC = 16 / EB;             // K elements per 16-byte core-matrix row
+    constexpr int NS = SPLIT ? 2 : 1;        // operand images (hi, lo)
     extern __shared__ __align__(16) unsigned char tc_smem[];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int Kp = a.Kp, Mp = a.Mp;
     // shared layout: A image | B tile | epilogue transpose | q bases | barrier, TMEM slot
+    const size_t aimg = (size_t)Mp * Kp * EB, bimg = (size_t)TC_NT * Kp * EB;   // one image each
     unsigned char *Asm = tc_smem;
-    unsigned char *Bsm = Asm + (size_t)Mp * Kp * 2;
-    float *Ep = reinterpret_cast<float *>(Bsm + (size_t)TC_NT * Kp * 2);
+    unsigned char *Bsm = Asm + NS * aimg;
+    float *Ep = reinterpret_cast<float *>(Bsm + NS * bimg);
     int64_t *xbase = reinterpret_cast<int64_t *>(Ep + 128 * TC_EP_STRIDE);
     int64_t *ybase = xbase + TC_NT;
     uint64_t *bar = reinterpret_cast<uint64_t *>(ybase + TC_NT);
@@ -145,7 +167,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mode_tc(const TcArgs a) {
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
     }
     {
-        const int n16 = Mp * Kp * 2 / 16;
+        const int n16 = (int)(NS * aimg / 16);
         uint4 *dst = reinterpret_cast<uint4 *>(Asm);
         for (int e = tid; e < n16; e += TC_THREADS) dst[e] = a.Aimg[e];
     }
@@ -154,9 +176,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mode_tc(const TcArgs a) {
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tslot;
-    const uint32_t sbo_a = (uint32_t)(Kp / 8) * 128, sbo_b = sbo_a;   // 8-row groups along M / N
-    const uint32_t idesc = tc_idesc_bf16(128, TC_NT);
-    const int kg_n = Kp / 8;
+    const uint32_t sbo_a = (uint32_t)(Kp / EPC) * 128, sbo_b = sbo_a;   // 8-row groups along M / N
+    const uint32_t idesc = tc_idesc(128, TC_NT, SPLIT ? 2u : 1u);
+    const int kg_n = Kp / EPC;
     uint32_t phase = 0;
 
     for (int tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x) {
@@ -175,25 +197,37 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mode_tc(const TcArgs a) {
             }
         }
         __syncthreads();
-        // 1. gather + round to BF16 into the K-major B tile: item (n, kg) = 8 consecutive j of row n
+        // 1. gather into the K-major B tile: item (n, kg) = EPC consecutive j of row n, rounded to
+        //    BF16, or split into TF32 hi / lo
         const int items = TC_NT * kg_n;
         for (int e = tid; e < items; e += TC_THREADS) {
             int n, kg;
             if (a.left > 1) { n = e % TC_NT; kg = e / TC_NT; }   // consecutive threads: consecutive l
             else { kg = e % kg_n; n = e / kg_n; }                // leading axis: consecutive j
             const int64_t xb = xbase[n];
-            float v[8];
+            float v[EPC];
 #pragma unroll
-            for (int t = 0; t < 8; ++t) {
-                const int j = kg * 8 + t;
+            for (int t = 0; t < EPC; ++t) {
+                const int j = kg * EPC + t;
                 v[t] = (xb >= 0 && j < a.d) ? __ldg(a.X + xb + a.left * (int64_t)j) : 0.f;
             }
-            uint4 pk;
-            pk.x = pack_bf16x2(v[0], v[1]);
-            pk.y = pack_bf16x2(v[2], v[3]);
-            pk.z = pack_bf16x2(v[4], v[5]);
-            pk.w = pack_bf16x2(v[6], v[7]);
-            *reinterpret_cast<uint4 *>(Bsm + (size_t)(n >> 3) * sbo_b + (size_t)kg * 128 + (n & 7) * 16) = pk;
+            const size_t at = (size_t)(n >> 3) * sbo_b + (size_t)kg * 128 + (n & 7) * 16;
+            if constexpr (SPLIT) {
+                uint4 h, l;
+                tf32_split(v[0], h.x, l.x);
+                tf32_split(v[1], h.y, l.y);
+                tf32_split(v[2], h.z, l.z);
+                tf32_split(v[3], h.w, l.w);
+                *reinterpret_cast<uint4 *>(Bsm + at) = h;
+                *reinterpret_cast<uint4 *>(Bsm + bimg + at) = l;
+            } else {
+                uint4 pk;
+                pk.x = pack_bf16x2(v[0], v[1]);
+                pk.y = pack_bf16x2(v[2], v[3]);
+                pk.z = pack_bf16x2(v[4], v[5]);
+                pk.w = pack_bf16x2(v[6], v[7]);
+                *reinterpret_cast<uint4 *>(Bsm + at) = pk;
+            }
         }
         fence_proxy_async();
         tc_fence_before();
@@ -203,11 +237,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mode_tc(const TcArgs a) {
         if (tid == 0) {
             tc_fence_after();
             const uint32_t a0 = smem_u32(Asm), b0 = smem_u32(Bsm);
+            const int nks = Kp * EB / 32;   // 32 bytes of K per instruction
             for (int mt = 0; mt < Mp / 128; ++mt) {
-                for (int ks = 0; ks < Kp / 16; ++ks) {
-                    const uint64_t ad = tc_desc(a0 + (uint32_t)mt * 16 * sbo_a + (uint32_t)ks * 256, 128, sbo_a);
-                    const uint64_t bd = tc_desc(b0 + (uint32_t)ks * 256, 128, sbo_b);
-                    tc_mma(tmem + (uint32_t)mt * TC_NT, ad, bd, idesc, ks > 0 ? 1u : 0u);
+                for (int ks = 0; ks < nks; ++ks) {
+                    const uint32_t ao = (uint32_t)mt * 16 * sbo_a + (uint32_t)ks * 256, bo = (uint32_t)ks * 256;
+                    const uint64_t ad = tc_desc(a0 + ao, 128, sbo_a), bd = tc_desc(b0 + bo, 128, sbo_b);
+                    tc_mma<SPLIT>(tmem + (uint32_t)mt * TC_NT, ad, bd, idesc, ks > 0 ? 1u : 0u);
+                    if constexpr (SPLIT) {
+                        const uint64_t al = tc_desc(a0 + (uint32_t)aimg + ao, 128, sbo_a);
+                        const uint64_t bl = tc_desc(b0 + (uint32_t)bimg + bo, 128, sbo_b);
+                        tc_mma<true>(tmem + (uint32_t)mt * TC_NT, ad, bl, idesc, 1u);   // hi * lo
+                        tc_mma<true>(tmem + (uint32_t)mt * TC_NT, al, bd, idesc, 1u);   // lo * hi
+                    }
                 }
             }
             tc_commit(bar);
@@ -301,23 +342,39 @@ uint16_t bf16_bits(float f) {
 
 int tc_mode_layout_ok(int d) { return d >= 1 && d <= 256; }
 
-TcMatrix tc_matrix_create(const double *A, int d, bool transpose) {
+TcMatrix tc_matrix_create(const double *A, int d, bool transpose, bool split) {
     KF_REQUIRE(tc_mode_layout_ok(d), KF_EINVAL, "tensor-core mode product: axis length must be 1..256");
     TcMatrix m;
     m.d = d;
+    m.split = split ? 1 : 0;
     m.Mp = d <= 128 ? 128 : 256;
     m.Kp = (d + 15) / 16 * 16;
-    const size_t sbo = (size_t)(m.Kp / 8) * 128;
-    std::vector<uint16_t> img((size_t)m.Mp * m.Kp, 0);
+    const int eb = split ? 4 : 2, epc = 16 / eb;
+    const size_t sbo = (size_t)(m.Kp / epc) * 128, img_bytes = (size_t)m.Mp * m.Kp * eb;
+    std::vector<unsigned char> img(img_bytes * (split ? 2 : 1), 0);
     for (int i = 0; i < d; ++i)
         for (int j = 0; j < d; ++j) {
             // operator entry (i, j): A[i + d j], or A[j + d i] when transposed
             const double v = transpose ? A[j + (size_t)d * i] : A[i + (size_t)d * j];
-            const size_t byte = (size_t)(i >> 3) * sbo + (size_t)(j >> 3) * 128 + (size_t)(i & 7) * 16 + (size_t)(j & 7) * 2;
-            img[byte / 2] = bf16_bits((float)v);
+            const size_t byte = (size_t)(i >> 3) * sbo + (size_t)(j / epc) * 128 + (size_t)(i & 7) * 16 +
+                                (size_t)(j % epc) * eb;
+            if (split) {
+                float f = (float)v;
+                uint32_t u;
+                std::memcpy(&u, &f, 4);
+                u &= 0xFFFFE000u;
+                float hi;
+                std::memcpy(&hi, &u, 4);
+                const float lo = (float)(v - (double)hi);
+                std::memcpy(&img[byte], &hi, 4);
+                std::memcpy(&img[img_bytes + byte], &lo, 4);
+            } else {
+                const uint16_t b = bf16_bits((float)v);
+                std::memcpy(&img[byte], &b, 2);
+            }
         }
-    KF_CUDA(cudaMalloc(&m.img, img.size() * 2));
-    KF_CUDA(cudaMemcpy(m.img, img.data(), img.size() * 2, cudaMemcpyHostToDevice));
+    KF_CUDA(cudaMalloc(&m.img, img.size()));
+    KF_CUDA(cudaMemcpy(m.img, img.data(), img.size(), cudaMemcpyHostToDevice));
     return m;
 }
 
@@ -326,8 +383,23 @@ void tc_matrix_free(TcMatrix &m) {
     m.img = nullptr;
 }
 
+// whether the kernel's shared-memory image of a d x d operator fits this device
+bool tc_mode_fits(int d, bool split) {
+    if (!tc_mode_layout_ok(d)) return false;
+    TcMatrix m;
+    m.d = d;
+    m.split = split ? 1 : 0;
+    m.Mp = d <= 128 ? 128 : 256;
+    m.Kp = (d + 15) / 16 * 16;
+    int optin = 0, dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return false;
+    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return false;
+    return tc_mode_smem(m) + 1024 <= (size_t)optin;
+}
+
 size_t tc_mode_smem(const TcMatrix &m) {
-    return (size_t)m.Mp * m.Kp * 2 + (size_t)TC_NT * m.Kp * 2 + (size_t)128 * TC_EP_STRIDE * 4 +
+    const size_t eb = m.split ? 4 : 2, ns = m.split ? 2 : 1;
+    return ns * ((size_t)m.Mp * m.Kp * eb + (size_t)TC_NT * m.Kp * eb) + (size_t)128 * TC_EP_STRIDE * 4 +
            (size_t)2 * TC_NT * 8 + 16;
 }
 
@@ -357,13 +429,15 @@ void tc_mode_product(float *Y, int64_t ldy, const float *X, int64_t ldx, const T
     KF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     KF_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     cudaFuncAttributes fa;
-    KF_CUDA(cudaFuncGetAttributes(&fa, k_mode_tc));
+    if (A.split) KF_CUDA(cudaFuncGetAttributes(&fa, k_mode_tc<true>));
+    else KF_CUDA(cudaFuncGetAttributes(&fa, k_mode_tc<false>));
     const size_t dyn_max = (size_t)optin - fa.sharedSizeBytes;
     KF_REQUIRE(smem <= dyn_max, KF_EINVAL, "tensor-core mode product: shared-memory image too large");
     {
         std::lock_guard<std::mutex> lk(g_tc_mu);
         if (!g_tc_attr) {
-            KF_CUDA(cudaFuncSetAttribute(k_mode_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn_max));
+            KF_CUDA(cudaFuncSetAttribute(k_mode_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn_max));
+            KF_CUDA(cudaFuncSetAttribute(k_mode_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn_max));
             g_tc_attr = true;
         }
     }
@@ -374,7 +448,8 @@ void tc_mode_product(float *Y, int64_t ldy, const float *X, int64_t ldx, const T
     if (per_sm > 4) per_sm = 4;
     if (per_sm < 1) per_sm = 1;
     const int grid = a.ntiles < sms * per_sm ? a.ntiles : sms * per_sm;
-    k_mode_tc<<<grid, TC_THREADS, smem, s>>>(a);
+    if (A.split) k_mode_tc<true><<<grid, TC_THREADS, smem, s>>>(a);
+    else k_mode_tc<false><<<grid, TC_THREADS, smem, s>>>(a);
     KF_LAUNCH_CHECK();
 }
 

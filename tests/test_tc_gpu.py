@@ -4,9 +4,10 @@ reference: the axes of the three-mode leaf (41 x 256 x 64), of the dense parent 
 lengths that exercise the padding of M (to 128 / 256) and K (to a multiple of 16), several
 column counts, alpha and accumulation into Y (beta = 1).
 
-Tolerances: BF16 keeps 8 significant bits, so the tensor-core result is checked to 1e-2 of the
-column norm (the separable preconditioner only steers search directions); the SIMT kernel to
-1e-5.
+Tolerances: BF16 keeps 8 significant bits, so the BF16 tensor-core result is checked to 1e-2 of
+the column norm (the separable preconditioner only steers search directions); the TF32 hi / lo
+variant (the FP32 apply of dense factors, axes up to 96) to 2e-6, like the SIMT FP32 kernel (1e-5
+here, 2e-6 in the apply tests).
 """
 import ctypes as C
 
@@ -27,6 +28,8 @@ CASES = [
     ((7, 129), 1, 1),
     ((16,), 0, 1),
     ((3, 256, 2), 1, 7),
+    ((96, 5, 7), 0, 3),
+    ((5, 64, 9), 1, 4),
 ]
 
 
@@ -70,6 +73,11 @@ def test_tensor_core_mode_product(cuda, dims, axis, b):
     Yt = _run(torch, 1, X, A, dims, axis)
     err = torch.linalg.norm(Yt - ref, dim=1) / nref
     assert float(torch.max(err)) < 1e-2, err
+    if d <= 96:
+        # TF32 hi / lo operands, three MMAs per K step: FP32-level products
+        Ys3 = _run(torch, 2, X, A, dims, axis)
+        err3 = torch.linalg.norm(Ys3 - ref, dim=1) / nref
+        assert float(torch.max(err3)) < 2e-6, err3
 
 
 def test_tensor_core_alpha_beta(cuda):
