@@ -64,11 +64,51 @@ def peaks():
         return 6800.0, "fallback"
 
 
+class Dist:
+    """Replicas, one process per GPU (torchrun's RANK / LOCAL_RANK / WORLD_SIZE): the path has no
+    exchange step, so each rank solves its own theta draws on its own GPU and only host-side
+    scalars meet, over a gloo process group -- a barrier around the timed region, the largest
+    time over ranks, sums of the work done."""
+
+    def __init__(self):
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.dist = None
+        if self.world > 1:
+            import torch.distributed as dist
+            if not dist.is_initialized():
+                dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.dist is not None:
+            self.dist.barrier()
+
+    def _reduce(self, x, op):
+        if self.dist is None:
+            return float(x)
+        import torch
+        t = torch.tensor([float(x)], dtype=torch.float64)
+        self.dist.all_reduce(t, op=op)
+        return float(t.item())
+
+    def max(self, x):
+        return self._reduce(x, self.dist.ReduceOp.MAX if self.dist else None)
+
+    def sum(self, x):
+        return self._reduce(x, self.dist.ReduceOp.SUM if self.dist else None)
+
+    def close(self):
+        if self.dist is not None and self.dist.is_initialized():
+            self.dist.destroy_process_group()
+
+
 class Clocks:
     """nvidia-smi samples during the timed region."""
 
-    def __init__(self):
-        self.rows, self._stop, self._t = [], threading.Event(), None
+    def __init__(self, gpu=0):
+        self.rows, self._stop, self._t, self.gpu = [], threading.Event(), None, gpu
 
     def start(self):
         def run():
@@ -76,7 +116,8 @@ class Clocks:
                  "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
             while not self._stop.is_set():
                 try:
-                    out = subprocess.run(["nvidia-smi", "-i", "0", f"--query-gpu={q}", "--format=csv,noheader,nounits"],
+                    out = subprocess.run(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits"],
                                          capture_output=True, text=True, timeout=5).stdout.strip()
                     if out:
                         self.rows.append([x.strip() for x in out.split(",")])
@@ -119,18 +160,21 @@ def measure_apply(torch, H, f32, b=16, reps=20):
     return e0.elapsed_time(e1) / reps / 1e3
 
 
-def run_ours(args):
+def run_ours(args, D):
     import torch
     from kfgpu import KronFreeOperator, LOBPCG, circuits, solve
     from kfgpu._abi import launch_count
     from kfgpu.build import build_library
 
     assert torch.cuda.is_available(), "bench.py needs a CUDA device"
-    torch.cuda.set_device(0)
-    build_library()
+    torch.cuda.set_device(D.local)
+    if D.rank == 0:
+        build_library()
+    D.barrier()
     ths = thetas()
     K, W = args.steps, args.warmup
-    idx = [(W + k) % NDRAWS for k in range(K)]
+    # each replica solves its own draws (weak scaling: K solves per GPU)
+    idx = [(W + D.rank * K + k) % NDRAWS for k in range(K)]
     # operators prepared before the timed region (inputs resident); each solve builds its product
     # seed on the device, as the reference's solve builds it (src/lobpcg.jl:247)
     ops = {}
@@ -153,7 +197,9 @@ def run_ours(args):
         one(w, "mixed")
     torch.cuda.synchronize()
     n0 = launch_count()
-    clocks = Clocks().start()
+    clocks = Clocks(D.local).start()
+    D.barrier()
+    torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     conv, stats = 0, []
@@ -163,12 +209,16 @@ def run_ours(args):
         stats.append(st)
     e1.record(stream)
     torch.cuda.synchronize()
+    D.barrier()
     clk = clocks.stop()
-    t_mixed = e0.elapsed_time(e1) / 1e3
-    launches = launch_count() - n0
-    value = conv / t_mixed
+    # the job's time is the slowest replica's; its work is every replica's
+    t_mixed = D.max(e0.elapsed_time(e1) / 1e3)
+    conv_all = D.sum(conv)
+    launches = int(D.sum(launch_count() - n0))
+    value = conv_all / t_mixed
     # plain FP64 on a subset of the same draws (the metric's denominator)
     kp = max(1, min(args.plain_steps, K))
+    D.barrier()
     f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     f0.record(stream)
     conv64, st64 = 0, []
@@ -178,8 +228,8 @@ def run_ours(args):
         st64.append(st)
     f1.record(stream)
     torch.cuda.synchronize()
-    t64 = f0.elapsed_time(f1) / 1e3
-    plain = conv64 / t64
+    t64 = D.max(f0.elapsed_time(f1) / 1e3)
+    plain = D.sum(conv64) / t64
     # the same FP64 solver with the separable preconditioner (what precision alone buys)
     g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     g0.record(stream)
@@ -191,6 +241,7 @@ def run_ours(args):
     ke = max(1, min(args.e2e_steps, K))
     h2d = d2h = 0
     torch.cuda.synchronize()
+    D.barrier()
     t0 = time.perf_counter()
     conv_e = 0
     for i in idx[:ke]:
@@ -203,7 +254,8 @@ def run_ours(args):
         d2h += V.nbytes + E.nbytes
         H.close()
     torch.cuda.synchronize()
-    te = time.perf_counter() - t0
+    te = D.max(time.perf_counter() - t0)
+    conv_e = D.sum(conv_e)
     # roofline of the dominant kernel of a solve (the FP32 Gram product, by the ncu launch list):
     # the orthogonalisation's X' [W P] at 16 x 32 columns; and of the fused stencil apply
     H0 = ops[idx[0]][0]
@@ -215,12 +267,13 @@ def run_ours(args):
     achieved = alg / t_apply / 1e9
     line = {
         "metric": "converged eigenpairs/s at 1e-8 resid: warm-start mixed vs plain FP64, 1 GB300",
-        "value": value, "unit": "eigenpairs/s", "n_gpus": 1, "steps": K, "warmup": W,
+        "value": value, "unit": "eigenpairs/s", "n_gpus": D.world, "steps": K, "warmup": W,
         "ms_per_step": 1e3 * t_mixed / K, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 bulk + f64 refinement", "data": "synthetic",
         "config": {"workload": "three-mode leaf 41x256x64 (N=671,744), LOBPCG m=12 block=16, product seed, "
                                "tol 1e-8*||H||, theta ~ U(ranges) seed 20261205",
                    "l2": "inputs larger than L2 (a 16-column FP32 block is 43 MB; a solve streams ~10 GB)"},
+        "replicas": D.world,
         "plain_f64": {"value": plain, "steps": kp, "ms_per_step": 1e3 * t64 / kp,
                       "iterations": [s["iterations"] for s in st64]},
         "speedup_mixed_vs_f64": value / plain if plain > 0 else None,
@@ -238,10 +291,10 @@ def run_ours(args):
                            "algorithmic_bytes": alg, "launch_us": t_apply * 1e6, "peak_kind": kind},
         "clocks": clk, "gpu_launches": launches,
     }
-    if not args.no_cpu:
+    if not args.no_cpu and D.world == 1:
         line["cpu_baseline"] = cpu_baseline(ths[idx[0]], bounded=True,
                                             iters=int(round(np.mean([s["iterations"] for s in st64]))))
-    return line
+    return line if D.rank == 0 else None
 
 
 def profile_one(args):
@@ -551,8 +604,11 @@ def main():
     if args.impl == "reference":
         line = run_reference(args)
     else:
-        rank = int(os.environ.get("RANK", "0"))
-        line = run_ours(args) if rank == 0 else None
+        D = Dist()
+        try:
+            line = run_ours(args, D)
+        finally:
+            D.close()
     if line is not None:
         print(json.dumps(line), flush=True)
 
