@@ -44,9 +44,9 @@ SEED = 20261205          # theta draws of the three-mode leaf workload
 NDRAWS = 64
 # ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch (profiles/*.md): the FP32 16-column
 # fused apply at N = 671,744 (written Y stays in L2: reads 45.7 MB, writes 9.9 MB); the 16 x 32 FP32
-# Gram (None until captured)
+# Gram (reads 129.0 MB = every element once, writes 3.3 MB of partials)
 APPLY_TRAFFIC_BYTES = 55641088
-GRAM_TRAFFIC_BYTES = None
+GRAM_TRAFFIC_BYTES = 132320768
 
 
 def thetas():
@@ -368,6 +368,40 @@ def time_gram(torch, ka, kb, N, reps=10):
 GRAM_SHAPES = ((16, 32), (32, 32), (16, 16), (16, 2), (2, 4))
 
 
+def time_update(torch, path, kx0, kx1, ky, N, reps=10):
+    """Mean device time of one FP32 block update Y = [X0 X1] C (path 0: SIMT, 1: tcgen05), through
+    the library's test-only timing entry point."""
+    import ctypes as C
+    from kfgpu import _abi
+    X0 = torch.randn(kx0, N, dtype=torch.float32, device="cuda")
+    X1 = torch.randn(max(kx1, 1), N, dtype=torch.float32, device="cuda")
+    Y = torch.empty(ky, N, dtype=torch.float32, device="cuda")
+    Cm = np.asfortranarray(np.random.default_rng(0).standard_normal((kx0 + kx1, ky)))
+    ms = C.c_float(0)
+    _abi.check(_abi.lib().kf_test_update(path, C.c_void_p(Y.data_ptr()), N, ky, C.c_void_p(X0.data_ptr()), N, kx0,
+                                         C.c_void_p(X1.data_ptr()), N, kx1, Cm.ctypes.data_as(C.c_void_p), kx0 + kx1,
+                                         1.0, 0.0, N, reps, None, C.byref(ms)))
+    return ms.value / 1e3
+
+
+UPDATE_SHAPES = ((32, 16, 32), (16, 32, 16), (16, 0, 16), (2, 0, 1))
+
+
+def run_update_workload(args):
+    """The FP32 block updates of LOBPCG on N = 671,744 rows: tcgen05 (TF32 hi / lo) and SIMT."""
+    import torch
+    N = 671744
+    peak, kind = peaks()
+    out = {"workload": "FP32 block update Y = [X0 X1] C, N=671,744 rows", "hbm_peak_gbs": peak, "peak_kind": kind}
+    for kx0, kx1, ky in UPDATE_SHAPES:
+        for path, name in ((1, "tc"), (0, "simt")):
+            t = time_update(torch, path, kx0, kx1, ky, N)
+            key = f"update_{kx0}+{kx1}_to_{ky}_{name}"
+            out[key + "_us"] = t * 1e6
+            out[key + "_gbs"] = (kx0 + kx1 + ky) * N * 4 / t / 1e9
+    return out
+
+
 def run_gram_workload(args):
     """The FP32 Gram products of LOBPCG's orthogonalisation and Rayleigh-Ritz on N = 671,744 rows."""
     import torch
@@ -583,7 +617,7 @@ def main():
                          "extrapolation (868: the mean over the first two timed draws measured on GB300)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="leaf3",
-                    choices=["leaf3", "batch", "warmstart", "dense", "apply", "mode", "gram"],
+                    choices=["leaf3", "batch", "warmstart", "dense", "apply", "mode", "gram", "update"],
                     help="leaf3 (the benchmarked workload) or one of the other measured configurations")
     ap.add_argument("--n-train", type=int, default=4096)
     ap.add_argument("--n-test", type=int, default=1024)
@@ -596,7 +630,8 @@ def main():
         return
     if args.workload != "leaf3":
         fn = {"batch": run_batch_workload, "warmstart": run_warmstart_workload, "dense": run_dense_workload,
-              "apply": run_apply_workload, "mode": run_mode_workload, "gram": run_gram_workload}
+              "apply": run_apply_workload, "mode": run_mode_workload, "gram": run_gram_workload,
+              "update": run_update_workload}
         print(json.dumps(fn[args.workload](args)), flush=True)
         return
     if args.warmup < 3:

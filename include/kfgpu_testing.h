@@ -40,6 +40,17 @@ int kf_test_time_mode_product(int path, const float *X, float *Y, const double *
 int kf_test_time_gram(const float *A, int64_t lda, int ka, const float *B, int64_t ldb, int kb, int64_t N, int reps,
                       void *stream, float *ms_per_launch, double *G_out);
 
+/*
+ * The FP32 block update Y = alpha [X0 X1] C + beta Y (device blocks: X0 N x kx0, X1 N x kx1 (kx1 may
+ * be 0), Y N x ky; C: host, (kx0 + kx1) x ky, column-major FP64, leading dimension ldc), `reps`
+ * times on `stream`, timed with CUDA events: path 0 the SIMT kernel, path 1 the tcgen05 kernel
+ * (TF32 hi / lo operands; kx0 + kx1 <= 64, ky <= 128).  *ms_per_launch: mean device time.  With
+ * beta != 0 every launch reads the Y the previous one wrote.
+ */
+int kf_test_update(int path, float *Y, int64_t ldy, int ky, const float *X0, int64_t ldx0, int kx0, const float *X1,
+                   int64_t ldx1, int kx1, const double *C, int ldc, double alpha, double beta, int64_t N, int reps,
+                   void *stream, float *ms_per_launch);
+
 #ifdef __cplusplus
 }
 #endif

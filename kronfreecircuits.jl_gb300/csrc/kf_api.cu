@@ -341,4 +341,39 @@ int kf_test_time_gram(const float *A, int64_t lda, int ka, const float *B, int64
     });
 }
 
+int kf_test_update(int path, float *Y, int64_t ldy, int ky, const float *X0, int64_t ldx0, int kx0, const float *X1,
+                   int64_t ldx1, int kx1, const double *C, int ldc, double alpha, double beta, int64_t N, int reps,
+                   void *stream, float *ms_per_launch) {
+    return guarded([&] {
+        KF_REQUIRE(Y && X0 && C && ms_per_launch && reps >= 1 && N >= 1 && ky >= 1 && kx0 >= 1 && kx1 >= 0,
+                   KF_EINVAL, "kf_test_update: bad argument");
+        KF_REQUIRE(kx1 == 0 || X1, KF_EINVAL, "kf_test_update: X1 is NULL");
+        cudaStream_t s = (cudaStream_t)stream;
+        const int kx = kx0 + kx1;
+        double *dC = nullptr;
+        KF_CUDA(cudaMalloc(&dC, sizeof(double) * (size_t)ldc * ky));
+        KF_CUDA(cudaMemcpy(dC, C, sizeof(double) * (size_t)ldc * ky, cudaMemcpyHostToDevice));
+        auto launch = [&] {
+            if (path == 1) kf::update_tc(Y, ldy, ky, X0, ldx0, kx0, X1, ldx1, kx1, dC, ldc, alpha, beta, N, s);
+            else kf::update2<float>(Y, ldy, ky, X0, ldx0, kx0, kx1 ? X1 : X0, kx1 ? ldx1 : ldx0, kx1, dC, ldc, alpha,
+                                    beta, N, s, false);
+        };
+        (void)kx;
+        cudaEvent_t e0, e1;
+        KF_CUDA(cudaEventCreate(&e0));
+        KF_CUDA(cudaEventCreate(&e1));
+        KF_CUDA(cudaEventRecord(e0, s));
+        for (int r = 0; r < reps; ++r) launch();
+        KF_CUDA(cudaEventRecord(e1, s));
+        KF_CUDA(cudaEventSynchronize(e1));
+        float ms = 0;
+        KF_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        cudaFree(dC);
+        if (const int t = kf::tc_take_error()) throw kf::Error(t, "tensor-core update: device wait timed out");
+        *ms_per_launch = ms / reps;
+    });
+}
+
 }  // extern "C"

@@ -516,8 +516,20 @@ void update(T *Y, int64_t ldy, int ky, const T *X, int64_t ldx, int kx, const do
 // ((kx0 + kx1) x ky, FP64, leading dimension ldc)
 template <typename T>
 void update2(T *Y, int64_t ldy, int ky, const T *X0, int64_t ldx0, int kx0, const T *X1, int64_t ldx1, int kx1,
-             const double *C, int ldc, double alpha, double beta, int64_t N, cudaStream_t s) {
+             const double *C, int ldc, double alpha, double beta, int64_t N, cudaStream_t s, bool allow_tc) {
     if (ky <= 0 || N <= 0) return;
+    if constexpr (sizeof(T) == 4) {
+        // wide FP32 updates (kx ky >= 1024, e.g. the orthogonalisation's [Z X] -> Z at 48 -> 32) are
+        // FMA-bound on the SIMT pipes; the tcgen05 kernel (TF32 hi / lo) measured faster there
+        const int kx = kx0 + kx1;
+        if (allow_tc && N >= 65536 && update_tc_ok(kx, ky) && kx * ky >= 1024) {
+            update_tc((float *)Y, ldy, ky, (const float *)X0, ldx0, kx0, (const float *)X1, ldx1, kx1, C, ldc, alpha,
+                      beta, N, s);
+            return;
+        }
+    } else {
+        (void)allow_tc;
+    }
     constexpr int UC = sizeof(T) == 8 ? 4 : 8;
     const int kx = kx0 + kx1;
     const int kyp = (ky + UC - 1) / UC * UC;
@@ -863,7 +875,7 @@ void copy_block(const T *X, int64_t ldx, T *Y, int64_t ldy, int k, int64_t N, cu
 #define KF_INST(T)                                                                                                   \
     template void gram<T>(const T *, int64_t, int, const T *, int64_t, int, int64_t, double *, double *, cudaStream_t); \
     template void update2<T>(T *, int64_t, int, const T *, int64_t, int, const T *, int64_t, int, const double *, int,   \
-                             double, double, int64_t, cudaStream_t);                                                \
+                             double, double, int64_t, cudaStream_t, bool);                                          \
     template void update<T>(T *, int64_t, int, const T *, int64_t, int, const double *, int, double, double, int64_t, \
                             cudaStream_t);                                                                           \
     template void colnorms2<T>(const T *, int64_t, int, int64_t, double *, double *, cudaStream_t);                  \

@@ -104,7 +104,12 @@ size_t tc_mode_smem(const TcMatrix &m);
 bool tc_mode_fits(int d, bool split);
 void tc_mode_product(float *Y, int64_t ldy, const float *X, int64_t ldx, const TcMatrix &A, int64_t left, int64_t N,
                      int64_t b, double alpha, double beta, cudaStream_t s);
-int tc_take_error();   // a pending device-side timeout (KF_ETIMEOUT) of a tensor-core launch, cleared
+int tc_take_error();
+int *tc_error_word();  // the host-mapped word device-side waits report KF_ETIMEOUT in
+// FP32 block update on the tensor cores (kf_tcgemm.cu), TF32 hi / lo operands, kx <= 64, ky <= 128
+bool update_tc_ok(int kx, int ky);
+void update_tc(float *Y, int64_t ldy, int ky, const float *X0, int64_t ldx0, int kx0, const float *X1, int64_t ldx1,
+               int kx1, const double *C, int ldc, double alpha, double beta, int64_t N, cudaStream_t s);   // a pending device-side timeout (KF_ETIMEOUT) of a tensor-core launch, cleared
 
 }  // namespace kf
 
@@ -186,7 +191,7 @@ void gram32_sets(const float *A0, int64_t lda0, int ka0, const float *A1, int64_
 // Y = alpha [X0 X1] C + beta Y
 template <typename T>
 void update2(T *Y, int64_t ldy, int ky, const T *X0, int64_t ldx0, int kx0, const T *X1, int64_t ldx1, int kx1,
-             const double *C, int ldc, double alpha, double beta, int64_t N, cudaStream_t s);
+             const double *C, int ldc, double alpha, double beta, int64_t N, cudaStream_t s, bool allow_tc = true);
 size_t gram_partials_size(int ka, int kb, int64_t N);
 template <typename T>
 void update(T *Y, int64_t ldy, int ky, const T *X, int64_t ldx, int kx, const double *C_dev, int ldc,

@@ -199,34 +199,48 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mode_tc(const TcArgs a) {
         __syncthreads();
         // 1. gather into the K-major B tile: item (n, kg) = EPC consecutive j of row n, rounded to
         //    BF16, or split into TF32 hi / lo
+        // BG items per batch: all their loads in flight together, then the packing and stores
         const int items = TC_NT * kg_n;
-        for (int e = tid; e < items; e += TC_THREADS) {
-            int n, kg;
-            if (a.left > 1) { n = e % TC_NT; kg = e / TC_NT; }   // consecutive threads: consecutive l
-            else { kg = e % kg_n; n = e / kg_n; }                // leading axis: consecutive j
-            const int64_t xb = xbase[n];
-            float v[EPC];
+        constexpr int BG = SPLIT ? 4 : 1;   // BF16: 8 loads per item already; more costs occupancy
+        for (int e0 = tid; e0 < items; e0 += BG * TC_THREADS) {
+            float v[BG][EPC];
 #pragma unroll
-            for (int t = 0; t < EPC; ++t) {
-                const int j = kg * EPC + t;
-                v[t] = (xb >= 0 && j < a.d) ? __ldg(a.X + xb + a.left * (int64_t)j) : 0.f;
+            for (int g = 0; g < BG; ++g) {
+                const int e = e0 + g * TC_THREADS;
+                int n, kg;
+                if (a.left > 1) { n = e % TC_NT; kg = e / TC_NT; }   // consecutive threads: consecutive l
+                else { kg = e % kg_n; n = e / kg_n; }                // leading axis: consecutive j
+                const int64_t xb = e < items ? xbase[n] : -1;
+#pragma unroll
+                for (int t = 0; t < EPC; ++t) {
+                    const int j = kg * EPC + t;
+                    v[g][t] = (xb >= 0 && j < a.d) ? __ldg(a.X + xb + a.left * (int64_t)j) : 0.f;
+                }
             }
-            const size_t at = (size_t)(n >> 3) * sbo_b + (size_t)kg * 128 + (n & 7) * 16;
-            if constexpr (SPLIT) {
-                uint4 h, l;
-                tf32_split(v[0], h.x, l.x);
-                tf32_split(v[1], h.y, l.y);
-                tf32_split(v[2], h.z, l.z);
-                tf32_split(v[3], h.w, l.w);
-                *reinterpret_cast<uint4 *>(Bsm + at) = h;
-                *reinterpret_cast<uint4 *>(Bsm + bimg + at) = l;
-            } else {
-                uint4 pk;
-                pk.x = pack_bf16x2(v[0], v[1]);
-                pk.y = pack_bf16x2(v[2], v[3]);
-                pk.z = pack_bf16x2(v[4], v[5]);
-                pk.w = pack_bf16x2(v[6], v[7]);
-                *reinterpret_cast<uint4 *>(Bsm + at) = pk;
+#pragma unroll
+            for (int g = 0; g < BG; ++g) {
+                const int e = e0 + g * TC_THREADS;
+                if (e >= items) break;
+                int n, kg;
+                if (a.left > 1) { n = e % TC_NT; kg = e / TC_NT; }
+                else { kg = e % kg_n; n = e / kg_n; }
+                const size_t at = (size_t)(n >> 3) * sbo_b + (size_t)kg * 128 + (n & 7) * 16;
+                if constexpr (SPLIT) {
+                    uint4 h, l;
+                    tf32_split(v[g][0], h.x, l.x);
+                    tf32_split(v[g][1], h.y, l.y);
+                    tf32_split(v[g][2], h.z, l.z);
+                    tf32_split(v[g][3], h.w, l.w);
+                    *reinterpret_cast<uint4 *>(Bsm + at) = h;
+                    *reinterpret_cast<uint4 *>(Bsm + bimg + at) = l;
+                } else {
+                    uint4 pk;
+                    pk.x = pack_bf16x2(v[g][0], v[g][1]);
+                    pk.y = pack_bf16x2(v[g][2], v[g][3]);
+                    pk.z = pack_bf16x2(v[g][4], v[g][5]);
+                    pk.w = pack_bf16x2(v[g][6], v[g][7]);
+                    *reinterpret_cast<uint4 *>(Bsm + at) = pk;
+                }
             }
         }
         fence_proxy_async();
@@ -452,6 +466,8 @@ void tc_mode_product(float *Y, int64_t ldy, const float *X, int64_t ldx, const T
     else k_mode_tc<false><<<grid, TC_THREADS, smem, s>>>(a);
     KF_LAUNCH_CHECK();
 }
+
+int *tc_error_word() { return tc_err_word(); }
 
 int tc_take_error() {
     std::lock_guard<std::mutex> lk(g_tc_mu);

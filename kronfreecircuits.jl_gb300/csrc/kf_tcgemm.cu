@@ -1,0 +1,330 @@
+// Block updates Y = alpha [X0 X1] C + beta Y on the tensor cores (tcgen05), FP32 blocks with
+// FP32-accurate products: X and C split into TF32 hi / lo parts, hi*hi + hi*lo + lo*hi per K step.
+//
+// The tall-skinny product of LOBPCG's orthogonalisation and Rayleigh-Ritz updates (the reference's
+// gemms inside LOBPCGEigensolver, called at src/lobpcg.jl:268, and src/chebyshev.jl:60,79,126): N
+// rows, kx <= 64 inputs, ky <= 128 outputs.  GEMM view: D[128 rows, Np] += A[128 rows, K] B[K, Np]
+// per 128-row tile, A = the tile of [X0 X1] (K-major after the gather), B = C' (K-major as C is
+// stored), D in TMEM.
+//
+// One persistent CTA per SM, warp-specialised:
+//   warps 0-7   producers: gather a tile of X (4 columns per 16-byte core-matrix row), split it
+//               into TF32 hi / lo, store into shared-memory stage t % 2, arrive on full[s];
+//   warp 8      issuer (one lane): waits full[s] and a free accumulator slot, issues the MMA
+//               chain, commits to empty[s] (stage reusable) and accf[a] (accumulator ready);
+//   warps 9-12  epilogue: wait accf[a], tcgen05.ld their 32 TMEM lanes (= tile rows), write Y
+//               (consecutive lanes = consecutive rows: coalesced), arrive on acce[a].
+// Every wait is an mbarrier wait with a cycle budget; when one runs out the CTA records
+// KF_ETIMEOUT in the host-mapped error word, every role leaves its loop at its next check, the
+// issuer waits (bounded) for its MMAs in flight and TMEM is freed.  No named barrier is used
+// inside the loops, so an early exit cannot strand a warp.
+#include <cstring>
+#include <mutex>
+
+#include "kf_internal.h"
+
+namespace kf {
+
+namespace {
+
+constexpr int UG_PROD = 256;                  // producer threads (warps 0-7)
+constexpr int UG_THREADS = UG_PROD + 32 + 128;
+constexpr int UG_TM = 128;                    // rows per tile (MMA M)
+constexpr long long UG_WAIT_CYCLES = 4000000000LL;
+
+__device__ __forceinline__ uint32_t su32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t ug_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;
+}
+
+__device__ __forceinline__ void ug_mma(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ void ug_commit(uint64_t *bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(su32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void ug_bar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(su32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void ug_arrive(uint64_t *bar) {
+    asm volatile(
+        "{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}\n" ::"r"(su32(bar))
+        : "memory");
+}
+
+// completion number `n` (0-based) of the barrier's phases; false when the budget ran out or the
+// CTA is aborting
+__device__ __forceinline__ bool ug_wait(uint64_t *bar, uint32_t n, volatile int *abort) {
+    const uint32_t parity = n & 1u;
+    const long long t0 = clock64();
+    for (;;) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.b32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(done)
+            : "r"(su32(bar)), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (*abort) return false;
+        if (clock64() - t0 > UG_WAIT_CYCLES) return false;
+    }
+}
+
+__device__ __forceinline__ void ug_split(float x, uint32_t &hi, uint32_t &lo) {
+    hi = __float_as_uint(x) & 0xFFFFE000u;
+    lo = __float_as_uint(x - __uint_as_float(hi));
+}
+
+struct UgArgs {
+    float *Y;
+    const float *X0, *X1;
+    const double *C;
+    int *err;
+    int64_t ldy, ldx0, ldx1, N;
+    int kx0, kx, ky, ldc, Kp, Np, ntiles;
+    uint32_t tcols;     // TMEM columns allocated (two accumulator slots)
+    float alpha, beta;
+};
+
+__global__ void __launch_bounds__(UG_THREADS, 1) k_update_tc(const UgArgs a) {
+    extern __shared__ __align__(16) unsigned char ug_smem[];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int Kp = a.Kp, Np = a.Np;
+    const uint32_t sbo = (uint32_t)(Kp / 4) * 128;          // 8-row groups (rows of A, columns of C)
+    const size_t aimg = (size_t)UG_TM * Kp * 4;             // one A image (hi or lo)
+    const size_t bimg = (size_t)Np * Kp * 4;                // one B image
+    unsigned char *Bsm = ug_smem;                           // B hi | B lo
+    unsigned char *Asm = Bsm + 2 * bimg;                    // stage s: A hi | A lo at 2 s aimg
+    uint64_t *bars = reinterpret_cast<uint64_t *>(Asm + 4 * aimg);
+    uint64_t *full = bars, *empty = bars + 2, *accf = bars + 4, *acce = bars + 6, *fin = bars + 8;
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(bars + 9);
+    __shared__ volatile int s_abort;
+
+    if (tid == 0) {
+        for (int q = 0; q < 2; ++q) {
+            ug_bar_init(full + q, UG_PROD);
+            ug_bar_init(empty + q, 1);
+            ug_bar_init(accf + q, 1);
+            ug_bar_init(acce + q, 128);
+        }
+        ug_bar_init(fin, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        s_abort = 0;
+    }
+    if (warp == 8) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(su32(tslot)),
+                     "r"(a.tcols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    // B = C' as TF32 hi / lo, K-major: entry (j, i) = C[i + ldc j], zero padding
+    for (int e = tid; e < Np * (Kp / 4); e += UG_THREADS) {
+        const int j = e / (Kp / 4), ig = e % (Kp / 4);
+        uint32_t h[4], l[4];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+            const int i = ig * 4 + t;
+            const float v = (j < a.ky && i < a.kx) ? (float)a.C[i + (size_t)a.ldc * j] : 0.f;
+            ug_split(v, h[t], l[t]);
+        }
+        const size_t at = (size_t)(j >> 3) * sbo + (size_t)ig * 128 + (j & 7) * 16;
+        *reinterpret_cast<uint4 *>(Bsm + at) = make_uint4(h[0], h[1], h[2], h[3]);
+        *reinterpret_cast<uint4 *>(Bsm + bimg + at) = make_uint4(l[0], l[1], l[2], l[3]);
+    }
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = *tslot;
+    const uint32_t slot_cols = a.tcols / 2;
+    int my = 0;   // tiles handled by this CTA
+    for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) ++my;
+
+    if (warp < 8) {
+        // ---- producers
+        for (int k = 0; k < my; ++k) {
+            const int s = k & 1;
+            if (k >= 2 && !ug_wait(empty + s, (uint32_t)(k / 2 - 1), &s_abort)) { s_abort = 1; break; }
+            const int64_t row0 = (int64_t)(blockIdx.x + (int64_t)k * gridDim.x) * UG_TM;
+            unsigned char *Ah = Asm + (size_t)s * 2 * aimg, *Al = Ah + aimg;
+            // all of this thread's loads first (up to 8 items x 4 columns in flight), then the
+            // splits and stores: item e = (row e % 128, columns 4 (e / 128) .. + 3)
+            const int items = UG_TM * (Kp / 4);
+            constexpr int MAXIT = (UG_TM * 64 / 4) / UG_PROD;   // Kp <= 64
+            float v[MAXIT][4];
+#pragma unroll
+            for (int it = 0; it < MAXIT; ++it) {
+                const int e = tid + it * UG_PROD;
+                const int r = e % UG_TM, ig = e / UG_TM;
+                const int64_t row = row0 + r;
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int i = ig * 4 + q;
+                    v[it][q] = 0.f;
+                    if (e < items && row < a.N && i < a.kx)
+                        v[it][q] = i < a.kx0 ? __ldg(a.X0 + row + (int64_t)i * a.ldx0)
+                                             : __ldg(a.X1 + row + (int64_t)(i - a.kx0) * a.ldx1);
+                }
+            }
+#pragma unroll
+            for (int it = 0; it < MAXIT; ++it) {
+                const int e = tid + it * UG_PROD;
+                if (e >= items) break;
+                const int r = e % UG_TM, ig = e / UG_TM;
+                uint32_t h[4], l[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) ug_split(v[it][q], h[q], l[q]);
+                const size_t at = (size_t)(r >> 3) * sbo + (size_t)ig * 128 + (r & 7) * 16;
+                *reinterpret_cast<uint4 *>(Ah + at) = make_uint4(h[0], h[1], h[2], h[3]);
+                *reinterpret_cast<uint4 *>(Al + at) = make_uint4(l[0], l[1], l[2], l[3]);
+            }
+            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+            ug_arrive(full + s);
+        }
+    } else if (warp == 8) {
+        // ---- MMA issuer (one lane)
+        if (lane == 0) {
+            const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(Np >> 3) << 17) |
+                                   ((uint32_t)(UG_TM >> 4) << 24);
+            const uint32_t b0 = su32(Bsm);
+            int issued = 0;
+            for (int k = 0; k < my; ++k) {
+                const int s = k & 1, sl = k & 1;
+                if (!ug_wait(full + s, (uint32_t)(k / 2), &s_abort)) { s_abort = 1; break; }
+                if (k >= 2 && !ug_wait(acce + sl, (uint32_t)(k / 2 - 1), &s_abort)) { s_abort = 1; break; }
+                asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                const uint32_t ah = su32(Asm + (size_t)s * 2 * aimg), al = ah + (uint32_t)aimg;
+                const uint32_t d = tmem + (uint32_t)sl * slot_cols;
+                for (int ks = 0; ks < Kp / 8; ++ks) {
+                    const uint32_t o = (uint32_t)ks * 256;
+                    const uint64_t dah = ug_desc(ah + o, 128, sbo), dal = ug_desc(al + o, 128, sbo);
+                    const uint64_t dbh = ug_desc(b0 + o, 128, sbo), dbl = ug_desc(b0 + (uint32_t)bimg + o, 128, sbo);
+                    ug_mma(d, dah, dbh, idesc, ks > 0 ? 1u : 0u);
+                    ug_mma(d, dah, dbl, idesc, 1u);
+                    ug_mma(d, dal, dbh, idesc, 1u);
+                }
+                ug_commit(empty + s);
+                ug_commit(accf + sl);
+                ++issued;
+            }
+            // all MMAs retired before TMEM is freed (bounded)
+            if (issued > 0) {
+                ug_commit(fin);
+                volatile int never = 0;
+                (void)ug_wait(fin, 0, &never);
+            }
+        }
+    } else {
+        // ---- epilogue: warps 9-12 read TMEM lanes 32 (w % 4) .. + 31
+        const int q = warp & 3;
+        for (int k = 0; k < my; ++k) {
+            const int sl = k & 1;
+            if (!ug_wait(accf + sl, (uint32_t)(k / 2), &s_abort)) { s_abort = 1; break; }
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const int64_t row = (int64_t)(blockIdx.x + (int64_t)k * gridDim.x) * UG_TM + q * 32 + lane;
+            const uint32_t base = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)sl * slot_cols;
+            for (int j0 = 0; j0 < a.ky; j0 += 16) {
+                uint32_t r[16];
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
+                    "%13, %14, %15}, [%16];\n"
+                    : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                      "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                      "=r"(r[15])
+                    : "r"(base + (uint32_t)j0));
+                asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+                if (row < a.N) {
+#pragma unroll
+                    for (int t = 0; t < 16; ++t) {
+                        const int j = j0 + t;
+                        if (j < a.ky) {
+                            float *yp = a.Y + row + (int64_t)j * a.ldy;
+                            const float v = a.alpha * __uint_as_float(r[t]);
+                            *yp = a.beta == 0.f ? v : v + a.beta * *yp;
+                        }
+                    }
+                }
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+            ug_arrive(acce + sl);
+        }
+    }
+    if (s_abort && tid == 0) {
+        *(volatile int *)a.err = KF_ETIMEOUT;
+        __threadfence_system();
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    if (warp == 8) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(a.tcols));
+}
+
+std::mutex g_ug_mu;
+bool g_ug_attr = false;
+
+}  // namespace
+
+bool update_tc_ok(int kx, int ky) { return kx >= 1 && kx <= 64 && ky >= 1 && ky <= 128; }
+
+void update_tc(float *Y, int64_t ldy, int ky, const float *X0, int64_t ldx0, int kx0, const float *X1, int64_t ldx1,
+               int kx1, const double *C, int ldc, double alpha, double beta, int64_t N, cudaStream_t s) {
+    const int kx = kx0 + kx1;
+    KF_REQUIRE(update_tc_ok(kx, ky), KF_EINVAL, "update_tc: kx must lie in 1:64 and ky in 1:128");
+    if (N <= 0) return;
+    UgArgs a;
+    a.Y = Y;
+    a.X0 = X0;
+    a.X1 = kx1 > 0 ? X1 : X0;
+    a.C = C;
+    a.err = tc_error_word();
+    a.ldy = ldy;
+    a.ldx0 = ldx0;
+    a.ldx1 = kx1 > 0 ? ldx1 : ldx0;
+    a.N = N;
+    a.kx0 = kx0;
+    a.kx = kx;
+    a.ky = ky;
+    a.ldc = ldc;
+    a.Kp = (kx + 7) / 8 * 8;
+    a.Np = (ky + 15) / 16 * 16;
+    uint32_t tc = 32;
+    while (tc < (uint32_t)(2 * a.Np)) tc <<= 1;
+    a.tcols = tc;
+    a.alpha = (float)alpha;
+    a.beta = (float)beta;
+    a.ntiles = (int)((N + UG_TM - 1) / UG_TM);
+    const size_t smem = (size_t)2 * a.Np * a.Kp * 4 + (size_t)4 * UG_TM * a.Kp * 4 + 16 * 8;
+    int sms = 152, dev = 0, optin = 0;
+    KF_CUDA(cudaGetDevice(&dev));
+    KF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    KF_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    cudaFuncAttributes fa;
+    KF_CUDA(cudaFuncGetAttributes(&fa, k_update_tc));
+    const size_t dyn_max = (size_t)optin - fa.sharedSizeBytes;
+    KF_REQUIRE(smem <= dyn_max, KF_EINVAL, "update_tc: shared-memory stages too large");
+    {
+        std::lock_guard<std::mutex> lk(g_ug_mu);
+        if (!g_ug_attr) {
+            KF_CUDA(cudaFuncSetAttribute(k_update_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn_max));
+            g_ug_attr = true;
+        }
+    }
+    const int grid = a.ntiles < sms ? a.ntiles : sms;
+    k_update_tc<<<grid, UG_THREADS, smem, s>>>(a);
+    KF_LAUNCH_CHECK();
+}
+
+}  // namespace kf

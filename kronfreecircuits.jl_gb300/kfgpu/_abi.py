@@ -128,6 +128,9 @@ def lib():
                                                 C.c_int32, P, C.POINTER(C.c_float)]),
         "kf_test_time_gram": (C.c_int, [P, C.c_int64, C.c_int32, P, C.c_int64, C.c_int32, C.c_int64, C.c_int32, P,
                                         C.POINTER(C.c_float), P]),
+        "kf_test_update": (C.c_int, [C.c_int32, P, C.c_int64, C.c_int32, P, C.c_int64, C.c_int32, P, C.c_int64,
+                                     C.c_int32, P, C.c_int32, C.c_double, C.c_double, C.c_int64, C.c_int32, P,
+                                     C.POINTER(C.c_float)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

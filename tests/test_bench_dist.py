@@ -18,11 +18,16 @@ def _free_port():
 
 
 def test_replica_aggregation_two_gloo_ranks():
-    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2", "--master-addr",
-           "127.0.0.1", "--master-port", str(_free_port()), os.path.join(ROOT, "tests", "dist_replicas_worker.py")]
     env = dict(os.environ, OMP_NUM_THREADS="1")
-    r = subprocess.run(cmd, capture_output=True, text=True, timeout=240, env=env, cwd=ROOT)
-    assert r.returncode == 0, r.stderr[-2000:]
+    # the free port is picked here and bound later by torchrun: on a busy host another process can
+    # take it in between, so a failed rendezvous is retried on a fresh port
+    for attempt in range(3):
+        cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2", "--master-addr",
+               "127.0.0.1", "--master-port", str(_free_port()), os.path.join(ROOT, "tests", "dist_replicas_worker.py")]
+        r = subprocess.run(cmd, capture_output=True, text=True, timeout=240, env=env, cwd=ROOT)
+        if r.returncode == 0:
+            break
+    assert r.returncode == 0, r.stderr[-3000:]
     rows = [json.loads(l) for l in r.stdout.splitlines() if l.startswith("{")]
     assert sorted(x["rank"] for x in rows) == [0, 1]
     for x in rows:
