@@ -717,6 +717,26 @@ void add_f32_into_f64(double *Y, int64_t ldy, const float *P, int64_t ldp, float
     KF_LAUNCH_CHECK();
 }
 
+// Y[:, j] = d_j X[:, j] + (double) P[:, j] (FP64, one FMA per element) and Y32 its FP32 rounding;
+// all blocks with leading dimension N
+__global__ void k_scale_add(double *__restrict__ Y, const double *__restrict__ X, const double *__restrict__ d,
+                            const float *__restrict__ P, float *__restrict__ Y32, int64_t N, int64_t total) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= total) return;
+    const int64_t c = t / N;
+    const double v = fma(d[c], X[t], (double)P[t]);
+    Y[t] = v;
+    Y32[t] = (float)v;
+}
+
+void scale_add(double *Y, const double *X, const double *d, const float *P, float *Y32, int k, int64_t N,
+               cudaStream_t s) {
+    if (k <= 0 || N <= 0) return;
+    const int64_t total = N * k;
+    k_scale_add<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(Y, X, d, P, Y32, N, total);
+    KF_LAUNCH_CHECK();
+}
+
 // theta_j = sum_i D_i X_ij^2 / sum_i X_ij^2 (ext/KronFreeCircuitsCUDAExt.jl:16-44): two
 // partial sums per column, weighted then plain.
 __global__ void k_diag_expect(const double *__restrict__ D, const double *__restrict__ X, int64_t ld, int64_t N,

@@ -182,6 +182,9 @@ void perturb_block(double *X, int64_t N, int k, double delta, uint64_t key, doub
 void residual_mixed(const double *X, const double *HX, int64_t ld, int k, int64_t N, const double *theta,
                     const double *thetap, const double *D, double eta, int mode, float *R, int64_t ldr, float *W,
                     int64_t ldw, double *norms2, double *partials, cudaStream_t s);
+// Y[:, j] = d_j X[:, j] + (double) P[:, j] and Y32 = FP32(Y) (leading dimension N)
+void scale_add(double *Y, const double *X, const double *d, const float *P, float *Y32, int k, int64_t N,
+               cudaStream_t s);
 void add_f32_into_f64(double *Y, int64_t ldy, const float *P, int64_t ldp, float *Y32, int64_t ld32, int k, int64_t N,
                       cudaStream_t s);
 // G = [A0 A1]' [B0 B1] for FP32 column blocks (a block with 0 columns is skipped)

@@ -201,6 +201,7 @@ struct LobParams {
 
 struct LobOut {
     int iters = 0;
+    int fast_updates = 0;   // refinement: updates that took the FP64-diagonal + FP32-mixing form
     int64_t nmv = 0;
     int nlocked = 0;
     bool converged = false;
@@ -530,11 +531,12 @@ static LobOut lobpcg_run(kf_op *op, LobWork<T> &Wk, const double *D, const LobPa
 struct RefineWork {
     int64_t N;
     int w;
-    DevMem X, HX, Xn, HXn, R32, T32;
+    DevMem X, HX, Xn, HXn, R32, T32, HX32, dd;
     RefineWork(int64_t N_, int w_)
         : N(N_), w(w_), X((size_t)N_ * w_ * sizeof(double)), HX((size_t)N_ * w_ * sizeof(double)),
           Xn((size_t)N_ * w_ * sizeof(double)), HXn((size_t)N_ * w_ * sizeof(double)),
-          R32((size_t)N_ * w_ * sizeof(float)), T32((size_t)N_ * w_ * sizeof(float)) {}
+          R32((size_t)N_ * w_ * sizeof(float)), T32((size_t)N_ * w_ * sizeof(float)),
+          HX32((size_t)N_ * w_ * sizeof(float)), dd((size_t)w_ * sizeof(double)) {}
 };
 
 // X64 (in R.X) on entry: orthonormalise it in FP64, H X64 with a fresh FP64 apply, Rayleigh-Ritz
@@ -567,6 +569,7 @@ static void refine_start(kf_op *op, RefineWork &R, LobWork<float> &W32, double c
     update<double>(X, N, w, Xn, N, w, C, w, 1.0, 0.0, N, s);
     update<double>(HX, N, w, HXn, N, w, C, w, 1.0, 0.0, N, s);
     convert<double, float>(X, N, W32.X.as<float>(), N, w, N, s);
+    convert<double, float>(HX, N, R.HX32.as<float>(), N, w, N, s);
 }
 
 static LobOut lobpcg_refine(kf_op *op, RefineWork &Rw, LobWork<float> &Wk, const double *D, const LobParams &prm,
@@ -684,25 +687,60 @@ static LobOut lobpcg_refine(kf_op *op, RefineWork &Rw, LobWork<float> &Wk, const
         std::vector<double> lam(ns), V((size_t)ns * ns);
         if (timed_sym_eig(ns, A.data(), ns, lam.data(), V.data(), ns) != 0)
             throw Error(KF_EBREAKDOWN, "LOBPCG: Rayleigh-Ritz eigenproblem did not converge");
-        std::memcpy(hC, V.data(), sizeof(double) * (size_t)ns * na3);
-        h2d(C, hC, (size_t)ns * na3, s);
-        // X_a <- X_a C_x (FP64) + Q C_z (FP32); HX_a likewise with H Q; P <- Q C_z
+        // Ritz vectors' signs are free: make diag(C_x) non-negative
+        for (int j = 0; j < na3; ++j)
+            if (V[j + (size_t)ns * j] < 0)
+                for (int i = 0; i < ns; ++i) V[i + (size_t)ns * j] = -V[i + (size_t)ns * j];
+        // X and HX are both updated, so the FP32 roundings of X_a E and HX_a E (E = C_x - D) do not
+        // cancel in R = HX - X theta: they move the tracked residual by ~ eps32 |theta| max|E|.
+        // The FP32 form is taken only while max|E| <= 1e-4 (a drift below ~1e-11 |theta|).
+        bool near_identity = true;
+        for (int j = 0; j < na3; ++j)
+            for (int i = 0; i < na3; ++i)
+                if (i != j && std::fabs(V[i + (size_t)ns * j]) > 1e-4) near_identity = false;
+        if (near_identity) ++out.fast_updates;
         double *Xa = X + (int64_t)nl * N, *HXa = HX + (int64_t)nl * N;
         double *Xna = Xn + (int64_t)nl * N, *HXna = HXn + (int64_t)nl * N;
-        update<double>(Xna, N, na3, Xa, N, na3, C, ns, 1.0, 0.0, N, s);
-        update<float>(Pn, N, na3, Q, N, k, C + na3, ns, 1.0, 0.0, N, s);
-        add_f32_into_f64(Xna, N, Pn, N, X32 + (int64_t)nl * N, N, na3, N, s);
-        update<double>(HXna, N, na3, HXa, N, na3, C, ns, 1.0, 0.0, N, s);
-        update<float>(T32, N, na3, HZ, N, k, C + na3, ns, 1.0, 0.0, N, s);
-        add_f32_into_f64(HXna, N, T32, N, nullptr, 0, na3, N, s);
+        float *X32a = X32 + (int64_t)nl * N, *HX32a = Rw.HX32.as<float>() + (int64_t)nl * N;
+        if (near_identity) {
+            // X_a C_x = X_a D + X_a (C_x - D), D = diag(C_x): the scaling in FP64, the rest in FP32
+            // with Q C_z -- its rounding is proportional to the mixing C_x - D, which is small
+            // unless two Ritz values are close (then their mixing moves the residual little)
+            double *dg = hv + 2 * w;   // pinned staging, rewritten only after later synchronisations
+            for (int j = 0; j < na3; ++j) {
+                dg[j] = V[j + (size_t)ns * j];
+                V[j + (size_t)ns * j] = 0.0;
+            }
+            std::memcpy(hC, V.data(), sizeof(double) * (size_t)ns * na3);
+            h2d(C, hC, (size_t)ns * na3, s);
+            h2d(Rw.dd.as<double>(), dg, na3, s);
+            update2<float>(T32, N, na3, X32a, N, na3, Q, N, k, C, ns, 1.0, 0.0, N, s);
+            scale_add(Xna, Xa, Rw.dd.as<double>(), T32, X32a, na3, N, s);
+            update2<float>(T32, N, na3, HX32a, N, na3, HZ, N, k, C, ns, 1.0, 0.0, N, s);
+            scale_add(HXna, HXa, Rw.dd.as<double>(), T32, HX32a, na3, N, s);
+            update<float>(Pn, N, na3, Q, N, k, C + na3, ns, 1.0, 0.0, N, s);
+        } else {
+            // a large rotation inside X (Ritz values reordered): X_a C_x in FP64
+            std::memcpy(hC, V.data(), sizeof(double) * (size_t)ns * na3);
+            h2d(C, hC, (size_t)ns * na3, s);
+            update<double>(Xna, N, na3, Xa, N, na3, C, ns, 1.0, 0.0, N, s);
+            update<float>(Pn, N, na3, Q, N, k, C + na3, ns, 1.0, 0.0, N, s);
+            add_f32_into_f64(Xna, N, Pn, N, X32a, N, na3, N, s);
+            update<double>(HXna, N, na3, HXa, N, na3, C, ns, 1.0, 0.0, N, s);
+            update<float>(T32, N, na3, HZ, N, k, C + na3, ns, 1.0, 0.0, N, s);
+            add_f32_into_f64(HXna, N, T32, N, HX32a, N, na3, N, s);
+        }
         np = na3;
         std::swap(X, Xn);
         std::swap(HX, HXn);
         for (int j = 0; j < na3; ++j) theta[nl + j] = lam[j];
     }
     if (trace_on())
-        std::fprintf(stderr, "kf lobpcg refine: %d iterations, %.4f s; blocked on the stream %.4f s (%d syncs), host eig %.4f s\n",
-                     out.iters, now_s() - tw0, g_tt.sync - tt0.sync, g_tt.nsync - tt0.nsync, g_tt.eig - tt0.eig);
+        std::fprintf(stderr,
+                     "kf lobpcg refine: %d iterations (%d FP32-mixing updates), %.4f s; blocked on the stream %.4f s "
+                     "(%d syncs), host eig %.4f s\n",
+                     out.iters, out.fast_updates, now_s() - tw0, g_tt.sync - tt0.sync, g_tt.nsync - tt0.nsync,
+                     g_tt.eig - tt0.eig);
     if (X != Rw.X.as<double>()) {
         copy_block<double>(X, N, Rw.X.as<double>(), N, w, N, s);
         copy_block<double>(HX, N, Rw.HX.as<double>(), N, w, N, s);
