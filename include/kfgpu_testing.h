@@ -51,6 +51,15 @@ int kf_test_update(int path, float *Y, int64_t ldy, int ky, const float *X0, int
                    int64_t ldx1, int kx1, const double *C, int ldc, double alpha, double beta, int64_t N, int reps,
                    void *stream, float *ms_per_launch);
 
+/*
+ * kf_op_apply (device blocks, flags as there) with the fused-apply kernel variant forced instead of
+ * the tuned one: 0-4 the point-per-thread kernel's shapes, 5 the plane-marching kernel (where its
+ * geometry applies; otherwise variant 4 runs); `reps` launches timed with CUDA events on the op's
+ * stream, *ms_per_launch (may be NULL) receives the mean.
+ */
+int kf_test_apply_variant(kf_op *op, int variant, const void *X, void *Y, int64_t ld, int64_t b, int32_t flags,
+                          int reps, float *ms_per_launch);
+
 #ifdef __cplusplus
 }
 #endif

@@ -376,4 +376,37 @@ int kf_test_update(int path, float *Y, int64_t ldy, int ky, const float *X0, int
     });
 }
 
+int kf_test_apply_variant(kf_op *op, int variant, const void *X, void *Y, int64_t ld, int64_t b, int32_t flags,
+                          int reps, float *ms_per_launch) {
+    return guarded([&] {
+        KF_REQUIRE(op && X && Y && variant >= 0 && variant < kf::KF_APPLY_VARIANTS && reps >= 1, KF_EINVAL,
+                   "kf_test_apply_variant: bad argument");
+        KF_REQUIRE(!(flags & KF_HOST), KF_EINVAL, "kf_test_apply_variant: device blocks only");
+        cudaEvent_t e0, e1;
+        KF_CUDA(cudaEventCreate(&e0));
+        KF_CUDA(cudaEventCreate(&e1));
+        op->force_variant = variant;
+        float ms = 0;
+        try {
+            kf::launch_apply(op, (flags & KF_F32) != 0, X, Y, ld, ld, b, 1.0, 0.0, nullptr, 0, 0.0, op->stream);
+            KF_CUDA(cudaEventRecord(e0, op->stream));
+            for (int r = 0; r < reps; ++r)
+                kf::launch_apply(op, (flags & KF_F32) != 0, X, Y, ld, ld, b, 1.0, 0.0, nullptr, 0, 0.0, op->stream);
+            KF_CUDA(cudaEventRecord(e1, op->stream));
+            KF_CUDA(cudaEventSynchronize(e1));
+            KF_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        } catch (...) {
+            op->force_variant = -1;
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            throw;
+        }
+        op->force_variant = -1;
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        if (ms_per_launch) *ms_per_launch = ms / reps;
+        if (const int t = kf::tc_take_error()) throw kf::Error(t, "plane-marching apply: device wait timed out");
+    });
+}
+
 }  // extern "C"

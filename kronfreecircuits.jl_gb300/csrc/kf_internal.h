@@ -49,7 +49,7 @@ extern std::atomic<uint64_t> g_launches;
 
 constexpr int MAXDIMS = 8;     // axes of a state tensor
 constexpr int MAXB = 24;       // bands of one banded factor (a periodic order-8 stencil has 16)
-constexpr int KF_APPLY_VARIANTS = 5;   // (columns per thread, columns at once) candidates
+constexpr int KF_APPLY_VARIANTS = 6;   // five (columns per thread, unroll) shapes + the plane-marching kernel
 constexpr int MAXE = 48;       // stencil entries (products of bands) over all fused terms
 
 // The fused kernel's stencil entries.  Every term built only of diagonal, banded and shift
@@ -120,6 +120,7 @@ struct kf_op {
     bool own_stream = true;
     kf::ApplyPlan plan{};
     int apply_variant[16] = {-1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1};
+    int force_variant = -1;   // test-only: run this fused-apply variant instead of the tuned one
     float apply_variant_ms[16] = {};
     int64_t N = 0;
     std::vector<int64_t> dims;
@@ -166,6 +167,25 @@ struct kf_op {
 };
 
 namespace kf {
+
+// plane-marching fused apply (kf_apply_tiled.cu): the slowest axis m with an offset is walked
+// plane by plane, plane slices staged in shared memory by TMA bulk copies
+struct TiledGeom {
+    int m;          // march axis
+    int P;          // plane size (product of the axes before m)
+    int nm;         // planes (length of axis m)
+    int N;          // column length
+    int H;          // largest |offset| along m
+    int R;          // largest |in-plane offset|
+    int SL;         // ring slot length per column, elements
+    int L;          // planes per CTA
+    int nseg, ntile, nouter;
+};
+bool tiled_geometry(const kf_op *op, int64_t b, size_t elem, TiledGeom &g);
+template <typename T>
+void launch_apply_tiled(const kf_op *op, const TiledGeom &g, const T *D, const T *W, const T *X, T *Y, int64_t ldx,
+                        int64_t ldy, int64_t b, T alpha, T beta, const T *Z, int64_t ldz, T gamma, int epi,
+                        cudaStream_t s);
 
 // kernels of kf_op.cu
 void launch_apply(kf_op *op, bool f32, const void *X, void *Y, int64_t ldx, int64_t ldy, int64_t b,

@@ -213,7 +213,15 @@ static void apply_t(kf_op *op, const T *X, T *Y, int64_t ldx, int64_t ldy, int64
     const bool trivial_epi = alpha == 1.0 && beta == 0.0 && (Z == nullptr || gamma == 0.0);
     const int epi = (!chains && !trivial_epi) ? 1 : 0;
     const int ne = op->plan.ne;
+    // the plane-marching kernel (variant 5) where its geometry applies and X is 16-byte aligned
+    TiledGeom tg;
+    const int G = 16 / (int)sizeof(T);
+    const bool tiled_ok = tiled_geometry(op, b, sizeof(T), tg) && ldx % G == 0 && (uintptr_t)X % 16 == 0;
     auto run = [&](int variant) {
+        if (variant == 5 && tiled_ok) {
+            launch_apply_tiled<T>(op, tg, D, W, X, Y, ldx, ldy, b, (T)alpha, (T)beta, Z, ldz, (T)gamma, epi, s);
+            return;
+        }
 #define KF_FUSED(CPT, U, ME)                                                                                  \
     k_apply_fused<T, CPT, U, ME><<<dim3((unsigned)((N + 255) / 256), (unsigned)((b + CPT - 1) / CPT)), 256, 0, s>>>( \
         op->plan, D, W, X, Y, ldx, ldy, (int)b, (T)alpha, (T)beta, Z, ldz, (T)gamma, epi)
@@ -236,6 +244,10 @@ static void apply_t(kf_op *op, const T *X, T *Y, int64_t ldx, int64_t ldy, int64
     // operators of the same stencil shape (a parameter sweep rebuilds the same structure with new
     // coefficients) share one tuning per process and device
     const std::string key = tune_key(op, slot);
+    if (op->force_variant >= 0) {
+        run(op->force_variant);
+        goto chained;
+    }
     if (op->apply_variant[slot] < 0) {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         auto it = g_tune.find(key);
@@ -248,6 +260,7 @@ static void apply_t(kf_op *op, const T *X, T *Y, int64_t ldx, int64_t ldy, int64
         float best = 1e30f;
         int bestv = 0;
         for (int v = 0; v < KF_APPLY_VARIANTS; ++v) {
+            if (v == 5 && !tiled_ok) continue;
             run(v);                                   // warm
             KF_CUDA(cudaEventRecord(e0, s));
             for (int r = 0; r < 3; ++r) run(v);
@@ -265,6 +278,7 @@ static void apply_t(kf_op *op, const T *X, T *Y, int64_t ldx, int64_t ldy, int64
         g_tune[key] = bestv;
     }
     run(op->apply_variant[slot]);
+chained:
     if (!chains) return;
     // dense-containing terms: chain through scratch, one contiguous (N x b) block per buffer
     const size_t need = (size_t)2 * N * b * sizeof(T);

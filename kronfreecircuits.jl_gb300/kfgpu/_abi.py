@@ -128,6 +128,8 @@ def lib():
                                                 C.c_int32, P, C.POINTER(C.c_float)]),
         "kf_test_time_gram": (C.c_int, [P, C.c_int64, C.c_int32, P, C.c_int64, C.c_int32, C.c_int64, C.c_int32, P,
                                         C.POINTER(C.c_float), P]),
+        "kf_test_apply_variant": (C.c_int, [P, C.c_int32, P, P, C.c_int64, C.c_int64, C.c_int32, C.c_int32,
+                                            C.POINTER(C.c_float)]),
         "kf_test_update": (C.c_int, [C.c_int32, P, C.c_int64, C.c_int32, P, C.c_int64, C.c_int32, P, C.c_int64,
                                      C.c_int32, P, C.c_int32, C.c_double, C.c_double, C.c_int64, C.c_int32, P,
                                      C.POINTER(C.c_float)]),

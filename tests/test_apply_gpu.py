@@ -199,3 +199,46 @@ def test_errors(cuda):
         H.apply(np.zeros((13, 1)))
     # an empty block is a no-op
     H.apply_device(X.data_ptr(), X.data_ptr() + 8 * 12, 0)
+
+
+@pytest.mark.parametrize("f32", [False, True])
+@pytest.mark.parametrize("shape", ["three_mode", "wide", "outer_axes"])
+def test_plane_marching_apply(cuda, f32, shape):
+    """The plane-marching kernel (variant 5: plane slices staged in shared memory by TMA bulk
+    copies) against the point-per-thread kernel and the oracle, forced past the autotuner: the
+    three-mode structure, a plane wider than a tile, and axes after the marching axis."""
+    import ctypes as C
+    torch = cuda
+    from kfgpu import _abi, circuits, ops as P
+    rng = np.random.default_rng(11)
+
+    def banded(n, offs):
+        return P.BandedOp(n, list(offs), [rng.standard_normal(n) for _ in offs])
+
+    if shape == "three_mode":
+        th = circuits.three_mode_theta(rng)
+        dims, terms = circuits.three_mode_leaf(th, ncut=6, n2=48, n3=20)
+    elif shape == "wide":
+        dims = [41, 300, 5]
+        terms = [(1.0, [(0, P.ShiftOp(41, 1, 1.0))]), (0.7, [(1, banded(300, (-2, -1, 0, 1, 2)))]),
+                 (0.3, [(2, banded(5, (-1, 1)))]), (0.5, [(0, P.DiagonalOp(rng.standard_normal(41)))])]
+    else:
+        dims = [8, 20, 12, 3]
+        terms = [(1.0, [(0, P.ShiftOp(8, -1, 2.0)), (1, banded(20, (-2, 0, 1)))]),
+                 (0.4, [(3, P.DiagonalOp(rng.standard_normal(3)))]), (0.9, [(2, P.DiagonalOp(rng.standard_normal(12)))])]
+    H, Ho = _pair(dims, terms)
+    N, b = H.N, 5
+    dt = torch.float32 if f32 else torch.float64
+    X = torch.as_tensor(rng.standard_normal((b, N)), dtype=dt, device="cuda")
+    Ys = []
+    flags = _abi.KF_DEVICE | (_abi.KF_F32 if f32 else _abi.KF_F64)
+    for v in (0, 5):
+        Y = torch.full_like(X, float("nan"))
+        _abi.check(_abi.lib().kf_test_apply_variant(H.handle, v, C.c_void_p(X.data_ptr()), C.c_void_p(Y.data_ptr()), N,
+                                                    b, flags, 1, None))
+        Ys.append(Y.double().cpu().numpy())
+    R = Ho.matvec(X.double().cpu().numpy().T).T
+    scale = max(1.0, np.max(np.abs(R)))
+    tol = TOL32 if f32 else TOL64
+    assert np.max(np.abs(Ys[1] - R)) / scale < tol
+    assert np.max(np.abs(Ys[1] - Ys[0])) / scale < tol
