@@ -190,7 +190,9 @@ def run_ours(args, D):
         H, seedb = ops[i]
         tol = 1e-8 * H.gershgorin_bound()
         pc = precond or ("separable" if precision == "mixed" else "ritz")
-        E, V, st = solve(LOBPCG(tol=tol, precision=precision, preconditioner=pc), H, M_PAIRS, seed_block=seedb)
+        buf = args.buffer if precision == "mixed" else None
+        E, V, st = solve(LOBPCG(tol=tol, precision=precision, preconditioner=pc, buffer=buf), H, M_PAIRS,
+                         seed_block=seedb)
         return st["converged"], st
 
     for w in range(W):
@@ -248,7 +250,8 @@ def run_ours(args, D):
         dims, terms = circuits.three_mode_leaf(ths[i])
         H = KronFreeOperator(dims, terms)
         tol = 1e-8 * H.gershgorin_bound()
-        E, V, st = solve(LOBPCG(tol=tol, precision="mixed", preconditioner="separable"), H, M_PAIRS)
+        E, V, st = solve(LOBPCG(tol=tol, precision="mixed", preconditioner="separable", buffer=args.buffer), H,
+                         M_PAIRS)
         conv_e += st["converged"]
         h2d += H.N * 8 + sum(op.n * 8 * 5 for _, fs in terms for _, op in fs)
         d2h += V.nbytes + E.nbytes
@@ -272,6 +275,7 @@ def run_ours(args, D):
         "vs_baseline": None, "dtype": "f32 bulk + f64 refinement", "data": "synthetic",
         "config": {"workload": "three-mode leaf 41x256x64 (N=671,744), LOBPCG m=12 block=16, product seed, "
                                "tol 1e-8*||H||, theta ~ U(ranges) seed 20261205",
+                   "buffer_columns": "library default (2, mixed only)" if args.buffer is None else args.buffer,
                    "l2": "inputs larger than L2 (a 16-column FP32 block is 43 MB; a solve streams ~10 GB)"},
         "replicas": D.world,
         "plain_f64": {"value": plain, "steps": kp, "ms_per_step": 1e3 * t64 / kp,
@@ -307,8 +311,8 @@ def profile_one(args):
     H = KronFreeOperator(dims, terms)
     n0 = launch_count()
     t0 = time.perf_counter()
-    E, V, st = solve(LOBPCG(tol=1e-8 * H.gershgorin_bound(), precision="mixed", preconditioner="separable"), H,
-                     M_PAIRS)
+    E, V, st = solve(LOBPCG(tol=1e-8 * H.gershgorin_bound(), precision="mixed", preconditioner="separable",
+                            buffer=args.buffer), H, M_PAIRS)
     torch.cuda.synchronize()
     return {"seconds": time.perf_counter() - t0, "launches": launch_count() - n0, "iterations": st["iterations"],
             "iterations_f64": st["iterations_f64"], "seconds_f64": st["seconds_f64"]}
@@ -365,16 +369,17 @@ def time_mode_product(torch, path, dims, axis, b=16, reps=10):
     return ms.value / 1e3
 
 
-def time_gram(torch, ka, kb, N, reps=10):
+def time_gram(torch, ka, kb, N, reps=10, path=0):
     """Mean device time of one FP32 Gram product A'B (A: N x ka, B: N x kb; the Gram kernel with its
-    fixed-order partial reduction), through the library's test-only timing entry point."""
+    fixed-order partial reduction), through the library's test-only timing entry point.  path 0:
+    the solvers' choice (tcgen05 where the shapes fit), 1: the SIMT kernel."""
     import ctypes as C
     from kfgpu import _abi
     A = torch.randn(ka, N, dtype=torch.float32, device="cuda")
     B = torch.randn(kb, N, dtype=torch.float32, device="cuda")
     ms = C.c_float(0)
-    _abi.check(_abi.lib().kf_test_time_gram(C.c_void_p(A.data_ptr()), N, ka, C.c_void_p(B.data_ptr()), N, kb, N, reps,
-                                            None, C.byref(ms), None))
+    _abi.check(_abi.lib().kf_test_time_gram(path, C.c_void_p(A.data_ptr()), N, ka, C.c_void_p(B.data_ptr()), N, kb,
+                                            N, reps, None, C.byref(ms), None))
     return ms.value / 1e3
 
 
@@ -421,10 +426,11 @@ def run_gram_workload(args):
     N = 671744
     peak, kind = peaks()
     out = {"workload": "FP32 Gram A'B, N=671,744 rows", "hbm_peak_gbs": peak, "peak_kind": kind}
-    for ka, kb in GRAM_SHAPES:
-        t = time_gram(torch, ka, kb, N)
-        out[f"gram_{ka}x{kb}_us"] = t * 1e6
-        out[f"gram_{ka}x{kb}_gbs"] = (ka + kb) * N * 4 / t / 1e9
+    for ka, kb in GRAM_SHAPES + ((20, 40), (48, 48)):
+        for path, name in ((0, "gram"), (1, "simt")):
+            t = time_gram(torch, ka, kb, N, path=path)
+            out[f"{name}_{ka}x{kb}_us"] = t * 1e6
+            out[f"{name}_{ka}x{kb}_gbs"] = (ka + kb) * N * 4 / t / 1e9
     return out
 
 
@@ -629,6 +635,8 @@ def main():
                     help="LOBPCG iterations the plain FP64 solve of this workload takes, for the reference arm's "
                          "extrapolation (868: the mean over the first two timed draws measured on GB300)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--buffer", type=int, default=None,
+                    help="unchecked LOBPCG columns beyond the guards in the mixed solves (default: the library's)")
     ap.add_argument("--workload", default="leaf3",
                     choices=["leaf3", "batch", "warmstart", "dense", "apply", "mode", "gram", "update"],
                     help="leaf3 (the benchmarked workload) or one of the other measured configurations")

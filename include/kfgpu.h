@@ -186,7 +186,15 @@ typedef struct {
     int32_t seed_kind;         /* LOBPCG / Chebyshev `seed` (src/tree.jl:66-87, 293-321):
                                   KF_SEED_PRODUCT (default) or KF_SEED_RANDOM; used when
                                   kf_solve's seed argument is NULL                             */
+    int32_t buffer;            /* LOBPCG: unchecked columns carried beyond the guards; they
+                                  speed the convergence of the top guard when an eigenvalue
+                                  just above the block is nearly degenerate with it, and
+                                  never count toward convergence or the returned pairs.
+                                  KF_BUFFER_AUTO (default): 2 for KF_PREC_MIXED, 0 for
+                                  KF_PREC_F64 (the reference algorithm column for column)     */
 } kf_solver_opts;
+
+#define KF_BUFFER_AUTO (-1)
 
 #define KF_SEED_PRODUCT 0   /* seed=:product, product_seed(H, w) built by the library         */
 #define KF_SEED_RANDOM  1   /* seed=:random                                                    */

@@ -33,12 +33,26 @@ int kf_test_time_mode_product(int path, const float *X, float *Y, const double *
 /*
  * The FP32 Gram product G = A' B (A: N x ka, B: N x kb, device, column-major with leading
  * dimensions lda, ldb; ka, kb <= 128) launched `reps` times on `stream` and timed with CUDA events
- * around the launches (the Gram kernel and its fixed-order partial reduction together);
+ * around the launches (the Gram kernel and its fixed-order partial reduction together).  path 0:
+ * the solvers' choice (the tensor cores when the shapes fit), path 1: the SIMT kernel;
  * *ms_per_launch receives the mean device time of one product, G_out (host, ka x kb column-major,
  * may be NULL) the last result.  Returns a KF_* status.
  */
-int kf_test_time_gram(const float *A, int64_t lda, int ka, const float *B, int64_t ldb, int kb, int64_t N, int reps,
-                      void *stream, float *ms_per_launch, double *G_out);
+int kf_test_time_gram(int path, const float *A, int64_t lda, int ka, const float *B, int64_t ldb, int kb, int64_t N,
+                      int reps, void *stream, float *ms_per_launch, double *G_out);
+
+/*
+ * The tensor-core FP32 Gram (tcgen05, TF32 hi / lo operands) on a pool of nsrc (1..4) device
+ * blocks: srcs[q] (N x ks[q], leading dimension lds[q]) stacked in order; G_out (host, nr x nc
+ * column-major FP64, nr = sum of ks[r0 .. r1-1], nc = sum of ks[c0 .. c1-1]) receives
+ * [srcs r0..r1-1]' [srcs c0..c1-1].  `reps` launches on `stream`, timed with CUDA events
+ * (*ms_per_launch: mean device time, Gram and reduction); accs: TMEM accumulators per 32-row chunk
+ * (0: the library's choice).  Returns KF_EINVAL when the shapes do not
+ * fit the kernel (the solvers then take the SIMT Gram), else a KF_* status.
+ */
+int kf_test_gram_tc(const float *const *srcs, const int64_t *lds, const int32_t *ks, int32_t nsrc, int32_t r0,
+                    int32_t r1, int32_t c0, int32_t c1, int64_t N, int32_t accs, int32_t reps, void *stream,
+                    float *ms_per_launch, double *G_out);
 
 /*
  * The FP32 block update Y = alpha [X0 X1] C + beta Y (device blocks: X0 N x kx0, X1 N x kx1 (kx1 may

@@ -226,6 +226,7 @@ void kf_solver_opts_default(kf_solver_opts *o, int32_t kind) {
     o->fallback_iters = 3;
     o->fallback_resid = 0.0;
     o->seed_kind = KF_SEED_PRODUCT;
+    o->buffer = KF_BUFFER_AUTO;
 }
 
 int kf_solve(kf_op *op, const kf_solver_opts *opts, int32_t m, const double *X0, const double *seed, double *E_out,
@@ -313,8 +314,8 @@ int kf_test_time_mode_product(int path, const float *X, float *Y, const double *
     });
 }
 
-int kf_test_time_gram(const float *A, int64_t lda, int ka, const float *B, int64_t ldb, int kb, int64_t N, int reps,
-                      void *stream, float *ms_per_launch, double *G_out) {
+int kf_test_time_gram(int path, const float *A, int64_t lda, int ka, const float *B, int64_t ldb, int kb, int64_t N,
+                      int reps, void *stream, float *ms_per_launch, double *G_out) {
     return guarded([&] {
         KF_REQUIRE(A && B && ms_per_launch && reps >= 1 && N >= 1, KF_EINVAL, "kf_test_time_gram: bad argument");
         KF_REQUIRE(lda >= N && ldb >= N, KF_EDIM, "kf_test_time_gram: leading dimensions must be >= N");
@@ -325,9 +326,10 @@ int kf_test_time_gram(const float *A, int64_t lda, int ka, const float *B, int64
         cudaEvent_t e0, e1;
         KF_CUDA(cudaEventCreate(&e0));
         KF_CUDA(cudaEventCreate(&e1));
-        kf::gram<float>(A, lda, ka, B, ldb, kb, N, G, part, s);   // warm
+        KF_REQUIRE(path == 0 || path == 1, KF_EINVAL, "kf_test_time_gram: path must be 0 or 1");
+        kf::gram<float>(A, lda, ka, B, ldb, kb, N, G, part, s, path == 0);   // warm
         KF_CUDA(cudaEventRecord(e0, s));
-        for (int r = 0; r < reps; ++r) kf::gram<float>(A, lda, ka, B, ldb, kb, N, G, part, s);
+        for (int r = 0; r < reps; ++r) kf::gram<float>(A, lda, ka, B, ldb, kb, N, G, part, s, path == 0);
         KF_CUDA(cudaEventRecord(e1, s));
         KF_CUDA(cudaEventSynchronize(e1));
         float ms = 0;
@@ -337,6 +339,51 @@ int kf_test_time_gram(const float *A, int64_t lda, int ka, const float *B, int64
         cudaEventDestroy(e1);
         cudaFree(G);
         cudaFree(part);
+        *ms_per_launch = ms / reps;
+    });
+}
+
+int kf_test_gram_tc(const float *const *srcs, const int64_t *lds, const int32_t *ks, int32_t nsrc, int32_t r0,
+                    int32_t r1, int32_t c0, int32_t c1, int64_t N, int32_t accs, int32_t reps, void *stream,
+                    float *ms_per_launch, double *G_out) {
+    return guarded([&] {
+        KF_REQUIRE(srcs && lds && ks && ms_per_launch && reps >= 1 && N >= 1 && nsrc >= 1 && nsrc <= 4, KF_EINVAL,
+                   "kf_test_gram_tc: bad argument");
+        KF_REQUIRE(r0 >= 0 && r0 < r1 && r1 <= nsrc && c0 >= 0 && c0 < c1 && c1 <= nsrc, KF_EINVAL,
+                   "kf_test_gram_tc: source ranges out of bounds");
+        std::vector<kf::GramTcSrc> src(nsrc);
+        for (int q = 0; q < nsrc; ++q) {
+            KF_REQUIRE(srcs[q] && ks[q] >= 1 && lds[q] >= N, KF_EINVAL, "kf_test_gram_tc: bad source block");
+            src[q] = {srcs[q], lds[q], ks[q]};
+        }
+        int nr = 0, nc = 0;
+        for (int q = r0; q < r1; ++q) nr += ks[q];
+        for (int q = c0; q < c1; ++q) nc += ks[q];
+        cudaStream_t s = (cudaStream_t)stream;
+        double *G = nullptr;
+        void *part = nullptr;
+        const size_t pb = kf::gram_tc_partials_size(nr, nc);
+        KF_CUDA(cudaMalloc(&G, (size_t)nr * nc * sizeof(double)));
+        KF_CUDA(cudaMalloc(&part, pb));
+        KF_REQUIRE(accs >= 0 && accs <= 12, KF_EINVAL, "kf_test_gram_tc: accs must lie in 0:12");
+        auto run = [&] { return kf::gram_tc(src.data(), nsrc, r0, r1, c0, c1, N, G, part, pb, s, accs); };
+        bool ok = run();   // warm
+        cudaEvent_t e0, e1;
+        KF_CUDA(cudaEventCreate(&e0));
+        KF_CUDA(cudaEventCreate(&e1));
+        KF_CUDA(cudaEventRecord(e0, s));
+        for (int r = 0; ok && r < reps; ++r) run();
+        KF_CUDA(cudaEventRecord(e1, s));
+        KF_CUDA(cudaEventSynchronize(e1));
+        float ms = 0;
+        KF_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (ok && G_out) KF_CUDA(cudaMemcpy(G_out, G, (size_t)nr * nc * sizeof(double), cudaMemcpyDeviceToHost));
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        cudaFree(G);
+        cudaFree(part);
+        if (const int e = kf::tc_take_error()) throw kf::Error(e, "kf_test_gram_tc: the tensor-core Gram timed out");
+        KF_REQUIRE(ok, KF_EINVAL, "kf_test_gram_tc: the shapes do not fit the tensor-core Gram");
         *ms_per_launch = ms / reps;
     });
 }

@@ -39,7 +39,7 @@ size_t gram_partials_size(int ka, int kb, int64_t N) {
     const int nc = num_ctas_for(N, gram_rows_per_cta(N, 1));
     const size_t a = (size_t)nc * ka * kb;
     const size_t b = (size_t)1216 * 128;  // also enough for the column reductions
-    return (a > b ? a : b) * sizeof(double);
+    return std::max((a > b ? a : b) * sizeof(double), gram_tc_partials_size(ka, kb));
 }
 
 // partial[cta][i + ka*j] = sum over this CTA's rows of A[r,i] B[r,j], for one RI x RJ chunk of
@@ -316,12 +316,42 @@ __global__ void __launch_bounds__(256, 2) k_gram32(const Cols2 A, int ka, const 
     }
 }
 
-// G ((ka0 + ka1) x (kb0 + kb1), column-major, FP64) = [A0 A1]' [B0 B1] for FP32 column blocks
+// The tensor-core Gram for [A0 A1]' [B0 B1] when it fits: a B set that is A1 (the orthogonalisation's
+// [X Z]'Z) or A0 (a self Gram) is loaded once; otherwise the pool is [A0 A1 B0 B1].
+static bool gram32_try_tc(const float *A0, int64_t lda0, int ka0, const float *A1, int64_t lda1, int ka1,
+                          const float *B0, int64_t ldb0, int kb0, const float *B1, int64_t ldb1, int kb1, int64_t N,
+                          double *G, double *partials, cudaStream_t s) {
+    if (N < GRAM_TC_MIN_ROWS) return false;
+    // a tcgen05.mma (K = 8 rows) costs about the same whatever its width up to N = 128, so the
+    // tensor-core Gram takes a near-constant time per row; the SIMT kernel's grows with the padded
+    // output (measured on 671,744 rows: 16 x 32 SIMT 68 us vs 120 us, 32 x 32 110 vs 114, 24 x 40
+    // 148 vs 117, 48 x 48 512 vs 131)
+    const int pa = (ka0 + ka1 + 7) / 8 * 8, pb = (kb0 + kb1 + 7) / 8 * 8;
+    if (pa * pb < 1024) return false;
+    const size_t cap = gram_partials_size(ka0 + ka1, kb0 + kb1, N);
+    GramTcSrc src[4];
+    int n = 0;
+    src[n++] = {A0, lda0, ka0};
+    if (ka1 > 0) src[n++] = {A1, lda1, ka1};
+    const int na = n;
+    if (kb1 == 0 && ka1 > 0 && B0 == A1 && ldb0 == lda1 && kb0 == ka1)
+        return gram_tc(src, n, 0, na, na - 1, na, N, G, partials, cap, s);
+    if (kb1 == 0 && ka1 == 0 && B0 == A0 && ldb0 == lda0 && kb0 == ka0)
+        return gram_tc(src, n, 0, 1, 0, 1, N, G, partials, cap, s);
+    src[n++] = {B0, ldb0, kb0};
+    if (kb1 > 0) src[n++] = {B1, ldb1, kb1};
+    return gram_tc(src, n, 0, na, na, n, N, G, partials, cap, s);
+}
+
+// G ((ka0 + ka1) x (kb0 + kb1), column-major, FP64) = [A0 A1]' [B0 B1] for FP32 column blocks; on
+// the tensor cores when the shapes fit (allow_tc), else the SIMT kernel below
 void gram32_sets(const float *A0, int64_t lda0, int ka0, const float *A1, int64_t lda1, int ka1, const float *B0,
                  int64_t ldb0, int kb0, const float *B1, int64_t ldb1, int kb1, int64_t N, double *G, double *partials,
-                 cudaStream_t s) {
+                 cudaStream_t s, bool allow_tc) {
     const int ka = ka0 + ka1, kb = kb0 + kb1;
     KF_REQUIRE(ka >= 1 && kb >= 1 && ka <= 128 && kb <= 128, KF_EINVAL, "gram: block widths out of range");
+    if (allow_tc && gram32_try_tc(A0, lda0, ka0, A1, lda1, ka1, B0, ldb0, kb0, B1, ldb1, kb1, N, G, partials, s))
+        return;
     const Cols2 A{A0, ka1 > 0 ? A1 : A0, lda0, ka1 > 0 ? lda1 : lda0, ka0};
     const Cols2 B{B0, kb1 > 0 ? B1 : B0, ldb0, kb1 > 0 ? ldb1 : ldb0, kb0};
     const Gram32Shape sh = gram32_shape(ka, kb);
@@ -356,11 +386,11 @@ void gram32_sets(const float *A0, int64_t lda0, int ka0, const float *A1, int64_
 
 template <typename T>
 void gram(const T *A, int64_t lda, int ka, const T *B, int64_t ldb, int kb, int64_t N, double *G, double *partials,
-          cudaStream_t s) {
+          cudaStream_t s, bool allow_tc) {
     KF_REQUIRE(ka >= 1 && kb >= 1 && ka <= 128 && kb <= 128, KF_EINVAL, "gram: block widths out of range");
     if constexpr (sizeof(T) == 4) {
         gram32_sets((const float *)A, lda, ka, nullptr, 0, 0, (const float *)B, ldb, kb, nullptr, 0, 0, N, G, partials,
-                    s);
+                    s, allow_tc);
         return;
     }
     // FP64: output chunks of 4 x 8 accumulators per thread
@@ -737,6 +767,81 @@ void scale_add(double *Y, const double *X, const double *d, const float *P, floa
     KF_LAUNCH_CHECK();
 }
 
+// Second orthogonalisation pass without the host: from G = [X Z]'Z ((wx + r) x r, FP64, the
+// rows of X'Z first), S = Z'Z - (X'Z)'(X'Z) (the Gram of (I - XX')Z), its Cholesky factor
+// S = R'R (R upper), and the coefficients C = [R^-1 ; -(X'Z) R^-1] ((r + wx) x r) with which
+// [Z X] C = (I - XX') Z R^-1 is orthonormal.  One CTA; *status = 0, or 1 when a pivot is not
+// finite or below 1e-4 (C is then not to be used).  r <= 48 (2 r^2 doubles of shared memory).
+__global__ void k_chol2_coeffs(const double *__restrict__ G, int wx, int r, double *__restrict__ C,
+                               int *__restrict__ status) {
+    extern __shared__ double cs[];
+    double *S = cs;               // r x r, column-major; becomes R (upper)
+    double *Ri = cs + r * r;      // r x r, R^-1
+    __shared__ int bad;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int ld = wx + r;
+    if (tid == 0) bad = 0;
+    for (int e = tid; e < r * r; e += nt) {
+        const int i = e % r, j = e / r;
+        double v = G[wx + i + (size_t)ld * j];
+        for (int q = 0; q < wx; ++q) v -= G[q + (size_t)ld * i] * G[q + (size_t)ld * j];
+        S[e] = v;
+        Ri[e] = 0.0;
+    }
+    __syncthreads();
+    // right-looking Cholesky, upper factor: column k of R is row k of the trailing matrix
+    for (int k = 0; k < r; ++k) {
+        if (tid == 0) {
+            const double d = S[k + r * k];
+            // S is the Gram of a block the first pass already orthonormalised (S ~ I): a pivot
+            // below 1e-4 is a nearly dependent direction, left to the host's SVQB
+            if (!(d > 1e-4) || !isfinite(d)) bad = 1;
+            S[k + r * k] = sqrt(d > 0.0 ? d : 1.0);
+        }
+        __syncthreads();
+        const double rkk = S[k + r * k];
+        for (int j = k + 1 + tid; j < r; j += nt) S[k + r * j] /= rkk;
+        __syncthreads();
+        for (int e = tid; e < (r - k - 1) * (r - k - 1); e += nt) {
+            const int i = k + 1 + e % (r - k - 1), j = k + 1 + e / (r - k - 1);
+            if (i <= j) S[i + r * j] -= S[k + r * i] * S[k + r * j];
+        }
+        __syncthreads();
+    }
+    // R^-1 column by column (back substitution), one thread per column
+    for (int j = tid; j < r; j += nt) {
+        Ri[j + r * j] = 1.0 / S[j + r * j];
+        for (int i = j - 1; i >= 0; --i) {
+            double v = 0.0;
+            for (int k = i + 1; k <= j; ++k) v += S[i + r * k] * Ri[k + r * j];
+            Ri[i + r * j] = -v / S[i + r * i];
+        }
+    }
+    __syncthreads();
+    const int lc = r + wx;
+    for (int e = tid; e < lc * r; e += nt) {
+        const int i = e % lc, j = e / lc;
+        double v;
+        if (i < r) {
+            v = Ri[i + r * j];
+        } else {
+            const int q = i - r;
+            v = 0.0;
+            for (int t = 0; t <= j; ++t) v += G[q + (size_t)ld * t] * Ri[t + r * j];
+            v = -v;
+        }
+        C[i + (size_t)lc * j] = v;
+    }
+    if (tid == 0) *status = bad;
+}
+
+void chol2_coeffs(const double *G, int wx, int r, double *C, int *status, cudaStream_t s) {
+    KF_REQUIRE(r >= 1 && r <= CHOL2_MAX_R, KF_EINVAL, "chol2_coeffs: block width out of range");
+    const size_t smem = (size_t)2 * r * r * sizeof(double);
+    k_chol2_coeffs<<<1, 256, smem, s>>>(G, wx, r, C, status);
+    KF_LAUNCH_CHECK();
+}
+
 // theta_j = sum_i D_i X_ij^2 / sum_i X_ij^2 (ext/KronFreeCircuitsCUDAExt.jl:16-44): two
 // partial sums per column, weighted then plain.
 __global__ void k_diag_expect(const double *__restrict__ D, const double *__restrict__ X, int64_t ld, int64_t N,
@@ -893,7 +998,8 @@ void copy_block(const T *X, int64_t ldx, T *Y, int64_t ldy, int k, int64_t N, cu
 
 // explicit instantiations
 #define KF_INST(T)                                                                                                   \
-    template void gram<T>(const T *, int64_t, int, const T *, int64_t, int, int64_t, double *, double *, cudaStream_t); \
+    template void gram<T>(const T *, int64_t, int, const T *, int64_t, int, int64_t, double *, double *, cudaStream_t, \
+                          bool);                                                                                     \
     template void update2<T>(T *, int64_t, int, const T *, int64_t, int, const T *, int64_t, int, const double *, int,   \
                              double, double, int64_t, cudaStream_t, bool);                                          \
     template void update<T>(T *, int64_t, int, const T *, int64_t, int, const double *, int, double, double, int64_t, \

@@ -193,15 +193,35 @@ void launch_apply(kf_op *op, bool f32, const void *X, void *Y, int64_t ldx, int6
 
 // dense linear algebra on tall-skinny blocks (kf_blas.cu); T = float or double.
 // Column-major blocks with leading dimension ld.
+// G = A' B (ka x kb, column-major, FP64); FP32 blocks of N >= GRAM_TC_MIN_ROWS rows on the tensor
+// cores when the shapes fit and allow_tc, else on the SIMT pipes
+constexpr int64_t GRAM_TC_MIN_ROWS = 65536;
 template <typename T>
 void gram(const T *A, int64_t lda, int ka, const T *B, int64_t ldb, int kb, int64_t N, double *G_dev,
-          double *partials, cudaStream_t s);                 // G = A' B (ka x kb, column-major, FP64)
+          double *partials, cudaStream_t s, bool allow_tc = true);
 void perturb_block(double *X, int64_t N, int k, double delta, uint64_t key, double *R, double *nrm, double *partials,
                    cudaStream_t s);
 // refinement phase: FP64 iterate, FP32 residual / directions
 void residual_mixed(const double *X, const double *HX, int64_t ld, int k, int64_t N, const double *theta,
                     const double *thetap, const double *D, double eta, int mode, float *R, int64_t ldr, float *W,
                     int64_t ldw, double *norms2, double *partials, cudaStream_t s);
+// FP32 Gram on the tensor cores: the sources are stacked as the rows of one pool (each at a multiple
+// of 8 rows); G (nr x nc, column-major, ld nr) = [sources r0..r1-1]' [sources c0..c1-1], in FP64.
+// Returns false, launching nothing, when the shapes do not fit the kernel (pool over 144 rows, rows
+// of G past pool row 128, unaligned columns, too small a partial buffer).
+struct GramTcSrc {
+    const float *p;
+    int64_t ld;
+    int k;
+};
+// accs: accumulators per chunk (0: the default; capped by TMEM)
+bool gram_tc(const GramTcSrc *src, int nsrc, int r0, int r1, int c0, int c1, int64_t N, double *G, void *partials,
+             size_t partial_bytes, cudaStream_t s, int accs = 0);
+size_t gram_tc_partials_size(int nr, int nc);
+// second orthogonalisation pass on the device: from G = [X Z]'Z, coefficients C ((r + wx) x r)
+// with [Z X] C orthonormal and orthogonal to X (Cholesky of Z'Z - (X'Z)'(X'Z)); *status 1 on failure
+constexpr int CHOL2_MAX_R = 48;
+void chol2_coeffs(const double *G, int wx, int r, double *C, int *status, cudaStream_t s);
 // Y[:, j] = d_j X[:, j] + (double) P[:, j] and Y32 = FP32(Y) (leading dimension N)
 void scale_add(double *Y, const double *X, const double *d, const float *P, float *Y32, int k, int64_t N,
                cudaStream_t s);
@@ -210,7 +230,7 @@ void add_f32_into_f64(double *Y, int64_t ldy, const float *P, int64_t ldp, float
 // G = [A0 A1]' [B0 B1] for FP32 column blocks (a block with 0 columns is skipped)
 void gram32_sets(const float *A0, int64_t lda0, int ka0, const float *A1, int64_t lda1, int ka1, const float *B0,
                  int64_t ldb0, int kb0, const float *B1, int64_t ldb1, int kb1, int64_t N, double *G, double *partials,
-                 cudaStream_t s);
+                 cudaStream_t s, bool allow_tc = true);
 // Y = alpha [X0 X1] C + beta Y
 template <typename T>
 void update2(T *Y, int64_t ldy, int ky, const T *X0, int64_t ldx0, int kx0, const T *X1, int64_t ldx1, int kx1,

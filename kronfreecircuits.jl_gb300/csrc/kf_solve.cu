@@ -202,6 +202,7 @@ struct LobParams {
 struct LobOut {
     int iters = 0;
     int fast_updates = 0;   // refinement: updates that took the FP64-diagonal + FP32-mixing form
+    int ortho_fallbacks = 0;  // FP32 iterations whose device second orthogonalisation pass gave way to the host
     int64_t nmv = 0;
     int nlocked = 0;
     bool converged = false;
@@ -213,8 +214,8 @@ template <typename T>
 struct LobWork {
     int64_t N;
     int w;
-    DevMem X, HX, Xn, HXn, Z, HZ, Zt, Pn, F1, F2, dG, dC, dpart, dth, dthp, dnorm, dD;
-    HostMem hG, hC, hv;
+    DevMem X, HX, Xn, HXn, Z, HZ, Zt, Pn, F1, F2, dG, dC, dpart, dth, dthp, dnorm, dD, dstat;
+    HostMem hG, hC, hv, hstat;
     LobWork(int64_t N_, int w_)
         : N(N_), w(w_),
           X((size_t)N_ * w_ * sizeof(T)), HX((size_t)N_ * w_ * sizeof(T)), Xn((size_t)N_ * w_ * sizeof(T)),
@@ -223,9 +224,9 @@ struct LobWork {
           F1((size_t)N_ * w_ * sizeof(float)), F2((size_t)N_ * w_ * sizeof(float)),
           dG((size_t)9 * w_ * w_ * sizeof(double)), dC((size_t)9 * w_ * w_ * sizeof(double)),
           dpart(gram_partials_size(3 * w_, 3 * w_, N_)), dth(w_ * sizeof(double)), dthp(w_ * sizeof(double)),
-          dnorm(2 * w_ * sizeof(double)), dD(0),
+          dnorm(2 * w_ * sizeof(double)), dD(0), dstat(16),
           hG((size_t)9 * w_ * w_ * sizeof(double)), hC((size_t)9 * w_ * w_ * sizeof(double)),
-          hv((size_t)4 * w_ * sizeof(double)) {}
+          hv((size_t)4 * w_ * sizeof(double)), hstat(16) {}
 };
 
 template <typename T>
@@ -252,7 +253,7 @@ static void h2d(double *d, const double *h, size_t n, cudaStream_t s) {
 // FP64 blocks project with one classical Gram-Schmidt step and then run SVQB, per pass.
 template <typename T>
 static int ortho_against(kf_op *op, LobWork<T> &W, T *Zb, int k, const T *X, int wx, T *tmp, T *&result,
-                         double cutoff, cudaStream_t s) {
+                         double cutoff, cudaStream_t s, int npass = 2) {
     const int64_t N = W.N;
     double *G = W.dG.template as<double>();
     double *part = W.dpart.template as<double>();
@@ -261,7 +262,7 @@ static int ortho_against(kf_op *op, LobWork<T> &W, T *Zb, int k, const T *X, int
     double *C = W.dC.template as<double>();
     T *cur = Zb, *other = tmp;
     int r = k;
-    for (int pass = 0; pass < 2; ++pass) {
+    for (int pass = 0; pass < npass; ++pass) {
         if constexpr (sizeof(T) == 4) {
             if (wx > 0) {
                 // [X Z]' Z: rows 0..wx-1 = G = X'Z, rows wx.. = S = Z'Z ((wx + r) x r, column-major)
@@ -317,12 +318,96 @@ static int ortho_against(kf_op *op, LobWork<T> &W, T *Zb, int k, const T *X, int
     return r;
 }
 
+// ---- FP32 search directions with two host waits per iteration instead of four --------------
+//
+// merged_gram_sync: for Z = [W P] (nz = na + np columns; W for every active column, P for every
+// previous one), one Gram [X Z]'Z and, in the same host wait, the active residual norms.
+// merged_finish: after the caller's lock decision (`newly` leading active columns lock), the
+// directions of the newly locked columns get zero coefficients; SVQB of the projected Gram
+// Z'Z - G'G over the kept columns (host), one update to Z1 = (I - XX') Z T; then the second pass on
+// the device -- Gram [X Z1]'Z1, Cholesky coefficients (k_chol2_coeffs), one update -- so no host
+// wait.  Its failure flag travels with the Rayleigh-Ritz blocks; the caller falls back to the host
+// pass from Z1 (left in Zt) when it is set.
+// the separable preconditioner on n FP32 columns in place (column j shifted by dth[j])
+static void precondition_f32(kf_op *op, LobWork<float> &W, const LobParams &prm, float *Wb, int n, const double *dth,
+                             cudaStream_t s) {
+    if (prm.precond != KF_PRECOND_SEPARABLE || n <= 0) return;
+    const double eta_s = std::max(prm.eta, 1e-3 * std::fabs(op->gershgorin));
+    float *outp = sep_apply(op, Wb, W.F1.as<float>(), n, dth, eta_s, s);
+    if (outp != Wb) copy_block<float>(outp, W.N, Wb, W.N, n, W.N, s);
+}
+
+static void merged_gram_sync(LobWork<float> &W, const float *X, int wx, const float *Zb, int nz, const double *dnorm,
+                             int na, double *hnorm, cudaStream_t s) {
+    const int64_t N = W.N;
+    double *G = W.dG.as<double>();
+    gram32_sets(X, N, wx, Zb, N, nz, Zb, N, nz, nullptr, 0, 0, N, G, W.dpart.as<double>(), s);
+    if (na > 0) KF_CUDA(cudaMemcpyAsync(hnorm, dnorm, sizeof(double) * na, cudaMemcpyDeviceToHost, s));
+    d2h_sync<float>(W.hG.as<double>(), G, (size_t)(wx + nz) * nz, s);
+}
+
+// returns k (columns of Q, in W.Z) or 0 when the directions vanished
+static int merged_finish(kf_op *op, LobWork<float> &W, const float *X, int wx, float *Zb, int na, int np, int newly,
+                         double cutoff, cudaStream_t s) {
+    const int64_t N = W.N;
+    const int nz = na + np, ld = wx + nz;
+    const double *hG = W.hG.as<double>();
+    std::vector<int> keep;
+    for (int c = newly; c < na; ++c) keep.push_back(c);
+    for (int c = na + newly; c < nz; ++c) keep.push_back(c);
+    const int r0 = (int)keep.size();
+    if (r0 == 0) return 0;
+    std::vector<double> Sp((size_t)r0 * r0);
+    for (int jj = 0; jj < r0; ++jj)
+        for (int ii = 0; ii < r0; ++ii) {
+            const int i = keep[ii], j = keep[jj];
+            double v = hG[wx + i + (size_t)ld * j];
+            for (int q = 0; q < wx; ++q) v -= hG[q + (size_t)ld * i] * hG[q + (size_t)ld * j];
+            Sp[ii + (size_t)r0 * jj] = v;
+        }
+    std::vector<double> Tc;
+    const int r1 = svqb_coeffs(r0, Sp.data(), cutoff, Tc);
+    if (r1 == 0) return 0;
+    // coefficients of [Z X]: T (rows of the kept columns, zero elsewhere), then -G T
+    const int lc = nz + wx;
+    double *hC = W.hC.as<double>();
+    std::fill(hC, hC + (size_t)lc * r1, 0.0);
+    for (int j = 0; j < r1; ++j) {
+        for (int ii = 0; ii < r0; ++ii) hC[keep[ii] + (size_t)lc * j] = Tc[ii + (size_t)r0 * j];
+        for (int q = 0; q < wx; ++q) {
+            double v = 0;
+            for (int ii = 0; ii < r0; ++ii) v += hG[q + (size_t)ld * keep[ii]] * Tc[ii + (size_t)r0 * j];
+            hC[nz + q + (size_t)lc * j] = -v;
+        }
+    }
+    double *C = W.dC.as<double>();
+    h2d(C, hC, (size_t)lc * r1, s);
+    float *Z1 = W.Zt.as<float>();
+    update2<float>(Z1, N, r1, Zb, N, nz, X, N, wx, C, lc, 1.0, 0.0, N, s);
+    if (r1 > CHOL2_MAX_R) {
+        // wider than the device Cholesky takes: the second pass on the host, result in W.Z
+        float *Q = nullptr;
+        const int r2 = ortho_against<float>(op, W, Z1, r1, X, wx, Zb, Q, cutoff, s, 1);
+        KF_CUDA(cudaMemsetAsync(W.dstat.as<int>(), 0, sizeof(int), s));
+        return r2;
+    }
+    // second pass on the device
+    double *G = W.dG.as<double>();
+    gram32_sets(X, N, wx, Z1, N, r1, Z1, N, r1, nullptr, 0, 0, N, G, W.dpart.as<double>(), s);
+    chol2_coeffs(G, wx, r1, C, W.dstat.as<int>(), s);
+    update2<float>(W.Z.as<float>(), N, r1, Z1, N, r1, X, N, wx, C, r1 + wx, 1.0, 0.0, N, s);
+    return r1;
+}
+
 template <typename T>
 static LobOut lobpcg_run(kf_op *op, LobWork<T> &Wk, const double *D, const LobParams &prm, cudaStream_t s,
                          std::vector<double> &theta) {
     const int64_t N = Wk.N;
     const int w = Wk.w;
     const bool f32 = sizeof(T) == 4;
+    // FP32 blocks: norms and the first Gram of [W P] share one wait, the second orthogonalisation
+    // pass runs on the device (merged_gram_sync / merged_finish); FP64 keeps the plain sequence
+    constexpr bool merged = sizeof(T) == 4;
     LobOut out;
     T *X = Wk.X.template as<T>(), *HX = Wk.HX.template as<T>();
     T *Xn = Wk.Xn.template as<T>(), *HXn = Wk.HXn.template as<T>();
@@ -378,7 +463,14 @@ static LobOut lobpcg_run(kf_op *op, LobWork<T> &Wk, const double *D, const LobPa
         const int mode = prm.precond == KF_PRECOND_RITZ ? 0 : prm.precond == KF_PRECOND_JACOBI ? 1 : 2;  // separable: 2, then below
         residual_precond<T>(X + (int64_t)nl * N, HX + (int64_t)nl * N, N, na, N, dth, dthp, D, prm.eta, mode, Z, N,
                             dnorm, part, s);
-        d2h_sync<T>(hv + w, dnorm, na, s);
+        if constexpr (merged) {
+            // W for every active column (those that lock now get zero weight later), P after it
+            precondition_f32(op, Wk, prm, (float *)Z, na, dth, s);
+            if (np > 0) copy_block<float>((const float *)Pn, N, (float *)Z + (int64_t)na * N, N, np, N, s);
+            merged_gram_sync(Wk, (const float *)X, w, (const float *)Z, na + np, dnorm, na, hv + w, s);
+        } else {
+            d2h_sync<T>(hv + w, dnorm, na, s);
+        }
         for (int j = 0; j < na; ++j) res[nl + j] = std::sqrt(hv[w + j]);
         int newly = 0;
         while (nl + newly < w && res[nl + newly] <= prm.lock_tol) ++newly;
@@ -393,8 +485,11 @@ static LobOut lobpcg_run(kf_op *op, LobWork<T> &Wk, const double *D, const LobPa
             out.converged = true;
             break;
         }
+        // the checked columns (m + guards); buffer columns beyond them do not enter the judge,
+        // the stall test or the convergence count
+        const int ncc = prm.n_conv_check;
         double worst = 0, bestr = INFINITY;
-        for (int j = nl; j < w; ++j) {
+        for (int j = nl; j < ncc; ++j) {
             worst = std::max(worst, res[j]);
             bestr = std::min(bestr, res[j]);
         }
@@ -411,8 +506,8 @@ static LobOut lobpcg_run(kf_op *op, LobWork<T> &Wk, const double *D, const LobPa
             // geometric mean of the active residuals has not halved (single columns stall for
             // stretches while the block as a whole still converges)
             double lg = 0;
-            for (int j = nl; j < w; ++j) lg += std::log(std::max(res[j], 1e-300));
-            lg /= std::max(w - nl, 1);
+            for (int j = nl; j < ncc; ++j) lg += std::log(std::max(res[j], 1e-300));
+            lg /= std::max(ncc - nl, 1);
             if (newly > 0 || lg < best - std::log(2.0)) {
                 best = std::min(best, lg);
                 since_best = 0;
@@ -421,50 +516,67 @@ static LobOut lobpcg_run(kf_op *op, LobWork<T> &Wk, const double *D, const LobPa
             }
         }
         if (it >= prm.maxiter) break;
-        // W = Z[:, newly : na] (na2 columns), P = previous Pn[:, newly : na] placed right after it
-        const int na2 = na - newly;
-        T *Wb = Z + (int64_t)newly * N;
-        if (prm.precond == KF_PRECOND_SEPARABLE && na2 > 0) {
-            // the separable preconditioner always runs in FP32: it only steers the search
-            // directions, the FP64 orthogonalisation and Rayleigh-Ritz keep the accuracy
-            const double eta_s = std::max(prm.eta, 1e-3 * std::fabs(op->gershgorin));
-            float *f1 = Wk.F1.template as<float>(), *f2 = Wk.F2.template as<float>();
-            float *in = f2;
-            if constexpr (sizeof(T) == 4) in = (float *)Wb;
-            else convert<double, float>((const double *)Wb, N, f2, N, na2, N, s);
-            float *outp = sep_apply(op, in, f1, na2, dth + newly, eta_s, s);
-            if constexpr (sizeof(T) == 4) {
-                if (outp != (float *)Wb) copy_block<float>(outp, N, (float *)Wb, N, na2, N, s);
-            } else {
+        T *Qc = nullptr;
+        int k = 0, r1 = 0;
+        if constexpr (merged) {
+            k = r1 = merged_finish(op, Wk, (const float *)X, w, (float *)Z, na, np, newly, prm.cutoff, s);
+            Qc = Z;
+            nl += newly;
+        } else {
+            // W = Z[:, newly : na] (na2 columns), P = previous Pn[:, newly : na] placed right after it
+            const int na2 = na - newly;
+            T *Wb = Z + (int64_t)newly * N;
+            if (prm.precond == KF_PRECOND_SEPARABLE && na2 > 0) {
+                // the separable preconditioner always runs in FP32: it only steers the search
+                // directions, the FP64 orthogonalisation and Rayleigh-Ritz keep the accuracy
+                const double eta_s = std::max(prm.eta, 1e-3 * std::fabs(op->gershgorin));
+                float *f1 = Wk.F1.template as<float>(), *f2 = Wk.F2.template as<float>();
+                convert<double, float>((const double *)Wb, N, f2, N, na2, N, s);
+                float *outp = sep_apply(op, f2, f1, na2, dth + newly, eta_s, s);
                 convert<float, double>(outp, N, (double *)Wb, N, na2, N, s);
             }
-        }
-        int nz = na2;
-        if (np > 0) {
-            const int np2 = np - newly;
-            if (np2 > 0) {
-                copy_block<T>(Pn + (int64_t)newly * N, N, Wb + (int64_t)na2 * N, N, np2, N, s);
-                nz += np2;
+            int nz = na2;
+            if (np > 0) {
+                const int np2 = np - newly;
+                if (np2 > 0) {
+                    copy_block<T>(Pn + (int64_t)newly * N, N, Wb + (int64_t)na2 * N, N, np2, N, s);
+                    nz += np2;
+                }
             }
+            nl += newly;
+            // orthonormalise [W P] against X and itself (result in Z or Zt)
+            k = ortho_against<T>(op, Wk, Wb, nz, X, w, Zt, Qc, prm.cutoff, s);   // Qc in Zt, or in Z
         }
-        nl += newly;
-        // orthonormalise [W P] against X and itself (result in Z or Zt)
-        T *Q = nullptr;
-        const int k = ortho_against<T>(op, Wk, Wb, nz, X, w, Zt, Q, prm.cutoff, s);
         if (k == 0) throw Error(KF_EBREAKDOWN, "LOBPCG: the search directions vanished");
-        T *Qc = Q;   // in Zt, or in Z at the offset of Wb
-        launch_apply(op, f32, Qc, HZ, N, N, k, 1, 0, nullptr, 0, 0, s);
-        out.nmv += k;
         // Rayleigh-Ritz on S = [X_act, Q]: A = S' H S assembled from three Gram blocks
         const int na3 = w - nl;
-        const int ns = na3 + k;
         T *Xa = X + (int64_t)nl * N, *HXa = HX + (int64_t)nl * N;
+        auto apply_rr = [&]() {
+            launch_apply(op, f32, Qc, HZ, N, N, k, 1, 0, nullptr, 0, 0, s);
+            out.nmv += k;
+            double *G2 = G + (size_t)na3 * na3, *G3 = G2 + (size_t)na3 * k;
+            gram<T>(Xa, N, na3, HXa, N, na3, N, G, part, s);
+            gram<T>(Xa, N, na3, HZ, N, k, N, G2, part, s);
+            gram<T>(Qc, N, k, HZ, N, k, N, G3, part, s);
+            if (merged)
+                KF_CUDA(cudaMemcpyAsync(Wk.hstat.template as<int>(), Wk.dstat.template as<int>(), sizeof(int),
+                                        cudaMemcpyDeviceToHost, s));
+            d2h_sync<T>(hG, G, (size_t)na3 * na3 + (size_t)na3 * k + (size_t)k * k, s);
+        };
+        apply_rr();
+        if constexpr (merged) {
+            if (*Wk.hstat.template as<int>() != 0) {
+                // the device Cholesky met a nearly dependent direction: the host SVQB pass from Z1
+                ++out.ortho_fallbacks;
+                T *Q2 = nullptr;
+                k = ortho_against<T>(op, Wk, Zt, r1, X, w, Z, Q2, prm.cutoff, s, 1);
+                if (k == 0) throw Error(KF_EBREAKDOWN, "LOBPCG: the search directions vanished");
+                Qc = Q2;
+                apply_rr();
+            }
+        }
+        const int ns = na3 + k;
         std::vector<double> A((size_t)ns * ns);
-        double *G1 = G, *G2 = G + (size_t)na3 * na3, *G3 = G2 + (size_t)na3 * k;
-        gram<T>(Xa, N, na3, HXa, N, na3, N, G1, part, s);
-        gram<T>(Xa, N, na3, HZ, N, k, N, G2, part, s);
-        gram<T>(Qc, N, k, HZ, N, k, N, G3, part, s);
-        d2h_sync<T>(hG, G, (size_t)na3 * na3 + (size_t)na3 * k + (size_t)k * k, s);
         const double *h1 = hG, *h2 = hG + (size_t)na3 * na3, *h3 = h2 + (size_t)na3 * k;
         for (int j = 0; j < na3; ++j)
             for (int i = 0; i < na3; ++i) A[i + (size_t)ns * j] = h1[i + (size_t)na3 * j];
@@ -483,10 +595,8 @@ static LobOut lobpcg_run(kf_op *op, LobWork<T> &Wk, const double *D, const LobPa
         h2d(C, hC, (size_t)ns * na3, s);
         // X_act <- Xa Cx + Q Cz ; HX likewise ; P <- Q Cz
         T *Xna = Xn + (int64_t)nl * N, *HXna = HXn + (int64_t)nl * N;
-        update<T>(Xna, N, na3, Xa, N, na3, C, ns, 1.0, 0.0, N, s);
-        update<T>(Xna, N, na3, Qc, N, k, C + na3, ns, 1.0, 1.0, N, s);
-        update<T>(HXna, N, na3, HXa, N, na3, C, ns, 1.0, 0.0, N, s);
-        update<T>(HXna, N, na3, HZ, N, k, C + na3, ns, 1.0, 1.0, N, s);
+        update2<T>(Xna, N, na3, Xa, N, na3, Qc, N, k, C, ns, 1.0, 0.0, N, s);
+        update2<T>(HXna, N, na3, HXa, N, na3, HZ, N, k, C, ns, 1.0, 0.0, N, s);
         update<T>(Pn, N, na3, Qc, N, k, C + na3, ns, 1.0, 0.0, N, s);
         np = na3;
         std::swap(X, Xn);
@@ -496,9 +606,11 @@ static LobOut lobpcg_run(kf_op *op, LobWork<T> &Wk, const double *D, const LobPa
     }
     (void)na_prev;
     if (trace_on())
-        std::fprintf(stderr, "kf lobpcg %s: %d iterations, %.4f s; blocked on the stream %.4f s (%d syncs), host eig %.4f s\n",
+        std::fprintf(stderr,
+                     "kf lobpcg %s: %d iterations, %.4f s; blocked on the stream %.4f s (%d syncs), host eig %.4f s, "
+                     "%d host second passes\n",
                      f32 ? "f32" : "f64", out.iters, now_s() - tw0, g_tt.sync - tt0.sync, g_tt.nsync - tt0.nsync,
-                     g_tt.eig - tt0.eig);
+                     g_tt.eig - tt0.eig, out.ortho_fallbacks);
     // make sure the final block sits in Wk.X / Wk.HX
     if (X != Wk.X.template as<T>()) {
         copy_block<T>(X, N, Wk.X.template as<T>(), N, w, N, s);
@@ -613,7 +725,10 @@ static LobOut lobpcg_refine(kf_op *op, RefineWork &Rw, LobWork<float> &Wk, const
         const int mode = prm.precond == KF_PRECOND_RITZ ? 0 : prm.precond == KF_PRECOND_JACOBI ? 1 : 2;
         residual_mixed(X + (int64_t)nl * N, HX + (int64_t)nl * N, N, na, N, dth, dthp, D, prm.eta, mode, R32, N, Z, N,
                        dnorm, part, s);
-        d2h_sync<double>(hv + w, dnorm, na, s);
+        // W for every active column, P after it: one wait for the norms and the first Gram
+        precondition_f32(op, Wk, prm, Z, na, dth, s);
+        if (np > 0) copy_block<float>(Pn, N, Z + (int64_t)na * N, N, np, N, s);
+        merged_gram_sync(Wk, X32, w, Z, na + np, dnorm, na, hv + w, s);
         for (int j = 0; j < na; ++j) res[nl + j] = std::sqrt(hv[w + j]);
         int newly = 0;
         while (nl + newly < w && res[nl + newly] <= prm.lock_tol) ++newly;
@@ -627,8 +742,11 @@ static LobOut lobpcg_refine(kf_op *op, RefineWork &Rw, LobWork<float> &Wk, const
             out.converged = true;
             break;
         }
+        // the checked columns (m + guards); buffer columns beyond them do not enter the judge,
+        // the stall test or the convergence count
+        const int ncc = prm.n_conv_check;
         double worst = 0, bestr = INFINITY;
-        for (int j = nl; j < w; ++j) {
+        for (int j = nl; j < ncc; ++j) {
             worst = std::max(worst, res[j]);
             bestr = std::min(bestr, res[j]);
         }
@@ -637,39 +755,35 @@ static LobOut lobpcg_refine(kf_op *op, RefineWork &Rw, LobWork<float> &Wk, const
                          bestr, worst);
         if (!std::isfinite(worst)) throw Error(KF_ENOTFINITE, "LOBPCG: the residual block is not finite");
         if (it >= prm.maxiter) break;
-        const int na2 = na - newly;
-        float *Wb = Z + (int64_t)newly * N;
-        if (prm.precond == KF_PRECOND_SEPARABLE && na2 > 0) {
-            const double eta_s = std::max(prm.eta, 1e-3 * std::fabs(op->gershgorin));
-            float *f1 = Wk.F1.as<float>();
-            float *outp = sep_apply(op, Wb, f1, na2, dth + newly, eta_s, s);
-            if (outp != Wb) copy_block<float>(outp, N, Wb, N, na2, N, s);
-        }
-        int nz = na2;
-        if (np > 0) {
-            const int np2 = np - newly;
-            if (np2 > 0) {
-                copy_block<float>(Pn + (int64_t)newly * N, N, Wb + (int64_t)na2 * N, N, np2, N, s);
-                nz += np2;
-            }
-        }
         nl += newly;
-        float *Q = nullptr;
         // the FP32 blocks' Gram eigenvalues below 1e-6 of the largest are rounding noise
-        const int k = ortho_against<float>(op, Wk, Wb, nz, X32, w, Zt, Q, 1e-6, s);
+        int k = merged_finish(op, Wk, X32, w, Z, na, np, newly, 1e-6, s);
+        const int r1 = k;
         if (k == 0) throw Error(KF_EBREAKDOWN, "LOBPCG: the search directions vanished");
-        launch_apply(op, true, Q, HZ, N, N, k, 1, 0, nullptr, 0, 0, s);
-        out.nmv += k;
+        float *Q = Z;
         // Rayleigh-Ritz on [X_a, Q]: X_a' R, R' Q and Q' H Q, one transfer
         const int na3 = w - nl;
-        const int ns = na3 + k;
         const float *Ra = R32 + (int64_t)newly * N;
         const float *Xa32 = X32 + (int64_t)nl * N;
-        double *G1 = G, *G2 = G + (size_t)na3 * na3, *G3 = G2 + (size_t)na3 * k;
-        gram<float>(Xa32, N, na3, Ra, N, na3, N, G1, part, s);
-        gram<float>(Ra, N, na3, Q, N, k, N, G2, part, s);
-        gram<float>(Q, N, k, HZ, N, k, N, G3, part, s);
-        d2h_sync<double>(hG, G, (size_t)na3 * na3 + (size_t)na3 * k + (size_t)k * k, s);
+        auto apply_rr = [&]() {
+            launch_apply(op, true, Q, HZ, N, N, k, 1, 0, nullptr, 0, 0, s);
+            out.nmv += k;
+            double *G2 = G + (size_t)na3 * na3, *G3 = G2 + (size_t)na3 * k;
+            gram<float>(Xa32, N, na3, Ra, N, na3, N, G, part, s);
+            gram<float>(Ra, N, na3, Q, N, k, N, G2, part, s);
+            gram<float>(Q, N, k, HZ, N, k, N, G3, part, s);
+            KF_CUDA(cudaMemcpyAsync(Wk.hstat.as<int>(), Wk.dstat.as<int>(), sizeof(int), cudaMemcpyDeviceToHost, s));
+            d2h_sync<double>(hG, G, (size_t)na3 * na3 + (size_t)na3 * k + (size_t)k * k, s);
+        };
+        apply_rr();
+        if (*Wk.hstat.as<int>() != 0) {
+            // the device Cholesky met a nearly dependent direction: the host SVQB pass from Z1
+            ++out.ortho_fallbacks;
+            k = ortho_against<float>(op, Wk, Zt, r1, X32, w, Z, Q, 1e-6, s, 1);
+            if (k == 0) throw Error(KF_EBREAKDOWN, "LOBPCG: the search directions vanished");
+            apply_rr();
+        }
+        const int ns = na3 + k;
         const double *h1 = hG, *h2 = hG + (size_t)na3 * na3, *h3 = h2 + (size_t)na3 * k;
         std::vector<double> A((size_t)ns * ns);
         for (int j = 0; j < na3; ++j)
@@ -738,9 +852,9 @@ static LobOut lobpcg_refine(kf_op *op, RefineWork &Rw, LobWork<float> &Wk, const
     if (trace_on())
         std::fprintf(stderr,
                      "kf lobpcg refine: %d iterations (%d FP32-mixing updates), %.4f s; blocked on the stream %.4f s "
-                     "(%d syncs), host eig %.4f s\n",
+                     "(%d syncs), host eig %.4f s, %d host second passes\n",
                      out.iters, out.fast_updates, now_s() - tw0, g_tt.sync - tt0.sync, g_tt.nsync - tt0.nsync,
-                     g_tt.eig - tt0.eig);
+                     g_tt.eig - tt0.eig, out.ortho_fallbacks);
     if (X != Rw.X.as<double>()) {
         copy_block<double>(X, N, Rw.X.as<double>(), N, w, N, s);
         copy_block<double>(HX, N, Rw.HX.as<double>(), N, w, N, s);
@@ -802,6 +916,7 @@ static void solve_lobpcg(kf_op *op, const kf_solver_opts &o, int m, const double
                "LOBPCG: preconditioner must be :ritz, :jacobi, :none or :separable");
     KF_REQUIRE(o.precision == KF_PREC_F64 || o.precision == KF_PREC_MIXED, KF_EINVAL, "LOBPCG: unknown precision mode");
     KF_REQUIRE(o.guard >= 0, KF_EINVAL, "LOBPCG: guard must be nonnegative");
+    KF_REQUIRE(o.buffer >= KF_BUFFER_AUTO, KF_EINVAL, "LOBPCG: buffer must be nonnegative (or KF_BUFFER_AUTO)");
     if (X0) {
         for (int j = 0; j < m; ++j) {
             bool nz = false;
@@ -815,11 +930,16 @@ static void solve_lobpcg(kf_op *op, const kf_solver_opts &o, int m, const double
     }
     const int g = (int)std::min<int64_t>(o.guard, (N - 5) / 3 - m);
     const int w = m + g;
+    // buffer columns: carried in the block (the iteration runs on wi columns) but never checked,
+    // locked for the count or returned; the same N >= 3 wi + 5 bound as the guards
+    const int b_req = o.buffer == KF_BUFFER_AUTO ? (o.precision == KF_PREC_MIXED ? 2 : 0) : o.buffer;
+    const int b = (int)std::max<int64_t>(0, std::min<int64_t>(b_req, (N - 5) / 3 - w));
+    const int wi = w + b;
     const double hn = op->gershgorin;
     st.hnorm = hn;
     DevMem dD((size_t)N * sizeof(double));
     KF_CUDA(cudaMemcpyAsync(dD.p, op->h_fulldiag.data(), N * sizeof(double), cudaMemcpyHostToDevice, s));
-    LobWork<double> W64(N, w);
+    LobWork<double> W64(N, wi);
     // the initial block, built on the device (src/lobpcg.jl:179-190): the warm start's / the
     // product seed's columns with the sqrt(eps) perturbation, random normal columns otherwise
     const double delta = std::sqrt(std::numeric_limits<double>::epsilon());
@@ -828,13 +948,14 @@ static void solve_lobpcg(kf_op *op, const kf_solver_opts &o, int m, const double
         double *R = W64.Z.as<double>();   // scratch, 2 N w
         double *nrm = W64.dnorm.as<double>();
         double *part = W64.dpart.as<double>();
-        bool guards_random = true;
+        bool guards_random = true, buffer_random = true;
         if (use_inputs && X0) {
-            if (!seed && o.seed_kind == KF_SEED_PRODUCT && g > 0) {
-                // the guards of a warm start are the product seed's columns m+1:w (src/lobpcg.jl:182-190)
-                product_seed_device(op, w, Xd, s);
-                perturb_block(Xd + (size_t)N * m, N, g, delta, 0x4b47, R, nrm, part, s);
-                guards_random = false;
+            if (!seed && o.seed_kind == KF_SEED_PRODUCT && g + b > 0) {
+                // the guards of a warm start are the product seed's columns m+1:w (src/lobpcg.jl:182-190),
+                // the buffer columns its next ones
+                product_seed_device(op, wi, Xd, s);
+                perturb_block(Xd + (size_t)N * m, N, g + b, delta, 0x4b47, R, nrm, part, s);
+                guards_random = buffer_random = false;
             }
             KF_CUDA(cudaMemcpyAsync(Xd, X0, sizeof(double) * (size_t)N * m, cudaMemcpyHostToDevice, s));
             perturb_block(Xd, N, m, delta, 0x4b46, R, nrm, part, s);
@@ -843,19 +964,21 @@ static void solve_lobpcg(kf_op *op, const kf_solver_opts &o, int m, const double
                                         cudaMemcpyHostToDevice, s));
                 perturb_block(Xd + (size_t)N * m, N, g, delta, 0x4b47, R, nrm, part, s);
                 guards_random = false;
+                buffer_random = true;
             }
         } else if (use_inputs && seed) {
             KF_CUDA(cudaMemcpyAsync(Xd, seed, sizeof(double) * (size_t)N * w, cudaMemcpyHostToDevice, s));
             perturb_block(Xd, N, w, delta, 0x4b46, R, nrm, part, s);
             guards_random = false;
         } else if (use_inputs && o.seed_kind == KF_SEED_PRODUCT) {
-            product_seed_device(op, w, Xd, s);
-            perturb_block(Xd, N, w, delta, 0x4b46, R, nrm, part, s);
-            guards_random = false;
+            product_seed_device(op, wi, Xd, s);
+            perturb_block(Xd, N, wi, delta, 0x4b46, R, nrm, part, s);
+            guards_random = buffer_random = false;
         } else {
             fill_normal<double>(Xd, N, m, N, rkey, 1, s);
         }
         if (guards_random) fill_normal<double>(Xd + (size_t)N * m, N, g, N, rkey, 2, s);
+        if (buffer_random && b > 0) fill_normal<double>(Xd + (size_t)N * w, N, b, N, rkey, 3, s);
     };
     if (X0) st.warm = 1;
     LobParams p64{o.tol, o.maxiter, o.preconditioner, o.eta, w, 1e-12, false, o.fallback_iters,
@@ -869,8 +992,8 @@ static void solve_lobpcg(kf_op *op, const kf_solver_opts &o, int m, const double
         int iters32 = 0;
         int64_t nmv32 = 0;
         if (o.precision == KF_PREC_MIXED) {
-            LobWork<float> W32(N, w);
-            convert<double, float>(W64.X.as<double>(), N, W32.X.as<float>(), N, w, N, s);
+            LobWork<float> W32(N, wi);
+            convert<double, float>(W64.X.as<double>(), N, W32.X.as<float>(), N, wi, N, s);
             LobParams p32 = q;
             p32.lock_tol = std::max(o.tol, o.mixed_switch * hn);
             p32.cutoff = 1e-6;
@@ -884,11 +1007,11 @@ static void solve_lobpcg(kf_op *op, const kf_solver_opts &o, int m, const double
             }
             q.judge_resid = 0;
             // FP64 refinement with FP32 search directions
-            RefineWork RW(N, w);
-            convert<float, double>(W32.X.as<float>(), N, RW.X.as<double>(), N, w, N, s);
+            RefineWork RW(N, wi);
+            convert<float, double>(W32.X.as<float>(), N, RW.X.as<double>(), N, wi, N, s);
             const double tf = now_s();
             r = lobpcg_refine(op, RW, W32, dD.as<double>(), q, s, theta);
-            KF_CUDA(cudaMemcpyAsync(W64.X.p, RW.X.p, sizeof(double) * (size_t)N * w, cudaMemcpyDeviceToDevice, s));
+            KF_CUDA(cudaMemcpyAsync(W64.X.p, RW.X.p, sizeof(double) * (size_t)N * wi, cudaMemcpyDeviceToDevice, s));
             st.seconds_f64 = now_s() - tf;
             st.iterations_f64 = r.iters;
             r.iters += iters32;

@@ -35,7 +35,7 @@ mutable struct KfSolverOpts
     kind::Int32; precision::Int32; tol::Float64; maxiter::Int32; preconditioner::Int32; eta::Float64
     guard::Int32; degree::Int32; extra::Int32; rescale_every::Int32; ortho::Int32; bound::Float64
     krylovdim::Int32; rng_seed::UInt64; mixed_switch::Float64; fallback_iters::Int32; fallback_resid::Float64
-    seed_kind::Int32
+    seed_kind::Int32; buffer::Int32
     KfSolverOpts() = new()
 end
 mutable struct KfSolveStats

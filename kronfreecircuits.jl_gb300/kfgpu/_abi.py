@@ -39,6 +39,7 @@ class KfOpDesc(C.Structure):
 
 
 KF_SEED_PRODUCT, KF_SEED_RANDOM = 0, 1
+KF_BUFFER_AUTO = -1
 
 
 class KfSolverOpts(C.Structure):
@@ -46,7 +47,8 @@ class KfSolverOpts(C.Structure):
                 ("preconditioner", C.c_int32), ("eta", C.c_double), ("guard", C.c_int32), ("degree", C.c_int32),
                 ("extra", C.c_int32), ("rescale_every", C.c_int32), ("ortho", C.c_int32), ("bound", C.c_double),
                 ("krylovdim", C.c_int32), ("rng_seed", C.c_uint64), ("mixed_switch", C.c_double),
-                ("fallback_iters", C.c_int32), ("fallback_resid", C.c_double), ("seed_kind", C.c_int32)]
+                ("fallback_iters", C.c_int32), ("fallback_resid", C.c_double), ("seed_kind", C.c_int32),
+                ("buffer", C.c_int32)]
 
 
 class KfSolveStats(C.Structure):
@@ -126,8 +128,10 @@ def lib():
                                            C.c_double, C.c_double, P]),
         "kf_test_time_mode_product": (C.c_int, [C.c_int32, P, P, P, C.c_int32, C.c_int64, C.c_int64, C.c_int64,
                                                 C.c_int32, P, C.POINTER(C.c_float)]),
-        "kf_test_time_gram": (C.c_int, [P, C.c_int64, C.c_int32, P, C.c_int64, C.c_int32, C.c_int64, C.c_int32, P,
+        "kf_test_time_gram": (C.c_int, [C.c_int32, P, C.c_int64, C.c_int32, P, C.c_int64, C.c_int32, C.c_int64, C.c_int32, P,
                                         C.POINTER(C.c_float), P]),
+        "kf_test_gram_tc": (C.c_int, [P, P, P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int64,
+                                      C.c_int32, C.c_int32, P, C.POINTER(C.c_float), P]),
         "kf_test_apply_variant": (C.c_int, [P, C.c_int32, P, P, C.c_int64, C.c_int64, C.c_int32, C.c_int32,
                                             C.POINTER(C.c_float)]),
         "kf_test_update": (C.c_int, [C.c_int32, P, C.c_int64, C.c_int32, P, C.c_int64, C.c_int32, P, C.c_int64,

@@ -29,7 +29,8 @@ def _arg(cond, msg):
 
 class LOBPCG:
     def __init__(self, tol=1e-8, maxiter=1000, preconditioner="ritz", eta=0.01, guard=4, seed="product",
-                 precision="f64", mixed_switch=2e-6, fallback_iters=3, fallback_resid=0.0, rng_seed=0x4B46):
+                 precision="f64", mixed_switch=2e-6, fallback_iters=3, fallback_resid=0.0, rng_seed=0x4B46,
+                 buffer=None):
         _arg(tol > 0 and math.isfinite(tol), f"LOBPCG: tol must be positive and finite, got {tol}")
         _arg(maxiter >= 1, f"LOBPCG: maxiter must be at least 1, got {maxiter}")
         _arg(preconditioner in ("ritz", "jacobi", "none", "separable"),
@@ -38,14 +39,18 @@ class LOBPCG:
         _arg(guard >= 0, f"LOBPCG: guard must be nonnegative, got {guard}")
         _arg(seed in ("product", "random"), f"LOBPCG: seed must be :product or :random, got {seed!r}")
         _arg(precision in _PREC, f"LOBPCG: precision must be f64 or mixed, got {precision!r}")
+        _arg(buffer is None or buffer >= 0, f"LOBPCG: buffer must be nonnegative, got {buffer}")
         self.tol, self.maxiter, self.preconditioner, self.eta = tol, maxiter, preconditioner, eta
         self.guard, self.seed, self.precision = guard, seed, precision
         self.mixed_switch, self.fallback_iters, self.fallback_resid = mixed_switch, fallback_iters, fallback_resid
         self.rng_seed = rng_seed
+        # unchecked columns beyond the guards (None: the library's choice, 2 for mixed, 0 for f64)
+        self.buffer = buffer
 
     def opts(self):
         o = _abi.KfSolverOpts()
         lib().kf_solver_opts_default(C.byref(o), _abi.KF_SOLVER_LOBPCG)
+        o.buffer = _abi.KF_BUFFER_AUTO if self.buffer is None else self.buffer
         o.precision, o.tol, o.maxiter = _PREC[self.precision], self.tol, self.maxiter
         o.preconditioner = {"ritz": 0, "jacobi": 1, "none": 2, "separable": 3}[self.preconditioner]
         o.eta, o.guard, o.mixed_switch = self.eta, self.guard, self.mixed_switch

@@ -12,5 +12,7 @@ D = bench.Dist()
 D.barrier()
 t = D.max(1.0 + D.rank)            # the slowest replica's time
 w = D.sum(12 * (D.rank + 1))       # every replica's converged pairs
-print(json.dumps({"rank": D.rank, "world": D.world, "t": t, "w": w, "value": w / t}), flush=True)
+# one file per rank: two ranks printing to one pipe can interleave their lines
+with open(os.path.join(os.environ["KF_TEST_OUT"], f"rank{D.rank}.json"), "w") as f:
+    json.dump({"rank": D.rank, "world": D.world, "t": t, "w": w, "value": w / t}, f)
 D.close()

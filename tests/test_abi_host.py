@@ -68,6 +68,13 @@ def test_solver_option_validation():
     with pytest.raises(ArgumentError):
         LOBPCG(guard=-1)
     with pytest.raises(ArgumentError):
+        LOBPCG(buffer=-1)
+    # buffer columns: the library's choice unless given; never part of the returned width
+    from kfgpu import _abi
+    assert LOBPCG().opts().buffer == _abi.KF_BUFFER_AUTO
+    assert LOBPCG(buffer=3).opts().buffer == 3
+    assert LOBPCG(buffer=3).width(671744, 12) == 16
+    with pytest.raises(ArgumentError):
         ChebyshevFilter(extra=1)
     with pytest.raises(ArgumentError):
         ChebyshevFilter(degree=201)

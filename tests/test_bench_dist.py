@@ -17,8 +17,8 @@ def _free_port():
         return s.getsockname()[1]
 
 
-def test_replica_aggregation_two_gloo_ranks():
-    env = dict(os.environ, OMP_NUM_THREADS="1")
+def test_replica_aggregation_two_gloo_ranks(tmp_path):
+    env = dict(os.environ, OMP_NUM_THREADS="1", KF_TEST_OUT=str(tmp_path))
     # the free port is picked here and bound later by torchrun: on a busy host another process can
     # take it in between, so a failed rendezvous is retried on a fresh port
     for attempt in range(3):
@@ -28,7 +28,7 @@ def test_replica_aggregation_two_gloo_ranks():
         if r.returncode == 0:
             break
     assert r.returncode == 0, r.stderr[-3000:]
-    rows = [json.loads(l) for l in r.stdout.splitlines() if l.startswith("{")]
+    rows = [json.loads((tmp_path / f"rank{k}.json").read_text()) for k in range(2)]
     assert sorted(x["rank"] for x in rows) == [0, 1]
     for x in rows:
         assert x["world"] == 2 and x["t"] == 2.0 and x["w"] == 36.0 and x["value"] == 18.0
