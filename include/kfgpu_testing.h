@@ -46,12 +46,11 @@ int kf_test_time_gram(int path, const float *A, int64_t lda, int ka, const float
  * blocks: srcs[q] (N x ks[q], leading dimension lds[q]) stacked in order; G_out (host, nr x nc
  * column-major FP64, nr = sum of ks[r0 .. r1-1], nc = sum of ks[c0 .. c1-1]) receives
  * [srcs r0..r1-1]' [srcs c0..c1-1].  `reps` launches on `stream`, timed with CUDA events
- * (*ms_per_launch: mean device time, Gram and reduction); accs: TMEM accumulators per 32-row chunk
- * (0: the library's choice).  Returns KF_EINVAL when the shapes do not
+ * (*ms_per_launch: mean device time, Gram and reduction).  Returns KF_EINVAL when the shapes do not
  * fit the kernel (the solvers then take the SIMT Gram), else a KF_* status.
  */
 int kf_test_gram_tc(const float *const *srcs, const int64_t *lds, const int32_t *ks, int32_t nsrc, int32_t r0,
-                    int32_t r1, int32_t c0, int32_t c1, int64_t N, int32_t accs, int32_t reps, void *stream,
+                    int32_t r1, int32_t c0, int32_t c1, int64_t N, int32_t reps, void *stream,
                     float *ms_per_launch, double *G_out);
 
 /*

@@ -344,7 +344,7 @@ int kf_test_time_gram(int path, const float *A, int64_t lda, int ka, const float
 }
 
 int kf_test_gram_tc(const float *const *srcs, const int64_t *lds, const int32_t *ks, int32_t nsrc, int32_t r0,
-                    int32_t r1, int32_t c0, int32_t c1, int64_t N, int32_t accs, int32_t reps, void *stream,
+                    int32_t r1, int32_t c0, int32_t c1, int64_t N, int32_t reps, void *stream,
                     float *ms_per_launch, double *G_out) {
     return guarded([&] {
         KF_REQUIRE(srcs && lds && ks && ms_per_launch && reps >= 1 && N >= 1 && nsrc >= 1 && nsrc <= 4, KF_EINVAL,
@@ -365,8 +365,7 @@ int kf_test_gram_tc(const float *const *srcs, const int64_t *lds, const int32_t 
         const size_t pb = kf::gram_tc_partials_size(nr, nc);
         KF_CUDA(cudaMalloc(&G, (size_t)nr * nc * sizeof(double)));
         KF_CUDA(cudaMalloc(&part, pb));
-        KF_REQUIRE(accs >= 0 && accs <= 12, KF_EINVAL, "kf_test_gram_tc: accs must lie in 0:12");
-        auto run = [&] { return kf::gram_tc(src.data(), nsrc, r0, r1, c0, c1, N, G, part, pb, s, accs); };
+        auto run = [&] { return kf::gram_tc(src.data(), nsrc, r0, r1, c0, c1, N, G, part, pb, s); };
         bool ok = run();   // warm
         cudaEvent_t e0, e1;
         KF_CUDA(cudaEventCreate(&e0));

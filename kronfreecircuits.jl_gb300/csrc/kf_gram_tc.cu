@@ -5,35 +5,47 @@
 // The Gram products of LOBPCG's orthogonalisation and Rayleigh-Ritz (the reference's X' W, W' W,
 // S' H S inside LOBPCGEigensolver, called at src/lobpcg.jl:268, and the Gram of SVQB at
 // src/chebyshev.jl:68-81) are tall-skinny: N rows, a few dozen columns.  On the SIMT pipes they are
-// FMA-bound (every element of A meets every column of B); here each element is read from memory
-// once and the products run on the tensor cores, so the kernel is bound by HBM.
+// FMA-bound and their cost grows with the output; here every element is read from memory once.
 //
-// The operand blocks (up to four sources, e.g. [X Z] for [X Z]'Z or [X_a Q HX_a HZ] for one merged
-// Rayleigh-Ritz Gram) are stacked as the rows of one "pool" image in shared memory, each source
-// starting at a multiple of 8 rows.  Per chunk of GT_KC data rows the image holds pool row m, data
-// rows k (K-major, no swizzle: 8-row x 16-byte core matrices).  One MMA chain computes
-//   D[m, n] += sum_k pool[m, k] pool[b_off + n, k]      (m < 128, n < Nb)
-// i.e. every pool column against the contiguous range of B columns; the entries that the caller
-// asked for are picked out of D at the end (rows of sources [r0, r1), columns of [c0, c1)).
+// What bounds this kernel is the number of MMAs, not their width: a kind::tf32 MMA consumes K = 8
+// rows and, measured, costs about the same at N = 16 as at N = 112 (about 100 cycles).  So the
+// images are laid out to let one wide MMA carry several of the split products:
+//   the pool (up to four source blocks, each starting at a multiple of 8 rows) puts the sources
+//   that only give rows of G first and the B sources (the columns of G) last, ending at row RB of
+//   the hi image; the lo image follows it and starts with the B rows (then the others).  The B
+//   operand "hi rows [b_off, RB) + lo rows [0, nbr)" is then one contiguous [B_hi; B_lo].
+//   RB = 64 (pools up to 64 rows): the A operand "hi rows 0..63 + lo rows 0..63" is [A_hi; A_lo]
+//     and ONE MMA per K step gives hi*hi | hi*lo (accumulator rows 0..63) and lo*hi | lo*lo
+//     (rows 64..127; lo*lo is not used);
+//   RB = 128: two MMAs per K step, A_hi x [B_hi; B_lo] and A_lo x [B_hi; B_lo] (whose lo*lo half
+//     is not used either).
+// The epilogue adds hi*hi + hi*lo on the lanes of the hi rows and lo*hi on the lanes of the lo
+// rows into two FP32 partial sets per CTA; the reduction sums both.
+//
+// Measured on GB300, a kind::tf32 MMA with M = 128 occupies the tensor core for a fixed ~150 ns
+// whatever its N (16 .. 256): this kernel is bound by the count of MMAs, one per 8 rows (RB = 64) or
+// two (RB = 128), about 80 us per 671,744 rows for the one-MMA layout.  Two accumulator slots and
+// producers that refill the stage of chunk t - 2 keep the tensor core fed (four slots and a refill
+// distance of four measured slower).
 //
 // One persistent CTA per SM (or per chunk when there are fewer), warp-specialised:
 //   warps 0-7   producers: 16-byte cp.async copies of their pieces of the chunk straight into the
-//               core-matrix layout of stage t % S (S - 2 chunks in flight ahead),
+//               core-matrix layout of the hi image of stage t % S (S - R chunks in flight ahead),
 //               then the split of their own pieces into hi (in place) and lo, arrive on full[s];
 //   warp 8      issuer (one lane): waits full[s] and a drained accumulator slot, issues the chunk's
-//               MMA chain into slot t % 2 (starting it afresh), commits to empty[s] and accf[t % 2];
-//   warps 9-16  epilogue: TMEM lane = pool row (warp % 4 picks the lane quarter), (warp - 9) / 4
-//               the half of the B columns; add slot t % 2 into FP32 registers (round to nearest),
-//               arrive on acce[t % 2]; at the end write the CTA's FP32 partial sums.
+//               MMAs into slot t % 2 (starting it afresh), commits to empty[s] and accf[t % 2];
+//   warps 9-16  epilogue: TMEM lane = accumulator row (warp % 4 picks the lane quarter), (warp - 9)
+//               / 4 the half of the B columns; adds slot t % 2 into FP32 registers (round to
+//               nearest), arrives on acce[t % 2]; at the end writes the CTA's FP32 partial sums.
 // The tensor cores' FP32 accumulation rounds toward zero, a bias of about 2^-24 of the running sum
-// per addition: over a CTA's ~4,400 rows (1,650 MMAs) that reached 1e-4 of a sum of squares.
-// Chains of one chunk (12 MMAs) keep it near 1e-6, like the SIMT kernel's FP32 partial sums.
+// per addition: accumulator chains of one chunk (4 MMAs per accumulator) keep it near 1e-7.
 // Every wait is an mbarrier wait with a cycle budget; when one runs out the CTA records
 // KF_ETIMEOUT in the host-mapped error word, every role leaves its loop at its next check, the
 // issuer waits (bounded) for its MMAs in flight, and TMEM is freed.
 #include <algorithm>
 #include <cstring>
 #include <mutex>
+#include <vector>
 
 #include "kf_internal.h"
 
@@ -44,30 +56,29 @@ namespace {
 constexpr int GT_PROD = 256;                          // producer threads (warps 0-7)
 constexpr int GT_EPI = 256;                           // epilogue threads (warps 9-16)
 constexpr int GT_THREADS = GT_PROD + 32 + GT_EPI;     // + the issuer warp
-constexpr int GT_NBMAX = 128;                         // B columns (TMEM: two slots of Nb)
-constexpr int GT_NBH = GT_NBMAX / 2;                  // B columns per epilogue thread
-constexpr int GT_KC = 32;                             // data rows per chunk (MMA K per chunk)
-constexpr int GT_ROWS = 144;                          // pool rows at most: the A window 128 + B overhang
-constexpr int GT_SBO = (GT_KC / 4) * 128;             // bytes between 8-row groups
-
-// Shared-memory plan for a pool of at most R rows: S stages of hi | lo images (R rows each), then a
-// zeroed guard that the 128-row A window of the last images may reach past R (those rows only feed
-// accumulator rows nobody reads).  Narrow pools get more stages: about 60 KB of loads in flight per
-// SM whatever the pool.
-template <int R, int S>
-struct GtPlan {
-    static constexpr int IMG = R * GT_KC * 4;
-    static constexpr int STAGE = 2 * IMG;
-    static constexpr int GUARD = R >= 128 ? 0 : (128 - R) * GT_KC * 4;
-    static constexpr int PIECES = R * (GT_KC / 4);
-    static constexpr int PPT = (PIECES + GT_PROD - 1) / GT_PROD;
-    static constexpr int LA = S - 2;                   // chunks loading ahead of the one being split
-    static constexpr size_t BARS = (size_t)S * STAGE + GUARD;
-    static constexpr size_t SMEM = BARS + 8 * (2 * S + 6);
-};
+constexpr int GT_KC = 32;                             // data rows per chunk (4 MMA K steps)
+constexpr int GT_SBO = (GT_KC / 4) * 128;             // bytes between 8-row groups of an image
+constexpr int GT_NBR_MAX = 64;                        // B columns
+constexpr int GT_NBH = GT_NBR_MAX / 2;                // B columns per epilogue thread
 constexpr long long GT_WAIT_CYCLES = 4000000000LL;
 constexpr int GT_MAX_SRC = 4;
-constexpr int GRAM_TC_DEFAULT_ACCS = 4;
+
+constexpr int GT_MAX_SLOTS = 2;                       // accumulator slots
+
+// Shared-memory plan for RB image rows: S stages of hi | lo images; the producers refill the stage
+// of chunk t - R.
+template <int RB, int S, int R>
+struct GtPlan {
+    static constexpr int IMG = RB * GT_KC * 4;
+    static constexpr int STAGE = 2 * IMG;
+    static constexpr int PIECES = RB * (GT_KC / 4);    // 16-byte pieces of one image
+    static constexpr int PPT = PIECES / GT_PROD;       // pieces per producer thread
+    static constexpr int LA = S - R;                   // chunks loading ahead of the one being split
+    static constexpr size_t BARS = (size_t)S * STAGE;
+    static constexpr size_t SMEM = BARS + 8 * (2 * S + 2 * GT_MAX_SLOTS + 2);
+    static_assert(PIECES % GT_PROD == 0, "pieces per thread");
+    static_assert(LA >= 2, "loads in flight");
+};
 
 __device__ __forceinline__ uint32_t gsu32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -126,38 +137,49 @@ __device__ __forceinline__ void gt_cp16(uint32_t dst, const void *src, int src_b
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
 }
 
+// 16 consecutive accumulator columns of this warp's 32 TMEM lanes
+__device__ __forceinline__ void gt_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15}, [%16];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+}
+
 struct GtArgs {
     const float *p[GT_MAX_SRC];
     int64_t ld[GT_MAX_SRC];
-    int off[GT_MAX_SRC], k[GT_MAX_SRC];
+    int off[GT_MAX_SRC], k[GT_MAX_SRC];   // hi image rows [off, off + k) per source
     int nsrc;
     int64_t N;
     int64_t nchunks;
-    int b_off, Nb;                 // B operand: pool rows [b_off, b_off + Nb)
+    int b_off, nbr;                // B rows: hi rows [b_off, RB) = lo rows [0, nbr); nbr % 16 == 0
     int nr, nc;                    // output entries (nr x nc, column-major)
-    uint8_t rinv[128];             // pool row -> output row (255: not wanted)
-    uint8_t cinv[GT_ROWS];         // B column -> output column (255: not wanted)
-    float *part;                   // [gridDim.x][nr * nc]
+    uint8_t rinv_hi[128];          // hi image row -> output row (255: not wanted)
+    uint8_t rinv_lo[128];          // lo image row -> output row
+    uint8_t cinv[GT_NBR_MAX];      // B column -> output column (255: padding)
+    float *part;                   // [gridDim.x][2][nr * nc]: hi-row sums, lo-row sums
     int *err;
-    uint32_t tcols;                // TMEM columns allocated: 2 x nacc accumulators of astride
-    int nacc;                      // accumulators per chunk: MMA j of a chunk adds into j % nacc
-    uint32_t astride;              // TMEM columns per accumulator (a power of two >= max(Nb, 32))
-    int h0;                        // B columns [0, h0) to epilogue half 0, [h0, Nb) to half 1
 };
 
-template <int R, int S>
+template <int RB, int S, int R>
 __global__ void __launch_bounds__(GT_THREADS, 1) k_gram_tc(const GtArgs a) {
-    using P = GtPlan<R, S>;
+    using P = GtPlan<RB, S, R>;
+    constexpr bool ONE = RB == 64;             // one MMA per K step ([A_hi; A_lo] x [B_hi; B_lo])
+    // two accumulator slots at power-of-two column offsets (measured faster than packed slots);
+    // RB = 128: the second MMA's accumulator 128 columns into the slot
+    constexpr uint32_t SLOT = ONE ? 128 : 256;
     extern __shared__ __align__(1024) unsigned char gt_smem[];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     unsigned char *stages = gt_smem;
     uint64_t *bars = reinterpret_cast<uint64_t *>(gt_smem + P::BARS);
-    uint64_t *full = bars, *empty = bars + S, *accf = bars + 2 * S, *acce = accf + 2,
-             *fin = acce + 2;
+    uint64_t *full = bars, *empty = bars + S, *accf = bars + 2 * S, *acce = accf + GT_MAX_SLOTS,
+             *fin = acce + GT_MAX_SLOTS;
     uint32_t *tslot = reinterpret_cast<uint32_t *>(fin + 1);
     __shared__ volatile int s_abort;
 
-    // zero the images once: rows that no source fills (gaps, the A window past the pool) stay zero
+    // zero the images once: rows that no source fills (alignment gaps) stay zero
     for (size_t o = (size_t)tid * 16; o < P::BARS; o += (size_t)GT_THREADS * 16)
         *reinterpret_cast<uint4 *>(stages + o) = make_uint4(0u, 0u, 0u, 0u);
     if (tid == 0) {
@@ -165,7 +187,7 @@ __global__ void __launch_bounds__(GT_THREADS, 1) k_gram_tc(const GtArgs a) {
             gt_bar_init(full + q, GT_PROD);
             gt_bar_init(empty + q, 1);
         }
-        for (int q = 0; q < 2; ++q) {
+        for (int q = 0; q < GT_MAX_SLOTS; ++q) {
             gt_bar_init(accf + q, 1);
             gt_bar_init(acce + q, GT_EPI);
         }
@@ -175,7 +197,7 @@ __global__ void __launch_bounds__(GT_THREADS, 1) k_gram_tc(const GtArgs a) {
     }
     if (warp == 8) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(gsu32(tslot)),
-                     "r"(a.tcols));
+                     "r"(512));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
     }
     asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
@@ -187,25 +209,24 @@ __global__ void __launch_bounds__(GT_THREADS, 1) k_gram_tc(const GtArgs a) {
     if ((int64_t)blockIdx.x < a.nchunks) my = (a.nchunks - 1 - blockIdx.x) / gridDim.x + 1;
 
     if (warp < 8) {
-        // ---- producers.  Piece e: pool row 8 (e / 64) + e % 8, data rows 4 ((e / 8) % 8) .. + 3 of
+        // ---- producers.  Piece e: hi row 8 (e / 64) + e % 8, data rows 4 ((e / 8) % 8) .. + 3 of
         // the chunk; a quarter-warp covers the 8 rows of one core matrix (conflict-free 16-byte
-        // stores), a warp 8 pool columns x 16 data rows (64-byte runs per column).
+        // stores), a warp 8 pool columns x 16 data rows (64-byte runs per column).  The lo part of
+        // hi row m goes to lo row m - b_off (B rows) or m + nbr (the others).
         const float *gp[P::PPT];
-        uint32_t soff[P::PPT];
+        uint32_t soff[P::PPT], loff[P::PPT];
         int k4[P::PPT];
 #pragma unroll
         for (int j = 0; j < P::PPT; ++j) {
             const int e = tid + j * GT_PROD;
+            const int m = (e / 64) * 8 + (e & 7);
+            const int ml = m >= a.b_off ? m - a.b_off : m + a.nbr;
+            k4[j] = (e >> 3) & 7;
+            soff[j] = (uint32_t)((m >> 3) * GT_SBO + k4[j] * 128 + (m & 7) * 16);
+            loff[j] = (uint32_t)(P::IMG + (ml >> 3) * GT_SBO + k4[j] * 128 + (ml & 7) * 16);
             gp[j] = nullptr;
-            soff[j] = 0;
-            k4[j] = 0;
-            if (e < P::PIECES) {
-                const int m = (e / 64) * 8 + (e & 7);
-                k4[j] = (e >> 3) & 7;
-                soff[j] = (uint32_t)((m >> 3) * GT_SBO + k4[j] * 128 + (m & 7) * 16);
-                for (int q = 0; q < a.nsrc; ++q)
-                    if (m >= a.off[q] && m < a.off[q] + a.k[q]) gp[j] = a.p[q] + (int64_t)(m - a.off[q]) * a.ld[q];
-            }
+            for (int q = 0; q < a.nsrc; ++q)
+                if (m >= a.off[q] && m < a.off[q] + a.k[q]) gp[j] = a.p[q] + (int64_t)(m - a.off[q]) * a.ld[q];
         }
         const uint32_t sbase = gsu32(stages);
         auto issue = [&](int64_t t) {
@@ -221,9 +242,8 @@ __global__ void __launch_bounds__(GT_THREADS, 1) k_gram_tc(const GtArgs a) {
                 gt_cp16(hi + soff[j], nb > 0 ? (const void *)(gp[j] + r) : (const void *)gp[j], (int)nb);
             }
         };
-        // P::LA chunks in flight ahead of the one being split; the slot refilled at step t held chunk
-        // t - 2, whose MMAs had a whole step to retire (refilling t - 1's slot would wait on MMAs
-        // issued a moment before and serialise the pipeline)
+        // P::LA chunks in flight ahead of the one being split; the stage refilled at step t held chunk
+        // t - R, whose MMAs had R - 1 steps to retire
         for (int t = 0; t < P::LA; ++t) {
             if (t < my) issue(t);
             asm volatile("cp.async.commit_group;\n" ::: "memory");
@@ -242,19 +262,19 @@ __global__ void __launch_bounds__(GT_THREADS, 1) k_gram_tc(const GtArgs a) {
             asm volatile("cp.async.wait_group %0;\n" ::"n"(P::LA) : "memory");
             // this thread's pieces of chunk t have landed: split them into hi (in place) and lo
             const int s = (int)(t % S);
-            unsigned char *hi = stages + (size_t)s * P::STAGE, *lo = hi + P::IMG;
+            unsigned char *st = stages + (size_t)s * P::STAGE;
 #pragma unroll
             for (int j = 0; j < P::PPT; ++j) {
                 if (!gp[j]) continue;
-                uint4 v = *reinterpret_cast<const uint4 *>(hi + soff[j]);
+                uint4 v = *reinterpret_cast<const uint4 *>(st + soff[j]);
                 uint32_t x[4] = {v.x, v.y, v.z, v.w}, h[4], l[4];
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
                     h[q] = x[q] & 0xFFFFE000u;
                     l[q] = __float_as_uint(__uint_as_float(x[q]) - __uint_as_float(h[q]));
                 }
-                *reinterpret_cast<uint4 *>(hi + soff[j]) = make_uint4(h[0], h[1], h[2], h[3]);
-                *reinterpret_cast<uint4 *>(lo + soff[j]) = make_uint4(l[0], l[1], l[2], l[3]);
+                *reinterpret_cast<uint4 *>(st + soff[j]) = make_uint4(h[0], h[1], h[2], h[3]);
+                *reinterpret_cast<uint4 *>(st + loff[j]) = make_uint4(l[0], l[1], l[2], l[3]);
             }
             asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
             gt_arrive(full + s);
@@ -263,8 +283,8 @@ __global__ void __launch_bounds__(GT_THREADS, 1) k_gram_tc(const GtArgs a) {
     } else if (warp == 8) {
         // ---- MMA issuer (one lane)
         if (lane == 0) {
-            const uint32_t idesc =
-                (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(a.Nb >> 3) << 17) | ((128u >> 4) << 24);
+            const uint32_t n1 = (uint32_t)(2 * a.nbr);
+            const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((n1 >> 3) << 17) | ((128u >> 4) << 24);
             const uint32_t sbase = gsu32(stages);
             const uint32_t boff = (uint32_t)(a.b_off >> 3) * GT_SBO;
             int64_t issued = 0;
@@ -274,17 +294,13 @@ __global__ void __launch_bounds__(GT_THREADS, 1) k_gram_tc(const GtArgs a) {
                 if (t >= 2 && !gt_wait(acce + sl, (uint32_t)(t / 2 - 1), &s_abort)) { s_abort = 1; break; }
                 asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
                 const uint32_t hi = sbase + (uint32_t)s * P::STAGE, lo = hi + P::IMG;
-                const uint32_t d0 = tmem + (uint32_t)(sl * a.nacc) * a.astride;
-                // the chunk's 12 MMAs (4 K steps x hi*hi, hi*lo, lo*hi) spread over nacc accumulators:
-                // consecutive MMAs are independent, so the tensor pipe is not held by one chain
+                const uint32_t d = tmem + (uint32_t)sl * SLOT;
 #pragma unroll
-                for (int j = 0; j < 3 * (GT_KC / 8); ++j) {
-                    const int ks = j / 3, part = j % 3;
+                for (int ks = 0; ks < GT_KC / 8; ++ks) {
                     const uint32_t o = (uint32_t)ks * 256;
-                    const uint64_t da = gt_desc((part == 2 ? lo : hi) + o, 128, GT_SBO);
-                    const uint64_t db = gt_desc((part == 1 ? lo : hi) + boff + o, 128, GT_SBO);
-                    const int q = j % a.nacc;
-                    gt_mma(d0 + (uint32_t)q * a.astride, da, db, idesc, j >= a.nacc ? 1u : 0u);
+                    const uint64_t db = gt_desc(hi + boff + o, 128, GT_SBO);   // [B_hi; B_lo]
+                    gt_mma(d, gt_desc(hi + o, 128, GT_SBO), db, idesc, ks > 0 ? 1u : 0u);
+                    if (!ONE) gt_mma(d + 128, gt_desc(lo + o, 128, GT_SBO), db, idesc, ks > 0 ? 1u : 0u);
                 }
                 gt_commit(empty + s);
                 gt_commit(accf + sl);
@@ -298,14 +314,18 @@ __global__ void __launch_bounds__(GT_THREADS, 1) k_gram_tc(const GtArgs a) {
             }
         }
     } else {
-        // ---- epilogue (warps 9-16): TMEM lane = pool row 32 (warp % 4) + lane, B columns
-        // [cb, ce) of the half (warp - 9) / 4
+        // ---- epilogue (warps 9-16): TMEM lane = accumulator row 32 (warp % 4) + lane, B columns
+        // [cb, ce) of the half (warp - 9) / 4.  ONE: lanes 0-63 are hi rows (hi*hi at column n,
+        // hi*lo at nbr + n), lanes 64-127 lo rows (lo*hi at n).  Otherwise every lane has hi row m
+        // (slot columns n, nbr + n) and lo row m (slot column 128 + n).
         const int q = warp & 3, m = q * 32 + lane, h = (warp - 9) >> 2;
-        const int cb = h == 0 ? 0 : a.h0, ce = h == 0 ? a.h0 : a.Nb;
-        const uint32_t base = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)cb;
-        float acc[GT_NBH];
+        const int h0 = min(a.nbr, (a.nbr / 2 + 15) / 16 * 16);
+        const int cb = h == 0 ? 0 : h0, ce = h == 0 ? h0 : a.nbr;
+        const uint32_t lb = (uint32_t)(q * 32) << 16;
+        const bool has_hi = !ONE || q < 2, has_lo = !ONE || q >= 2;
+        float acc_hi[GT_NBH], acc_lo[GT_NBH];
 #pragma unroll
-        for (int c = 0; c < GT_NBH; ++c) acc[c] = 0.f;
+        for (int c = 0; c < GT_NBH; ++c) acc_hi[c] = acc_lo[c] = 0.f;
         bool ok = true;
         for (int64_t t = 0; t < my; ++t) {
             const int sl = (int)(t & 1);
@@ -313,35 +333,44 @@ __global__ void __launch_bounds__(GT_THREADS, 1) k_gram_tc(const GtArgs a) {
             ok = __all_sync(0xffffffffu, ok);   // tcgen05.ld is warp-collective
             if (!ok) { s_abort = 1; break; }
             asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-            for (int qa = 0; qa < a.nacc; ++qa) {
-                const uint32_t d = base + (uint32_t)(sl * a.nacc + qa) * a.astride;
+            const uint32_t d = tmem + lb + (uint32_t)sl * SLOT;
 #pragma unroll
-                for (int c0 = 0; c0 < GT_NBH; c0 += 16) {
-                    if (cb + c0 >= ce) break;
-                    uint32_t r[16];
-                    asm volatile(
-                        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
-                        "%12, %13, %14, %15}, [%16];\n"
-                        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-                          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-                          "=r"(r[14]), "=r"(r[15])
-                        : "r"(d + (uint32_t)c0));
+            for (int c0 = 0; c0 < GT_NBH; c0 += 16) {
+                if (cb + c0 >= ce) break;
+                const uint32_t col = (uint32_t)(cb + c0);
+                uint32_t r1[16];
+                if (has_hi) {
+                    gt_ld16(d + col, r1);
                     asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
 #pragma unroll
-                    for (int u = 0; u < 16; ++u) acc[c0 + u] += __uint_as_float(r[u]);
+                    for (int u = 0; u < 16; ++u) acc_hi[c0 + u] += __uint_as_float(r1[u]);
+                    gt_ld16(d + (uint32_t)a.nbr + col, r1);
+                    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+                    for (int u = 0; u < 16; ++u) acc_hi[c0 + u] += __uint_as_float(r1[u]);
+                }
+                if (has_lo) {
+                    gt_ld16(d + (ONE ? 0u : 128u) + col, r1);
+                    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+                    for (int u = 0; u < 16; ++u) acc_lo[c0 + u] += __uint_as_float(r1[u]);
                 }
             }
             asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
             gt_arrive(acce + sl);
         }
-        const int i = a.rinv[m];
-        if (ok && i != 255) {
-            float *out = a.part + (size_t)blockIdx.x * a.nr * a.nc;
+        if (ok) {
+            const size_t E = (size_t)a.nr * a.nc;
+            float *out = a.part + (size_t)blockIdx.x * 2 * E;
+            const int ih = has_hi ? a.rinv_hi[m] : 255;
+            const int il = has_lo ? a.rinv_lo[ONE ? m - 64 : m] : 255;
 #pragma unroll
             for (int c = 0; c < GT_NBH; ++c) {
                 if (cb + c >= ce) break;
                 const int j = a.cinv[cb + c];
-                if (j != 255) out[i + (size_t)a.nr * j] = acc[c];
+                if (j == 255) continue;
+                if (ih != 255) out[ih + (size_t)a.nr * j] = acc_hi[c];
+                if (il != 255) out[E + il + (size_t)a.nr * j] = acc_lo[c];
             }
         }
     }
@@ -352,7 +381,7 @@ __global__ void __launch_bounds__(GT_THREADS, 1) k_gram_tc(const GtArgs a) {
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-    if (warp == 8) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(a.tcols));
+    if (warp == 8) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(512));
 }
 
 // G[e] = sum over the CTAs' FP32 partials, in FP64, one warp per entry
@@ -367,18 +396,18 @@ __global__ void k_reduce_partials_f32(const float *__restrict__ part, int nparts
     if (lane == 0) G[e] = s;
 }
 
+using GtKernel = void (*)(const GtArgs);
+const GtKernel g_gt_kern[2] = {k_gram_tc<64, 12, 2>, k_gram_tc<128, 6, 2>};
+const size_t g_gt_smem[2] = {GtPlan<64, 12, 2>::SMEM, GtPlan<128, 6, 2>::SMEM};
+
 // per device: SM count and, per plan, whether the kernel fits and its attribute is set
 struct GtDevice {
     bool ready = false;
     int sms = 0;
-    bool fits[3] = {false, false, false};
+    bool fits[2] = {false, false};
 };
 std::mutex g_gt_mu;
 GtDevice g_gt_dev[32];
-
-using GtKernel = void (*)(const GtArgs);
-const GtKernel g_gt_kern[3] = {k_gram_tc<48, 14>, k_gram_tc<80, 8>, k_gram_tc<144, 5>};
-const size_t g_gt_smem[3] = {GtPlan<48, 14>::SMEM, GtPlan<80, 8>::SMEM, GtPlan<144, 5>::SMEM};
 
 const GtDevice &gt_device() {
     int dev = 0;
@@ -390,7 +419,7 @@ const GtDevice &gt_device() {
         int optin = 0;
         KF_CUDA(cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, dev));
         KF_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-        for (int p = 0; p < 3; ++p) {
+        for (int p = 0; p < 2; ++p) {
             cudaFuncAttributes fa;
             KF_CUDA(cudaFuncGetAttributes(&fa, g_gt_kern[p]));
             d.fits[p] = g_gt_smem[p] + fa.sharedSizeBytes <= (size_t)optin;
@@ -405,71 +434,83 @@ const GtDevice &gt_device() {
 
 }  // namespace
 
-int gram_tc_sms() { return gt_device().sms; }
-
-size_t gram_tc_partials_size(int nr, int nc) { return (size_t)256 * nr * nc * sizeof(float); }
+size_t gram_tc_partials_size(int nr, int nc) { return (size_t)2 * 256 * nr * nc * sizeof(float); }
 
 bool gram_tc(const GramTcSrc *src, int nsrc, int r0, int r1, int c0, int c1, int64_t N, double *G, void *partials,
-             size_t partial_bytes, cudaStream_t s, int accs) {
+             size_t partial_bytes, cudaStream_t s) {
     if (nsrc < 1 || nsrc > GT_MAX_SRC || r0 < 0 || r1 > nsrc || r0 >= r1 || c0 < 0 || c1 > nsrc || c0 >= c1) return false;
     if (N < GT_KC) return false;
-    GtArgs a;
-    std::memset(&a, 0, sizeof a);
-    int off = 0;
     for (int q = 0; q < nsrc; ++q) {
         const GramTcSrc &c = src[q];
         if (c.k < 1 || !c.p || c.ld % 4 != 0 || (uintptr_t)c.p % 16 != 0) return false;
-        a.p[q] = c.p;
-        a.ld[q] = c.ld;
-        a.k[q] = c.k;
-        a.off[q] = off;
-        off = (off + c.k + 7) / 8 * 8;
     }
-    if (off > GT_ROWS) return false;
-    // rows of G: pool rows below 128 (the MMA's M); columns: the B window inside the image
-    if (a.off[r1 - 1] + a.k[r1 - 1] > 128) return false;
-    a.b_off = a.off[c0];
-    const int bend = a.off[c1 - 1] + a.k[c1 - 1];
-    a.Nb = (bend - a.b_off + 15) / 16 * 16;
-    if (a.b_off + a.Nb > GT_ROWS || a.Nb > GT_NBMAX) return false;
-    a.nsrc = nsrc;
+    GtArgs a;
+    std::memset(&a, 0, sizeof a);
+    // the pool: the row-only sources first (8-aligned from row 0), the column sources last, ending
+    // at row RB; `order` lists the pool's sources by their index in src
+    std::vector<int> order;
+    int aspan = 0, cspan = 0;
+    for (int q = r0; q < r1; ++q)
+        if (q < c0 || q >= c1) {
+            a.off[order.size()] = aspan;
+            aspan = (aspan + src[q].k + 7) / 8 * 8;
+            order.push_back(q);
+        }
+    const int na = (int)order.size();
+    int coff[GT_MAX_SRC];
+    for (int q = c0; q < c1; ++q) {
+        coff[q - c0] = cspan;
+        cspan = (cspan + src[q].k + 7) / 8 * 8;
+        order.push_back(q);
+    }
+    const int nbr = (cspan + 15) / 16 * 16;
+    if (nbr > GT_NBR_MAX) return false;
+    const int RB = aspan + nbr <= 64 ? 64 : aspan + nbr <= 128 ? 128 : 0;
+    if (!RB) return false;
+    a.nbr = nbr;
+    a.b_off = RB - nbr;
+    a.nsrc = (int)order.size();
+    for (int i = 0; i < a.nsrc; ++i) {
+        const int q = order[i];
+        a.p[i] = src[q].p;
+        a.ld[i] = src[q].ld;
+        a.k[i] = src[q].k;
+        if (i >= na) a.off[i] = a.b_off + coff[i - na];
+    }
     a.N = N;
     a.nchunks = (N + GT_KC - 1) / GT_KC;
-    std::memset(a.rinv, 255, sizeof a.rinv);
+    std::memset(a.rinv_hi, 255, sizeof a.rinv_hi);
+    std::memset(a.rinv_lo, 255, sizeof a.rinv_lo);
     std::memset(a.cinv, 255, sizeof a.cinv);
+    // output rows: the sources r0..r1-1 in order, wherever they sit in the pool
     int nr = 0, nc = 0;
-    for (int q = r0; q < r1; ++q)
-        for (int c = 0; c < a.k[q]; ++c) a.rinv[a.off[q] + c] = (uint8_t)nr++;
+    for (int q = r0; q < r1; ++q) {
+        const int i = (int)(std::find(order.begin(), order.end(), q) - order.begin());
+        for (int c = 0; c < src[q].k; ++c) {
+            const int m = a.off[i] + c;
+            const int ml = m >= a.b_off ? m - a.b_off : m + nbr;
+            a.rinv_hi[m] = (uint8_t)nr;
+            a.rinv_lo[ml] = (uint8_t)nr;
+            ++nr;
+        }
+    }
     for (int q = c0; q < c1; ++q)
-        for (int c = 0; c < a.k[q]; ++c) a.cinv[a.off[q] + c - a.b_off] = (uint8_t)nc++;
+        for (int c = 0; c < src[q].k; ++c) a.cinv[coff[q - c0] + c] = (uint8_t)nc++;
     if (nr > 254 || nc > 254) return false;
     a.nr = nr;
     a.nc = nc;
     const GtDevice &dv = gt_device();
+    const int plan = RB == 64 ? 0 : 1;
+    if (!dv.fits[plan]) return false;
     const int grid = (int)std::min<int64_t>(dv.sms, a.nchunks);
-    if ((size_t)grid * nr * nc * sizeof(float) > partial_bytes) return false;
+    if ((size_t)2 * grid * nr * nc * sizeof(float) > partial_bytes) return false;
     a.part = (float *)partials;
     a.err = tc_error_word();
-    // accumulators: two chunk slots x nacc, each a power of two >= max(Nb, 32) columns, within the
-    // 512 TMEM columns of the SM
-    uint32_t as = 32;
-    while (as < (uint32_t)a.Nb) as <<= 1;
-    const int amax = (int)(256 / as);
-    int nacc = accs > 0 ? accs : GRAM_TC_DEFAULT_ACCS;
-    nacc = std::min(nacc, std::min(amax, 12));
-    a.nacc = nacc;
-    a.astride = as;
-    uint32_t tc = 32;
-    while (tc < 2u * (uint32_t)nacc * as) tc <<= 1;
-    a.tcols = tc;
-    a.h0 = std::min(a.Nb, (a.Nb / 2 + 15) / 16 * 16);
-    // the plan by pool rows (a multiple of 8): more stages for narrower pools
-    const int plan = off <= 48 ? 0 : off <= 80 ? 1 : 2;
-    if (!dv.fits[plan]) return false;
+
     g_gt_kern[plan]<<<grid, GT_THREADS, g_gt_smem[plan], s>>>(a);
     KF_LAUNCH_CHECK();
     const int n = nr * nc;
-    k_reduce_partials_f32<<<(n + 7) / 8, 256, 0, s>>>((const float *)partials, grid, n, G);
+    k_reduce_partials_f32<<<(n + 7) / 8, 256, 0, s>>>((const float *)partials, 2 * grid, n, G);
     KF_LAUNCH_CHECK();
     return true;
 }

@@ -207,16 +207,16 @@ void residual_mixed(const double *X, const double *HX, int64_t ld, int k, int64_
                     int64_t ldw, double *norms2, double *partials, cudaStream_t s);
 // FP32 Gram on the tensor cores: the sources are stacked as the rows of one pool (each at a multiple
 // of 8 rows); G (nr x nc, column-major, ld nr) = [sources r0..r1-1]' [sources c0..c1-1], in FP64.
-// Returns false, launching nothing, when the shapes do not fit the kernel (pool over 144 rows, rows
-// of G past pool row 128, unaligned columns, too small a partial buffer).
+// Returns false, launching nothing, when the shapes do not fit the kernel (the row-only sources and
+// the column sources over 128 rows, column sources over 64 columns, unaligned columns, too small a
+// partial buffer).
 struct GramTcSrc {
     const float *p;
     int64_t ld;
     int k;
 };
-// accs: accumulators per chunk (0: the default; capped by TMEM)
 bool gram_tc(const GramTcSrc *src, int nsrc, int r0, int r1, int c0, int c1, int64_t N, double *G, void *partials,
-             size_t partial_bytes, cudaStream_t s, int accs = 0);
+             size_t partial_bytes, cudaStream_t s);
 size_t gram_tc_partials_size(int nr, int nc);
 // second orthogonalisation pass on the device: from G = [X Z]'Z, coefficients C ((r + wx) x r)
 // with [Z X] C orthonormal and orthogonal to X (Cholesky of Z'Z - (X'Z)'(X'Z)); *status 1 on failure

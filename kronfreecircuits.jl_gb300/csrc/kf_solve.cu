@@ -216,6 +216,7 @@ struct LobWork {
     int w;
     DevMem X, HX, Xn, HXn, Z, HZ, Zt, Pn, F1, F2, dG, dC, dpart, dth, dthp, dnorm, dD, dstat;
     HostMem hG, hC, hv, hstat;
+    size_t part_bytes;
     LobWork(int64_t N_, int w_)
         : N(N_), w(w_),
           X((size_t)N_ * w_ * sizeof(T)), HX((size_t)N_ * w_ * sizeof(T)), Xn((size_t)N_ * w_ * sizeof(T)),
@@ -226,7 +227,7 @@ struct LobWork {
           dpart(gram_partials_size(3 * w_, 3 * w_, N_)), dth(w_ * sizeof(double)), dthp(w_ * sizeof(double)),
           dnorm(2 * w_ * sizeof(double)), dD(0), dstat(16),
           hG((size_t)9 * w_ * w_ * sizeof(double)), hC((size_t)9 * w_ * w_ * sizeof(double)),
-          hv((size_t)4 * w_ * sizeof(double)), hstat(16) {}
+          hv((size_t)4 * w_ * sizeof(double)), hstat(16), part_bytes(gram_partials_size(3 * w_, 3 * w_, N_)) {}
 };
 
 template <typename T>
@@ -399,6 +400,16 @@ static int merged_finish(kf_op *op, LobWork<float> &W, const float *X, int wx, f
     return r1;
 }
 
+// The Rayleigh-Ritz Gram blocks of [X_a Q] against [Y HZ] in one tensor-core launch when it fits
+// (rows X_a, Q; columns Y, HZ): the caller unpacks the blocks it needs from the (na + k)^2 result.
+static bool rr_gram_merged(LobWork<float> &W, const float *Xa, const float *Q, const float *Y, const float *HZ, int na,
+                           int k, cudaStream_t s) {
+    if (W.N < GRAM_TC_MIN_ROWS) return false;
+    const int64_t N = W.N;
+    const GramTcSrc src[4] = {{Xa, N, na}, {Q, N, k}, {Y, N, na}, {HZ, N, k}};
+    return gram_tc(src, 4, 0, 2, 2, 4, N, W.dG.as<double>(), W.dpart.as<double>(), W.part_bytes, s);
+}
+
 template <typename T>
 static LobOut lobpcg_run(kf_op *op, LobWork<T> &Wk, const double *D, const LobParams &prm, cudaStream_t s,
                          std::vector<double> &theta) {
@@ -554,14 +565,32 @@ static LobOut lobpcg_run(kf_op *op, LobWork<T> &Wk, const double *D, const LobPa
         auto apply_rr = [&]() {
             launch_apply(op, f32, Qc, HZ, N, N, k, 1, 0, nullptr, 0, 0, s);
             out.nmv += k;
-            double *G2 = G + (size_t)na3 * na3, *G3 = G2 + (size_t)na3 * k;
-            gram<T>(Xa, N, na3, HXa, N, na3, N, G, part, s);
-            gram<T>(Xa, N, na3, HZ, N, k, N, G2, part, s);
-            gram<T>(Qc, N, k, HZ, N, k, N, G3, part, s);
+            bool one = false;
+            if constexpr (merged)
+                one = rr_gram_merged(Wk, (const float *)Xa, (const float *)Qc, (const float *)HXa, (const float *)HZ,
+                                     na3, k, s);
+            if (!one) {
+                double *G2 = G + (size_t)na3 * na3, *G3 = G2 + (size_t)na3 * k;
+                gram<T>(Xa, N, na3, HXa, N, na3, N, G, part, s);
+                gram<T>(Xa, N, na3, HZ, N, k, N, G2, part, s);
+                gram<T>(Qc, N, k, HZ, N, k, N, G3, part, s);
+            }
             if (merged)
                 KF_CUDA(cudaMemcpyAsync(Wk.hstat.template as<int>(), Wk.dstat.template as<int>(), sizeof(int),
                                         cudaMemcpyDeviceToHost, s));
-            d2h_sync<T>(hG, G, (size_t)na3 * na3 + (size_t)na3 * k + (size_t)k * k, s);
+            const int ld = na3 + k;
+            d2h_sync<T>(hG, G, one ? (size_t)ld * ld : (size_t)na3 * na3 + (size_t)na3 * k + (size_t)k * k, s);
+            if (one) {
+                // [X_a Q]'[HX_a HZ] -> X_a' H X_a, X_a' H Z, Q' H Z as three packed blocks
+                std::vector<double> g(hG, hG + (size_t)ld * ld);
+                double *b1 = hG, *b2 = hG + (size_t)na3 * na3, *b3 = b2 + (size_t)na3 * k;
+                for (int j = 0; j < na3; ++j)
+                    for (int i = 0; i < na3; ++i) b1[i + (size_t)na3 * j] = g[i + (size_t)ld * j];
+                for (int j = 0; j < k; ++j)
+                    for (int i = 0; i < na3; ++i) b2[i + (size_t)na3 * j] = g[i + (size_t)ld * (na3 + j)];
+                for (int j = 0; j < k; ++j)
+                    for (int i = 0; i < k; ++i) b3[i + (size_t)k * j] = g[(na3 + i) + (size_t)ld * (na3 + j)];
+            }
         };
         apply_rr();
         if constexpr (merged) {
@@ -768,12 +797,27 @@ static LobOut lobpcg_refine(kf_op *op, RefineWork &Rw, LobWork<float> &Wk, const
         auto apply_rr = [&]() {
             launch_apply(op, true, Q, HZ, N, N, k, 1, 0, nullptr, 0, 0, s);
             out.nmv += k;
-            double *G2 = G + (size_t)na3 * na3, *G3 = G2 + (size_t)na3 * k;
-            gram<float>(Xa32, N, na3, Ra, N, na3, N, G, part, s);
-            gram<float>(Ra, N, na3, Q, N, k, N, G2, part, s);
-            gram<float>(Q, N, k, HZ, N, k, N, G3, part, s);
+            // one tensor-core Gram [X_a Q]'[R HZ] holds X_a' R, (R' Q)' and Q' H Z
+            const bool one = rr_gram_merged(Wk, Xa32, Q, Ra, HZ, na3, k, s);
+            if (!one) {
+                double *G2 = G + (size_t)na3 * na3, *G3 = G2 + (size_t)na3 * k;
+                gram<float>(Xa32, N, na3, Ra, N, na3, N, G, part, s);
+                gram<float>(Ra, N, na3, Q, N, k, N, G2, part, s);
+                gram<float>(Q, N, k, HZ, N, k, N, G3, part, s);
+            }
             KF_CUDA(cudaMemcpyAsync(Wk.hstat.as<int>(), Wk.dstat.as<int>(), sizeof(int), cudaMemcpyDeviceToHost, s));
-            d2h_sync<double>(hG, G, (size_t)na3 * na3 + (size_t)na3 * k + (size_t)k * k, s);
+            const int ld = na3 + k;
+            d2h_sync<double>(hG, G, one ? (size_t)ld * ld : (size_t)na3 * na3 + (size_t)na3 * k + (size_t)k * k, s);
+            if (one) {
+                std::vector<double> g(hG, hG + (size_t)ld * ld);
+                double *b1 = hG, *b2 = hG + (size_t)na3 * na3, *b3 = b2 + (size_t)na3 * k;
+                for (int j = 0; j < na3; ++j)
+                    for (int i = 0; i < na3; ++i) b1[i + (size_t)na3 * j] = g[i + (size_t)ld * j];
+                for (int j = 0; j < k; ++j)   // R' Q = (Q' R)'
+                    for (int i = 0; i < na3; ++i) b2[i + (size_t)na3 * j] = g[(na3 + j) + (size_t)ld * i];
+                for (int j = 0; j < k; ++j)
+                    for (int i = 0; i < k; ++i) b3[i + (size_t)k * j] = g[(na3 + i) + (size_t)ld * (na3 + j)];
+            }
         };
         apply_rr();
         if (*Wk.hstat.as<int>() != 0) {

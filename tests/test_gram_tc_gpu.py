@@ -16,7 +16,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def _run(blocks, r0, r1, c0, c1, N, reps=1, accs=0):
+def _run(blocks, r0, r1, c0, c1, N, reps=1):
     """blocks: torch (k x ld) FP32 tensors = column-major N x k blocks, leading dimension ld."""
     from kfgpu import _abi
     ns = len(blocks)
@@ -28,14 +28,13 @@ def _run(blocks, r0, r1, c0, c1, N, reps=1, accs=0):
     G = np.zeros(nr * nc)
     ms = C.c_float(0)
     st = _abi.lib().kf_test_gram_tc(C.cast(ptrs, C.c_void_p), C.cast(lds, C.c_void_p), C.cast(ks, C.c_void_p), ns,
-                                    r0, r1, c0, c1, N, accs, reps, None, C.byref(ms),
-                                    G.ctypes.data_as(C.c_void_p))
+                                    r0, r1, c0, c1, N, reps, None, C.byref(ms), G.ctypes.data_as(C.c_void_p))
     return st, G.reshape(nc, nr).T, ms.value
 
 
-def _check(torch, blocks, r0, r1, c0, c1, N, accs=0):
+def _check(torch, blocks, r0, r1, c0, c1, N):
     from kfgpu import _abi
-    st, G, _ = _run(blocks, r0, r1, c0, c1, N, accs=accs)
+    st, G, _ = _run(blocks, r0, r1, c0, c1, N)
     _abi.check(st)
     R = torch.cat([b[:, :N] for b in blocks[r0:r1]]).double()
     Q = torch.cat([b[:, :N] for b in blocks[c0:c1]]).double()
@@ -52,17 +51,17 @@ def _blocks(torch, widths, N, ld=None, seed=0):
 
 
 POOLS = [
-    # (widths, r0, r1, c0, c1, N)
-    ((16, 32), 0, 2, 1, 2, 671744),              # [X Z]'Z, block 16
-    ((20, 40), 0, 2, 1, 2, 671744),              # [X Z]'Z, block 20
+    # (widths, r0, r1, c0, c1, N); the pools up to 64 rows take one MMA per K step, the others two
+    ((16, 32), 0, 2, 1, 2, 671744),              # [X Z]'Z, block 16 (64-row pool)
+    ((20, 40), 0, 2, 1, 2, 671744),              # [X Z]'Z, block 20 (128-row pool)
     ((16, 32, 16, 32), 0, 2, 2, 4, 671744),      # [X_a Q]'[HX_a HZ]
-    ((20, 40, 20, 40), 0, 2, 2, 4, 671744),
-    ((20, 20, 40, 40), 0, 3, 1, 4, 671744),      # [X_a R Q]'[R Q HZ]: B window past pool row 128
+    ((20, 40, 20, 40), 0, 2, 2, 4, 671744),      # also the refinement's [X_a Q]'[R HZ]
+    ((8, 16, 24), 0, 2, 1, 3, 131072),           # a source both in the rows and the columns
     ((16,), 0, 1, 0, 1, 671744),                 # self Gram
+    ((32, 32), 0, 2, 0, 2, 110592),              # self Gram of 64 columns
     ((7, 13), 0, 2, 1, 2, 100000),
     ((1, 3), 0, 1, 1, 2, 5000),
-    ((3, 5, 2, 9), 1, 3, 2, 4, 131072),
-    ((64, 64), 0, 2, 0, 2, 110592),              # 128 pool rows
+    ((3, 5, 2, 9), 1, 3, 2, 4, 131072),          # a source in neither range
     ((12, 24), 0, 2, 1, 2, 33),                  # two chunks, the second one row long
 ]
 
@@ -82,23 +81,14 @@ def test_gram_tc_ragged_rows(cuda, N):
     _check(torch, _blocks(torch, (16, 32), N, ld=ld, seed=N), 0, 2, 1, 2, N)
 
 
-@pytest.mark.parametrize("accs", [1, 2, 3, 5, 8, 12])
-def test_gram_tc_accumulator_counts(cuda, accs):
-    """A chunk's 12 MMAs spread over 1..12 TMEM accumulators (capped by the 512 columns): the same
-    Gram whatever the spread."""
-    torch = cuda
-    _check(torch, _blocks(torch, (16, 32), 131072, seed=accs), 0, 2, 1, 2, 131072, accs=accs)
-    _check(torch, _blocks(torch, (20, 40, 20, 40), 131072, seed=accs), 0, 2, 2, 4, 131072, accs=accs)
-
-
 def test_gram_tc_rejects_unfit_shapes(cuda):
     torch = cuda
     from kfgpu import _abi
     N = 4096
-    # pool rows over 144
-    st, _, _ = _run(_blocks(torch, (80, 80), N), 0, 2, 1, 2, N)
+    # column sources over 64 columns
+    st, _, _ = _run(_blocks(torch, (8, 72), N), 0, 2, 1, 2, N)
     assert st == _abi.KF_EINVAL
-    # rows of G past pool row 128
+    # row-only and column sources over 128 rows
     st, _, _ = _run(_blocks(torch, (64, 64, 8), N), 0, 3, 0, 1, N)
     assert st == _abi.KF_EINVAL
     # leading dimension not a multiple of 4 (16-byte copies)
