@@ -771,49 +771,52 @@ void scale_add(double *Y, const double *X, const double *d, const float *P, floa
 // rows of X'Z first), S = Z'Z - (X'Z)'(X'Z) (the Gram of (I - XX')Z), its Cholesky factor
 // S = R'R (R upper), and the coefficients C = [R^-1 ; -(X'Z) R^-1] ((r + wx) x r) with which
 // [Z X] C = (I - XX') Z R^-1 is orthonormal.  One CTA; *status = 0, or 1 when a pivot is not
-// finite or below 1e-4 (C is then not to be used).  r <= 48 (2 r^2 doubles of shared memory).
+// finite or below 1e-4 (C is then not to be used).  r <= 64 (2 r^2 floats of shared memory).
+// The arithmetic is FP32: Z is an FP32 block that the first pass already orthonormalised, so S is
+// near the identity (a pivot below 1e-4 goes to the host) and FP32 factors are as accurate as the
+// FP32 update that applies them; GB300's FP64 rate made the FP64 version ~50 us.
 __global__ void k_chol2_coeffs(const double *__restrict__ G, int wx, int r, double *__restrict__ C,
                                int *__restrict__ status) {
-    extern __shared__ double cs[];
-    double *S = cs;               // r x r, column-major; becomes R (upper)
-    double *Ri = cs + r * r;      // r x r, R^-1
+    extern __shared__ float cs[];
+    float *S = cs;               // r x r, column-major; becomes R (upper)
+    float *Ri = cs + r * r;      // r x r, R^-1
     __shared__ int bad;
     const int tid = threadIdx.x, nt = blockDim.x;
     const int ld = wx + r;
     if (tid == 0) bad = 0;
     for (int e = tid; e < r * r; e += nt) {
         const int i = e % r, j = e / r;
-        double v = G[wx + i + (size_t)ld * j];
-        for (int q = 0; q < wx; ++q) v -= G[q + (size_t)ld * i] * G[q + (size_t)ld * j];
+        float v = (float)G[wx + i + (size_t)ld * j];
+        for (int q = 0; q < wx; ++q) v = fmaf(-(float)G[q + (size_t)ld * i], (float)G[q + (size_t)ld * j], v);
         S[e] = v;
-        Ri[e] = 0.0;
+        Ri[e] = 0.f;
     }
     __syncthreads();
     // right-looking Cholesky, upper factor: column k of R is row k of the trailing matrix
     for (int k = 0; k < r; ++k) {
         if (tid == 0) {
-            const double d = S[k + r * k];
+            const float d = S[k + r * k];
             // S is the Gram of a block the first pass already orthonormalised (S ~ I): a pivot
             // below 1e-4 is a nearly dependent direction, left to the host's SVQB
-            if (!(d > 1e-4) || !isfinite(d)) bad = 1;
-            S[k + r * k] = sqrt(d > 0.0 ? d : 1.0);
+            if (!(d > 1e-4f) || !isfinite(d)) bad = 1;
+            S[k + r * k] = sqrtf(d > 0.f ? d : 1.f);
         }
         __syncthreads();
-        const double rkk = S[k + r * k];
+        const float rkk = S[k + r * k];
         for (int j = k + 1 + tid; j < r; j += nt) S[k + r * j] /= rkk;
         __syncthreads();
         for (int e = tid; e < (r - k - 1) * (r - k - 1); e += nt) {
             const int i = k + 1 + e % (r - k - 1), j = k + 1 + e / (r - k - 1);
-            if (i <= j) S[i + r * j] -= S[k + r * i] * S[k + r * j];
+            if (i <= j) S[i + r * j] = fmaf(-S[k + r * i], S[k + r * j], S[i + r * j]);
         }
         __syncthreads();
     }
     // R^-1 column by column (back substitution), one thread per column
     for (int j = tid; j < r; j += nt) {
-        Ri[j + r * j] = 1.0 / S[j + r * j];
+        Ri[j + r * j] = 1.f / S[j + r * j];
         for (int i = j - 1; i >= 0; --i) {
-            double v = 0.0;
-            for (int k = i + 1; k <= j; ++k) v += S[i + r * k] * Ri[k + r * j];
+            float v = 0.f;
+            for (int k = i + 1; k <= j; ++k) v = fmaf(S[i + r * k], Ri[k + r * j], v);
             Ri[i + r * j] = -v / S[i + r * i];
         }
     }
@@ -821,23 +824,23 @@ __global__ void k_chol2_coeffs(const double *__restrict__ G, int wx, int r, doub
     const int lc = r + wx;
     for (int e = tid; e < lc * r; e += nt) {
         const int i = e % lc, j = e / lc;
-        double v;
+        float v;
         if (i < r) {
             v = Ri[i + r * j];
         } else {
             const int q = i - r;
-            v = 0.0;
-            for (int t = 0; t <= j; ++t) v += G[q + (size_t)ld * t] * Ri[t + r * j];
+            v = 0.f;
+            for (int t = 0; t <= j; ++t) v = fmaf((float)G[q + (size_t)ld * t], Ri[t + r * j], v);
             v = -v;
         }
-        C[i + (size_t)lc * j] = v;
+        C[i + (size_t)lc * j] = (double)v;
     }
     if (tid == 0) *status = bad;
 }
 
 void chol2_coeffs(const double *G, int wx, int r, double *C, int *status, cudaStream_t s) {
     KF_REQUIRE(r >= 1 && r <= CHOL2_MAX_R, KF_EINVAL, "chol2_coeffs: block width out of range");
-    const size_t smem = (size_t)2 * r * r * sizeof(double);
+    const size_t smem = (size_t)2 * r * r * sizeof(float);
     k_chol2_coeffs<<<1, 256, smem, s>>>(G, wx, r, C, status);
     KF_LAUNCH_CHECK();
 }

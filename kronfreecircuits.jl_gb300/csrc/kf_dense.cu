@@ -8,6 +8,8 @@
 // Tile: 64 rows x 64 columns x 16 reduction per step, 256 threads, a 4 x 4 register tile per
 // thread.  The X tile loader walks l fastest when the axis stride is > 1 (coalesced along l) and
 // j fastest when the axis is the leading one (coalesced along j).
+#include <algorithm>
+
 #include "kf_internal.h"
 
 namespace kf {
@@ -115,34 +117,52 @@ template void mode_product<float>(float *, int64_t, const float *, int64_t, cons
 template void mode_product<double>(double *, int64_t, const double *, int64_t, const double *, int, int64_t, int64_t,
                                    int64_t, double, double, cudaStream_t);
 
+constexpr int SEP_SCALE_MAX_K = 256;   // columns per scale pass
+
 // W[:, j] <- W[:, j] / hypot(S(p) - theta_j, eta) with S(p) = sum_a lam_a[i_a(p)] (the separable
-// spectrum evaluated from per-axis eigenvalues, no N-sized table).  The sum is FP64 (S and theta
-// are close where it matters); the scale is FP32 -- it only steers the search directions, and
-// GB300's FP64 hypot / divide rate would make this pass FP64-bound.
+// spectrum evaluated from per-axis eigenvalues, no N-sized table).  One thread per grid point: the
+// point's indices and S(p) (FP64, one sum per point) serve every column.  S and theta are close
+// where it matters, so both are split into FP32 hi + lo parts and S - theta = (S_hi - theta_hi) +
+// (S_lo - theta_lo), the first difference exact there; the scale itself is FP32 -- it only steers
+// the search directions, and GB300's FP64 rate would make a per-element FP64 pass FP64-bound.
 template <typename T>
 __global__ void k_sep_scale(T *__restrict__ W, int64_t ld, int64_t N, int k, int ndims, const int *__restrict__ dims,
                             const double *__restrict__ lam, const int *__restrict__ lam_off,
                             const double *__restrict__ theta, double eta) {
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= N * k) return;
-    const int64_t c = t / N, p = t % N;
-    int64_t rem = p;
-    double S = -theta[c];
-    for (int a = 0; a < ndims; ++a) {
-        const int i = (int)(rem % dims[a]);
-        rem /= dims[a];
-        S += lam[lam_off[a] + i];
+    __shared__ float th_hi[SEP_SCALE_MAX_K], th_lo[SEP_SCALE_MAX_K];
+    for (int c = threadIdx.x; c < k; c += blockDim.x) {
+        const float h = (float)theta[c];
+        th_hi[c] = h;
+        th_lo[c] = (float)(theta[c] - (double)h);
     }
-    const float f = 1.0f / hypotf((float)S, (float)eta);
-    W[c * ld + p] = W[c * ld + p] * (T)f;
+    __syncthreads();
+    const float eta2 = (float)(eta * eta);
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < N; p += (int64_t)gridDim.x * blockDim.x) {
+        uint32_t rem = (uint32_t)p;
+        double S = 0.0;
+        for (int a = 0; a < ndims; ++a) {
+            const uint32_t d = (uint32_t)dims[a];
+            const uint32_t i = rem % d;
+            rem /= d;
+            S += lam[lam_off[a] + (int)i];
+        }
+        const float s_hi = (float)S, s_lo = (float)(S - (double)s_hi);
+        for (int c = 0; c < k; ++c) {
+            const float dlt = (s_hi - th_hi[c]) + (s_lo - th_lo[c]);
+            const float f = rsqrtf(fmaf(dlt, dlt, eta2));
+            W[c * ld + p] = W[c * ld + p] * (T)f;
+        }
+    }
 }
 
 template <typename T>
 void sep_scale(T *W, int64_t ld, int64_t N, int k, int ndims, const int *dims, const double *lam, const int *lam_off,
                const double *theta, double eta, cudaStream_t s) {
     if (k <= 0) return;
-    const int64_t tot = N * k;
-    k_sep_scale<T><<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(W, ld, N, k, ndims, dims, lam, lam_off, theta, eta);
+    KF_REQUIRE(k <= SEP_SCALE_MAX_K, KF_EINVAL, "sep_scale: too many columns");
+    KF_REQUIRE(N < ((int64_t)1 << 32), KF_EINVAL, "sep_scale: operator dimension too large");
+    const int64_t blocks = std::min<int64_t>((N + 255) / 256, 152 * 8);
+    k_sep_scale<T><<<(unsigned)blocks, 256, 0, s>>>(W, ld, N, k, ndims, dims, lam, lam_off, theta, eta);
     KF_LAUNCH_CHECK();
 }
 

@@ -220,7 +220,7 @@ bool gram_tc(const GramTcSrc *src, int nsrc, int r0, int r1, int c0, int c1, int
 size_t gram_tc_partials_size(int nr, int nc);
 // second orthogonalisation pass on the device: from G = [X Z]'Z, coefficients C ((r + wx) x r)
 // with [Z X] C orthonormal and orthogonal to X (Cholesky of Z'Z - (X'Z)'(X'Z)); *status 1 on failure
-constexpr int CHOL2_MAX_R = 48;
+constexpr int CHOL2_MAX_R = 64;
 void chol2_coeffs(const double *G, int wx, int r, double *C, int *status, cudaStream_t s);
 // Y[:, j] = d_j X[:, j] + (double) P[:, j] and Y32 = FP32(Y) (leading dimension N)
 void scale_add(double *Y, const double *X, const double *d, const float *P, float *Y32, int k, int64_t N,
