@@ -412,7 +412,7 @@ def time_update(torch, path, kx0, kx1, ky, N, reps=10):
     return ms.value / 1e3
 
 
-UPDATE_SHAPES = ((32, 16, 32), (16, 32, 16), (16, 0, 16), (2, 0, 1))
+UPDATE_SHAPES = ((32, 16, 32), (36, 18, 36), (18, 36, 18), (16, 32, 16), (16, 0, 16), (2, 0, 1))
 
 
 def run_update_workload(args):

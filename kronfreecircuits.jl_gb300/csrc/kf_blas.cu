@@ -518,6 +518,11 @@ void update(T *Y, int64_t ldy, int ky, const T *X, int64_t ldx, int kx, const do
             for (int j = 0; j < ky; ++j) KF_CUDA(cudaMemsetAsync(Y + (int64_t)j * ldy, 0, N * sizeof(T), s));
         return;
     }
+    if constexpr (sizeof(T) == 4) {
+        if (N >= 4096 && update_pipe((float *)Y, ldy, ky, nullptr, 0, 0, (const float *)X, ldx, kx, nullptr, 0, 0, C,
+                                     ldc, alpha, beta, N, s))
+            return;
+    }
     const unsigned grid = (unsigned)((N + 255) / 256);
     constexpr int UC = sizeof(T) == 8 ? 4 : 8;
     const int kyp = (ky + UC - 1) / UC * UC;
@@ -549,8 +554,13 @@ void update2(T *Y, int64_t ldy, int ky, const T *X0, int64_t ldx0, int kx0, cons
              const double *C, int ldc, double alpha, double beta, int64_t N, cudaStream_t s, bool allow_tc) {
     if (ky <= 0 || N <= 0) return;
     if constexpr (sizeof(T) == 4) {
-        // wide FP32 updates (kx ky >= 1024, e.g. the orthogonalisation's [Z X] -> Z at 48 -> 32) are
-        // FMA-bound on the SIMT pipes; the tcgen05 kernel (TF32 hi / lo) measured faster there
+        // up to 64 x 64: the pipelined SIMT kernel (loads overlapped with the FMAs)
+        if (N >= 4096 && kx0 > 0 &&
+            update_pipe((float *)Y, ldy, ky, nullptr, 0, 0, (const float *)X0, ldx0, kx0, (const float *)X1, ldx1, kx1,
+                        C, ldc, alpha, beta, N, s))
+            return;
+        // wider FP32 updates are FMA-bound on the SIMT pipes; the tcgen05 kernel (TF32 hi / lo)
+        // measured faster there
         const int kx = kx0 + kx1;
         if (allow_tc && N >= 65536 && update_tc_ok(kx, ky) && kx * ky >= 1024) {
             update_tc((float *)Y, ldy, ky, (const float *)X0, ldx0, kx0, (const float *)X1, ldx1, kx1, C, ldc, alpha,

@@ -231,6 +231,11 @@ void add_f32_into_f64(double *Y, int64_t ldy, const float *P, int64_t ldp, float
 void gram32_sets(const float *A0, int64_t lda0, int ka0, const float *A1, int64_t lda1, int ka1, const float *B0,
                  int64_t ldb0, int kb0, const float *B1, int64_t ldb1, int kb1, int64_t N, double *G, double *partials,
                  cudaStream_t s, bool allow_tc = true);
+// FP32 [Y0 Y1] = alpha [X0 X1] C + beta [Y0 Y1] (ky0 + ky1 <= 64 outputs, kx0 + kx1 <= 64 inputs,
+// X blocks 16-byte aligned with ld % 4 == 0), a pipelined SIMT kernel; false when it does not apply
+bool update_pipe(float *Y0, int64_t ldy0, int ky0, float *Y1, int64_t ldy1, int ky1, const float *X0, int64_t ldx0,
+                 int kx0, const float *X1, int64_t ldx1, int kx1, const double *C, int ldc, double alpha, double beta,
+                 int64_t N, cudaStream_t s);
 // Y = alpha [X0 X1] C + beta Y
 template <typename T>
 void update2(T *Y, int64_t ldy, int ky, const T *X0, int64_t ldx0, int kx0, const T *X1, int64_t ldx1, int kx1,

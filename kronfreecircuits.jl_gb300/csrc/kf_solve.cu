@@ -619,14 +619,20 @@ static LobOut lobpcg_run(kf_op *op, LobWork<T> &Wk, const double *D, const LobPa
         std::vector<double> lam(ns), V((size_t)ns * ns);
         if (timed_sym_eig(ns, A.data(), ns, lam.data(), V.data(), ns) != 0)
             throw Error(KF_EBREAKDOWN, "LOBPCG: Rayleigh-Ritz eigenproblem did not converge");
-        // C = V[:, 0:na3]  (ns x na3)
+        // C = V[:, 0:na3] (ns x na3), then [0; C_z] beside it: [X_new P_new] = [X_a Q] [C | [0; C_z]]
         std::memcpy(hC, V.data(), sizeof(double) * (size_t)ns * na3);
-        h2d(C, hC, (size_t)ns * na3, s);
+        for (int j = 0; j < na3; ++j)
+            for (int i = 0; i < ns; ++i) hC[(size_t)ns * (na3 + j) + i] = i < na3 ? 0.0 : V[i + (size_t)ns * j];
+        h2d(C, hC, (size_t)ns * 2 * na3, s);
         // X_act <- Xa Cx + Q Cz ; HX likewise ; P <- Q Cz
         T *Xna = Xn + (int64_t)nl * N, *HXna = HXn + (int64_t)nl * N;
-        update2<T>(Xna, N, na3, Xa, N, na3, Qc, N, k, C, ns, 1.0, 0.0, N, s);
+        bool fused = false;
+        if constexpr (merged)
+            fused = update_pipe((float *)Xna, N, na3, (float *)Pn, N, na3, (const float *)Xa, N, na3,
+                                (const float *)Qc, N, k, C, ns, 1.0, 0.0, N, s);
+        if (!fused) update2<T>(Xna, N, na3, Xa, N, na3, Qc, N, k, C, ns, 1.0, 0.0, N, s);
         update2<T>(HXna, N, na3, HXa, N, na3, HZ, N, k, C, ns, 1.0, 0.0, N, s);
-        update<T>(Pn, N, na3, Qc, N, k, C + na3, ns, 1.0, 0.0, N, s);
+        if (!fused) update<T>(Pn, N, na3, Qc, N, k, C + na3, ns, 1.0, 0.0, N, s);
         np = na3;
         std::swap(X, Xn);
         std::swap(HX, HXn);
