@@ -13,8 +13,11 @@ fresh FP64 application.
   e2e              the public API end to end with host buffers: kf_op_create from the host term
                    list, solve (product seed built by the library), host eigenpairs out, kf_op_destroy,
                    every step
-  roofline         the fused stencil apply (FP32, 16 columns): algorithmic bytes 2 N b 4 per launch
-                   over its CUDA-event time, against the measured HBM copy bandwidth
+  roofline         the dominant kernel of a warm solve by the ncu launch list, the separable
+                   preconditioner's tcgen05 mode product (256-point axis, 18 columns): algorithmic
+                   bytes 2 N b 4 per launch over its CUDA-event time, against the measured HBM copy
+                   bandwidth; roofline_gram / roofline_apply: the tensor-core Gram of the
+                   orthogonalisation ([X Z]'Z, 18 + 36 columns, N b 4) and the fused stencil apply
   cpu_baseline     the oracle's restatement of the reference CPU path (C/OpenMP mul! + NumPy LOBPCG)
                    on the host cores, a bounded sample
 
@@ -42,11 +45,14 @@ for _p in (ROOT, PKG):
 M_PAIRS = 12
 SEED = 20261205          # theta draws of the three-mode leaf workload
 NDRAWS = 64
-# ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch (profiles/*.md): the FP32 16-column
-# fused apply at N = 671,744 (written Y stays in L2: reads 45.7 MB, writes 9.9 MB); the 16 x 32 FP32
-# Gram (reads 129.0 MB = every element once, writes 3.3 MB of partials)
+# ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch (profiles/*.md), N = 671,744: the
+# FP32 16-column fused apply (written Y stays in L2: reads 45.7 MB, writes 9.9 MB); the tcgen05
+# mode product, 256-point axis, 18 columns (reads 48.7 MB = X once, writes 1.9 MB: Y stays in L2);
+# the tensor-core Gram of [X Z]'Z at 18 + 36 columns (reads 145.2 MB = every element once, writes
+# 0.1 MB of partials)
 APPLY_TRAFFIC_BYTES = 55641088
-GRAM_TRAFFIC_BYTES = 132320768
+MODE_TRAFFIC_BYTES = 50668032
+GRAM_TC_TRAFFIC_BYTES = 145235200
 
 
 def thetas():
@@ -259,12 +265,14 @@ def run_ours(args, D):
     torch.cuda.synchronize()
     te = D.max(time.perf_counter() - t0)
     conv_e = D.sum(conv_e)
-    # roofline of the dominant kernel of a solve (the FP32 Gram product, by the ncu launch list):
-    # the orthogonalisation's X' [W P] at 16 x 32 columns; and of the fused stencil apply
+    # roofline of the dominant kernel of a warm solve (by the ncu launch list: the preconditioner's
+    # tcgen05 mode product), of the tensor-core Gram and of the fused stencil apply
     H0 = ops[idx[0]][0]
     peak, kind = peaks()
-    t_gram = time_gram(torch, 16, 32, H0.N)
-    alg_gram = (16 + 32) * H0.N * 4
+    t_mode = time_mode_product(torch, 1, (41, 256, 64), 1, b=MODE_COLS)
+    alg_mode = 2 * H0.N * MODE_COLS * 4
+    t_gram = time_gram_tc(torch, (18, 36), (0, 2, 1, 2), H0.N)
+    alg_gram = (18 + 36) * H0.N * 4
     t_apply = measure_apply(torch, H0, True)
     alg = 2 * H0.N * 16 * 4
     achieved = alg / t_apply / 1e9
@@ -286,10 +294,14 @@ def run_ours(args, D):
         "max_residual_rel": max(s["max_residual"] / s["hnorm"] for s in stats),
         "e2e": {"value": conv_e / te, "unit": "eigenpairs/s", "h2d_bytes_per_step": int(h2d / ke),
                 "d2h_bytes_per_step": int(d2h / ke), "steps": ke},
-        "roofline": {"bound": "hbm", "achieved": alg_gram / t_gram / 1e9, "peak": peak, "unit": "GB/s",
-                     "frac": alg_gram / t_gram / 1e9 / peak, "traffic": GRAM_TRAFFIC_BYTES,
-                     "kernel": "k_gram32 + k_reduce_partials (FP32 Gram, 16 x 32 columns, N=671,744)",
-                     "algorithmic_bytes": alg_gram, "launch_us": t_gram * 1e6, "peak_kind": kind},
+        "roofline": {"bound": "hbm", "achieved": alg_mode / t_mode / 1e9, "peak": peak, "unit": "GB/s",
+                     "frac": alg_mode / t_mode / 1e9 / peak, "traffic": MODE_TRAFFIC_BYTES,
+                     "kernel": f"k_mode_tc<0> (tcgen05 BF16 mode product, 256-point axis, {MODE_COLS} columns)",
+                     "algorithmic_bytes": alg_mode, "launch_us": t_mode * 1e6, "peak_kind": kind},
+        "roofline_gram": {"bound": "hbm", "achieved": alg_gram / t_gram / 1e9, "peak": peak, "unit": "GB/s",
+                          "frac": alg_gram / t_gram / 1e9 / peak, "traffic": GRAM_TC_TRAFFIC_BYTES,
+                          "kernel": "k_gram_tc + k_reduce_partials_f32 ([X Z]'Z, 18 + 36 FP32 columns)",
+                          "algorithmic_bytes": alg_gram, "launch_us": t_gram * 1e6, "peak_kind": kind},
         "roofline_apply": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                            "traffic": APPLY_TRAFFIC_BYTES, "kernel": "k_apply_fused<float> (16 columns)",
                            "algorithmic_bytes": alg, "launch_us": t_apply * 1e6, "peak_kind": kind},
@@ -396,6 +408,22 @@ def time_gram(torch, ka, kb, N, reps=10, path=0):
 GRAM_SHAPES = ((16, 32), (32, 32), (16, 16), (16, 2), (2, 4))
 
 
+def time_gram_tc(torch, widths, rr, N, reps=10):
+    """Mean device time of one tensor-core Gram of a pool of FP32 blocks (the sources `widths`; rows
+    of G from sources rr[0]..rr[1]-1, columns from rr[2]..rr[3]-1), with its reduction."""
+    import ctypes as C
+    from kfgpu import _abi
+    blocks = [torch.randn(k, N, dtype=torch.float32, device="cuda") for k in widths]
+    ns = len(blocks)
+    ptrs = (C.c_void_p * ns)(*[b.data_ptr() for b in blocks])
+    lds = (C.c_int64 * ns)(*[N] * ns)
+    ks = (C.c_int32 * ns)(*widths)
+    ms = C.c_float(0)
+    _abi.check(_abi.lib().kf_test_gram_tc(C.cast(ptrs, C.c_void_p), C.cast(lds, C.c_void_p), C.cast(ks, C.c_void_p),
+                                          ns, rr[0], rr[1], rr[2], rr[3], N, reps, None, C.byref(ms), None))
+    return ms.value / 1e3
+
+
 def time_update(torch, path, kx0, kx1, ky, N, reps=10):
     """Mean device time of one FP32 block update Y = [X0 X1] C (path 0: SIMT, 1: tcgen05), through
     the library's test-only timing entry point."""
@@ -415,6 +443,20 @@ def time_update(torch, path, kx0, kx1, ky, N, reps=10):
 UPDATE_SHAPES = ((32, 16, 32), (36, 18, 36), (18, 36, 18), (16, 32, 16), (16, 0, 16), (2, 0, 1))
 
 
+def time_update_f64(torch, path, kx, ky, N, reps=10):
+    """Mean device time of one FP64 block update Y = X C (path 0: the FP64 kernel, 1: double-float
+    arithmetic on the FP32 pipes), through the library's test-only timing entry point."""
+    import ctypes as C
+    from kfgpu import _abi
+    X = torch.randn(kx, N, dtype=torch.float64, device="cuda")
+    Y = torch.empty(ky, N, dtype=torch.float64, device="cuda")
+    Cm = np.asfortranarray(np.random.default_rng(0).standard_normal((kx, ky)))
+    ms = C.c_float(0)
+    _abi.check(_abi.lib().kf_test_update_f64(path, C.c_void_p(Y.data_ptr()), C.c_void_p(X.data_ptr()), kx, ky,
+                                             Cm.ctypes.data_as(C.c_void_p), N, reps, None, C.byref(ms)))
+    return ms.value / 1e3
+
+
 def run_update_workload(args):
     """The FP32 block updates of LOBPCG on N = 671,744 rows: tcgen05 (TF32 hi / lo) and SIMT."""
     import torch
@@ -427,6 +469,10 @@ def run_update_workload(args):
             key = f"update_{kx0}+{kx1}_to_{ky}_{name}"
             out[key + "_us"] = t * 1e6
             out[key + "_gbs"] = (kx0 + kx1 + ky) * N * 4 / t / 1e9
+    for path, name in ((0, "f64"), (1, "double_float")):
+        t = time_update_f64(torch, path, 18, 18, N)
+        out[f"update_f64_18_to_18_{name}_us"] = t * 1e6
+        out[f"update_f64_18_to_18_{name}_gbs"] = 36 * N * 8 / t / 1e9
     return out
 
 
@@ -441,24 +487,34 @@ def run_gram_workload(args):
             t = time_gram(torch, ka, kb, N, path=path)
             out[f"{name}_{ka}x{kb}_us"] = t * 1e6
             out[f"{name}_{ka}x{kb}_gbs"] = (ka + kb) * N * 4 / t / 1e9
+    # the solve's tensor-core pools: [X Z]'Z of the orthogonalisation and the merged Rayleigh-Ritz
+    # [X_a Q]'[HX_a HZ] (block 18 = 12 + 4 guards + 2 buffer columns)
+    for name, widths, rr in (("xz", (18, 36), (0, 2, 1, 2)), ("rr", (18, 36, 18, 36), (0, 2, 2, 4))):
+        t = time_gram_tc(torch, widths, rr, N)
+        out[f"tc_pool_{name}_us"] = t * 1e6
+        out[f"tc_pool_{name}_gbs"] = sum(widths) * N * 4 / t / 1e9
     return out
 
 
+MODE_COLS = 18   # the active block of a solve with m = 12, 4 guards, 2 buffer columns
+
+
 def run_mode_workload(args):
-    """The separable preconditioner's mode products on the three-mode leaf grid (16 FP32 columns):
-    tensor cores (tcgen05, BF16 operands) and the SIMT FP32 kernel, per non-diagonal axis."""
+    """The separable preconditioner's mode products on the three-mode leaf grid (18 FP32 columns, the
+    active block of a solve): tensor cores (tcgen05, BF16 operands) and the SIMT FP32 kernel, per
+    non-diagonal axis."""
     import torch
     dims = (41, 256, 64)
     N = int(np.prod(dims))
     peak, kind = peaks()
-    out = {"workload": "mode products, three-mode grid 41x256x64 (N=671,744), 16 FP32 columns"}
+    out = {"workload": f"mode products, three-mode grid 41x256x64 (N=671,744), {MODE_COLS} FP32 columns"}
     for axis in (1, 2):
         for path, name in ((1, "tc"), (0, "simt")):
-            t = time_mode_product(torch, path, dims, axis)
-            by = 2 * N * 16 * 4
+            t = time_mode_product(torch, path, dims, axis, b=MODE_COLS)
+            by = 2 * N * MODE_COLS * 4
             out[f"axis{axis}_{name}_us"] = t * 1e6
             out[f"axis{axis}_{name}_gbs"] = by / t / 1e9
-            out[f"axis{axis}_{name}_tflops"] = 2 * N * dims[axis] * 16 / t / 1e12
+            out[f"axis{axis}_{name}_tflops"] = 2 * N * dims[axis] * MODE_COLS / t / 1e12
     out["hbm_peak_gbs"] = peak
     out["peak_kind"] = kind
     return out

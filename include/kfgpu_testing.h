@@ -54,6 +54,14 @@ int kf_test_gram_tc(const float *const *srcs, const int64_t *lds, const int32_t 
                     float *ms_per_launch, double *G_out);
 
 /*
+ * The FP64 block update Y = X C (device blocks X: N x kx, Y: N x ky, leading dimension N; C: host,
+ * kx x ky column-major FP64), `reps` times on `stream`: path 0 the FP64 kernel, path 1 double-float
+ * arithmetic on the FP32 pipes (kx, ky <= 32).  *ms_per_launch: mean device time.
+ */
+int kf_test_update_f64(int path, double *Y, const double *X, int kx, int ky, const double *C, int64_t N, int reps,
+                       void *stream, float *ms_per_launch);
+
+/*
  * The FP32 block update Y = alpha [X0 X1] C + beta Y (device blocks: X0 N x kx0, X1 N x kx1 (kx1 may
  * be 0), Y N x ky; C: host, (kx0 + kx1) x ky, column-major FP64, leading dimension ldc), `reps`
  * times on `stream`, timed with CUDA events: path 0 the SIMT kernel, path 1 the tcgen05 kernel

@@ -387,6 +387,37 @@ int kf_test_gram_tc(const float *const *srcs, const int64_t *lds, const int32_t 
     });
 }
 
+int kf_test_update_f64(int path, double *Y, const double *X, int kx, int ky, const double *C, int64_t N, int reps,
+                       void *stream, float *ms_per_launch) {
+    return guarded([&] {
+        KF_REQUIRE(Y && X && C && ms_per_launch && reps >= 1 && N >= 1 && kx >= 1 && ky >= 1, KF_EINVAL,
+                   "kf_test_update_f64: bad argument");
+        KF_REQUIRE(path == 0 || (path == 1 && kx <= 32 && ky <= 32), KF_EINVAL, "kf_test_update_f64: bad path");
+        cudaStream_t s = (cudaStream_t)stream;
+        double *dC = nullptr;
+        KF_CUDA(cudaMalloc(&dC, sizeof(double) * (size_t)kx * ky));
+        KF_CUDA(cudaMemcpy(dC, C, sizeof(double) * (size_t)kx * ky, cudaMemcpyHostToDevice));
+        auto launch = [&] {
+            if (path == 1) (void)kf::update_f64_df(Y, N, ky, X, N, kx, dC, kx, N, s);
+            else kf::update<double>(Y, N, ky, X, N, kx, dC, kx, 1.0, 0.0, N, s);
+        };
+        launch();
+        cudaEvent_t e0, e1;
+        KF_CUDA(cudaEventCreate(&e0));
+        KF_CUDA(cudaEventCreate(&e1));
+        KF_CUDA(cudaEventRecord(e0, s));
+        for (int r = 0; r < reps; ++r) launch();
+        KF_CUDA(cudaEventRecord(e1, s));
+        KF_CUDA(cudaEventSynchronize(e1));
+        float ms = 0;
+        KF_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        cudaFree(dC);
+        *ms_per_launch = ms / reps;
+    });
+}
+
 int kf_test_update(int path, float *Y, int64_t ldy, int ky, const float *X0, int64_t ldx0, int kx0, const float *X1,
                    int64_t ldx1, int kx1, const double *C, int ldc, double alpha, double beta, int64_t N, int reps,
                    void *stream, float *ms_per_launch) {

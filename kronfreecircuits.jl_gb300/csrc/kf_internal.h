@@ -236,6 +236,10 @@ void gram32_sets(const float *A0, int64_t lda0, int ka0, const float *A1, int64_
 bool update_pipe(float *Y0, int64_t ldy0, int ky0, float *Y1, int64_t ldy1, int ky1, const float *X0, int64_t ldx0,
                  int kx0, const float *X1, int64_t ldx1, int kx1, const double *C, int ldc, double alpha, double beta,
                  int64_t N, cudaStream_t s);
+// FP64 Y = X C (kx, ky <= 32) in double-float arithmetic on the FP32 pipes (relative error near
+// 2^-46); false when it does not apply
+bool update_f64_df(double *Y, int64_t ldy, int ky, const double *X, int64_t ldx, int kx, const double *C, int ldc,
+                   int64_t N, cudaStream_t s);
 // Y = alpha [X0 X1] C + beta Y
 template <typename T>
 void update2(T *Y, int64_t ldy, int ky, const T *X0, int64_t ldx0, int kx0, const T *X1, int64_t ldx1, int kx1,

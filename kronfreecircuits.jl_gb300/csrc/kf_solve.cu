@@ -884,13 +884,16 @@ static LobOut lobpcg_refine(kf_op *op, RefineWork &Rw, LobWork<float> &Wk, const
             scale_add(HXna, HXa, Rw.dd.as<double>(), T32, HX32a, na3, N, s);
             update<float>(Pn, N, na3, Q, N, k, C + na3, ns, 1.0, 0.0, N, s);
         } else {
-            // a large rotation inside X (Ritz values reordered): X_a C_x in FP64
+            // a large rotation inside X (Ritz values reordered): X_a C_x at FP64 accuracy, in
+            // double-float arithmetic where it applies
             std::memcpy(hC, V.data(), sizeof(double) * (size_t)ns * na3);
             h2d(C, hC, (size_t)ns * na3, s);
-            update<double>(Xna, N, na3, Xa, N, na3, C, ns, 1.0, 0.0, N, s);
+            if (!update_f64_df(Xna, N, na3, Xa, N, na3, C, ns, N, s))
+                update<double>(Xna, N, na3, Xa, N, na3, C, ns, 1.0, 0.0, N, s);
             update<float>(Pn, N, na3, Q, N, k, C + na3, ns, 1.0, 0.0, N, s);
             add_f32_into_f64(Xna, N, Pn, N, X32a, N, na3, N, s);
-            update<double>(HXna, N, na3, HXa, N, na3, C, ns, 1.0, 0.0, N, s);
+            if (!update_f64_df(HXna, N, na3, HXa, N, na3, C, ns, N, s))
+                update<double>(HXna, N, na3, HXa, N, na3, C, ns, 1.0, 0.0, N, s);
             update<float>(T32, N, na3, HZ, N, k, C + na3, ns, 1.0, 0.0, N, s);
             add_f32_into_f64(HXna, N, T32, N, HX32a, N, na3, N, s);
         }
