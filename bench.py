@@ -296,7 +296,7 @@ def run_ours(args, D):
                 "d2h_bytes_per_step": int(d2h / ke), "steps": ke},
         "roofline": {"bound": "hbm", "achieved": alg_mode / t_mode / 1e9, "peak": peak, "unit": "GB/s",
                      "frac": alg_mode / t_mode / 1e9 / peak, "traffic": MODE_TRAFFIC_BYTES,
-                     "kernel": f"k_mode_tc<0> (tcgen05 BF16 mode product, 256-point axis, {MODE_COLS} columns)",
+                     "kernel": f"k_mode_pipe<64> (pipelined tcgen05 BF16 mode product, 256-point axis, {MODE_COLS} columns)",
                      "algorithmic_bytes": alg_mode, "launch_us": t_mode * 1e6, "peak_kind": kind},
         "roofline_gram": {"bound": "hbm", "achieved": alg_gram / t_gram / 1e9, "peak": peak, "unit": "GB/s",
                           "frac": alg_gram / t_gram / 1e9 / peak, "traffic": GRAM_TC_TRAFFIC_BYTES,

@@ -327,11 +327,245 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mode_tc(const TcArgs a) {
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(ncols));
 }
 
+// ---- the BF16 mode product, pipelined -------------------------------------------------------
+//
+// k_mode_tc runs each tile's gather -> MMA -> epilogue one after another, so one CTA per SM waits
+// on global loads, then the tensor pipe, then the stores (0.25 of HBM on the three-mode leaf's
+// 256-point axis).  Here the roles overlap across tiles (the A image stays in shared memory):
+//   warps 0-7   gather tile t's B operand (TN columns q x Kp values of j, rounded to BF16) into
+//               stage t % 2, fence, arrive on full[s];
+//   warp 8      one lane issues the tile's MMA chain into TMEM slot t % 2, commits to empty[s]
+//               (stage free) and accf[slot];
+//   warps 9-12  read their 32 TMEM lanes (rows i of each 128-row A tile), transpose 32 x 32 blocks
+//               through a private shared-memory tile and store Y coalesced along q, arrive on
+//               acce[slot].
+// TN = 64 columns per tile when the operator is 256 long (its 128 KB image leaves room for two
+// 32 KB stages), 128 otherwise.  Every wait is a bounded mbarrier wait (~2 s); on expiry the CTA
+// records KF_ETIMEOUT, every role leaves at its next check, the issuer waits (bounded) for its MMAs
+// in flight and TMEM is freed.
+constexpr int MP_PROD = 256;
+constexpr int MP_THREADS = MP_PROD + 32 + 128;
+constexpr int MP_EPS = 33;   // transpose tile row stride (floats)
+
+__device__ __forceinline__ bool mp_wait(uint64_t *bar, uint32_t n, volatile int *abort) {
+    const uint32_t parity = n & 1u;
+    const long long t0 = clock64();
+    for (;;) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if (*abort) return false;
+        if (clock64() - t0 > TC_WAIT_CYCLES) return false;
+    }
+}
+
+__device__ __forceinline__ void mp_arrive(uint64_t *bar) {
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}\n" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+template <int TN>
+__global__ void __launch_bounds__(MP_THREADS, 1) k_mode_pipe(const TcArgs a) {
+    constexpr int EPC = 8;   // BF16 values per 16-byte core-matrix row
+    extern __shared__ __align__(16) unsigned char mp_smem[];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int Kp = a.Kp, Mp = a.Mp, kg_n = Kp / EPC;
+    const size_t aimg = (size_t)Mp * Kp * 2, bimg = (size_t)TN * Kp * 2;
+    unsigned char *Asm = mp_smem;
+    unsigned char *Bsm = Asm + aimg;                                 // two stages
+    float *Ep = reinterpret_cast<float *>(Bsm + 2 * bimg);          // 4 x [32][MP_EPS]
+    uint64_t *bars = reinterpret_cast<uint64_t *>(Ep + 4 * 32 * MP_EPS);
+    uint64_t *full = bars, *empty = bars + 2, *accf = bars + 4, *acce = bars + 6, *fin = bars + 8;
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(bars + 9);
+    __shared__ volatile int s_abort;
+    const int mtiles = Mp / 128;
+    const uint32_t slot_cols = (uint32_t)(mtiles * TN);   // 128
+    if (tid == 0) {
+        for (int q = 0; q < 2; ++q) {
+            mbar_init(full + q, MP_PROD);
+            mbar_init(empty + q, 1);
+            mbar_init(accf + q, 1);
+            mbar_init(acce + q, 128);
+        }
+        mbar_init(fin, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        s_abort = 0;
+    }
+    if (warp == 8) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(tslot)),
+                     "r"(2u * slot_cols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    {
+        const int n16 = (int)(aimg / 16);
+        uint4 *dst = reinterpret_cast<uint4 *>(Asm);
+        for (int e = tid; e < n16; e += MP_THREADS) dst[e] = a.Aimg[e];
+    }
+    fence_proxy_async();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tslot;
+    const uint32_t sbo = (uint32_t)kg_n * 128;   // 8-row groups of both operands (K extent Kp)
+    const int ntiles = (int)((a.Q + TN - 1) / TN);
+    int my = 0;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) ++my;
+
+    if (warp < 8) {
+        // ---- gather: item (n, kg) = EPC consecutive j of column q = q0 + n
+        const int items = TN * kg_n;
+        for (int k = 0; k < my; ++k) {
+            const int s = k & 1;
+            if (k >= 2 && !mp_wait(empty + s, (uint32_t)(k / 2 - 1), &s_abort)) { s_abort = 1; break; }
+            const int64_t q0 = (int64_t)(blockIdx.x + (int64_t)k * gridDim.x) * TN;
+            unsigned char *B = Bsm + (size_t)s * bimg;
+            for (int e0 = tid; e0 < items; e0 += 4 * MP_PROD) {
+                float v[4][EPC];
+                int nn[4], kk[4];
+#pragma unroll
+                for (int g = 0; g < 4; ++g) {
+                    const int e = e0 + g * MP_PROD;
+                    int n, kg;
+                    if (a.left > 1) { n = e % TN; kg = e / TN; }        // consecutive threads: consecutive l
+                    else { kg = e % kg_n; n = e / kg_n; }               // leading axis: consecutive j
+                    nn[g] = n;
+                    kk[g] = kg;
+                    int64_t xb = -1;
+                    const int64_t q = q0 + n;
+                    if (e < items && q < a.Q) {
+                        const int64_t c = q / a.rows_per_col, qq = q % a.rows_per_col;
+                        const int64_t l = qq % a.left, r = qq / a.left;
+                        xb = c * a.ldx + l + a.left * ((int64_t)a.d * r);
+                    }
+#pragma unroll
+                    for (int t = 0; t < EPC; ++t) {
+                        const int j = kg * EPC + t;
+                        v[g][t] = (xb >= 0 && j < a.d) ? __ldg(a.X + xb + a.left * (int64_t)j) : 0.f;
+                    }
+                }
+#pragma unroll
+                for (int g = 0; g < 4; ++g) {
+                    if (e0 + g * MP_PROD >= items) break;
+                    uint4 pk;
+                    pk.x = pack_bf16x2(v[g][0], v[g][1]);
+                    pk.y = pack_bf16x2(v[g][2], v[g][3]);
+                    pk.z = pack_bf16x2(v[g][4], v[g][5]);
+                    pk.w = pack_bf16x2(v[g][6], v[g][7]);
+                    const size_t at = (size_t)(nn[g] >> 3) * sbo + (size_t)kk[g] * 128 + (nn[g] & 7) * 16;
+                    *reinterpret_cast<uint4 *>(B + at) = pk;
+                }
+            }
+            fence_proxy_async();
+            mp_arrive(full + s);
+        }
+    } else if (warp == 8) {
+        // ---- MMA issuer (one lane)
+        if (lane == 0) {
+            const uint32_t idesc = tc_idesc(128, TN, 1u);
+            const uint32_t a0 = smem_u32(Asm), b0 = smem_u32(Bsm);
+            const int nks = Kp / 16;
+            int issued = 0;
+            for (int k = 0; k < my; ++k) {
+                const int s = k & 1, sl = k & 1;
+                if (!mp_wait(full + s, (uint32_t)(k / 2), &s_abort)) { s_abort = 1; break; }
+                if (k >= 2 && !mp_wait(acce + sl, (uint32_t)(k / 2 - 1), &s_abort)) { s_abort = 1; break; }
+                tc_fence_after();
+                const uint32_t bs = b0 + (uint32_t)(s * bimg);
+                for (int mt = 0; mt < mtiles; ++mt)
+                    for (int ks = 0; ks < nks; ++ks) {
+                        // a K step of 16 BF16 values spans two core matrices (LBO = 128 bytes apart)
+                        const uint64_t ad = tc_desc(a0 + (uint32_t)mt * 16 * sbo + (uint32_t)ks * 256, 128, sbo);
+                        const uint64_t bd = tc_desc(bs + (uint32_t)ks * 256, 128, sbo);
+                        tc_mma<false>(tmem + (uint32_t)sl * slot_cols + (uint32_t)(mt * TN), ad, bd, idesc,
+                                      ks > 0 ? 1u : 0u);
+                    }
+                tc_commit(empty + s);
+                tc_commit(accf + sl);
+                ++issued;
+            }
+            if (issued > 0 && s_abort) {
+                tc_commit(fin);
+                (void)mbar_wait_bounded(fin, 0);
+            }
+        }
+    } else {
+        // ---- epilogue (warps 9-12): TMEM lanes 32 (warp % 4) .. + 31 = rows i of each A tile
+        const int qw = warp & 3;
+        float *T = Ep + qw * 32 * MP_EPS;
+        for (int k = 0; k < my; ++k) {
+            const int sl = k & 1;
+            bool ok = mp_wait(accf + sl, (uint32_t)(k / 2), &s_abort);
+            ok = __all_sync(0xffffffffu, ok);   // tcgen05.ld is warp-collective
+            if (!ok) { s_abort = 1; break; }
+            tc_fence_after();
+            const int64_t q0 = (int64_t)(blockIdx.x + (int64_t)k * gridDim.x) * TN;
+            for (int mt = 0; mt < mtiles; ++mt) {
+                const int i0 = mt * 128 + qw * 32;   // this warp's first row i
+                for (int n0 = 0; n0 < TN; n0 += 32) {
+                    float v[32];
+                    const uint32_t ta = tmem + ((uint32_t)(qw * 32) << 16) + (uint32_t)sl * slot_cols +
+                                        (uint32_t)(mt * TN + n0);
+                    tmem_ld16(ta, v);
+                    tmem_ld16(ta + 16, v + 16);
+                    // this lane's column q = q0 + n0 + lane and its output base
+                    const int64_t q = q0 + n0 + lane;
+                    int64_t yb = -1;
+                    if (q < a.Q) {
+                        const int64_t c = q / a.rows_per_col, qq = q % a.rows_per_col;
+                        const int64_t l = qq % a.left, r = qq / a.left;
+                        yb = c * a.ldy + l + a.left * ((int64_t)a.d * r);
+                    }
+                    if (a.left == 1) {
+                        // leading axis: lanes = consecutive i = consecutive addresses, per column t
+                        const int i = i0 + lane;
+#pragma unroll
+                        for (int t = 0; t < 32; ++t) {
+                            const int64_t ybt = __shfl_sync(0xffffffffu, yb, t);
+                            if (ybt >= 0 && i < a.d) {
+                                float *yp = a.Y + ybt + i;
+                                *yp = (a.beta == 0.f) ? a.alpha * v[t] : a.alpha * v[t] + a.beta * *yp;
+                            }
+                        }
+                    } else {
+                        // transpose 32 rows x 32 columns through this warp's tile, store along q
+#pragma unroll
+                        for (int t = 0; t < 32; ++t) T[lane * MP_EPS + t] = v[t];
+                        __syncwarp();
+                        for (int rr = 0; rr < 32; ++rr) {
+                            const int i = i0 + rr;
+                            if (yb >= 0 && i < a.d) {
+                                float *yp = a.Y + yb + a.left * (int64_t)i;
+                                const float val = T[rr * MP_EPS + lane];
+                                *yp = (a.beta == 0.f) ? a.alpha * val : a.alpha * val + a.beta * *yp;
+                            }
+                        }
+                        __syncwarp();
+                    }
+                }
+            }
+            tc_fence_before();
+            mp_arrive(acce + sl);
+        }
+    }
+    if (s_abort && tid == 0) {
+        *(volatile int *)a.err = KF_ETIMEOUT;
+        __threadfence_system();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 8)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(2u * slot_cols));
+}
+
+static size_t mode_pipe_smem(const TcMatrix &m, int tn) {
+    return (size_t)m.Mp * m.Kp * 2 + (size_t)2 * tn * m.Kp * 2 + (size_t)4 * 32 * MP_EPS * 4 + 10 * 8 + 16;
+}
+
 // host-mapped error word shared by every tensor-core launch
 std::mutex g_tc_mu;
 int *g_tc_err_host = nullptr;
 int *g_tc_err_dev = nullptr;
 bool g_tc_attr = false;
+int g_mp_attr_mask = 0;   // devices whose pipelined-kernel attributes are set
 
 int *tc_err_word() {
     std::lock_guard<std::mutex> lk(g_tc_mu);
@@ -398,6 +632,51 @@ void tc_matrix_free(TcMatrix &m) {
 }
 
 // whether the kernel's shared-memory image of a d x d operator fits this device
+// the pipelined BF16 kernel, one persistent CTA per SM; false when its shared-memory plan does not fit
+static bool mode_pipe(float *Y, int64_t ldy, const float *X, int64_t ldx, const TcMatrix &A, int64_t left, int64_t N,
+                      int64_t b, double alpha, double beta, cudaStream_t s) {
+    const int tn = A.Mp > 128 ? 64 : 128;
+    const size_t smem = mode_pipe_smem(A, tn);
+    int sms = 152, optin = 0, dev = 0;
+    KF_CUDA(cudaGetDevice(&dev));
+    KF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    KF_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    cudaFuncAttributes fa;
+    if (tn == 64) KF_CUDA(cudaFuncGetAttributes(&fa, k_mode_pipe<64>));
+    else KF_CUDA(cudaFuncGetAttributes(&fa, k_mode_pipe<128>));
+    const size_t dyn_max = (size_t)optin - fa.sharedSizeBytes;
+    if (smem > dyn_max) return false;
+    {
+        std::lock_guard<std::mutex> lk(g_tc_mu);
+        if (dev < 31 && !(g_mp_attr_mask & (1 << dev))) {
+            KF_CUDA(cudaFuncSetAttribute(k_mode_pipe<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn_max));
+            KF_CUDA(cudaFuncSetAttribute(k_mode_pipe<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn_max));
+            g_mp_attr_mask |= 1 << dev;
+        }
+    }
+    TcArgs a;
+    a.Y = Y;
+    a.X = X;
+    a.Aimg = reinterpret_cast<const uint4 *>(A.img);
+    a.err = tc_err_word();
+    a.ldy = ldy;
+    a.ldx = ldx;
+    a.left = left;
+    a.rows_per_col = N / A.d;
+    a.Q = a.rows_per_col * b;
+    a.d = A.d;
+    a.Mp = A.Mp;
+    a.Kp = A.Kp;
+    a.ntiles = (int)((a.Q + tn - 1) / tn);
+    a.alpha = (float)alpha;
+    a.beta = (float)beta;
+    const int grid = a.ntiles < sms ? a.ntiles : sms;
+    if (tn == 64) k_mode_pipe<64><<<grid, MP_THREADS, smem, s>>>(a);
+    else k_mode_pipe<128><<<grid, MP_THREADS, smem, s>>>(a);
+    KF_LAUNCH_CHECK();
+    return true;
+}
+
 bool tc_mode_fits(int d, bool split) {
     if (!tc_mode_layout_ok(d)) return false;
     TcMatrix m;
@@ -420,6 +699,9 @@ size_t tc_mode_smem(const TcMatrix &m) {
 void tc_mode_product(float *Y, int64_t ldy, const float *X, int64_t ldx, const TcMatrix &A, int64_t left, int64_t N,
                      int64_t b, double alpha, double beta, cudaStream_t s) {
     if (b <= 0 || N <= 0) return;
+    // operators longer than 128: the pipelined kernel (one CTA per SM, its 128 KB image); shorter
+    // ones keep several serial CTAs per SM, which measured faster (64-point axis: 49.5 vs 72 us)
+    if (!A.split && A.Mp > 128 && mode_pipe(Y, ldy, X, ldx, A, left, N, b, alpha, beta, s)) return;
     const int64_t rows_per_col = N / A.d;
     TcArgs a;
     a.Y = Y;
