@@ -336,16 +336,28 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mode_tc(const TcArgs a) {
 //               stage t % 2, fence, arrive on full[s];
 //   warp 8      one lane issues the tile's MMA chain into TMEM slot t % 2, commits to empty[s]
 //               (stage free) and accf[slot];
-//   warps 9-12  read their 32 TMEM lanes (rows i of each 128-row A tile), transpose 32 x 32 blocks
-//               through a private shared-memory tile and store Y coalesced along q, arrive on
-//               acce[slot].
+//   warps 9-16  read their 32 TMEM lanes (rows i of each 128-row A tile; two warps per lane quarter
+//               share the tile's columns), transpose 32 x 32 blocks through a private
+//               shared-memory tile and store Y coalesced along q, arrive on acce[slot].
+// Column bases come from 32-bit index arithmetic (the host checks the sizes): 64-bit divisions per
+// gathered item made the first version of this kernel gather-bound.
 // TN = 64 columns per tile when the operator is 256 long (its 128 KB image leaves room for two
 // 32 KB stages), 128 otherwise.  Every wait is a bounded mbarrier wait (~2 s); on expiry the CTA
 // records KF_ETIMEOUT, every role leaves at its next check, the issuer waits (bounded) for its MMAs
 // in flight and TMEM is freed.
 constexpr int MP_PROD = 256;
-constexpr int MP_THREADS = MP_PROD + 32 + 128;
+constexpr int MP_EPI = 256;   // epilogue threads: 8 warps, two per TMEM lane quarter
+constexpr int MP_THREADS = MP_PROD + 32 + MP_EPI;
 constexpr int MP_EPS = 33;   // transpose tile row stride (floats)
+constexpr int MP_BG = 4;     // gather items per thread in flight (within the 96 registers of 544 threads)
+
+// the base offset of column q = (c, l, r) of a block: c ld + l + left d r (32-bit quotients)
+__device__ __forceinline__ int64_t mp_base(uint32_t q, int64_t rows_per_col, int64_t left, int d, int64_t ld) {
+    const uint32_t rpc = (uint32_t)rows_per_col, lf = (uint32_t)left;
+    const uint32_t c = q / rpc, qq = q - c * rpc;
+    const uint32_t r = qq / lf, l = qq - r * lf;
+    return (int64_t)c * ld + (int64_t)l + (int64_t)lf * d * (int64_t)r;
+}
 
 __device__ __forceinline__ bool mp_wait(uint64_t *bar, uint32_t n, volatile int *abort) {
     const uint32_t parity = n & 1u;
@@ -371,8 +383,8 @@ __global__ void __launch_bounds__(MP_THREADS, 1) k_mode_pipe(const TcArgs a) {
     const size_t aimg = (size_t)Mp * Kp * 2, bimg = (size_t)TN * Kp * 2;
     unsigned char *Asm = mp_smem;
     unsigned char *Bsm = Asm + aimg;                                 // two stages
-    float *Ep = reinterpret_cast<float *>(Bsm + 2 * bimg);          // 4 x [32][MP_EPS]
-    uint64_t *bars = reinterpret_cast<uint64_t *>(Ep + 4 * 32 * MP_EPS);
+    float *Ep = reinterpret_cast<float *>(Bsm + 2 * bimg);          // 8 x [32][MP_EPS]
+    uint64_t *bars = reinterpret_cast<uint64_t *>(Ep + 8 * 32 * MP_EPS);
     uint64_t *full = bars, *empty = bars + 2, *accf = bars + 4, *acce = bars + 6, *fin = bars + 8;
     uint32_t *tslot = reinterpret_cast<uint32_t *>(bars + 9);
     __shared__ volatile int s_abort;
@@ -383,7 +395,7 @@ __global__ void __launch_bounds__(MP_THREADS, 1) k_mode_pipe(const TcArgs a) {
             mbar_init(full + q, MP_PROD);
             mbar_init(empty + q, 1);
             mbar_init(accf + q, 1);
-            mbar_init(acce + q, 128);
+            mbar_init(acce + q, MP_EPI);
         }
         mbar_init(fin, 1);
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
@@ -417,11 +429,12 @@ __global__ void __launch_bounds__(MP_THREADS, 1) k_mode_pipe(const TcArgs a) {
             if (k >= 2 && !mp_wait(empty + s, (uint32_t)(k / 2 - 1), &s_abort)) { s_abort = 1; break; }
             const int64_t q0 = (int64_t)(blockIdx.x + (int64_t)k * gridDim.x) * TN;
             unsigned char *B = Bsm + (size_t)s * bimg;
-            for (int e0 = tid; e0 < items; e0 += 4 * MP_PROD) {
-                float v[4][EPC];
-                int nn[4], kk[4];
+            // MP_BG items per thread per batch: all their loads in flight together
+            for (int e0 = tid; e0 < items; e0 += MP_BG * MP_PROD) {
+                float v[MP_BG][EPC];
+                int nn[MP_BG], kk[MP_BG];
 #pragma unroll
-                for (int g = 0; g < 4; ++g) {
+                for (int g = 0; g < MP_BG; ++g) {
                     const int e = e0 + g * MP_PROD;
                     int n, kg;
                     if (a.left > 1) { n = e % TN; kg = e / TN; }        // consecutive threads: consecutive l
@@ -429,12 +442,8 @@ __global__ void __launch_bounds__(MP_THREADS, 1) k_mode_pipe(const TcArgs a) {
                     nn[g] = n;
                     kk[g] = kg;
                     int64_t xb = -1;
-                    const int64_t q = q0 + n;
-                    if (e < items && q < a.Q) {
-                        const int64_t c = q / a.rows_per_col, qq = q % a.rows_per_col;
-                        const int64_t l = qq % a.left, r = qq / a.left;
-                        xb = c * a.ldx + l + a.left * ((int64_t)a.d * r);
-                    }
+                    const uint32_t q = (uint32_t)q0 + (uint32_t)n;
+                    if (e < items && q < (uint32_t)a.Q) xb = mp_base(q, a.rows_per_col, a.left, a.d, a.ldx);
 #pragma unroll
                     for (int t = 0; t < EPC; ++t) {
                         const int j = kg * EPC + t;
@@ -442,7 +451,7 @@ __global__ void __launch_bounds__(MP_THREADS, 1) k_mode_pipe(const TcArgs a) {
                     }
                 }
 #pragma unroll
-                for (int g = 0; g < 4; ++g) {
+                for (int g = 0; g < MP_BG; ++g) {
                     if (e0 + g * MP_PROD >= items) break;
                     uint4 pk;
                     pk.x = pack_bf16x2(v[g][0], v[g][1]);
@@ -487,9 +496,10 @@ __global__ void __launch_bounds__(MP_THREADS, 1) k_mode_pipe(const TcArgs a) {
             }
         }
     } else {
-        // ---- epilogue (warps 9-12): TMEM lanes 32 (warp % 4) .. + 31 = rows i of each A tile
-        const int qw = warp & 3;
-        float *T = Ep + qw * 32 * MP_EPS;
+        // ---- epilogue (warps 9-16): TMEM lanes 32 (warp % 4) .. + 31 = rows i of each A tile; the
+        // two warps of a lane quarter take alternate 32-column chunks of the tile
+        const int qw = warp & 3, half = (warp - 9) >> 2;
+        float *T = Ep + (warp - 9) * 32 * MP_EPS;
         for (int k = 0; k < my; ++k) {
             const int sl = k & 1;
             bool ok = mp_wait(accf + sl, (uint32_t)(k / 2), &s_abort);
@@ -499,20 +509,15 @@ __global__ void __launch_bounds__(MP_THREADS, 1) k_mode_pipe(const TcArgs a) {
             const int64_t q0 = (int64_t)(blockIdx.x + (int64_t)k * gridDim.x) * TN;
             for (int mt = 0; mt < mtiles; ++mt) {
                 const int i0 = mt * 128 + qw * 32;   // this warp's first row i
-                for (int n0 = 0; n0 < TN; n0 += 32) {
+                for (int n0 = half * 32; n0 < TN; n0 += 64) {
                     float v[32];
                     const uint32_t ta = tmem + ((uint32_t)(qw * 32) << 16) + (uint32_t)sl * slot_cols +
                                         (uint32_t)(mt * TN + n0);
                     tmem_ld16(ta, v);
                     tmem_ld16(ta + 16, v + 16);
                     // this lane's column q = q0 + n0 + lane and its output base
-                    const int64_t q = q0 + n0 + lane;
-                    int64_t yb = -1;
-                    if (q < a.Q) {
-                        const int64_t c = q / a.rows_per_col, qq = q % a.rows_per_col;
-                        const int64_t l = qq % a.left, r = qq / a.left;
-                        yb = c * a.ldy + l + a.left * ((int64_t)a.d * r);
-                    }
+                    const uint32_t q = (uint32_t)q0 + (uint32_t)(n0 + lane);
+                    const int64_t yb = q < (uint32_t)a.Q ? mp_base(q, a.rows_per_col, a.left, a.d, a.ldy) : -1;
                     if (a.left == 1) {
                         // leading axis: lanes = consecutive i = consecutive addresses, per column t
                         const int i = i0 + lane;
@@ -557,7 +562,7 @@ __global__ void __launch_bounds__(MP_THREADS, 1) k_mode_pipe(const TcArgs a) {
 }
 
 static size_t mode_pipe_smem(const TcMatrix &m, int tn) {
-    return (size_t)m.Mp * m.Kp * 2 + (size_t)2 * tn * m.Kp * 2 + (size_t)4 * 32 * MP_EPS * 4 + 10 * 8 + 16;
+    return (size_t)m.Mp * m.Kp * 2 + (size_t)2 * tn * m.Kp * 2 + (size_t)8 * 32 * MP_EPS * 4 + 10 * 8 + 16;
 }
 
 // host-mapped error word shared by every tensor-core launch
@@ -636,6 +641,8 @@ void tc_matrix_free(TcMatrix &m) {
 static bool mode_pipe(float *Y, int64_t ldy, const float *X, int64_t ldx, const TcMatrix &A, int64_t left, int64_t N,
                       int64_t b, double alpha, double beta, cudaStream_t s) {
     const int tn = A.Mp > 128 ? 64 : 128;
+    // 32-bit column indices (mp_base)
+    if ((N / A.d) * b >= ((int64_t)1 << 31)) return false;
     const size_t smem = mode_pipe_smem(A, tn);
     int sms = 152, optin = 0, dev = 0;
     KF_CUDA(cudaGetDevice(&dev));
@@ -700,7 +707,7 @@ void tc_mode_product(float *Y, int64_t ldy, const float *X, int64_t ldx, const T
                      int64_t b, double alpha, double beta, cudaStream_t s) {
     if (b <= 0 || N <= 0) return;
     // operators longer than 128: the pipelined kernel (one CTA per SM, its 128 KB image); shorter
-    // ones keep several serial CTAs per SM, which measured faster (64-point axis: 49.5 vs 72 us)
+    // ones keep several serial CTAs per SM, which measured as fast (64-point axis: 49.5 us both)
     if (!A.split && A.Mp > 128 && mode_pipe(Y, ldy, X, ldx, A, left, N, b, alpha, beta, s)) return;
     const int64_t rows_per_col = N / A.d;
     TcArgs a;
