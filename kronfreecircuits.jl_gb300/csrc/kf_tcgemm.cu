@@ -1,9 +1,10 @@
 // Block updates Y = alpha [X0 X1] C + beta Y on the tensor cores (tcgen05), FP32 blocks with
-// FP32-accurate products: X and C split into TF32 hi / lo parts, hi*hi + hi*lo + lo*hi per K step.
+// FP32-accurate products: X and C split into TF32 hi / lo parts, hi*hi + hi*lo + lo*hi per K step,
+// in two MMAs (A_hi x [C_hi'; C_lo'], A_lo x C_hi').
 //
 // The tall-skinny product of LOBPCG's orthogonalisation and Rayleigh-Ritz updates (the reference's
 // gemms inside LOBPCGEigensolver, called at src/lobpcg.jl:268, and src/chebyshev.jl:60,79,126): N
-// rows, kx <= 64 inputs, ky <= 128 outputs.  GEMM view: D[128 rows, Np] += A[128 rows, K] B[K, Np]
+// rows, kx <= 64 inputs, ky <= 80 outputs.  GEMM view: D[128 rows, Np] += A[128 rows, K] B[K, Np]
 // per 128-row tile, A = the tile of [X0 X1] (K-major after the gather), B = C' (K-major as C is
 // stored), D in TMEM.
 //
@@ -197,8 +198,13 @@ __global__ void __launch_bounds__(UG_THREADS, 1) k_update_tc(const UgArgs a) {
     } else if (warp == 8) {
         // ---- MMA issuer (one lane)
         if (lane == 0) {
-            const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(Np >> 3) << 17) |
-                                   ((uint32_t)(UG_TM >> 4) << 24);
+            // the lo image of C' follows its hi image row for row, so [C_hi'; C_lo'] is one B operand of
+            // 2 Np rows: A_hi x [C_hi'; C_lo'] gives hi*hi | hi*lo, A_lo x C_hi' gives lo*hi -- two MMAs
+            // per K step (an MMA costs about the same whatever its N)
+            const uint32_t id2 = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(2 * Np >> 3) << 17) |
+                                 ((uint32_t)(UG_TM >> 4) << 24);
+            const uint32_t id1 = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(Np >> 3) << 17) |
+                                 ((uint32_t)(UG_TM >> 4) << 24);
             const uint32_t b0 = su32(Bsm);
             int issued = 0;
             for (int k = 0; k < my; ++k) {
@@ -211,10 +217,9 @@ __global__ void __launch_bounds__(UG_THREADS, 1) k_update_tc(const UgArgs a) {
                 for (int ks = 0; ks < Kp / 8; ++ks) {
                     const uint32_t o = (uint32_t)ks * 256;
                     const uint64_t dah = ug_desc(ah + o, 128, sbo), dal = ug_desc(al + o, 128, sbo);
-                    const uint64_t dbh = ug_desc(b0 + o, 128, sbo), dbl = ug_desc(b0 + (uint32_t)bimg + o, 128, sbo);
-                    ug_mma(d, dah, dbh, idesc, ks > 0 ? 1u : 0u);
-                    ug_mma(d, dah, dbl, idesc, 1u);
-                    ug_mma(d, dal, dbh, idesc, 1u);
+                    const uint64_t dbh = ug_desc(b0 + o, 128, sbo);
+                    ug_mma(d, dah, dbh, id2, ks > 0 ? 1u : 0u);                           // columns 0 .. 2 Np
+                    ug_mma(d + (uint32_t)(2 * Np), dal, dbh, id1, ks > 0 ? 1u : 0u);      // columns 2 Np .. 3 Np
                 }
                 ug_commit(empty + s);
                 ug_commit(accf + sl);
@@ -237,22 +242,31 @@ __global__ void __launch_bounds__(UG_THREADS, 1) k_update_tc(const UgArgs a) {
             const int64_t row = (int64_t)(blockIdx.x + (int64_t)k * gridDim.x) * UG_TM + q * 32 + lane;
             const uint32_t base = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)sl * slot_cols;
             for (int j0 = 0; j0 < a.ky; j0 += 16) {
-                uint32_t r[16];
-                asm volatile(
-                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
-                    "%13, %14, %15}, [%16];\n"
-                    : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-                      "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
-                      "=r"(r[15])
-                    : "r"(base + (uint32_t)j0));
-                asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+                // hi*hi (column j), hi*lo (Np + j), lo*hi (2 Np + j)
+                float sum[16];
+#pragma unroll
+                for (int t = 0; t < 16; ++t) sum[t] = 0.f;
+#pragma unroll
+                for (int part = 0; part < 3; ++part) {
+                    uint32_t r[16];
+                    asm volatile(
+                        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
+                        "%12, %13, %14, %15}, [%16];\n"
+                        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+                          "=r"(r[14]), "=r"(r[15])
+                        : "r"(base + (uint32_t)(part * Np + j0)));
+                    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+                    for (int t = 0; t < 16; ++t) sum[t] += __uint_as_float(r[t]);
+                }
                 if (row < a.N) {
 #pragma unroll
                     for (int t = 0; t < 16; ++t) {
                         const int j = j0 + t;
                         if (j < a.ky) {
                             float *yp = a.Y + row + (int64_t)j * a.ldy;
-                            const float v = a.alpha * __uint_as_float(r[t]);
+                            const float v = a.alpha * sum[t];
                             *yp = a.beta == 0.f ? v : v + a.beta * *yp;
                         }
                     }
@@ -277,12 +291,13 @@ bool g_ug_attr = false;
 
 }  // namespace
 
-bool update_tc_ok(int kx, int ky) { return kx >= 1 && kx <= 64 && ky >= 1 && ky <= 128; }
+// ky <= 80: two slots of 3 Np accumulator columns within the 512 TMEM columns
+bool update_tc_ok(int kx, int ky) { return kx >= 1 && kx <= 64 && ky >= 1 && ky <= 80; }
 
 void update_tc(float *Y, int64_t ldy, int ky, const float *X0, int64_t ldx0, int kx0, const float *X1, int64_t ldx1,
                int kx1, const double *C, int ldc, double alpha, double beta, int64_t N, cudaStream_t s) {
     const int kx = kx0 + kx1;
-    KF_REQUIRE(update_tc_ok(kx, ky), KF_EINVAL, "update_tc: kx must lie in 1:64 and ky in 1:128");
+    KF_REQUIRE(update_tc_ok(kx, ky), KF_EINVAL, "update_tc: kx must lie in 1:64 and ky in 1:80");
     if (N <= 0) return;
     UgArgs a;
     a.Y = Y;
@@ -301,7 +316,7 @@ void update_tc(float *Y, int64_t ldy, int ky, const float *X0, int64_t ldx0, int
     a.Kp = (kx + 7) / 8 * 8;
     a.Np = (ky + 15) / 16 * 16;
     uint32_t tc = 32;
-    while (tc < (uint32_t)(2 * a.Np)) tc <<= 1;
+    while (tc < (uint32_t)(6 * a.Np)) tc <<= 1;   // two slots of 3 Np columns
     a.tcols = tc;
     a.alpha = (float)alpha;
     a.beta = (float)beta;

@@ -1,5 +1,6 @@
-"""The tcgen05 block update (TF32 hi / lo operands, three MMAs per K step, warp-specialised
-pipeline) and the SIMT update against a plain PyTorch FP64 product of the same FP32 data: LOBPCG's
+"""The tcgen05 block update (TF32 hi / lo operands, hi*hi + hi*lo + lo*hi in two MMAs per K step,
+warp-specialised pipeline) and the SIMT update against a plain PyTorch FP64 product of the same FP32
+data: LOBPCG's
 shapes (the fused orthogonalisation update [Z X] -> Z at 32 + 16 -> 32 columns, the Rayleigh-Ritz
 updates), ragged row counts (not a multiple of the 128-row tile), wide outputs, leading dimensions
 larger than N, alpha and accumulation into Y.  FP32 results: 5e-6 of sum_i |X_ri| |C_ij| per entry.
@@ -11,8 +12,8 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-SHAPES = [(671744, 32, 16, 32), (671744, 16, 0, 16), (3721, 7, 0, 5), (1000, 48, 16, 128), (129, 3, 2, 1),
-          (20000, 64, 0, 17), (300, 1, 0, 128)]
+SHAPES = [(671744, 32, 16, 32), (671744, 36, 18, 36), (671744, 16, 0, 16), (3721, 7, 0, 5), (1000, 48, 16, 80),
+          (129, 3, 2, 1), (20000, 64, 0, 17), (300, 1, 0, 80)]
 
 
 def _update(torch, path, X0, X1, Cm, Y0, alpha, beta, ld, N):
@@ -52,3 +53,14 @@ def test_block_update(cuda, path, N, kx0, kx1, ky):
         # the padding rows of each column (ld > N) are untouched
         if ld > N:
             assert torch.equal(Y[:, N:], Y0[:, N:])
+
+
+def test_tensor_core_update_rejects_wide_outputs(cuda):
+    """Two accumulator slots of 3 Np columns fit TMEM up to 80 outputs; wider updates are refused
+    (the solvers keep the SIMT kernels there)."""
+    torch = cuda
+    from kfgpu._abi import ArgumentError
+    X0 = torch.zeros((8, 1024), dtype=torch.float32, device="cuda")
+    Y0 = torch.zeros((96, 1024), dtype=torch.float32, device="cuda")
+    with pytest.raises(ArgumentError):
+        _update(torch, 1, X0, None, np.zeros((8, 96)), Y0, 1.0, 0.0, 1024, 1024)
