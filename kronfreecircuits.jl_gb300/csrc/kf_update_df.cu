@@ -14,9 +14,8 @@ namespace kf {
 
 namespace {
 
-constexpr int DF_UC = 8;   // outputs per pass
-
-template <int KX>
+// KX: input columns held per thread (x_hi, x_lo in registers); UC: outputs per pass
+template <int KX, int UC>
 __global__ void __launch_bounds__(256) k_update_df(double *__restrict__ Y, int64_t ldy, int ky,
                                                    const double *__restrict__ X, int64_t ldx, int kx,
                                                    const double *__restrict__ C, int ldc, int64_t N) {
@@ -37,15 +36,15 @@ __global__ void __launch_bounds__(256) k_update_df(double *__restrict__ Y, int64
         xh[i] = (float)x;
         xl[i] = (float)(x - (double)xh[i]);
     }
-    for (int j0 = 0; j0 < ky; j0 += DF_UC) {
-        float sh[DF_UC], sl[DF_UC];
+    for (int j0 = 0; j0 < ky; j0 += UC) {
+        float sh[UC], sl[UC];
 #pragma unroll
-        for (int v = 0; v < DF_UC; ++v) sh[v] = sl[v] = 0.f;
+        for (int v = 0; v < UC; ++v) sh[v] = sl[v] = 0.f;
 #pragma unroll
         for (int i = 0; i < KX; ++i) {
             if (i < kx) {
 #pragma unroll
-                for (int v = 0; v < DF_UC; ++v) {
+                for (int v = 0; v < UC; ++v) {
                     // the error-free steps use the _rn intrinsics, which the compiler never
                     // contracts into FMAs
                     const float2 c = Cs[i * 32 + ((j0 + v) & 31)];
@@ -62,7 +61,7 @@ __global__ void __launch_bounds__(256) k_update_df(double *__restrict__ Y, int64
             }
         }
 #pragma unroll
-        for (int v = 0; v < DF_UC; ++v)
+        for (int v = 0; v < UC; ++v)
             if (j0 + v < ky) Y[r + (int64_t)(j0 + v) * ldy] = (double)sh[v] + (double)sl[v];
     }
 }
@@ -74,9 +73,19 @@ bool update_f64_df(double *Y, int64_t ldy, int ky, const double *X, int64_t ldx,
     if (N <= 0 || ky <= 0) return true;
     if (kx < 1 || kx > 32 || ky > 32) return false;
     const unsigned grid = (unsigned)((N + 255) / 256);
-    if (kx <= 8) k_update_df<8><<<grid, 256, 0, s>>>(Y, ldy, ky, X, ldx, kx, C, ldc, N);
-    else if (kx <= 16) k_update_df<16><<<grid, 256, 0, s>>>(Y, ldy, ky, X, ldx, kx, C, ldc, N);
-    else k_update_df<32><<<grid, 256, 0, s>>>(Y, ldy, ky, X, ldx, kx, C, ldc, N);
+    // the smallest register row that holds kx; output passes of 6 when they divide ky exactly and 8
+    // do not (18 outputs: three passes of 6 instead of 24 computed)
+    const bool six = ky % 6 == 0 && ky % 8 != 0;
+#define KF_DF(KXV)                                                                              \
+    do {                                                                                        \
+        if (six) k_update_df<KXV, 6><<<grid, 256, 0, s>>>(Y, ldy, ky, X, ldx, kx, C, ldc, N);   \
+        else k_update_df<KXV, 8><<<grid, 256, 0, s>>>(Y, ldy, ky, X, ldx, kx, C, ldc, N);       \
+    } while (0)
+    if (kx <= 8) KF_DF(8);
+    else if (kx <= 16) KF_DF(16);
+    else if (kx <= 24) KF_DF(24);
+    else KF_DF(32);
+#undef KF_DF
     KF_LAUNCH_CHECK();
     return true;
 }
