@@ -46,12 +46,13 @@ M_PAIRS = 12
 SEED = 20261205          # theta draws of the three-mode leaf workload
 NDRAWS = 64
 # ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch (profiles/*.md), N = 671,744: the
-# FP32 16-column fused apply (written Y stays in L2: reads 45.7 MB, writes 9.9 MB); the tcgen05
-# mode product, 256-point axis, 18 columns (reads 48.7 MB = X once, writes 1.9 MB: Y stays in L2);
+# FP32 16-column fused apply (written Y stays in L2: reads 45.7 MB, writes 9.9 MB); the pipelined
+# tcgen05 mode product, 256-point axis, 18 columns (reads 48.6 MB = X once, writes 1.9 MB: Y stays
+# in L2);
 # the tensor-core Gram of [X Z]'Z at 18 + 36 columns (reads 145.2 MB = every element once, writes
 # 0.1 MB of partials)
 APPLY_TRAFFIC_BYTES = 55641088
-MODE_TRAFFIC_BYTES = 50668032
+MODE_TRAFFIC_BYTES = 50463488
 GRAM_TC_TRAFFIC_BYTES = 145235200
 
 
