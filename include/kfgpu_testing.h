@@ -54,6 +54,23 @@ int kf_test_gram_tc(const float *const *srcs, const int64_t *lds, const int32_t 
                     float *ms_per_launch, double *G_out);
 
 /*
+ * The device second orthogonalisation pass's coefficients: from G ((wx + r) x r, host, FP64, column-
+ * major: rows of X'Z then Z'Z), C_out ((r + wx) x r) = [R^-1 ; -(X'Z) R^-1] with R the Cholesky
+ * factor of Z'Z - (X'Z)'(X'Z); *status_out 0, or 1 when a pivot is not finite or below 1e-4.
+ * r <= 64.
+ */
+int kf_test_chol2(const double *G, int wx, int r, double *C_out, int *status_out);
+
+/*
+ * The pipelined FP32 update with its output split over two blocks: [Y0 Y1] = alpha [X0 X1] C +
+ * beta [Y0 Y1] (device blocks, leading dimension ld; Y0: ky0 columns, Y1: ky1; X0: kx0, X1: kx1;
+ * C: host, (kx0 + kx1) x (ky0 + ky1) column-major FP64).  Returns KF_EINVAL when the shapes do not
+ * fit the kernel (more than 64 inputs or outputs, unaligned blocks).
+ */
+int kf_test_update_split(float *Y0, int ky0, float *Y1, int ky1, const float *X0, int kx0, const float *X1, int kx1,
+                         const double *C, double alpha, double beta, int64_t N, int64_t ld);
+
+/*
  * The FP64 block update Y = X C (device blocks X: N x kx, Y: N x ky, leading dimension N; C: host,
  * kx x ky column-major FP64), `reps` times on `stream`: path 0 the FP64 kernel, path 1 double-float
  * arithmetic on the FP32 pipes (kx, ky <= 32).  *ms_per_launch: mean device time.

@@ -387,6 +387,43 @@ int kf_test_gram_tc(const float *const *srcs, const int64_t *lds, const int32_t 
     });
 }
 
+int kf_test_chol2(const double *G, int wx, int r, double *C_out, int *status_out) {
+    return guarded([&] {
+        KF_REQUIRE(G && C_out && status_out && wx >= 0 && r >= 1 && r <= kf::CHOL2_MAX_R, KF_EINVAL,
+                   "kf_test_chol2: bad argument");
+        double *dG = nullptr, *dC = nullptr;
+        int *dst = nullptr;
+        const size_t ng = (size_t)(wx + r) * r, nc = (size_t)(r + wx) * r;
+        KF_CUDA(cudaMalloc(&dG, ng * sizeof(double)));
+        KF_CUDA(cudaMalloc(&dC, nc * sizeof(double)));
+        KF_CUDA(cudaMalloc(&dst, sizeof(int)));
+        KF_CUDA(cudaMemcpy(dG, G, ng * sizeof(double), cudaMemcpyHostToDevice));
+        kf::chol2_coeffs(dG, wx, r, dC, dst, nullptr);
+        KF_CUDA(cudaMemcpy(C_out, dC, nc * sizeof(double), cudaMemcpyDeviceToHost));
+        KF_CUDA(cudaMemcpy(status_out, dst, sizeof(int), cudaMemcpyDeviceToHost));
+        cudaFree(dG);
+        cudaFree(dC);
+        cudaFree(dst);
+    });
+}
+
+int kf_test_update_split(float *Y0, int ky0, float *Y1, int ky1, const float *X0, int kx0, const float *X1, int kx1,
+                         const double *C, double alpha, double beta, int64_t N, int64_t ld) {
+    return guarded([&] {
+        KF_REQUIRE(Y0 && X0 && C && N >= 1 && ld >= N && ky0 >= 1 && ky1 >= 0 && kx0 >= 1 && kx1 >= 0, KF_EINVAL,
+                   "kf_test_update_split: bad argument");
+        const int kx = kx0 + kx1, ky = ky0 + ky1;
+        double *dC = nullptr;
+        KF_CUDA(cudaMalloc(&dC, sizeof(double) * (size_t)kx * ky));
+        KF_CUDA(cudaMemcpy(dC, C, sizeof(double) * (size_t)kx * ky, cudaMemcpyHostToDevice));
+        const bool ok = kf::update_pipe(Y0, ld, ky0, Y1, ld, ky1, X0, ld, kx0, X1, ld, kx1, dC, kx, alpha, beta, N,
+                                        nullptr);
+        KF_CUDA(cudaDeviceSynchronize());
+        cudaFree(dC);
+        KF_REQUIRE(ok, KF_EINVAL, "kf_test_update_split: the shapes do not fit the pipelined kernel");
+    });
+}
+
 int kf_test_update_f64(int path, double *Y, const double *X, int kx, int ky, const double *C, int64_t N, int reps,
                        void *stream, float *ms_per_launch) {
     return guarded([&] {

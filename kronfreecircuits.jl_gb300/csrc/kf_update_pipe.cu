@@ -79,7 +79,9 @@ __global__ void __launch_bounds__(256, 2) k_update_pipe(const UpArgs a) {
         float acc[H];
 #pragma unroll
         for (int v = 0; v < H; ++v) acc[v] = 0.f;
-        // an empty half (ky small) skips the product: its jb need not be a multiple of 4
+        // an empty half (ky small) skips the product: its jb need not be a multiple of 4; unrolled so
+        // that the next inputs' shared loads are in flight while this one's FMAs issue
+#pragma unroll 4
         for (int i = 0; jb < je && i < a.kx; ++i) {
             const float xv = xs[i * UP_S];
             const float *cr = Cs + i * a.kyp + jb;
