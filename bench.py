@@ -426,8 +426,9 @@ def time_gram_tc(torch, widths, rr, N, reps=10):
 
 
 def time_update(torch, path, kx0, kx1, ky, N, reps=10):
-    """Mean device time of one FP32 block update Y = [X0 X1] C (path 0: SIMT, 1: tcgen05), through
-    the library's test-only timing entry point."""
+    """Mean device time of one FP32 block update Y = [X0 X1] C (path 0: SIMT, 1: tcgen05, 2-4: tcgen05
+    with the register gather, a two- or a three-tile staging ring), through the library's test-only
+    timing entry point."""
     import ctypes as C
     from kfgpu import _abi
     X0 = torch.randn(kx0, N, dtype=torch.float32, device="cuda")
@@ -441,7 +442,7 @@ def time_update(torch, path, kx0, kx1, ky, N, reps=10):
     return ms.value / 1e3
 
 
-UPDATE_SHAPES = ((32, 16, 32), (36, 18, 36), (18, 36, 18), (16, 32, 16), (16, 0, 16), (2, 0, 1))
+UPDATE_SHAPES = ((32, 16, 32), (36, 18, 36), (18, 36, 36), (18, 36, 18), (16, 32, 16), (16, 0, 16), (2, 0, 1))
 
 
 def time_update_f64(torch, path, kx, ky, N, reps=10):
@@ -464,9 +465,13 @@ def run_update_workload(args):
     N = 671744
     peak, kind = peaks()
     out = {"workload": "FP32 block update Y = [X0 X1] C, N=671,744 rows", "hbm_peak_gbs": peak, "peak_kind": kind}
+    from kfgpu._abi import ArgumentError
     for kx0, kx1, ky in UPDATE_SHAPES:
-        for path, name in ((1, "tc"), (0, "simt")):
-            t = time_update(torch, path, kx0, kx1, ky, N)
+        for path, name in ((1, "tc"), (2, "tc_gather"), (3, "tc_ring2"), (4, "tc_ring3"), (0, "simt")):
+            try:
+                t = time_update(torch, path, kx0, kx1, ky, N)
+            except ArgumentError:
+                continue   # the shape does not fit that producer mode
             key = f"update_{kx0}+{kx1}_to_{ky}_{name}"
             out[key + "_us"] = t * 1e6
             out[key + "_gbs"] = (kx0 + kx1 + ky) * N * 4 / t / 1e9

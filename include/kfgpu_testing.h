@@ -62,13 +62,14 @@ int kf_test_gram_tc(const float *const *srcs, const int64_t *lds, const int32_t 
 int kf_test_chol2(const double *G, int wx, int r, double *C_out, int *status_out);
 
 /*
- * The pipelined FP32 update with its output split over two blocks: [Y0 Y1] = alpha [X0 X1] C +
- * beta [Y0 Y1] (device blocks, leading dimension ld; Y0: ky0 columns, Y1: ky1; X0: kx0, X1: kx1;
- * C: host, (kx0 + kx1) x (ky0 + ky1) column-major FP64).  Returns KF_EINVAL when the shapes do not
- * fit the kernel (more than 64 inputs or outputs, unaligned blocks).
+ * The FP32 update with its output split over two blocks: [Y0 Y1] = alpha [X0 X1] C + beta [Y0 Y1]
+ * (device blocks, leading dimension ld; Y0: ky0 columns, Y1: ky1; X0: kx0, X1: kx1; C: host,
+ * (kx0 + kx1) x (ky0 + ky1) column-major FP64): path 0 the pipelined SIMT kernel, path 1 the
+ * tcgen05 kernel.  Returns KF_EINVAL when the shapes do not fit the kernel (path 0: more than 64
+ * inputs or outputs, unaligned blocks; path 1: more than 64 inputs or 80 outputs).
  */
-int kf_test_update_split(float *Y0, int ky0, float *Y1, int ky1, const float *X0, int kx0, const float *X1, int kx1,
-                         const double *C, double alpha, double beta, int64_t N, int64_t ld);
+int kf_test_update_split(int path, float *Y0, int ky0, float *Y1, int ky1, const float *X0, int kx0, const float *X1,
+                         int kx1, const double *C, double alpha, double beta, int64_t N, int64_t ld);
 
 /*
  * The FP64 block update Y = X C (device blocks X: N x kx, Y: N x ky, leading dimension N; C: host,
@@ -81,8 +82,10 @@ int kf_test_update_f64(int path, double *Y, const double *X, int kx, int ky, con
 /*
  * The FP32 block update Y = alpha [X0 X1] C + beta Y (device blocks: X0 N x kx0, X1 N x kx1 (kx1 may
  * be 0), Y N x ky; C: host, (kx0 + kx1) x ky, column-major FP64, leading dimension ldc), `reps`
- * times on `stream`, timed with CUDA events: path 0 the SIMT kernel, path 1 the tcgen05 kernel
- * (TF32 hi / lo operands; kx0 + kx1 <= 64, ky <= 128).  *ms_per_launch: mean device time.  With
+ * times on `stream`, timed with CUDA events: path 0 the SIMT kernels, path 1 the tcgen05 kernel
+ * (TF32 hi / lo operands; kx0 + kx1 <= 64, ky <= 80) with its producer mode picked by shape, paths
+ * 2-4 the same with the mode forced: 2 register gather, 3 and 4 a staging ring of 2 and 3 tiles
+ * (KF_EINVAL where it does not fit).  *ms_per_launch: mean device time.  With
  * beta != 0 every launch reads the Y the previous one wrote.
  */
 int kf_test_update(int path, float *Y, int64_t ldy, int ky, const float *X0, int64_t ldx0, int kx0, const float *X1,

@@ -407,17 +407,23 @@ int kf_test_chol2(const double *G, int wx, int r, double *C_out, int *status_out
     });
 }
 
-int kf_test_update_split(float *Y0, int ky0, float *Y1, int ky1, const float *X0, int kx0, const float *X1, int kx1,
-                         const double *C, double alpha, double beta, int64_t N, int64_t ld) {
+int kf_test_update_split(int path, float *Y0, int ky0, float *Y1, int ky1, const float *X0, int kx0, const float *X1,
+                         int kx1, const double *C, double alpha, double beta, int64_t N, int64_t ld) {
     return guarded([&] {
-        KF_REQUIRE(Y0 && X0 && C && N >= 1 && ld >= N && ky0 >= 1 && ky1 >= 0 && kx0 >= 1 && kx1 >= 0, KF_EINVAL,
-                   "kf_test_update_split: bad argument");
+        KF_REQUIRE(Y0 && X0 && C && N >= 1 && ld >= N && ky0 >= 1 && ky1 >= 0 && kx0 >= 1 && kx1 >= 0 &&
+                       (path == 0 || path == 1),
+                   KF_EINVAL, "kf_test_update_split: bad argument");
         const int kx = kx0 + kx1, ky = ky0 + ky1;
         double *dC = nullptr;
         KF_CUDA(cudaMalloc(&dC, sizeof(double) * (size_t)kx * ky));
         KF_CUDA(cudaMemcpy(dC, C, sizeof(double) * (size_t)kx * ky, cudaMemcpyHostToDevice));
-        const bool ok = kf::update_pipe(Y0, ld, ky0, Y1, ld, ky1, X0, ld, kx0, X1, ld, kx1, dC, kx, alpha, beta, N,
-                                        nullptr);
+        bool ok = true;
+        if (path == 1) {
+            KF_REQUIRE(kf::update_tc_ok(kx, ky), KF_EINVAL, "kf_test_update_split: the shapes do not fit the kernel");
+            kf::update_tc2(Y0, ld, ky0, Y1, ld, ky1, X0, ld, kx0, X1, ld, kx1, dC, kx, alpha, beta, N, nullptr, -1);
+        } else {
+            ok = kf::update_pipe(Y0, ld, ky0, Y1, ld, ky1, X0, ld, kx0, X1, ld, kx1, dC, kx, alpha, beta, N, nullptr);
+        }
         KF_CUDA(cudaDeviceSynchronize());
         cudaFree(dC);
         KF_REQUIRE(ok, KF_EINVAL, "kf_test_update_split: the shapes do not fit the pipelined kernel");
@@ -462,13 +468,18 @@ int kf_test_update(int path, float *Y, int64_t ldy, int ky, const float *X0, int
         KF_REQUIRE(Y && X0 && C && ms_per_launch && reps >= 1 && N >= 1 && ky >= 1 && kx0 >= 1 && kx1 >= 0,
                    KF_EINVAL, "kf_test_update: bad argument");
         KF_REQUIRE(kx1 == 0 || X1, KF_EINVAL, "kf_test_update: X1 is NULL");
+        KF_REQUIRE(path >= 0 && path <= 4, KF_EINVAL, "kf_test_update: bad path");
         cudaStream_t s = (cudaStream_t)stream;
         const int kx = kx0 + kx1;
         double *dC = nullptr;
         KF_CUDA(cudaMalloc(&dC, sizeof(double) * (size_t)ldc * ky));
         KF_CUDA(cudaMemcpy(dC, C, sizeof(double) * (size_t)ldc * ky, cudaMemcpyHostToDevice));
         auto launch = [&] {
-            if (path == 1) kf::update_tc(Y, ldy, ky, X0, ldx0, kx0, X1, ldx1, kx1, dC, ldc, alpha, beta, N, s);
+            // paths 2-4: the tensor-core kernel with its producer mode forced (register gather, two- and
+            // three-tile staging rings)
+            if (path >= 1)
+                kf::update_tc2(Y, ldy, ky, nullptr, 0, 0, X0, ldx0, kx0, X1, ldx1, kx1, dC, ldc, alpha, beta, N, s,
+                               path == 1 ? -1 : path == 2 ? 0 : path - 1);
             else kf::update2<float>(Y, ldy, ky, X0, ldx0, kx0, kx1 ? X1 : X0, kx1 ? ldx1 : ldx0, kx1, dC, ldc, alpha,
                                     beta, N, s, false);
         };

@@ -519,6 +519,10 @@ void update(T *Y, int64_t ldy, int ky, const T *X, int64_t ldx, int kx, const do
         return;
     }
     if constexpr (sizeof(T) == 4) {
+        if (update_tc_prefer(kx, ky, N, (const float *)X, ldx, nullptr, 0)) {
+            update_tc((float *)Y, ldy, ky, (const float *)X, ldx, kx, nullptr, 0, 0, C, ldc, alpha, beta, N, s);
+            return;
+        }
         if (N >= 4096 && update_pipe((float *)Y, ldy, ky, nullptr, 0, 0, (const float *)X, ldx, kx, nullptr, 0, 0, C,
                                      ldc, alpha, beta, N, s))
             return;
@@ -554,6 +558,14 @@ void update2(T *Y, int64_t ldy, int ky, const T *X0, int64_t ldx0, int kx0, cons
              const double *C, int ldc, double alpha, double beta, int64_t N, cudaStream_t s, bool allow_tc) {
     if (ky <= 0 || N <= 0) return;
     if constexpr (sizeof(T) == 4) {
+        // at least 40 inputs and 17 outputs: the tcgen05 kernel (TF32 hi / lo, staging ring), which
+        // measured faster there (54 -> 36 columns: 99 us vs 126 us on 671,744 rows)
+        if (allow_tc && kx0 > 0 &&
+            update_tc_prefer(kx0 + kx1, ky, N, (const float *)X0, ldx0, kx1 > 0 ? (const float *)X1 : nullptr, ldx1)) {
+            update_tc((float *)Y, ldy, ky, (const float *)X0, ldx0, kx0, (const float *)X1, ldx1, kx1, C, ldc, alpha,
+                      beta, N, s);
+            return;
+        }
         // up to 64 x 64: the pipelined SIMT kernel (loads overlapped with the FMAs)
         if (N >= 4096 && kx0 > 0 &&
             update_pipe((float *)Y, ldy, ky, nullptr, 0, 0, (const float *)X0, ldx0, kx0, (const float *)X1, ldx1, kx1,

@@ -106,10 +106,20 @@ void tc_mode_product(float *Y, int64_t ldy, const float *X, int64_t ldx, const T
                      int64_t b, double alpha, double beta, cudaStream_t s);
 int tc_take_error();
 int *tc_error_word();  // the host-mapped word device-side waits report KF_ETIMEOUT in
-// FP32 block update on the tensor cores (kf_tcgemm.cu), TF32 hi / lo operands, kx <= 64, ky <= 128
+// FP32 block update on the tensor cores (kf_tcgemm.cu), TF32 hi / lo operands, kx <= 64, ky <= 80
 bool update_tc_ok(int kx, int ky);
 void update_tc(float *Y, int64_t ldy, int ky, const float *X0, int64_t ldx0, int kx0, const float *X1, int64_t ldx1,
-               int kx1, const double *C, int ldc, double alpha, double beta, int64_t N, cudaStream_t s);   // a pending device-side timeout (KF_ETIMEOUT) of a tensor-core launch, cleared
+               int kx1, const double *C, int ldc, double alpha, double beta, int64_t N, cudaStream_t s);
+// the same with the outputs split over two blocks (columns [0, ky0) to Y0, the ky1 others to Y1);
+// force_nstg >= 0 forces the producer mode (0 register gather, 2 or 3 staging tiles; KF_EINVAL when
+// it does not fit), -1 picks the deepest staging ring that fits
+void update_tc2(float *Y0, int64_t ldy0, int ky0, float *Y1, int64_t ldy1, int ky1, const float *X0, int64_t ldx0,
+                int kx0, const float *X1, int64_t ldx1, int kx1, const double *C, int ldc, double alpha, double beta,
+                int64_t N, cudaStream_t s, int force_nstg);
+// whether the tensor-core update (with a staging ring) is the faster FP32 update for this shape: at
+// least 40 inputs and 17 outputs on 65,536 rows or more, 16-byte aligned columns (X1 may be NULL);
+// narrower updates are faster on the pipelined SIMT kernel
+bool update_tc_prefer(int kx, int ky, int64_t N, const float *X0, int64_t ldx0, const float *X1, int64_t ldx1);   // a pending device-side timeout (KF_ETIMEOUT) of a tensor-core launch, cleared
 
 }  // namespace kf
 

@@ -627,9 +627,16 @@ static LobOut lobpcg_run(kf_op *op, LobWork<T> &Wk, const double *D, const LobPa
         // X_act <- Xa Cx + Q Cz ; HX likewise ; P <- Q Cz
         T *Xna = Xn + (int64_t)nl * N, *HXna = HXn + (int64_t)nl * N;
         bool fused = false;
-        if constexpr (merged)
-            fused = update_pipe((float *)Xna, N, na3, (float *)Pn, N, na3, (const float *)Xa, N, na3,
-                                (const float *)Qc, N, k, C, ns, 1.0, 0.0, N, s);
+        if constexpr (merged) {
+            if (update_tc_prefer(na3 + k, 2 * na3, N, (const float *)Xa, N, (const float *)Qc, N)) {
+                update_tc2((float *)Xna, N, na3, (float *)Pn, N, na3, (const float *)Xa, N, na3, (const float *)Qc, N,
+                           k, C, ns, 1.0, 0.0, N, s, -1);
+                fused = true;
+            } else {
+                fused = update_pipe((float *)Xna, N, na3, (float *)Pn, N, na3, (const float *)Xa, N, na3,
+                                    (const float *)Qc, N, k, C, ns, 1.0, 0.0, N, s);
+            }
+        }
         if (!fused) update2<T>(Xna, N, na3, Xa, N, na3, Qc, N, k, C, ns, 1.0, 0.0, N, s);
         update2<T>(HXna, N, na3, HXa, N, na3, HZ, N, k, C, ns, 1.0, 0.0, N, s);
         if (!fused) update<T>(Pn, N, na3, Qc, N, k, C + na3, ns, 1.0, 0.0, N, s);

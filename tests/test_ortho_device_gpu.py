@@ -47,9 +47,10 @@ def test_chol2_reports_a_dependent_direction(cuda):
     assert st == 1
 
 
+@pytest.mark.parametrize("path", [0, 1])
 @pytest.mark.parametrize("N,kx0,kx1,ky0,ky1", [(671744, 18, 36, 18, 18), (100000, 16, 32, 16, 16), (4096, 7, 5, 3, 9),
-                                               (130000, 64, 0, 32, 32)])
-def test_update_split_outputs(cuda, N, kx0, kx1, ky0, ky1):
+                                               (130000, 64, 0, 32, 32), (100003, 20, 40, 20, 20)])
+def test_update_split_outputs(cuda, path, N, kx0, kx1, ky0, ky1):
     torch = cuda
     from kfgpu import _abi
     rng = np.random.default_rng(N + kx0)
@@ -61,7 +62,7 @@ def test_update_split_outputs(cuda, N, kx0, kx1, ky0, ky1):
     Cm = rng.standard_normal((kx0 + kx1, ky0 + ky1))
     Y0r, Y1r = Y0.clone(), Y1.clone()
     Cf = np.asfortranarray(Cm)
-    _abi.check(_abi.lib().kf_test_update_split(C.c_void_p(Y0.data_ptr()), ky0, C.c_void_p(Y1.data_ptr()), ky1,
+    _abi.check(_abi.lib().kf_test_update_split(path, C.c_void_p(Y0.data_ptr()), ky0, C.c_void_p(Y1.data_ptr()), ky1,
                                                C.c_void_p(X0.data_ptr()), kx0, C.c_void_p(X1.data_ptr()), kx1,
                                                Cf.ctypes.data_as(C.c_void_p), 0.5, 1.0, N, ld))
     Xa = torch.cat([X0[:, :N], X1[:kx1, :N]]).double()

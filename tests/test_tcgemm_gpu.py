@@ -64,3 +64,46 @@ def test_tensor_core_update_rejects_wide_outputs(cuda):
     Y0 = torch.zeros((96, 1024), dtype=torch.float32, device="cuda")
     with pytest.raises(ArgumentError):
         _update(torch, 1, X0, None, np.zeros((8, 96)), Y0, 1.0, 0.0, 1024, 1024)
+
+
+RING_SHAPES = [(671744, 18, 36, 36), (671744, 18, 36, 18), (100003, 7, 0, 5), (129, 3, 2, 1), (20000, 64, 0, 17),
+               (300, 1, 0, 80), (5000, 48, 16, 80)]
+
+
+def _ring_smem(kx, ky, nstg):
+    """Shared memory of the tensor-core update with an nstg-tile staging ring (bytes)."""
+    Kp, Np = (kx + 7) // 8 * 8, (ky + 15) // 16 * 16
+    return 2 * Np * Kp * 4 + 4 * 128 * Kp * 4 + 128 + nstg * Kp * 132 * 4
+
+
+@pytest.mark.parametrize("N,kx0,kx1,ky", RING_SHAPES)
+@pytest.mark.parametrize("path", [2, 3, 4])
+def test_block_update_producer_modes(cuda, path, N, kx0, kx1, ky):
+    """The tensor-core update with its producer mode forced: register gather (path 2), staging rings
+    of two and three tiles filled by 16-byte cp.async copies (paths 3, 4; the rows past N of the last
+    tile zero-filled).  A ring that does not fit shared memory is refused."""
+    torch = cuda
+    from kfgpu._abi import ArgumentError
+    rng = np.random.default_rng(N + 3 * kx0 + ky)
+    ld = (N + 3) // 4 * 4 + (4 if N % 3 == 0 else 0)
+    X0 = torch.as_tensor(rng.standard_normal((kx0, ld)), dtype=torch.float32, device="cuda")
+    X1 = torch.as_tensor(rng.standard_normal((kx1, ld)), dtype=torch.float32, device="cuda") if kx1 else None
+    Cm = rng.standard_normal((kx0 + kx1, ky))
+    Y0 = torch.as_tensor(rng.standard_normal((ky, ld)), dtype=torch.float32, device="cuda")
+    smem = _ring_smem(kx0 + kx1, ky, path - 1) if path >= 3 else 0
+    if smem > 232448:
+        with pytest.raises(ArgumentError):
+            _update(torch, path, X0, X1, Cm, Y0, 1.0, 0.0, ld, N)
+        return
+    for alpha, beta in ((1.0, 0.0), (0.75, -1.0)):
+        Y = _update(torch, path, X0, X1, Cm, Y0, alpha, beta, ld, N)
+        Xa = X0[:, :N] if X1 is None else torch.cat([X0[:, :N], X1[:, :N]])
+        Cf = Cm.astype(np.float32).astype(np.float64)
+        Ct = torch.as_tensor(Cf, dtype=torch.float64, device="cuda")
+        ref = alpha * (Ct.T @ Xa.double()) + beta * Y0[:, :N].double()
+        bound = abs(alpha) * (torch.as_tensor(np.abs(Cf), device="cuda").T @ Xa.double().abs()) + \
+            abs(beta) * Y0[:, :N].double().abs() + 1e-30
+        err = ((Y[:, :N].double() - ref).abs() / bound).max().item()
+        assert err < 5e-6, (path, alpha, beta, err)
+        if ld > N:
+            assert torch.equal(Y[:, N:], Y0[:, N:])
