@@ -54,6 +54,15 @@ int kf_test_gram_tc(const float *const *srcs, const int64_t *lds, const int32_t 
                     float *ms_per_launch, double *G_out);
 
 /*
+ * The host symmetric eigensolver of the small projected problems (Rayleigh-Ritz, SVQB, the per-axis
+ * eigenbases of the separable preconditioner): eigenvalues w (ascending) and orthonormal
+ * eigenvectors V (n x n, column-major, leading dimension ldv) of the symmetric A (n x n,
+ * column-major, leading dimension lda; both triangles read as their average).  Host only, no GPU
+ * call.  KF_EBREAKDOWN when the QR iteration does not converge.
+ */
+int kf_test_sym_eig(int n, const double *A, int lda, double *w, double *V, int ldv);
+
+/*
  * The device second orthogonalisation pass's coefficients: from G ((wx + r) x r, host, FP64, column-
  * major: rows of X'Z then Z'Z), C_out ((r + wx) x r) = [R^-1 ; -(X'Z) R^-1] with R the Cholesky
  * factor of Z'Z - (X'Z)'(X'Z); *status_out 0, or 1 when a pivot is not finite or below 1e-4.

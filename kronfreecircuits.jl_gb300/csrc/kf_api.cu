@@ -387,6 +387,15 @@ int kf_test_gram_tc(const float *const *srcs, const int64_t *lds, const int32_t 
     });
 }
 
+int kf_test_sym_eig(int n, const double *A, int lda, double *w, double *V, int ldv) {
+    return guarded([&] {
+        KF_REQUIRE(n >= 0 && (n == 0 || (A && w && V && lda >= n && ldv >= n)), KF_EINVAL,
+                   "kf_test_sym_eig: bad argument");
+        if (kf::sym_eig(n, A, lda, w, V, ldv) != 0)
+            throw kf::Error(KF_EBREAKDOWN, "kf_test_sym_eig: the QR iteration did not converge");
+    });
+}
+
 int kf_test_chol2(const double *G, int wx, int r, double *C_out, int *status_out) {
     return guarded([&] {
         KF_REQUIRE(G && C_out && status_out && wx >= 0 && r >= 1 && r <= kf::CHOL2_MAX_R, KF_EINVAL,

@@ -24,80 +24,111 @@
 
 namespace kf {
 
+namespace {
+
+// y += alpha x (n entries); no aliasing between x and y
+inline void axpy(int n, double alpha, const double *__restrict__ x, double *__restrict__ y) {
+    for (int i = 0; i < n; ++i) y[i] += alpha * x[i];
+}
+
+// y -= a x' + b (rank-2 column update): y[i] -= a[i] bj + b[i] aj
+inline void rank2_col(int n, const double *__restrict__ a, double bj, const double *__restrict__ b, double aj,
+                      double *__restrict__ y) {
+    for (int i = 0; i < n; ++i) y[i] -= a[i] * bj + b[i] * aj;
+}
+
+// plane rotation of two columns: (x, y) <- (c x + s y, -s x + c y)
+inline void rot(int n, double *__restrict__ x, double *__restrict__ y, double c, double s) {
+    for (int i = 0; i < n; ++i) {
+        const double u = x[i], v = y[i];
+        x[i] = c * u + s * v;
+        y[i] = c * v - s * u;
+    }
+}
+
+// dot product with four partial sums (independent FMA chains)
+inline double dot(int n, const double *__restrict__ x, const double *__restrict__ y) {
+    double s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+    int i = 0;
+    for (; i + 4 <= n; i += 4) {
+        s0 += x[i] * y[i];
+        s1 += x[i + 1] * y[i + 1];
+        s2 += x[i + 2] * y[i + 2];
+        s3 += x[i + 3] * y[i + 3];
+    }
+    for (; i < n; ++i) s0 += x[i] * y[i];
+    return (s0 + s1) + (s2 + s3);
+}
+
+}  // namespace
+
 // Eigenvalues (ascending) w[0..n) and orthonormal eigenvectors V (columns) of the symmetric A
 // (column-major, both triangles read as their average).  Returns 0, or -1 without convergence.
+// Every O(n^3) loop is a column axpy, a rank-2 column update or a plane rotation of two columns
+// (no reductions in the inner loops, so the compiler vectorises them); the reflectors are
+// accumulated right to left in the transposed layout for the same reason.
 int sym_eig(int n, const double *A, int lda, double *w, double *V, int ldv) {
     if (n <= 0) return 0;
-    // working copy, symmetrised
-    std::vector<double> a((size_t)n * n);
+    const size_t nn = (size_t)n;
+    std::vector<double> a(nn * nn);
     for (int j = 0; j < n; ++j)
-        for (int i = 0; i < n; ++i) a[i + (size_t)n * j] = 0.5 * (A[i + (size_t)lda * j] + A[j + (size_t)lda * i]);
-    auto at = [&](int i, int j) -> double & { return a[i + (size_t)n * j]; };
-    // Householder tridiagonalisation; reflector k acts on rows/cols k+1..n-1
-    std::vector<std::vector<double>> refl(n > 2 ? n - 2 : 0);
-    std::vector<double> p(n), q(n);
+        for (int i = 0; i < n; ++i) a[i + nn * j] = 0.5 * (A[i + (size_t)lda * j] + A[j + (size_t)lda * i]);
+    // Householder tridiagonalisation, both triangles kept: reflector k (unit vector in column k of
+    // R, rows k+1..n-1) maps column k below the diagonal onto its first entry
+    std::vector<double> R(nn * nn, 0.0), p(n), q(n), d(n), e(n > 1 ? n - 1 : 1, 0.0);
+    std::vector<char> has(n, 0);
     for (int k = 0; k + 2 < n; ++k) {
         const int m = n - k - 1;
-        double nx = 0;
-        for (int i = 0; i < m; ++i) nx += at(k + 1 + i, k) * at(k + 1 + i, k);
-        nx = std::sqrt(nx);
-        std::vector<double> &v = refl[k];
+        double *x = &a[(k + 1) + nn * k];
+        const double nx = std::sqrt(dot(m, x, x));
         if (nx == 0) continue;
-        const double x0 = at(k + 1, k);
+        const double x0 = x[0];
         const double alpha = x0 > 0 ? -nx : nx;
-        v.assign(m, 0.0);
-        for (int i = 0; i < m; ++i) v[i] = at(k + 1 + i, k);
+        double *v = &R[(k + 1) + nn * k];
+        std::memcpy(v, x, sizeof(double) * m);
         v[0] -= alpha;
-        double vn = 0;
-        for (int i = 0; i < m; ++i) vn += v[i] * v[i];
-        vn = std::sqrt(vn);
-        if (vn == 0) { v.clear(); continue; }
-        for (int i = 0; i < m; ++i) v[i] /= vn;
-        // p = A22 v, K = v'p, q = 2 (p - K v), A22 -= v q' + q v'
-        double K = 0;
-        for (int i = 0; i < m; ++i) {
-            // A22 is symmetric: row i read down column i (contiguous)
-            const double *col = &a[(size_t)(k + 1) + (size_t)n * (k + 1 + i)];
-            double s = 0;
-            for (int j = 0; j < m; ++j) s += col[j] * v[j];
-            p[i] = s;
-            K += v[i] * s;
-        }
+        const double vn = std::sqrt(dot(m, v, v));
+        if (vn == 0) continue;
+        const double iv = 1.0 / vn;
+        for (int i = 0; i < m; ++i) v[i] *= iv;
+        has[k] = 1;
+        // p = A22 v as a sum of columns, K = v'p, q = 2 (p - K v), A22 -= v q' + q v'
+        std::fill(p.begin(), p.begin() + m, 0.0);
+        for (int j = 0; j < m; ++j) axpy(m, v[j], &a[(k + 1) + nn * (k + 1 + j)], p.data());
+        const double K = dot(m, v, p.data());
         for (int i = 0; i < m; ++i) q[i] = 2.0 * (p[i] - K * v[i]);
-        for (int j = 0; j < m; ++j)
-            for (int i = 0; i < m; ++i) at(k + 1 + i, k + 1 + j) -= v[i] * q[j] + q[i] * v[j];
-        at(k + 1, k) = alpha;
-        at(k, k + 1) = alpha;
+        for (int j = 0; j < m; ++j) rank2_col(m, v, q[j], q.data(), v[j], &a[(k + 1) + nn * (k + 1 + j)]);
+        x[0] = alpha;
+        a[k + nn * (k + 1)] = alpha;
         for (int i = 1; i < m; ++i) {
-            at(k + 1 + i, k) = 0;
-            at(k, k + 1 + i) = 0;
+            x[i] = 0;
+            a[k + nn * (k + 1 + i)] = 0;
         }
     }
-    std::vector<double> d(n), e(n > 1 ? n - 1 : 1, 0.0);
-    for (int i = 0; i < n; ++i) d[i] = at(i, i);
-    for (int i = 0; i + 1 < n; ++i) e[i] = at(i + 1, i);
-    // Q = H_0 H_1 ... H_{n-3}, built by applying the reflectors right to left to the identity
-    std::vector<double> Z((size_t)n * n, 0.0);
-    for (int i = 0; i < n; ++i) Z[i + (size_t)n * i] = 1.0;
+    for (int i = 0; i < n; ++i) d[i] = a[i + nn * i];
+    for (int i = 0; i + 1 < n; ++i) e[i] = a[(i + 1) + nn * i];
+    // Q = H_0 H_1 ... H_{n-3}, built right to left on the identity in the transposed layout
+    // (Zt = Q'): Q <- H_k Q touches rows k+1.. of Q's columns k+1.., i.e. Zt <- Zt H_k on that block,
+    // y = Zt v (a sum of columns) then Zt -= 2 y v'
+    std::vector<double> Zt(nn * nn, 0.0), y(n);
+    for (int i = 0; i < n; ++i) Zt[i + nn * i] = 1.0;
     for (int k = n - 3; k >= 0; --k) {
-        const std::vector<double> &v = refl[k];
-        if (v.empty()) continue;
+        if (!has[k]) continue;
         const int m = n - k - 1;
-        for (int c = 0; c < n; ++c) {
-            double s = 0;
-            for (int i = 0; i < m; ++i) s += v[i] * Z[(k + 1 + i) + (size_t)n * c];
-            s *= 2.0;
-            if (s == 0) continue;
-            for (int i = 0; i < m; ++i) Z[(k + 1 + i) + (size_t)n * c] -= s * v[i];
-        }
+        const double *v = &R[(k + 1) + nn * k];
+        std::fill(y.begin(), y.begin() + m, 0.0);
+        for (int i = 0; i < m; ++i) axpy(m, v[i], &Zt[(k + 1) + nn * (k + 1 + i)], y.data());
+        for (int i = 0; i < m; ++i) axpy(m, -2.0 * v[i], y.data(), &Zt[(k + 1) + nn * (k + 1 + i)]);
     }
+    std::vector<double> Z(nn * nn);
+    for (int j = 0; j < n; ++j)
+        for (int i = 0; i < n; ++i) Z[i + nn * j] = Zt[j + nn * i];
     // implicit symmetric tridiagonal QR with Wilkinson shifts
     const double eps = std::numeric_limits<double>::epsilon();
     int hi = n - 1;
     int iters = 0;
     const int maxit = 60 * n + 60;
     while (hi > 0) {
-        // deflate negligible off-diagonals
         for (int i = 0; i < hi; ++i)
             if (std::fabs(e[i]) <= eps * (std::fabs(d[i]) + std::fabs(d[i + 1]))) e[i] = 0.0;
         while (hi > 0 && e[hi - 1] == 0.0) --hi;
@@ -105,16 +136,18 @@ int sym_eig(int n, const double *A, int lda, double *w, double *V, int ldv) {
         int lo = hi - 1;
         while (lo > 0 && e[lo - 1] != 0.0) --lo;
         if (++iters > maxit) return -1;
-        // Wilkinson shift from the trailing 2 x 2 of the unreduced block lo..hi
         const double delta = 0.5 * (d[hi - 1] - d[hi]);
         const double eh = e[hi - 1];
         const double sg = delta >= 0 ? 1.0 : -1.0;
         const double mu = d[hi] - eh * eh / (delta + sg * std::hypot(delta, eh));
         double x = d[lo] - mu, z = e[lo];
         for (int k = lo; k < hi; ++k) {
-            const double r = std::hypot(x, z);
-            const double c = r == 0 ? 1.0 : x / r;
-            const double s = r == 0 ? 0.0 : z / r;
+            // sqrt(x^2 + z^2) directly where neither square can overflow or underflow
+            const double ax = std::fabs(x), az = std::fabs(z), big = ax > az ? ax : az;
+            const double r = (big < 1e150 && big > 1e-150) ? std::sqrt(x * x + z * z) : std::hypot(x, z);
+            const double ir = r == 0 ? 0.0 : 1.0 / r;
+            const double c = r == 0 ? 1.0 : x * ir;
+            const double s = z * ir;
             if (k > lo) e[k - 1] = r;
             const double a0 = d[k], b0 = e[k], g0 = d[k + 1];
             d[k] = c * c * a0 + 2 * c * s * b0 + s * s * g0;
@@ -125,22 +158,16 @@ int sym_eig(int n, const double *A, int lda, double *w, double *V, int ldv) {
                 e[k + 1] = c * e[k + 1];
                 x = e[k];
             }
-            double *zk = &Z[(size_t)n * k], *zk1 = &Z[(size_t)n * (k + 1)];
-            for (int i = 0; i < n; ++i) {
-                const double u = zk[i], v = zk1[i];
-                zk[i] = c * u + s * v;
-                zk1[i] = -s * u + c * v;
-            }
+            rot(n, &Z[nn * k], &Z[nn * (k + 1)], c, s);
         }
     }
-    // sort ascending
     std::vector<int> ord(n);
     std::iota(ord.begin(), ord.end(), 0);
     std::stable_sort(ord.begin(), ord.end(), [&](int i, int j) { return d[i] < d[j]; });
     for (int jj = 0; jj < n; ++jj) {
         const int j = ord[jj];
         w[jj] = d[j];
-        for (int i = 0; i < n; ++i) V[i + (size_t)ldv * jj] = Z[i + (size_t)n * j];
+        for (int i = 0; i < n; ++i) V[i + (size_t)ldv * jj] = Z[i + nn * j];
     }
     return 0;
 }
