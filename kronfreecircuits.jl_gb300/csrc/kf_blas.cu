@@ -172,7 +172,9 @@ static Gram32Shape gram32_shape(int ka, int kb) {
     if (tr < 64) tr = 64;
     if (tr > 512) tr = 512;
     while (tr > 64 && (size_t)G32_STAGES * cols * (tr + G32_PAD) * 4 > (size_t)G32_SMEM) tr -= 64;
-    g.tr = tr;
+    // the kernel is compiled for batch heights 64, 128, 256 and 384 (shared-memory offsets as
+    // immediates); take the largest of them that fits
+    g.tr = tr >= 384 ? 384 : tr >= 256 ? 256 : tr >= 128 ? 128 : 64;
     return g;
 }
 
@@ -182,19 +184,29 @@ static size_t gram32_smem(const Gram32Shape &g) {
 
 // stage rows [row0, row0 + tr) of columns c0 .. c0 + nc - 1 of the column set `src` into dst
 // (column stride tr + G32_PAD); rows at or past `rend` are zero-filled
-template <bool VEC>
-__device__ __forceinline__ void g32_stage(float *dst, const Cols2 &src, int c0, int nc, int tr, int64_t row0,
-                                          int64_t rend) {
-    const int S = tr + G32_PAD;
+template <bool VEC, int TR>
+__device__ __forceinline__ void g32_stage(float *dst, const Cols2 &src, int c0, int nc, int64_t row0, int64_t rend) {
+    constexpr int tr = TR, S = TR + G32_PAD;
     if (VEC) {
-        const int per = tr / 4;
-        for (int e = threadIdx.x; e < nc * per; e += blockDim.x) {
-            const int c = e / per, q = e % per;
-            const int64_t r = row0 + 4 * q;
-            const int64_t left = rend - r;
-            const int bytes = left >= 4 ? 16 : left > 0 ? (int)left * 4 : 0;
-            const float *g = src.col(c0 + c) + (bytes > 0 ? r : 0);
-            cp_async16(dst + c * S + 4 * q, g, bytes);
+        // warp w stages columns w, w + 8, ...: the column pointer is warp-uniform and computed once
+        // per column, the lanes take consecutive 16-byte pieces; a batch wholly below rend (all
+        // but a CTA's last) skips the bounds arithmetic
+        constexpr int per = TR / 4;
+        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+        const bool full = row0 + tr <= rend;
+        for (int c = warp; c < nc; c += nw) {
+            const float *col = src.col(c0 + c) + row0;
+            float *d = dst + c * S;
+            if (full) {
+#pragma unroll
+                for (int q = lane; q < per; q += 32) cp_async16(d + 4 * q, col + 4 * q, 16);
+            } else {
+                for (int q = lane; q < per; q += 32) {
+                    const int64_t left = rend - (row0 + 4 * q);
+                    const int bytes = left >= 4 ? 16 : left > 0 ? (int)left * 4 : 0;
+                    cp_async16(d + 4 * q, bytes > 0 ? col + 4 * q : col - row0, bytes);
+                }
+            }
         }
     } else {
         for (int e = threadIdx.x; e < nc * tr; e += blockDim.x) {
@@ -218,11 +230,11 @@ __device__ __forceinline__ void g32_butterfly(float *f, int lane) {
     }
 }
 
-template <bool VEC>
+template <bool VEC, int TR>
 __global__ void __launch_bounds__(256, 2) k_gram32(const Cols2 A, int ka, const Cols2 B, int kb, int64_t N,
                                                    int64_t rows_per, Gram32Shape sh, double *__restrict__ partials) {
     extern __shared__ __align__(16) unsigned char g32_smem[];
-    const int tr = sh.tr, S = tr + G32_PAD;
+    constexpr int tr = TR, S = TR + G32_PAD;
     const int gi = blockIdx.y / sh.ngj, gj = blockIdx.y % sh.ngj;
     const int ti0 = gi * sh.gti, tj0 = gj * sh.gtj;
     const int gti = min(sh.gti, sh.nti - ti0), gtj = min(sh.gtj, sh.ntj - tj0);
@@ -231,10 +243,14 @@ __global__ void __launch_bounds__(256, 2) k_gram32(const Cols2 A, int ka, const 
     const int sa = gti * 8, sb = gtj * 8;                                     // slab widths (padded)
     float *const buf0 = reinterpret_cast<float *>(g32_smem);
     const int bstride = (sa + sb) * S;   // stage t starts at buf0 + t * bstride
-    // padding columns stay zero in every stage
-    for (int e = threadIdx.x; e < G32_STAGES * bstride; e += blockDim.x) {
-        const int c = (e % bstride) / S;
-        if ((c < sa && c >= nca) || (c >= sa && c - sa >= ncb)) buf0[e] = 0.f;
+    // padding columns (A's [nca, sa), B's [ncb, sb)) stay zero in every stage; only they are written
+    {
+        const int pa = sa - nca, pb = sb - ncb, pw = (pa + pb) * S;
+        for (int e = threadIdx.x; e < G32_STAGES * pw; e += blockDim.x) {
+            const int t = e / pw, rem = e - t * pw, pc = rem / S, q = rem - pc * S;
+            const int c = pc < pa ? nca + pc : sa + ncb + (pc - pa);
+            buf0[t * bstride + c * S + q] = 0.f;
+        }
     }
     const int ntile = gti * gtj;
     const int wpt = 8 / ntile;
@@ -257,8 +273,8 @@ __global__ void __launch_bounds__(256, 2) k_gram32(const Cols2 A, int ka, const 
         if (t < nb) {
             float *st = buf0 + t * bstride;
             const int64_t rn = r0 + (int64_t)t * tr;
-            g32_stage<VEC>(st, A, ca0, nca, tr, rn, r1);
-            g32_stage<VEC>(st + sa * S, B, cb0, ncb, tr, rn, r1);
+            g32_stage<VEC, TR>(st, A, ca0, nca, rn, r1);
+            g32_stage<VEC, TR>(st + sa * S, B, cb0, ncb, rn, r1);
         }
         cp_async_commit();
     }
@@ -268,8 +284,8 @@ __global__ void __launch_bounds__(256, 2) k_gram32(const Cols2 A, int ka, const 
         if (bn < nb) {
             float *st = buf0 + (bn % G32_STAGES) * bstride;
             const int64_t rn = r0 + (int64_t)bn * tr;
-            g32_stage<VEC>(st, A, ca0, nca, tr, rn, r1);
-            g32_stage<VEC>(st + sa * S, B, cb0, ncb, tr, rn, r1);
+            g32_stage<VEC, TR>(st, A, ca0, nca, rn, r1);
+            g32_stage<VEC, TR>(st + sa * S, B, cb0, ncb, rn, r1);
         }
         cp_async_commit();
         cp_async_wait<G32_STAGES - 1>();   // batch b has landed (this thread's copies)
@@ -324,10 +340,10 @@ static bool gram32_try_tc(const float *A0, int64_t lda0, int ka0, const float *A
     if (N < GRAM_TC_MIN_ROWS) return false;
     // a tcgen05.mma (K = 8 rows) costs about the same whatever its width up to N = 128, so the
     // tensor-core Gram takes a near-constant time per row; the SIMT kernel's grows with the padded
-    // output (measured on 671,744 rows: 16 x 32 SIMT 68 us vs 120 us, 32 x 32 110 vs 114, 24 x 40
-    // 148 vs 117, 48 x 48 512 vs 131)
+    // output (measured on 671,744 rows: 16 x 32 SIMT 43 us vs 120 us, 32 x 32 71 vs 90, 24 x 40
+    // 92 vs 116, 48 x 48 547 vs 127): the tensor cores from 24 8 x 8 output tiles on
     const int pa = (ka0 + ka1 + 7) / 8 * 8, pb = (kb0 + kb1 + 7) / 8 * 8;
-    if (pa * pb < 1024) return false;
+    if (pa * pb < 1536) return false;
     const size_t cap = gram_partials_size(ka0 + ka1, kb0 + kb1, N);
     GramTcSrc src[4];
     int n = 0;
@@ -366,20 +382,20 @@ void gram32_sets(const float *A0, int64_t lda0, int ka0, const float *A1, int64_
     const size_t smem = gram32_smem(sh);
     auto al = [](const float *p, int64_t ld) { return ld % 4 == 0 && (uintptr_t)p % 16 == 0; };
     const bool vec = al(A.p0, A.ld0) && al(A.p1, A.ld1) && al(B.p0, B.ld0) && al(B.p1, B.ld1);
-    static int attr_dev_mask[2] = {0, 0};   // devices whose kernel attribute is set, per variant
+    using Kern = void (*)(const Cols2, int, const Cols2, int, int64_t, int64_t, Gram32Shape, double *);
+    static const Kern kerns[2][4] = {
+        {k_gram32<false, 64>, k_gram32<false, 128>, k_gram32<false, 256>, k_gram32<false, 384>},
+        {k_gram32<true, 64>, k_gram32<true, 128>, k_gram32<true, 256>, k_gram32<true, 384>}};
+    const int ti = sh.tr == 64 ? 0 : sh.tr == 128 ? 1 : sh.tr == 256 ? 2 : 3;
+    static int attr_dev_mask = 0;   // devices whose kernel attributes are set
     int dev = 0;
     KF_CUDA(cudaGetDevice(&dev));
-    if (dev < 31 && !(attr_dev_mask[vec] & (1 << dev))) {
-        if (vec)
-            KF_CUDA(cudaFuncSetAttribute(k_gram32<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, G32_SMEM));
-        else
-            KF_CUDA(cudaFuncSetAttribute(k_gram32<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, G32_SMEM));
-        attr_dev_mask[vec] |= 1 << dev;
+    if (dev < 31 && !(attr_dev_mask & (1 << dev))) {
+        for (auto &row : kerns)
+            for (Kern k : row) KF_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, G32_SMEM));
+        attr_dev_mask |= 1 << dev;
     }
-    if (vec)
-        k_gram32<true><<<dim3(nc, groups), 256, smem, s>>>(A, ka, B, kb, N, rp, sh, partials);
-    else
-        k_gram32<false><<<dim3(nc, groups), 256, smem, s>>>(A, ka, B, kb, N, rp, sh, partials);
+    kerns[vec ? 1 : 0][ti]<<<dim3(nc, groups), 256, smem, s>>>(A, ka, B, kb, N, rp, sh, partials);
     KF_LAUNCH_CHECK();
     reduce_partials(partials, nc, ka * kb, G, s);
 }
@@ -793,54 +809,64 @@ void scale_add(double *Y, const double *X, const double *d, const float *P, floa
 // rows of X'Z first), S = Z'Z - (X'Z)'(X'Z) (the Gram of (I - XX')Z), its Cholesky factor
 // S = R'R (R upper), and the coefficients C = [R^-1 ; -(X'Z) R^-1] ((r + wx) x r) with which
 // [Z X] C = (I - XX') Z R^-1 is orthonormal.  One CTA; *status = 0, or 1 when a pivot is not
-// finite or below 1e-4 (C is then not to be used).  r <= 64 (2 r^2 floats of shared memory).
+// finite or below 1e-4 (C is then not to be used).  r <= 64.
 // The arithmetic is FP32: Z is an FP32 block that the first pass already orthonormalised, so S is
 // near the identity (a pivot below 1e-4 goes to the host) and FP32 factors are as accurate as the
 // FP32 update that applies them; GB300's FP64 rate made the FP64 version ~50 us.
+// The kernel is latency-bound: G is staged in shared memory by one coalesced pass (no global
+// load inside a dependent chain), and the factorisation and R^-1 run on warp 0 alone with warp
+// synchronisation (lane l owns columns l and l + 32), so no CTA barrier sits inside the loops.
 __global__ void k_chol2_coeffs(const double *__restrict__ G, int wx, int r, double *__restrict__ C,
                                int *__restrict__ status) {
     extern __shared__ float cs[];
-    float *S = cs;               // r x r, column-major; becomes R (upper)
-    float *Ri = cs + r * r;      // r x r, R^-1
-    __shared__ int bad;
-    const int tid = threadIdx.x, nt = blockDim.x;
     const int ld = wx + r;
-    if (tid == 0) bad = 0;
+    float *Gs = cs;              // ld x r, G in FP32
+    float *S = Gs + ld * r;      // r x r, column-major; becomes R (upper)
+    float *Ri = S + r * r;       // r x r, R^-1
+    const int tid = threadIdx.x, nt = blockDim.x;
+    for (int e = tid; e < ld * r; e += nt) Gs[e] = (float)G[e];
+    __syncthreads();
     for (int e = tid; e < r * r; e += nt) {
         const int i = e % r, j = e / r;
-        float v = (float)G[wx + i + (size_t)ld * j];
-        for (int q = 0; q < wx; ++q) v = fmaf(-(float)G[q + (size_t)ld * i], (float)G[q + (size_t)ld * j], v);
+        float v = Gs[wx + i + ld * j];
+        for (int q = 0; q < wx; ++q) v = fmaf(-Gs[q + ld * i], Gs[q + ld * j], v);
         S[e] = v;
         Ri[e] = 0.f;
     }
     __syncthreads();
-    // right-looking Cholesky, upper factor: column k of R is row k of the trailing matrix
-    for (int k = 0; k < r; ++k) {
-        if (tid == 0) {
+    if (tid < 32) {
+        const int lane = tid;
+        bool bad = false;
+        // right-looking Cholesky, upper factor: column k of R is row k of the trailing matrix
+        for (int k = 0; k < r; ++k) {
             const float d = S[k + r * k];
             // S is the Gram of a block the first pass already orthonormalised (S ~ I): a pivot
             // below 1e-4 is a nearly dependent direction, left to the host's SVQB
-            if (!(d > 1e-4f) || !isfinite(d)) bad = 1;
-            S[k + r * k] = sqrtf(d > 0.f ? d : 1.f);
+            if (!(d > 1e-4f) || !isfinite(d)) bad = true;
+            const float rkk = sqrtf(d > 0.f ? d : 1.f);
+            __syncwarp();
+            for (int j = lane; j < r; j += 32) {
+                if (j == k) S[k + r * k] = rkk;
+                else if (j > k) S[k + r * j] /= rkk;
+            }
+            __syncwarp();
+            for (int j = lane; j < r; j += 32) {
+                if (j <= k) continue;
+                const float skj = S[k + r * j];
+                for (int i = k + 1; i <= j; ++i) S[i + r * j] = fmaf(-S[k + r * i], skj, S[i + r * j]);
+            }
+            __syncwarp();
         }
-        __syncthreads();
-        const float rkk = S[k + r * k];
-        for (int j = k + 1 + tid; j < r; j += nt) S[k + r * j] /= rkk;
-        __syncthreads();
-        for (int e = tid; e < (r - k - 1) * (r - k - 1); e += nt) {
-            const int i = k + 1 + e % (r - k - 1), j = k + 1 + e / (r - k - 1);
-            if (i <= j) S[i + r * j] = fmaf(-S[k + r * i], S[k + r * j], S[i + r * j]);
+        // R^-1 column by column (back substitution), one lane per column
+        for (int j = lane; j < r; j += 32) {
+            Ri[j + r * j] = 1.f / S[j + r * j];
+            for (int i = j - 1; i >= 0; --i) {
+                float v = 0.f;
+                for (int k = i + 1; k <= j; ++k) v = fmaf(S[i + r * k], Ri[k + r * j], v);
+                Ri[i + r * j] = -v / S[i + r * i];
+            }
         }
-        __syncthreads();
-    }
-    // R^-1 column by column (back substitution), one thread per column
-    for (int j = tid; j < r; j += nt) {
-        Ri[j + r * j] = 1.f / S[j + r * j];
-        for (int i = j - 1; i >= 0; --i) {
-            float v = 0.f;
-            for (int k = i + 1; k <= j; ++k) v = fmaf(S[i + r * k], Ri[k + r * j], v);
-            Ri[i + r * j] = -v / S[i + r * i];
-        }
+        if (lane == 0) *status = bad ? 1 : 0;
     }
     __syncthreads();
     const int lc = r + wx;
@@ -852,17 +878,25 @@ __global__ void k_chol2_coeffs(const double *__restrict__ G, int wx, int r, doub
         } else {
             const int q = i - r;
             v = 0.f;
-            for (int t = 0; t <= j; ++t) v = fmaf((float)G[q + (size_t)ld * t], Ri[t + r * j], v);
+            for (int t = 0; t <= j; ++t) v = fmaf(Gs[q + ld * t], Ri[t + r * j], v);
             v = -v;
         }
         C[i + (size_t)lc * j] = (double)v;
     }
-    if (tid == 0) *status = bad;
 }
 
 void chol2_coeffs(const double *G, int wx, int r, double *C, int *status, cudaStream_t s) {
-    KF_REQUIRE(r >= 1 && r <= CHOL2_MAX_R, KF_EINVAL, "chol2_coeffs: block width out of range");
-    const size_t smem = (size_t)2 * r * r * sizeof(float);
+    KF_REQUIRE(r >= 1 && r <= CHOL2_MAX_R && wx >= 0 && wx <= 128, KF_EINVAL,
+               "chol2_coeffs: block width out of range");
+    const size_t smem = ((size_t)(wx + r) * r + (size_t)2 * r * r) * sizeof(float);
+    static int attr_dev_mask = 0;
+    int dev = 0;
+    KF_CUDA(cudaGetDevice(&dev));
+    if (dev < 31 && !(attr_dev_mask & (1 << dev))) {
+        // up to (128 + 64) x 64 + 2 x 64 x 64 floats
+        KF_CUDA(cudaFuncSetAttribute(k_chol2_coeffs, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
+        attr_dev_mask |= 1 << dev;
+    }
     k_chol2_coeffs<<<1, 256, smem, s>>>(G, wx, r, C, status);
     KF_LAUNCH_CHECK();
 }
