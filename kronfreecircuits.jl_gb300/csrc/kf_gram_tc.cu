@@ -18,7 +18,11 @@
 //     and ONE MMA per K step gives hi*hi | hi*lo (accumulator rows 0..63) and lo*hi | lo*lo
 //     (rows 64..127; lo*lo is not used);
 //   RB = 128: two MMAs per K step, A_hi x [B_hi; B_lo] and A_lo x [B_hi; B_lo] (whose lo*lo half
-//     is not used either).
+//     is not used either);
+//   SPLIT (the row sources and the column sources disjoint, up to 64 rows each -- the Rayleigh-Ritz
+//     Gram [X_a Q]'[HX_a HZ]): the stage's 256 rows hold A_hi | A_lo | B_hi | B_lo, so
+//     [A_hi; A_lo] (M = 128) x [B_hi; B_lo] is again ONE MMA per K step, with the RB = 64
+//     accumulator layout.
 // The epilogue adds hi*hi + hi*lo on the lanes of the hi rows and lo*hi on the lanes of the lo
 // rows into two FP32 partial sets per CTA; the reduction sums both.
 //
@@ -155,6 +159,7 @@ struct GtArgs {
     int64_t N;
     int64_t nchunks;
     int b_off, nbr;                // B rows: hi rows [b_off, RB) = lo rows [0, nbr); nbr % 16 == 0
+                                   // (SPLIT: stage rows RB + [0, nbr) and RB + nbr + [0, nbr))
     int nr, nc;                    // output entries (nr x nc, column-major)
     uint8_t rinv_hi[128];          // hi image row -> output row (255: not wanted)
     uint8_t rinv_lo[128];          // lo image row -> output row
@@ -163,10 +168,11 @@ struct GtArgs {
     int *err;
 };
 
-template <int RB, int S, int R>
+template <int RB, int S, int R, bool SPLIT = false>
 __global__ void __launch_bounds__(GT_THREADS, 1) k_gram_tc(const GtArgs a) {
     using P = GtPlan<RB, S, R>;
-    constexpr bool ONE = RB == 64;             // one MMA per K step ([A_hi; A_lo] x [B_hi; B_lo])
+    static_assert(!SPLIT || RB == 128, "the split layout fills two 128-row images");
+    constexpr bool ONE = RB == 64 || SPLIT;    // one MMA per K step ([A_hi; A_lo] x [B_hi; B_lo])
     // two accumulator slots at power-of-two column offsets (measured faster than packed slots);
     // RB = 128: the second MMA's accumulator 128 columns into the slot
     constexpr uint32_t SLOT = ONE ? 128 : 256;
@@ -209,10 +215,12 @@ __global__ void __launch_bounds__(GT_THREADS, 1) k_gram_tc(const GtArgs a) {
     if ((int64_t)blockIdx.x < a.nchunks) my = (a.nchunks - 1 - blockIdx.x) / gridDim.x + 1;
 
     if (warp < 8) {
-        // ---- producers.  Piece e: hi row 8 (e / 64) + e % 8, data rows 4 ((e / 8) % 8) .. + 3 of
+        // ---- producers.  Piece e: pool row 8 (e / 64) + e % 8, data rows 4 ((e / 8) % 8) .. + 3 of
         // the chunk; a quarter-warp covers the 8 rows of one core matrix (conflict-free 16-byte
-        // stores), a warp 8 pool columns x 16 data rows (64-byte runs per column).  The lo part of
-        // hi row m goes to lo row m - b_off (B rows) or m + nbr (the others).
+        // stores), a warp 8 pool columns x 16 data rows (64-byte runs per column).  Positions count
+        // the stage's rows across both images (the lo image starts at row RB).  Pool row m sits at
+        // hi row m and its lo part at lo row m - b_off (B rows) or m + nbr (the others); SPLIT: an A
+        // row m at m and 64 + m, B row b_off + r at RB + r and RB + nbr + r.
         const float *gp[P::PPT];
         uint32_t soff[P::PPT], loff[P::PPT];
         int k4[P::PPT];
@@ -220,10 +228,17 @@ __global__ void __launch_bounds__(GT_THREADS, 1) k_gram_tc(const GtArgs a) {
         for (int j = 0; j < P::PPT; ++j) {
             const int e = tid + j * GT_PROD;
             const int m = (e / 64) * 8 + (e & 7);
-            const int ml = m >= a.b_off ? m - a.b_off : m + a.nbr;
+            int ph, pl;
+            if (SPLIT) {
+                ph = m < a.b_off ? m : RB + (m - a.b_off);
+                pl = m < a.b_off ? 64 + m : RB + a.nbr + (m - a.b_off);
+            } else {
+                ph = m;
+                pl = RB + (m >= a.b_off ? m - a.b_off : m + a.nbr);
+            }
             k4[j] = (e >> 3) & 7;
-            soff[j] = (uint32_t)((m >> 3) * GT_SBO + k4[j] * 128 + (m & 7) * 16);
-            loff[j] = (uint32_t)(P::IMG + (ml >> 3) * GT_SBO + k4[j] * 128 + (ml & 7) * 16);
+            soff[j] = (uint32_t)((ph >> 3) * GT_SBO + k4[j] * 128 + (ph & 7) * 16);
+            loff[j] = (uint32_t)((pl >> 3) * GT_SBO + k4[j] * 128 + (pl & 7) * 16);
             gp[j] = nullptr;
             for (int q = 0; q < a.nsrc; ++q)
                 if (m >= a.off[q] && m < a.off[q] + a.k[q]) gp[j] = a.p[q] + (int64_t)(m - a.off[q]) * a.ld[q];
@@ -286,7 +301,7 @@ __global__ void __launch_bounds__(GT_THREADS, 1) k_gram_tc(const GtArgs a) {
             const uint32_t n1 = (uint32_t)(2 * a.nbr);
             const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((n1 >> 3) << 17) | ((128u >> 4) << 24);
             const uint32_t sbase = gsu32(stages);
-            const uint32_t boff = (uint32_t)(a.b_off >> 3) * GT_SBO;
+            const uint32_t boff = SPLIT ? (uint32_t)P::IMG : (uint32_t)(a.b_off >> 3) * GT_SBO;
             int64_t issued = 0;
             for (int64_t t = 0; t < my; ++t) {
                 const int s = (int)(t % S), sl = (int)(t & 1);
@@ -397,14 +412,14 @@ __global__ void k_reduce_partials_f32(const float *__restrict__ part, int nparts
 }
 
 using GtKernel = void (*)(const GtArgs);
-const GtKernel g_gt_kern[2] = {k_gram_tc<64, 12, 2>, k_gram_tc<128, 6, 2>};
-const size_t g_gt_smem[2] = {GtPlan<64, 12, 2>::SMEM, GtPlan<128, 6, 2>::SMEM};
+const GtKernel g_gt_kern[3] = {k_gram_tc<64, 12, 2>, k_gram_tc<128, 6, 2>, k_gram_tc<128, 6, 2, true>};
+const size_t g_gt_smem[3] = {GtPlan<64, 12, 2>::SMEM, GtPlan<128, 6, 2>::SMEM, GtPlan<128, 6, 2>::SMEM};
 
 // per device: SM count and, per plan, whether the kernel fits and its attribute is set
 struct GtDevice {
     bool ready = false;
     int sms = 0;
-    bool fits[2] = {false, false};
+    bool fits[3] = {false, false, false};
 };
 std::mutex g_gt_mu;
 GtDevice g_gt_dev[32];
@@ -419,7 +434,7 @@ const GtDevice &gt_device() {
         int optin = 0;
         KF_CUDA(cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, dev));
         KF_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-        for (int p = 0; p < 2; ++p) {
+        for (int p = 0; p < 3; ++p) {
             cudaFuncAttributes fa;
             KF_CUDA(cudaFuncGetAttributes(&fa, g_gt_kern[p]));
             d.fits[p] = g_gt_smem[p] + fa.sharedSizeBytes <= (size_t)optin;
@@ -467,6 +482,8 @@ bool gram_tc(const GramTcSrc *src, int nsrc, int r0, int r1, int c0, int c1, int
     if (nbr > GT_NBR_MAX) return false;
     const int RB = aspan + nbr <= 64 ? 64 : aspan + nbr <= 128 ? 128 : 0;
     if (!RB) return false;
+    // disjoint row and column sources of up to 64 rows each: the one-MMA split layout
+    const bool split = RB == 128 && (r1 <= c0 || c1 <= r0) && aspan <= 64;
     a.nbr = nbr;
     a.b_off = RB - nbr;
     a.nsrc = (int)order.size();
@@ -488,7 +505,7 @@ bool gram_tc(const GramTcSrc *src, int nsrc, int r0, int r1, int c0, int c1, int
         const int i = (int)(std::find(order.begin(), order.end(), q) - order.begin());
         for (int c = 0; c < src[q].k; ++c) {
             const int m = a.off[i] + c;
-            const int ml = m >= a.b_off ? m - a.b_off : m + nbr;
+            const int ml = split ? m : m >= a.b_off ? m - a.b_off : m + nbr;
             a.rinv_hi[m] = (uint8_t)nr;
             a.rinv_lo[ml] = (uint8_t)nr;
             ++nr;
@@ -500,7 +517,7 @@ bool gram_tc(const GramTcSrc *src, int nsrc, int r0, int r1, int c0, int c1, int
     a.nr = nr;
     a.nc = nc;
     const GtDevice &dv = gt_device();
-    const int plan = RB == 64 ? 0 : 1;
+    const int plan = RB == 64 ? 0 : split ? 2 : 1;
     if (!dv.fits[plan]) return false;
     const int grid = (int)std::min<int64_t>(dv.sms, a.nchunks);
     if ((size_t)2 * grid * nr * nc * sizeof(float) > partial_bytes) return false;

@@ -2,8 +2,9 @@
 across CTAs) against a plain PyTorch FP64 product of the same FP32 data: the pools the LOBPCG loops
 build -- [X Z]'Z of the orthogonalisation, [X_a Q]'[HX_a HZ] of the merged Rayleigh-Ritz Gram, the
 refinement's [X_a R Q]'[R Q HZ] -- at block 16 and 20, self Grams, ragged widths, N not a multiple
-of the 32-row chunk (zero-filled tail copies), a leading dimension above N, and the shapes the
-kernel turns down (the solvers then keep the SIMT Gram).
+of the 32-row chunk (zero-filled tail copies), a leading dimension above N, disjoint row and column
+sources of up to 64 rows each (one MMA per K step on [A_hi; A_lo] x [B_hi; B_lo]), and the shapes
+the kernel turns down (the solvers then keep the SIMT Gram).
 
 Tolerance: hi*hi + hi*lo + lo*hi drops lo*lo (2^-20 of a product) and TF32 keeps 10 mantissa bits
 of lo (2^-21): 2e-6 of sqrt(sum|a|^2 sum|b|^2) per entry, as for the SIMT FP32 Gram.
@@ -63,6 +64,12 @@ POOLS = [
     ((1, 3), 0, 1, 1, 2, 5000),
     ((3, 5, 2, 9), 1, 3, 2, 4, 131072),          # a source in neither range
     ((12, 24), 0, 2, 1, 2, 33),                  # two chunks, the second one row long
+    # disjoint row and column sources over 64 rows together: the one-MMA split layout
+    ((7, 13, 30, 2), 0, 2, 2, 4, 131072),
+    ((40, 24), 0, 1, 1, 2, 671744),
+    ((64, 64), 0, 1, 1, 2, 100000),              # 64 + 64 rows, the largest split pool
+    ((24, 40), 1, 2, 0, 1, 99999 + 1),           # the column source listed first
+    ((18, 36, 18, 36), 0, 2, 2, 4, 100003),      # the solver's block 18, ragged N
 ]
 
 
