@@ -211,8 +211,11 @@ __global__ void __launch_bounds__(GT_THREADS, 1) k_gram_tc(const GtArgs a) {
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     const uint32_t tmem = *tslot;
-    int64_t my = 0;   // chunks of this CTA: blockIdx.x, + gridDim.x, ...
-    if ((int64_t)blockIdx.x < a.nchunks) my = (a.nchunks - 1 - blockIdx.x) / gridDim.x + 1;
+    // this CTA's chunks: a contiguous range [c0, c0 + my) (each column streamed in order rather
+    // than in 128-byte pieces spread over the whole grid)
+    const int64_t cper = a.nchunks / gridDim.x, crem = a.nchunks % gridDim.x;
+    const int64_t my = cper + ((int64_t)blockIdx.x < crem ? 1 : 0);
+    const int64_t cfirst = (int64_t)blockIdx.x * cper + ((int64_t)blockIdx.x < crem ? (int64_t)blockIdx.x : crem);
 
     if (warp < 8) {
         // ---- producers.  Piece e: pool row 8 (e / 64) + e % 8, data rows 4 ((e / 8) % 8) .. + 3 of
@@ -246,7 +249,7 @@ __global__ void __launch_bounds__(GT_THREADS, 1) k_gram_tc(const GtArgs a) {
         const uint32_t sbase = gsu32(stages);
         auto issue = [&](int64_t t) {
             const int s = (int)(t % S);
-            const int64_t row0 = ((int64_t)blockIdx.x + t * gridDim.x) * GT_KC;
+            const int64_t row0 = (cfirst + t) * GT_KC;
             const uint32_t hi = sbase + (uint32_t)s * P::STAGE;
 #pragma unroll
             for (int j = 0; j < P::PPT; ++j) {
