@@ -816,6 +816,24 @@ void scale_add(double *Y, const double *X, const double *d, const float *P, floa
 // The kernel is latency-bound: G is staged in shared memory by one coalesced pass (no global
 // load inside a dependent chain), and the factorisation and R^-1 run on warp 0 alone with warp
 // synchronisation (lane l owns columns l and l + 32), so no CTA barrier sits inside the loops.
+// column j of the trailing matrix minus row k's outer product: colj[i] -= rowk[i] skj, i = k+1..j
+// (row k in its own buffer, so the loads need not wait for the stores)
+__device__ __forceinline__ void chol2_col_update(float *__restrict__ colj, const float *__restrict__ rowk, int k,
+                                                 int j, float skj) {
+#pragma unroll 4
+    for (int i = k + 1; i <= j; ++i) colj[i] = fmaf(-rowk[i], skj, colj[i]);
+}
+
+// column j of R^-1 by back substitution (R upper, r x r, column-major)
+__device__ __forceinline__ void chol2_inv_col(const float *__restrict__ R, float *__restrict__ y, int r, int j) {
+    y[j] = 1.f / R[j + r * j];
+    for (int i = j - 1; i >= 0; --i) {
+        float v = 0.f;
+        for (int k = i + 1; k <= j; ++k) v = fmaf(R[i + r * k], y[k], v);
+        y[i] = -v / R[i + r * i];
+    }
+}
+
 __global__ void k_chol2_coeffs(const double *__restrict__ G, int wx, int r, double *__restrict__ C,
                                int *__restrict__ status) {
     extern __shared__ float cs[];
@@ -823,6 +841,7 @@ __global__ void k_chol2_coeffs(const double *__restrict__ G, int wx, int r, doub
     float *Gs = cs;              // ld x r, G in FP32
     float *S = Gs + ld * r;      // r x r, column-major; becomes R (upper)
     float *Ri = S + r * r;       // r x r, R^-1
+    float *rowk = Ri + r * r;    // r: row k of R during step k
     const int tid = threadIdx.x, nt = blockDim.x;
     for (int e = tid; e < ld * r; e += nt) Gs[e] = (float)G[e];
     __syncthreads();
@@ -846,26 +865,21 @@ __global__ void k_chol2_coeffs(const double *__restrict__ G, int wx, int r, doub
             const float rkk = sqrtf(d > 0.f ? d : 1.f);
             __syncwarp();
             for (int j = lane; j < r; j += 32) {
-                if (j == k) S[k + r * k] = rkk;
-                else if (j > k) S[k + r * j] /= rkk;
+                if (j == k) {
+                    S[k + r * k] = rkk;
+                } else if (j > k) {
+                    const float v = S[k + r * j] / rkk;
+                    S[k + r * j] = v;
+                    rowk[j] = v;
+                }
             }
             __syncwarp();
-            for (int j = lane; j < r; j += 32) {
-                if (j <= k) continue;
-                const float skj = S[k + r * j];
-                for (int i = k + 1; i <= j; ++i) S[i + r * j] = fmaf(-S[k + r * i], skj, S[i + r * j]);
-            }
+            for (int j = lane; j < r; j += 32)
+                if (j > k) chol2_col_update(S + r * j, rowk, k, j, rowk[j]);
             __syncwarp();
         }
         // R^-1 column by column (back substitution), one lane per column
-        for (int j = lane; j < r; j += 32) {
-            Ri[j + r * j] = 1.f / S[j + r * j];
-            for (int i = j - 1; i >= 0; --i) {
-                float v = 0.f;
-                for (int k = i + 1; k <= j; ++k) v = fmaf(S[i + r * k], Ri[k + r * j], v);
-                Ri[i + r * j] = -v / S[i + r * i];
-            }
-        }
+        for (int j = lane; j < r; j += 32) chol2_inv_col(S, Ri + r * j, r, j);
         if (lane == 0) *status = bad ? 1 : 0;
     }
     __syncthreads();
@@ -888,7 +902,7 @@ __global__ void k_chol2_coeffs(const double *__restrict__ G, int wx, int r, doub
 void chol2_coeffs(const double *G, int wx, int r, double *C, int *status, cudaStream_t s) {
     KF_REQUIRE(r >= 1 && r <= CHOL2_MAX_R && wx >= 0 && wx <= 128, KF_EINVAL,
                "chol2_coeffs: block width out of range");
-    const size_t smem = ((size_t)(wx + r) * r + (size_t)2 * r * r) * sizeof(float);
+    const size_t smem = ((size_t)(wx + r) * r + (size_t)2 * r * r + r) * sizeof(float);
     static int attr_dev_mask = 0;
     int dev = 0;
     KF_CUDA(cudaGetDevice(&dev));
@@ -980,8 +994,10 @@ void residual_block(const T *X, const T *HX, int64_t ld, int k, int64_t N, const
     KF_LAUNCH_CHECK();
 }
 
-// A counter-based normal generator: splitmix64 of (seed, stream, column, row) into two
-// uniforms, Box-Muller.  Reproducible for a given seed whatever the launch shape.
+// A counter-based normal generator: splitmix64 of (seed, stream, column, row) into two 24-bit
+// uniforms, Box-Muller in FP32 (the draws are start and perturbation directions, where FP32
+// normals truncated at 5.8 sigma serve as well as FP64 ones, and GB300's FP64 log / cos made the
+// FP64 version ~1 ms per 13M draws).  Reproducible for a given seed whatever the launch shape.
 __device__ inline uint64_t mix64(uint64_t z) {
     z += 0x9e3779b97f4a7c15ull;
     z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
@@ -996,9 +1012,9 @@ __global__ void k_fill_normal(T *__restrict__ X, int64_t ld, int64_t N, int k, u
     const int64_t c = t / N, r = t % N;
     const uint64_t h = mix64(mix64(mix64(seed) ^ (sid * 0x632be59bd9b4e019ull)) ^ ((uint64_t)c << 40) ^ (uint64_t)r);
     const uint64_t h2 = mix64(h);
-    const double u1 = ((h >> 11) + 1) * (1.0 / 9007199254740993.0);   // (0, 1]
-    const double u2 = (h2 >> 11) * (1.0 / 9007199254740992.0);         // [0, 1)
-    X[c * ld + r] = (T)(sqrt(-2.0 * log(u1)) * cospi(2.0 * u2));
+    const float u1 = (float)((h >> 40) + 1) * (1.0f / 16777216.0f);   // (0, 1]
+    const float u2 = (float)(h2 >> 40) * (1.0f / 16777216.0f);         // [0, 1)
+    X[c * ld + r] = (T)(sqrtf(-2.0f * logf(u1)) * cospif(2.0f * u2));
 }
 
 template <typename T>
