@@ -13,11 +13,14 @@ fresh FP64 application.
   e2e              the public API end to end with host buffers: kf_op_create from the host term
                    list, solve (product seed built by the library), host eigenpairs out, kf_op_destroy,
                    every step
-  roofline         the dominant kernel of a warm solve by the ncu launch list, the separable
-                   preconditioner's tcgen05 mode product (256-point axis, 18 columns): algorithmic
-                   bytes 2 N b 4 per launch over its CUDA-event time, against the measured HBM copy
-                   bandwidth; roofline_gram / roofline_apply: the tensor-core Gram of the
-                   orthogonalisation ([X Z]'Z, 18 + 36 columns, N b 4) and the fused stencil apply
+  roofline         the dominant kernel of a warm solve by the ncu launch list (its template
+                   instantiations summed), the fused stencil apply k_apply_fused<float>: algorithmic
+                   bytes 2 N b 4 per launch (16 columns) over its CUDA-event time, against the measured
+                   HBM copy bandwidth; roofline_update / roofline_mode / roofline_gram: the tcgen05
+                   FP32 block update on the fused X/P Rayleigh-Ritz shape ([X_a Q] C, 18 + 36 -> 36
+                   columns, (54 + 36) N 4), the separable preconditioner's tcgen05 mode product
+                   (256-point axis, 18 columns, 2 N b 4) and the tensor-core Gram of the
+                   orthogonalisation ([X Z]'Z, 18 + 36 columns, N b 4)
   cpu_baseline     the oracle's restatement of the reference CPU path (C/OpenMP mul! + NumPy LOBPCG)
                    on the host cores, a bounded sample
 
@@ -53,6 +56,7 @@ NDRAWS = 64
 # 0.1 MB of partials)
 APPLY_TRAFFIC_BYTES = 55641088
 MODE_TRAFFIC_BYTES = 50463488
+UPDATE_TRAFFIC_BYTES = 200817152   # ncu dram bytes read + written, one launch (the rest of Y stays in L2)
 GRAM_TC_TRAFFIC_BYTES = 145235200
 
 
@@ -266,10 +270,13 @@ def run_ours(args, D):
     torch.cuda.synchronize()
     te = D.max(time.perf_counter() - t0)
     conv_e = D.sum(conv_e)
-    # roofline of the dominant kernel of a warm solve (by the ncu launch list: the preconditioner's
-    # tcgen05 mode product), of the tensor-core Gram and of the fused stencil apply
+    # roofline of the dominant kernel of a warm solve (by the ncu launch list: the fused stencil
+    # apply), of the tcgen05 block update on the fused X/P Rayleigh-Ritz shape, of the
+    # preconditioner's mode product and of the tensor-core Gram
     H0 = ops[idx[0]][0]
     peak, kind = peaks()
+    t_upd = time_update(torch, 1, 18, 36, 36, H0.N)
+    alg_upd = (18 + 36 + 36) * H0.N * 4
     t_mode = time_mode_product(torch, 1, (41, 256, 64), 1, b=MODE_COLS)
     alg_mode = 2 * H0.N * MODE_COLS * 4
     t_gram = time_gram_tc(torch, (18, 36), (0, 2, 1, 2), H0.N)
@@ -295,17 +302,23 @@ def run_ours(args, D):
         "max_residual_rel": max(s["max_residual"] / s["hnorm"] for s in stats),
         "e2e": {"value": conv_e / te, "unit": "eigenpairs/s", "h2d_bytes_per_step": int(h2d / ke),
                 "d2h_bytes_per_step": int(d2h / ke), "steps": ke},
-        "roofline": {"bound": "hbm", "achieved": alg_mode / t_mode / 1e9, "peak": peak, "unit": "GB/s",
-                     "frac": alg_mode / t_mode / 1e9 / peak, "traffic": MODE_TRAFFIC_BYTES,
-                     "kernel": f"k_mode_pipe<64> (pipelined tcgen05 BF16 mode product, 256-point axis, {MODE_COLS} columns)",
-                     "algorithmic_bytes": alg_mode, "launch_us": t_mode * 1e6, "peak_kind": kind},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": APPLY_TRAFFIC_BYTES, "kernel": "k_apply_fused<float> (fused stencil apply, 16 columns, the tuned variant)",
+                     "algorithmic_bytes": alg, "launch_us": t_apply * 1e6, "peak_kind": kind},
+        "roofline_update": {"bound": "hbm", "achieved": alg_upd / t_upd / 1e9, "peak": peak, "unit": "GB/s",
+                            "frac": alg_upd / t_upd / 1e9 / peak, "traffic": UPDATE_TRAFFIC_BYTES,
+                            "kernel": "k_update_tc<3> (tcgen05 FP32 block update, TF32 hi / lo, 3-tile staging ring: "
+                                      "[X_a Q] C, 18 + 36 -> 36 columns, the fused X/P Rayleigh-Ritz update)",
+                            "algorithmic_bytes": alg_upd, "launch_us": t_upd * 1e6, "peak_kind": kind},
+        "roofline_mode": {"bound": "hbm", "achieved": alg_mode / t_mode / 1e9, "peak": peak, "unit": "GB/s",
+                          "frac": alg_mode / t_mode / 1e9 / peak, "traffic": MODE_TRAFFIC_BYTES,
+                          "kernel": f"k_mode_pipe<64> (pipelined tcgen05 BF16 mode product, 256-point axis, "
+                                    f"{MODE_COLS} columns)",
+                          "algorithmic_bytes": alg_mode, "launch_us": t_mode * 1e6, "peak_kind": kind},
         "roofline_gram": {"bound": "hbm", "achieved": alg_gram / t_gram / 1e9, "peak": peak, "unit": "GB/s",
                           "frac": alg_gram / t_gram / 1e9 / peak, "traffic": GRAM_TC_TRAFFIC_BYTES,
                           "kernel": "k_gram_tc + k_reduce_partials_f32 ([X Z]'Z, 18 + 36 FP32 columns)",
                           "algorithmic_bytes": alg_gram, "launch_us": t_gram * 1e6, "peak_kind": kind},
-        "roofline_apply": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                           "traffic": APPLY_TRAFFIC_BYTES, "kernel": "k_apply_fused<float> (16 columns)",
-                           "algorithmic_bytes": alg, "launch_us": t_apply * 1e6, "peak_kind": kind},
         "clocks": clk, "gpu_launches": launches,
     }
     if not args.no_cpu and D.world == 1:

@@ -688,10 +688,24 @@ __global__ void k_residual_precond(const T *__restrict__ X, const T *__restrict_
     const T *x = X + (int64_t)col * ld;
     const T *hx = HX + (int64_t)col * ld;
     T *rr = R + (int64_t)col * ldr;
+    // FP32 data: eight squares summed in FP32, then added into the FP64 sum (GB300's FP64 pipe,
+    // about 1/64 of the FP32 rate, bounded this kernel when every square was converted and added
+    // in FP64; an eight-term FP32 sum is accurate to ~5e-7 relative)
     double s = 0;
+    T sf = 0;
+    int cnt = 0;
     for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
         const T v = hx[r] - th * x[r];
-        s += (double)v * (double)v;
+        if constexpr (sizeof(T) == 4) {
+            sf = fmaf(v, v, sf);
+            if (++cnt == 8) {
+                s += (double)sf;
+                sf = 0;
+                cnt = 0;
+            }
+        } else {
+            s += (double)v * (double)v;
+        }
         T out = v;
         if (mode == 0) {
             out = (T)((double)v / hypot(D[r] - tp, eta));
@@ -700,6 +714,7 @@ __global__ void k_residual_precond(const T *__restrict__ X, const T *__restrict_
         }
         rr[r] = out;
     }
+    if constexpr (sizeof(T) == 4) s += (double)sf;
     const double t = block_sum(s, red);
     if (threadIdx.x == 0) partials[(size_t)col * gridDim.x + blockIdx.x] = t;
 }
