@@ -733,10 +733,32 @@ void residual_precond(const T *X, const T *HX, int64_t ld, int k, int64_t N, con
     KF_LAUNCH_CHECK();
 }
 
-// Refinement-phase residual: R = HX - X theta from the FP64 iterate, its FP64 squared norms,
-// and two FP32 blocks: R itself (for the Rayleigh-Ritz blocks) and, unless Wout is null, the
+// x rounded to FP32 (to nearest, ties to even) by integer operations: the same result as the
+// conversion instruction, which GB300 runs on its FP64 pipe (about 2 per clock per SM).  Zeros,
+// subnormal results, overflows, infinities and NaNs take the conversion instruction.
+__device__ __forceinline__ float d2f_rn(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    int fe = (int)((b >> 52) & 0x7FF) - 1023 + 127;
+    if (fe <= 0 || fe >= 255) return (float)x;
+    const unsigned int sgn = (unsigned int)(b >> 32) & 0x80000000u;
+    const unsigned long long m = b & 0xFFFFFFFFFFFFFull;
+    unsigned int mant = (unsigned int)(m >> 29);
+    const unsigned int rem = (unsigned int)(m & 0x1FFFFFFFull);
+    if (rem > 0x10000000u || (rem == 0x10000000u && (mant & 1u))) {
+        if (++mant == 0x800000u) {
+            mant = 0u;
+            if (++fe >= 255) return (float)x;
+        }
+    }
+    return __uint_as_float(sgn | ((unsigned int)fe << 23) | mant);
+}
+
+// Refinement-phase residual: R = HX - X theta from the FP64 iterate, its squared norms, and two
+// FP32 blocks: R itself (for the Rayleigh-Ritz blocks) and, unless Wout is null, the
 // preconditioned direction (mode 0: / hypot(D - theta, eta), mode 1: / (D - sigma)) computed in
-// FP32 -- the preconditioner only steers the search directions.
+// FP32 -- the preconditioner only steers the search directions.  The residual and its squared norm
+// are formed in FP64 (the norms decide locking at the solve's tolerance); the FP32 roundings are
+// taken on the integer pipes instead of the conversion instruction, which shares the FP64 pipe.
 __global__ void k_residual_mixed(const double *__restrict__ X, const double *__restrict__ HX, int64_t ld, int64_t N,
                                  int64_t rows_per, const double *__restrict__ theta,
                                  const double *__restrict__ thetap, const double *__restrict__ D, double eta, int mode,
@@ -757,10 +779,10 @@ __global__ void k_residual_mixed(const double *__restrict__ X, const double *__r
     for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
         const double v = hx[r] - th * x[r];
         s += v * v;
-        const float vf = (float)v;
+        const float vf = d2f_rn(v);
         rr[r] = vf;
         if (ww) {
-            const float d = (float)D[r] - tp;
+            const float d = d2f_rn(D[r]) - tp;
             ww[r] = mode == 0 ? vf / hypotf(d, et) : mode == 1 ? vf / d : vf;
         }
     }

@@ -242,3 +242,29 @@ def test_plane_marching_apply(cuda, f32, shape):
     tol = TOL32 if f32 else TOL64
     assert np.max(np.abs(Ys[1] - R)) / scale < tol
     assert np.max(np.abs(Ys[1] - Ys[0])) / scale < tol
+
+
+@pytest.mark.parametrize("f32", [False, True])
+def test_every_point_variant_agrees(cuda, f32):
+    """Every forced point-per-thread variant of the fused apply (0-4: the (columns per thread, unroll)
+    shapes the tuner chooses from) gives the oracle's product on the three-mode structure, with more
+    columns than one pass of the widest shape covers."""
+    import ctypes as C
+    torch = cuda
+    from kfgpu import _abi, circuits
+    rng = np.random.default_rng(23)
+    th = circuits.three_mode_theta(rng)
+    dims, terms = circuits.three_mode_leaf(th, ncut=6, n2=48, n3=20)
+    H, Ho = _pair(dims, terms)
+    N, b = H.N, 37
+    dt = torch.float32 if f32 else torch.float64
+    X = torch.as_tensor(rng.standard_normal((b, N)), dtype=dt, device="cuda")
+    R = Ho.matvec(X.double().cpu().numpy().T).T
+    scale = max(1.0, np.max(np.abs(R)))
+    tol = TOL32 if f32 else TOL64
+    flags = _abi.KF_DEVICE | (_abi.KF_F32 if f32 else _abi.KF_F64)
+    for v in (0, 1, 2, 3, 4):
+        Y = torch.full_like(X, float("nan"))
+        _abi.check(_abi.lib().kf_test_apply_variant(H.handle, v, C.c_void_p(X.data_ptr()), C.c_void_p(Y.data_ptr()), N,
+                                                    b, flags, 1, None))
+        assert np.max(np.abs(Y.double().cpu().numpy() - R)) / scale < tol, v
