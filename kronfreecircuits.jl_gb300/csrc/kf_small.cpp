@@ -15,9 +15,11 @@
 //   Cholesky: the column-oriented A = U'U recurrence.
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstring>
 #include <limits>
 #include <numeric>
+#include <thread>
 #include <vector>
 
 #include "kf_internal.h"
@@ -107,22 +109,33 @@ int sym_eig(int n, const double *A, int lda, double *w, double *V, int ldv) {
     }
     for (int i = 0; i < n; ++i) d[i] = a[i + nn * i];
     for (int i = 0; i + 1 < n; ++i) e[i] = a[(i + 1) + nn * i];
-    // Q = H_0 H_1 ... H_{n-3}, built right to left on the identity in the transposed layout
-    // (Zt = Q'): Q <- H_k Q touches rows k+1.. of Q's columns k+1.., i.e. Zt <- Zt H_k on that block,
-    // y = Zt v (a sum of columns) then Zt -= 2 y v'
-    std::vector<double> Zt(nn * nn, 0.0), y(n);
-    for (int i = 0; i < n; ++i) Zt[i + nn * i] = 1.0;
-    for (int k = n - 3; k >= 0; --k) {
-        if (!has[k]) continue;
-        const int m = n - k - 1;
-        const double *v = &R[(k + 1) + nn * k];
-        std::fill(y.begin(), y.begin() + m, 0.0);
-        for (int i = 0; i < m; ++i) axpy(m, v[i], &Zt[(k + 1) + nn * (k + 1 + i)], y.data());
-        for (int i = 0; i < m; ++i) axpy(m, -2.0 * v[i], y.data(), &Zt[(k + 1) + nn * (k + 1 + i)]);
+    // Large problems (the per-axis eigenbases, n >= 128) record the QR rotations and then build the
+    // eigenvectors by row blocks on several host threads: a block of rows of Q = H_0 ... H_{n-3}
+    // (built left to right, Z <- Z H_k) followed by every recorded rotation depends on no other
+    // rows, so the blocks need no synchronisation and every row gets the same arithmetic whatever
+    // the thread count.  Small problems (every Rayleigh-Ritz and SVQB step) stay on one thread.
+    const bool par = n >= 128;
+    std::vector<double> Z;
+    if (!par) {
+        // Q built right to left on the identity in the transposed layout (Zt = Q'): Q <- H_k Q
+        // touches rows k+1.. of Q's columns k+1.., i.e. Zt <- Zt H_k on that block, y = Zt v (a sum
+        // of columns) then Zt -= 2 y v'
+        std::vector<double> Zt(nn * nn, 0.0), y(n);
+        for (int i = 0; i < n; ++i) Zt[i + nn * i] = 1.0;
+        for (int k = n - 3; k >= 0; --k) {
+            if (!has[k]) continue;
+            const int m = n - k - 1;
+            const double *v = &R[(k + 1) + nn * k];
+            std::fill(y.begin(), y.begin() + m, 0.0);
+            for (int i = 0; i < m; ++i) axpy(m, v[i], &Zt[(k + 1) + nn * (k + 1 + i)], y.data());
+            for (int i = 0; i < m; ++i) axpy(m, -2.0 * v[i], y.data(), &Zt[(k + 1) + nn * (k + 1 + i)]);
+        }
+        Z.resize(nn * nn);
+        for (int j = 0; j < n; ++j)
+            for (int i = 0; i < n; ++i) Z[i + nn * j] = Zt[j + nn * i];
     }
-    std::vector<double> Z(nn * nn);
-    for (int j = 0; j < n; ++j)
-        for (int i = 0; i < n; ++i) Z[i + nn * j] = Zt[j + nn * i];
+    std::vector<double> rc, rs;   // recorded rotations (large problems)
+    std::vector<int> rk;
     // implicit symmetric tridiagonal QR with Wilkinson shifts
     const double eps = std::numeric_limits<double>::epsilon();
     int hi = n - 1;
@@ -158,8 +171,51 @@ int sym_eig(int n, const double *A, int lda, double *w, double *V, int ldv) {
                 e[k + 1] = c * e[k + 1];
                 x = e[k];
             }
-            rot(n, &Z[nn * k], &Z[nn * (k + 1)], c, s);
+            if (par) {
+                rc.push_back(c);
+                rs.push_back(s);
+                rk.push_back(k);
+            } else {
+                rot(n, &Z[nn * k], &Z[nn * (k + 1)], c, s);
+            }
         }
+    }
+    // the row-block form's storage: 64-byte aligned, column stride padded past a power of two (so
+    // that the columns of a block spread over the cache sets and no two threads share a line)
+    std::vector<double> Zbuf;
+    double *Zp = nullptr;
+    const size_t ldz = nn + 8;
+    if (par) {
+        Zbuf.assign(ldz * nn + 8, 0.0);
+        Zp = Zbuf.data() + ((64 - (reinterpret_cast<uintptr_t>(Zbuf.data()) & 63)) & 63) / sizeof(double);
+        // rows [r0, r1) of Q, then of Q times the rotations
+        auto rows = [&](int r0, int r1) {
+            const int rb = r1 - r0;
+            if (rb <= 0) return;
+            for (int i = r0; i < r1; ++i) Zp[i + ldz * i] = 1.0;
+            std::vector<double> y(rb);
+            for (int k = 0; k + 2 < n; ++k) {
+                if (!has[k]) continue;
+                const int m = n - k - 1;
+                const double *v = &R[(k + 1) + nn * k];
+                std::fill(y.begin(), y.end(), 0.0);
+                for (int i = 0; i < m; ++i) axpy(rb, v[i], &Zp[r0 + ldz * (k + 1 + i)], y.data());
+                for (int i = 0; i < m; ++i) axpy(rb, -2.0 * v[i], y.data(), &Zp[r0 + ldz * (k + 1 + i)]);
+            }
+            const size_t nrot = rk.size();
+            for (size_t t = 0; t < nrot; ++t) {
+                double *zk = &Zp[r0 + ldz * rk[t]];
+                rot(rb, zk, zk + ldz, rc[t], rs[t]);
+            }
+        };
+        const unsigned hw = std::thread::hardware_concurrency();
+        const int nt = (int)std::max(1u, std::min(8u, hw));
+        // row blocks on 8-row (64-byte) boundaries: no two threads write one cache line
+        const int per = ((n + nt - 1) / nt + 7) / 8 * 8;
+        std::vector<std::thread> pool;
+        for (int t = 1; t < nt && t * per < n; ++t) pool.emplace_back(rows, t * per, std::min(n, (t + 1) * per));
+        rows(0, std::min(n, per));
+        for (auto &th : pool) th.join();
     }
     std::vector<int> ord(n);
     std::iota(ord.begin(), ord.end(), 0);
@@ -167,7 +223,7 @@ int sym_eig(int n, const double *A, int lda, double *w, double *V, int ldv) {
     for (int jj = 0; jj < n; ++jj) {
         const int j = ord[jj];
         w[jj] = d[j];
-        for (int i = 0; i < n; ++i) V[i + (size_t)ldv * jj] = Z[i + nn * j];
+        for (int i = 0; i < n; ++i) V[i + (size_t)ldv * jj] = par ? Zp[i + ldz * j] : Z[i + nn * j];
     }
     return 0;
 }

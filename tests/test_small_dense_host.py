@@ -4,6 +4,9 @@ the C ABI's host-only test entry (no GPU): random, graded, banded finite-differe
 diagonal, zero and tiny matrices, a leading dimension above n, and unsymmetric input (the average of
 the two triangles is what is solved, as the reference's Hermitian(...) wrappers do).
 
+From n = 128 the eigenvectors are built by independent row blocks on several host threads (the
+sizes 129 and 200 leave a short last block).
+
 Tolerances: eigenvalues within 1e-13 ||A|| of LAPACK's; ||A V - V diag(w)|| <= 1e-13 n ||A||;
 ||V'V - I|| <= 1e-13 n.
 """
@@ -56,7 +59,7 @@ def _fd(n, h=0.1):
     return A + np.diag(x ** 2)
 
 
-@pytest.mark.parametrize("n", [1, 2, 3, 4, 7, 18, 41, 54, 64, 128, 256])
+@pytest.mark.parametrize("n", [1, 2, 3, 4, 7, 18, 41, 54, 64, 127, 128, 129, 200, 256])
 def test_random_symmetric(lib, n):
     rng = np.random.default_rng(n)
     A = rng.standard_normal((n, n))
