@@ -688,24 +688,10 @@ __global__ void k_residual_precond(const T *__restrict__ X, const T *__restrict_
     const T *x = X + (int64_t)col * ld;
     const T *hx = HX + (int64_t)col * ld;
     T *rr = R + (int64_t)col * ldr;
-    // FP32 data: eight squares summed in FP32, then added into the FP64 sum (GB300's FP64 pipe,
-    // about 1/64 of the FP32 rate, bounded this kernel when every square was converted and added
-    // in FP64; an eight-term FP32 sum is accurate to ~5e-7 relative)
     double s = 0;
-    T sf = 0;
-    int cnt = 0;
     for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
         const T v = hx[r] - th * x[r];
-        if constexpr (sizeof(T) == 4) {
-            sf = fmaf(v, v, sf);
-            if (++cnt == 8) {
-                s += (double)sf;
-                sf = 0;
-                cnt = 0;
-            }
-        } else {
-            s += (double)v * (double)v;
-        }
+        s += (double)v * (double)v;
         T out = v;
         if (mode == 0) {
             out = (T)((double)v / hypot(D[r] - tp, eta));
@@ -714,7 +700,6 @@ __global__ void k_residual_precond(const T *__restrict__ X, const T *__restrict_
         }
         rr[r] = out;
     }
-    if constexpr (sizeof(T) == 4) s += (double)sf;
     const double t = block_sum(s, red);
     if (threadIdx.x == 0) partials[(size_t)col * gridDim.x + blockIdx.x] = t;
 }
@@ -733,32 +718,10 @@ void residual_precond(const T *X, const T *HX, int64_t ld, int k, int64_t N, con
     KF_LAUNCH_CHECK();
 }
 
-// x rounded to FP32 (to nearest, ties to even) by integer operations: the same result as the
-// conversion instruction, which GB300 runs on its FP64 pipe (about 2 per clock per SM).  Zeros,
-// subnormal results, overflows, infinities and NaNs take the conversion instruction.
-__device__ __forceinline__ float d2f_rn(double x) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-    int fe = (int)((b >> 52) & 0x7FF) - 1023 + 127;
-    if (fe <= 0 || fe >= 255) return (float)x;
-    const unsigned int sgn = (unsigned int)(b >> 32) & 0x80000000u;
-    const unsigned long long m = b & 0xFFFFFFFFFFFFFull;
-    unsigned int mant = (unsigned int)(m >> 29);
-    const unsigned int rem = (unsigned int)(m & 0x1FFFFFFFull);
-    if (rem > 0x10000000u || (rem == 0x10000000u && (mant & 1u))) {
-        if (++mant == 0x800000u) {
-            mant = 0u;
-            if (++fe >= 255) return (float)x;
-        }
-    }
-    return __uint_as_float(sgn | ((unsigned int)fe << 23) | mant);
-}
-
-// Refinement-phase residual: R = HX - X theta from the FP64 iterate, its squared norms, and two
-// FP32 blocks: R itself (for the Rayleigh-Ritz blocks) and, unless Wout is null, the
+// Refinement-phase residual: R = HX - X theta from the FP64 iterate, its FP64 squared norms,
+// and two FP32 blocks: R itself (for the Rayleigh-Ritz blocks) and, unless Wout is null, the
 // preconditioned direction (mode 0: / hypot(D - theta, eta), mode 1: / (D - sigma)) computed in
-// FP32 -- the preconditioner only steers the search directions.  The residual and its squared norm
-// are formed in FP64 (the norms decide locking at the solve's tolerance); the FP32 roundings are
-// taken on the integer pipes instead of the conversion instruction, which shares the FP64 pipe.
+// FP32 -- the preconditioner only steers the search directions.
 __global__ void k_residual_mixed(const double *__restrict__ X, const double *__restrict__ HX, int64_t ld, int64_t N,
                                  int64_t rows_per, const double *__restrict__ theta,
                                  const double *__restrict__ thetap, const double *__restrict__ D, double eta, int mode,
@@ -779,10 +742,10 @@ __global__ void k_residual_mixed(const double *__restrict__ X, const double *__r
     for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
         const double v = hx[r] - th * x[r];
         s += v * v;
-        const float vf = d2f_rn(v);
+        const float vf = (float)v;
         rr[r] = vf;
         if (ww) {
-            const float d = d2f_rn(D[r]) - tp;
+            const float d = (float)D[r] - tp;
             ww[r] = mode == 0 ? vf / hypotf(d, et) : mode == 1 ? vf / d : vf;
         }
     }
