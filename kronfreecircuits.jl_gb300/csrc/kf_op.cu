@@ -556,16 +556,38 @@ std::vector<double> factor_diagonal(const kf_factor &f) {
 }
 
 // acc[p] += c * prod over factors of vec_f[i_axis(p)]
+// acc[p] += c * prod_f v_f[i_{axis_f}(p)] over the grid (axis 0 fastest).  The factors before the
+// first one on axis 0 are constant along a run of axis 0, so each run is one scalar times the rest:
+// an inner loop the compiler vectorises, the odometer over the other axes stepping once per run.
+// The product is formed in the factors' order, as a point-by-point evaluation would.
 void add_separable(std::vector<double> &acc, const std::vector<int64_t> &dims, double c,
                    const std::vector<std::pair<int, std::vector<double>>> &vecs) {
     const int64_t N = (int64_t)acc.size();
     const int nd = (int)dims.size();
+    const int64_t d0 = dims[0];
+    const int nf = (int)vecs.size();
     std::vector<int64_t> idx(nd, 0);
-    for (int64_t p = 0; p < N; ++p) {
-        double v = c;
-        for (auto &pv : vecs) v *= pv.second[idx[pv.first]];
-        acc[p] += v;
-        for (int a = 0; a < nd; ++a) {
+    int f0 = nf;   // the first factor on axis 0
+    for (int k = 0; k < nf; ++k)
+        if (vecs[k].first == 0) { f0 = k; break; }
+    double *out = acc.data();
+    for (int64_t p0 = 0; p0 < N; p0 += d0) {
+        double pre = c;
+        for (int k = 0; k < f0; ++k) pre *= vecs[k].second[idx[vecs[k].first]];
+        double *row = out + p0;
+        if (f0 == nf) {
+            for (int64_t i = 0; i < d0; ++i) row[i] += pre;
+        } else if (f0 == nf - 1) {
+            const double *v0 = vecs[f0].second.data();
+            for (int64_t i = 0; i < d0; ++i) row[i] += pre * v0[i];
+        } else {
+            for (int64_t i = 0; i < d0; ++i) {
+                double v = pre;
+                for (int k = f0; k < nf; ++k) v *= vecs[k].second[vecs[k].first == 0 ? i : idx[vecs[k].first]];
+                row[i] += v;
+            }
+        }
+        for (int a = 1; a < nd; ++a) {
             if (++idx[a] < dims[a]) break;
             idx[a] = 0;
         }
