@@ -62,11 +62,7 @@ int kf_op_create(const kf_op_desc *desc, kf_op **out) {
         try {
             KF_CUDA(cudaGetDevice(&op->device));
             KF_CUDA(cudaStreamCreateWithFlags(&op->stream, cudaStreamNonBlocking));
-            build_op(desc, op);
-            // the separable preconditioner's per-axis eigendecompositions (host only) start now,
-            // on their own thread; the first solve that needs them waits for the result
-            if (!op->sep.M.empty())
-                op->sep.host_job = std::async(std::launch::async, [op] { kf::sep_host_prepare(op); });
+            build_op(desc, op);   // also starts the preconditioner's host job
         } catch (...) {
             free_op(op);
             delete op;

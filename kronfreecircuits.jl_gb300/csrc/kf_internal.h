@@ -286,7 +286,6 @@ template <typename T>
 void sep_scale(T *W, int64_t ld, int64_t N, int k, int ndims, const int *dims, const double *lam, const int *lam_off,
                const double *theta, double eta, cudaStream_t s);
 void sep_host_prepare(kf_op *op);   // host part only (no CUDA calls)
-void sep_host_prepare(kf_op *op);   // host part only (no CUDA calls)
 void sep_prepare(kf_op *op);
 // product_seed(H, k) into the device block X (N x k, leading dimension N), on stream s
 void product_seed_device(kf_op *op, int k, double *X, cudaStream_t s);

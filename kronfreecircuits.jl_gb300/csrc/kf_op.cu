@@ -689,6 +689,10 @@ void build_op(const kf_op_desc *desc, kf_op *op) {
             }
         }
     }
+    // the separable preconditioner's per-axis eigendecompositions (host only) start as soon as the
+    // per-axis sums exist, on their own thread, overlapping the rest of the construction; the first
+    // solve that needs them waits for the result (free_op waits for the job if construction fails)
+    if (!op->sep.M.empty()) op->sep.host_job = std::async(std::launch::async, [op] { sep_host_prepare(op); });
     // fused diagonal (src/apply.jl:234-241, 438-447)
     std::vector<double> D(N, desc->constant);
     if (desc->diag) for (int64_t p = 0; p < N; ++p) D[p] += desc->diag[p];
