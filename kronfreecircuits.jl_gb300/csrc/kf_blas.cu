@@ -1025,14 +1025,17 @@ void fill_normal(T *X, int64_t ld, int k, int64_t N, uint64_t seed, uint64_t sid
     KF_LAUNCH_CHECK();
 }
 
-// X[:, j] += delta * (||X_j|| / ||R_j||) R_j, the norms' squares in nrm[0..k) (X) and nrm[k..2k) (R)
+// X[:, j] += delta * (||X_j|| / ||R_j||) R_j, the norms' squares in nrm[0..k) (X) and nrm[k..2k) (R).
+// Column j = blockIdx.y; the factor is formed once per thread (FP64 square roots and divisions run
+// on GB300's narrow FP64 pipe), then a grid-stride loop over the rows.
 __global__ void k_perturb_add(double *__restrict__ X, const double *__restrict__ R, int64_t N, int k,
                               const double *__restrict__ nrm, double delta) {
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= N * k) return;
-    const int64_t c = t / N, r = t % N;
+    const int c = blockIdx.y;
     const double f = delta * sqrt(nrm[c]) / sqrt(nrm[k + c]);
-    X[c * N + r] += f * R[c * N + r];
+    double *x = X + (int64_t)c * N;
+    const double *rr = R + (int64_t)c * N;
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < N; r += (int64_t)gridDim.x * blockDim.x)
+        x[r] += f * rr[r];
 }
 
 // Each column of X (N x k, leading dimension N) plus a vector of norm delta * ||column|| along a
@@ -1044,8 +1047,8 @@ void perturb_block(double *X, int64_t N, int k, double delta, uint64_t key, doub
     fill_normal<double>(R, N, k, N, key, 0x50455254ull, s);
     colnorms2<double>(X, N, k, N, nrm, partials, s);
     colnorms2<double>(R, N, k, N, nrm + k, partials, s);
-    const int64_t tot = N * k;
-    k_perturb_add<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(X, R, N, k, nrm, delta);
+    const unsigned bx = (unsigned)std::min<int64_t>((N + 255) / 256, 1216);
+    k_perturb_add<<<dim3(bx, (unsigned)k), 256, 0, s>>>(X, R, N, k, nrm, delta);
     KF_LAUNCH_CHECK();
 }
 
