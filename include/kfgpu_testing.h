@@ -104,7 +104,8 @@ int kf_test_update(int path, float *Y, int64_t ldy, int ky, const float *X0, int
 /*
  * kf_op_apply (device blocks, flags as there) with the fused-apply kernel variant forced instead of
  * the tuned one: 0-4 the point-per-thread kernel's shapes, 5 the plane-marching kernel (where its
- * geometry applies; otherwise variant 4 runs); `reps` launches timed with CUDA events on the op's
+ * geometry applies; otherwise variant 4 runs), 6 the point-per-thread kernel with 36 columns per
+ * thread; `reps` launches timed with CUDA events on the op's
  * stream, *ms_per_launch (may be NULL) receives the mean.
  */
 int kf_test_apply_variant(kf_op *op, int variant, const void *X, void *Y, int64_t ld, int64_t b, int32_t flags,

@@ -49,7 +49,9 @@ extern std::atomic<uint64_t> g_launches;
 
 constexpr int MAXDIMS = 8;     // axes of a state tensor
 constexpr int MAXB = 24;       // bands of one banded factor (a periodic order-8 stencil has 16)
-constexpr int KF_APPLY_VARIANTS = 6;   // five (columns per thread, unroll) shapes + the plane-marching kernel
+// five (columns per thread, unroll) shapes, the plane-marching kernel, 36 columns per thread (a
+// 36-column block in one pass instead of 32 + 4)
+constexpr int KF_APPLY_VARIANTS = 7;
 constexpr int MAXE = 48;       // stencil entries (products of bands) over all fused terms
 
 // The fused kernel's stencil entries.  Every term built only of diagonal, banded and shift

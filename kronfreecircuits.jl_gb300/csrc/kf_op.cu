@@ -231,6 +231,7 @@ static void apply_t(kf_op *op, const T *X, T *Y, int64_t ldx, int64_t ldy, int64
         case 1: KF_FUSED(16, 2, ME); break;              \
         case 2: KF_FUSED(8, 2, ME); break;               \
         case 3: KF_FUSED(4, 4, ME); break;               \
+        case 6: KF_FUSED(36, 1, ME); break;              \
         default: KF_FUSED(32, 1, ME); break;             \
     }
         if (ne <= 16) { KF_VARIANTS(16) } else if (ne <= 32) { KF_VARIANTS(32) } else { KF_VARIANTS(48) }

@@ -246,9 +246,9 @@ def test_plane_marching_apply(cuda, f32, shape):
 
 @pytest.mark.parametrize("f32", [False, True])
 def test_every_point_variant_agrees(cuda, f32):
-    """Every forced point-per-thread variant of the fused apply (0-4: the (columns per thread, unroll)
-    shapes the tuner chooses from) gives the oracle's product on the three-mode structure, with more
-    columns than one pass of the widest shape covers."""
+    """Every forced point-per-thread variant of the fused apply (0-4 and 6: the (columns per thread,
+    unroll) shapes the tuner chooses from) gives the oracle's product on the three-mode structure,
+    with more columns than one pass of the widest shape covers."""
     import ctypes as C
     torch = cuda
     from kfgpu import _abi, circuits
@@ -263,7 +263,7 @@ def test_every_point_variant_agrees(cuda, f32):
     scale = max(1.0, np.max(np.abs(R)))
     tol = TOL32 if f32 else TOL64
     flags = _abi.KF_DEVICE | (_abi.KF_F32 if f32 else _abi.KF_F64)
-    for v in (0, 1, 2, 3, 4):
+    for v in (0, 1, 2, 3, 4, 6):
         Y = torch.full_like(X, float("nan"))
         _abi.check(_abi.lib().kf_test_apply_variant(H.handle, v, C.c_void_p(X.data_ptr()), C.c_void_p(Y.data_ptr()), N,
                                                     b, flags, 1, None))
