@@ -125,10 +125,42 @@ constexpr int SEP_SCALE_MAX_K = 256;   // columns per scale pass
 // where it matters, so both are split into FP32 hi + lo parts and S - theta = (S_hi - theta_hi) +
 // (S_lo - theta_lo), the first difference exact there; the scale itself is FP32 -- it only steers
 // the search directions, and GB300's FP64 rate would make a per-element FP64 pass FP64-bound.
+// S(p) = sum_a lam_a[i_a(p)] in FP64 (one sum per point), split into FP32 hi + lo
+__device__ __forceinline__ void sep_point(int64_t p, int ndims, const int *__restrict__ dims,
+                                          const double *__restrict__ lam, const int *__restrict__ lam_off, float &hi,
+                                          float &lo) {
+    uint32_t rem = (uint32_t)p;
+    double S = 0.0;
+    for (int a = 0; a < ndims; ++a) {
+        const uint32_t d = (uint32_t)dims[a];
+        const uint32_t i = rem % d;
+        rem /= d;
+        S += lam[lam_off[a] + (int)i];
+    }
+    hi = (float)S;
+    lo = (float)(S - (double)hi);
+}
+
+__global__ void k_sep_spectrum(float *__restrict__ shl, int64_t N, int ndims, const int *__restrict__ dims,
+                               const double *__restrict__ lam, const int *__restrict__ lam_off) {
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < N; p += (int64_t)gridDim.x * blockDim.x) {
+        float hi, lo;
+        sep_point(p, ndims, dims, lam, lam_off, hi, lo);
+        reinterpret_cast<float2 *>(shl)[p] = make_float2(hi, lo);
+    }
+}
+
+// W[:, j] <- W[:, j] / hypot(S(p) - theta_j, eta) with S(p) = sum_a lam_a[i_a(p)] (the separable
+// spectrum evaluated from per-axis eigenvalues).  One thread per grid point: the point's S(p) serves
+// every column, read from the operator's hi / lo table when there is one (it depends on the operator
+// only), else formed from the per-axis eigenvalues (FP64, one sum per point).  S and theta are close
+// where it matters, so both are split into FP32 hi + lo parts and S - theta = (S_hi - theta_hi) +
+// (S_lo - theta_lo), the first difference exact there; the scale itself is FP32 -- it only steers
+// the search directions, and GB300's FP64 rate would make a per-element FP64 pass FP64-bound.
 template <typename T>
 __global__ void k_sep_scale(T *__restrict__ W, int64_t ld, int64_t N, int k, int ndims, const int *__restrict__ dims,
                             const double *__restrict__ lam, const int *__restrict__ lam_off,
-                            const double *__restrict__ theta, double eta) {
+                            const double *__restrict__ theta, double eta, const float *__restrict__ shl) {
     __shared__ float th_hi[SEP_SCALE_MAX_K], th_lo[SEP_SCALE_MAX_K];
     for (int c = threadIdx.x; c < k; c += blockDim.x) {
         const float h = (float)theta[c];
@@ -138,15 +170,14 @@ __global__ void k_sep_scale(T *__restrict__ W, int64_t ld, int64_t N, int k, int
     __syncthreads();
     const float eta2 = (float)(eta * eta);
     for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < N; p += (int64_t)gridDim.x * blockDim.x) {
-        uint32_t rem = (uint32_t)p;
-        double S = 0.0;
-        for (int a = 0; a < ndims; ++a) {
-            const uint32_t d = (uint32_t)dims[a];
-            const uint32_t i = rem % d;
-            rem /= d;
-            S += lam[lam_off[a] + (int)i];
+        float s_hi, s_lo;
+        if (shl) {
+            const float2 v = reinterpret_cast<const float2 *>(shl)[p];
+            s_hi = v.x;
+            s_lo = v.y;
+        } else {
+            sep_point(p, ndims, dims, lam, lam_off, s_hi, s_lo);
         }
-        const float s_hi = (float)S, s_lo = (float)(S - (double)s_hi);
         for (int c = 0; c < k; ++c) {
             const float dlt = (s_hi - th_hi[c]) + (s_lo - th_lo[c]);
             const float f = rsqrtf(fmaf(dlt, dlt, eta2));
@@ -157,18 +188,26 @@ __global__ void k_sep_scale(T *__restrict__ W, int64_t ld, int64_t N, int k, int
 
 template <typename T>
 void sep_scale(T *W, int64_t ld, int64_t N, int k, int ndims, const int *dims, const double *lam, const int *lam_off,
-               const double *theta, double eta, cudaStream_t s) {
+               const double *theta, double eta, cudaStream_t s, const float *shl) {
     if (k <= 0) return;
     KF_REQUIRE(k <= SEP_SCALE_MAX_K, KF_EINVAL, "sep_scale: too many columns");
     KF_REQUIRE(N < ((int64_t)1 << 32), KF_EINVAL, "sep_scale: operator dimension too large");
     const int64_t blocks = std::min<int64_t>((N + 255) / 256, 152 * 8);
-    k_sep_scale<T><<<(unsigned)blocks, 256, 0, s>>>(W, ld, N, k, ndims, dims, lam, lam_off, theta, eta);
+    k_sep_scale<T><<<(unsigned)blocks, 256, 0, s>>>(W, ld, N, k, ndims, dims, lam, lam_off, theta, eta, shl);
+    KF_LAUNCH_CHECK();
+}
+
+void sep_spectrum(float *shl, int64_t N, int ndims, const int *dims, const double *lam, const int *lam_off,
+                  cudaStream_t s) {
+    KF_REQUIRE(N < ((int64_t)1 << 32), KF_EINVAL, "sep_spectrum: operator dimension too large");
+    const int64_t blocks = std::min<int64_t>((N + 255) / 256, 152 * 8);
+    k_sep_spectrum<<<(unsigned)blocks, 256, 0, s>>>(shl, N, ndims, dims, lam, lam_off);
     KF_LAUNCH_CHECK();
 }
 
 template void sep_scale<float>(float *, int64_t, int64_t, int, int, const int *, const double *, const int *,
-                               const double *, double, cudaStream_t);
+                               const double *, double, cudaStream_t, const float *);
 template void sep_scale<double>(double *, int64_t, int64_t, int, int, const int *, const double *, const int *,
-                                const double *, double, cudaStream_t);
+                                const double *, double, cudaStream_t, const float *);
 
 }  // namespace kf

@@ -175,6 +175,7 @@ struct kf_op {
         std::future<void> host_job;           // the host eigendecompositions, started at creation
         double *d_lam = nullptr;
         int *d_lam_off = nullptr, *d_dims = nullptr;
+        float *d_shl = nullptr;               // per point: S(p) as FP32 hi, lo (interleaved, 2N)
     } sep;
 };
 
@@ -284,9 +285,14 @@ void diag_expectation(const double *D, const double *X, int64_t ld, int k, int64
 template <typename T>
 void mode_product(T *Y, int64_t ldy, const T *X, int64_t ldx, const T *A, int d, int64_t left, int64_t N, int64_t b,
                   double alpha, double beta, cudaStream_t s);
+// W[:, j] /= hypot(S(p) - theta_j, eta); shl (may be NULL): S(p) as FP32 hi / lo pairs from
+// sep_spectrum, else S(p) is formed from the per-axis eigenvalues point by point
 template <typename T>
 void sep_scale(T *W, int64_t ld, int64_t N, int k, int ndims, const int *dims, const double *lam, const int *lam_off,
-               const double *theta, double eta, cudaStream_t s);
+               const double *theta, double eta, cudaStream_t s, const float *shl = nullptr);
+// shl[2p], shl[2p + 1] = S(p) = sum_a lam_a[i_a(p)] split into FP32 hi + lo (N points)
+void sep_spectrum(float *shl, int64_t N, int ndims, const int *dims, const double *lam, const int *lam_off,
+                  cudaStream_t s);
 void sep_host_prepare(kf_op *op);   // host part only (no CUDA calls)
 void sep_prepare(kf_op *op);
 // product_seed(H, k) into the device block X (N x k, leading dimension N), on stream s

@@ -894,6 +894,7 @@ void free_op(kf_op *op) {
     cudaFree(op->sep.d_lam);
     cudaFree(op->sep.d_lam_off);
     cudaFree(op->sep.d_dims);
+    cudaFree(op->sep.d_shl);
     if (op->own_stream && op->stream) cudaStreamDestroy(op->stream);
 }
 

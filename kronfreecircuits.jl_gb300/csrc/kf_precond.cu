@@ -108,6 +108,10 @@ void sep_prepare(kf_op *op) {
     KF_CUDA(cudaMemcpy(S.d_lam, S.lam.data(), S.lam.size() * 8, cudaMemcpyHostToDevice));
     KF_CUDA(cudaMemcpy(S.d_lam_off, off.data(), nd * sizeof(int), cudaMemcpyHostToDevice));
     KF_CUDA(cudaMemcpy(S.d_dims, dims.data(), nd * sizeof(int), cudaMemcpyHostToDevice));
+    // S(p) per point as FP32 hi / lo, once per operator (every scaling pass reads it)
+    KF_CUDA(cudaMalloc(&S.d_shl, (size_t)2 * op->N * sizeof(float)));
+    sep_spectrum(S.d_shl, op->N, nd, S.d_dims, S.d_lam, S.d_lam_off, op->stream);
+    KF_CUDA(cudaStreamSynchronize(op->stream));
     S.ready = true;
     const char *tr = std::getenv("KF_TRACE");
     if (tr && tr[0] && tr[0] != '0')
@@ -272,7 +276,7 @@ float *sep_apply(kf_op *op, float *W, float *s1, int k, const double *theta_dev,
     };
     for (int a = 0; a < nd; ++a)
         if (!S.ident[a]) product(a, true);
-    sep_scale<float>(cur, N, N, k, nd, S.d_dims, S.d_lam, S.d_lam_off, theta_dev, eta, s);
+    sep_scale<float>(cur, N, N, k, nd, S.d_dims, S.d_lam, S.d_lam_off, theta_dev, eta, s, S.d_shl);
     for (int a = nd - 1; a >= 0; --a)
         if (!S.ident[a]) product(a, false);
     return cur;
