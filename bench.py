@@ -7,31 +7,49 @@ uniform ranges (seeded; the draws cycle), lowest 12 eigenpairs with LOBPCG (bloc
 seed), every pair accepted at ||H x - lambda x|| <= 1e-8 ||H|| (||H|| = Gershgorin bound) by a
 fresh FP64 application.
 
-  value            converged pairs / s of the mixed-precision solver (FP32 bulk, FP64 Rayleigh-Ritz
-                   and refinement), operators already on the device when the timed region starts
-  plain_f64        the same for the plain FP64 solver (the metric's denominator)
+  value            converged pairs / s of the mixed-precision solver (FP32 bulk, FP64 Rayleigh-Ritz,
+                   refinement and acceptance) with the separable preconditioner, started from the
+                   product seed; operators already on the device when the timed region starts
+  max_rel_eig_err  the largest relative eigenvalue error of the timed solves against the FP64 CPU
+                   oracle's eigenvalues of the same draws (tests/golden/leaf3_eigs.json)
+  f64_separable    the FP64 solver with the same preconditioner on the same draws (what precision
+                   alone buys); plain_f64: the FP64 solver with the reference's default per-Ritz
+                   Jacobi preconditioner (the metric's denominator), with the runs that hit maxiter
+                   counted
   e2e              the public API end to end with host buffers: kf_op_create from the host term
                    list, solve (product seed built by the library), host eigenpairs out, kf_op_destroy,
                    every step
   roofline         the dominant kernel of a warm solve by the ncu launch list (its template
-                   instantiations summed), the fused stencil apply k_apply_fused<float>: algorithmic
-                   bytes 2 N b 4 per launch (16 columns) over its CUDA-event time, against the measured
-                   HBM copy bandwidth; roofline_update / roofline_mode / roofline_gram: the tcgen05
-                   FP32 block update on the fused X/P Rayleigh-Ritz shape ([X_a Q] C, 18 + 36 -> 36
-                   columns, (54 + 36) N 4), the separable preconditioner's tcgen05 mode product
-                   (256-point axis, 18 columns, 2 N b 4) and the tensor-core Gram of the
-                   orthogonalisation ([X Z]'Z, 18 + 36 columns, N b 4)
-  cpu_baseline     the oracle's restatement of the reference CPU path (C/OpenMP mul! + NumPy LOBPCG)
-                   on the host cores, a bounded sample
+                   instantiations summed), the fused stencil apply: algorithmic bytes 2 N b 4 per
+                   launch (16 columns) over its CUDA-event time, against the measured HBM copy
+                   bandwidth; roofline_update / roofline_mode / roofline_gram: the tcgen05 FP32 block
+                   update on the fused X/P Rayleigh-Ritz shape ([X_a Q] C, 18 + 36 -> 36 columns,
+                   (54 + 36) N 4), the separable preconditioner's tcgen05 mode product (256-point
+                   axis, 18 columns, 2 N b 4) and the tensor-core Gram of the orthogonalisation
+                   ([X Z]'Z, 18 + 36 columns, N b 4)
+  dense / batch / warmstart
+                   the other configurations, each with its own value, eigenvalue error against the
+                   oracle's fixture and roofline: the 48^3 dense parent, the batched sweep of 704
+                   leaves and 64 chain parents, the learned warm start on the two-transmon circuit
+  cpu_baseline     one complete solve of the first timed draw on the host cores, measured to
+                   convergence: the oracle's restatement of the reference CPU path (C/OpenMP mul!,
+                   LOBPCG, FP64) with the same separable preconditioner
 
 `--impl reference` times the reference's CPU path (the oracle port: the reference is Julia and
-cannot run here) on the same workload and metric.
+cannot run here) on the same workload and metric: one complete solve of the first timed draw with
+the reference's default preconditioner, and one with the separable preconditioner.
 """
 from __future__ import annotations
 
+import os
+
+# the CPU legs run the oracle's OpenMP passes next to threaded BLAS calls: idle threads of either
+# pool sleep instead of spinning, so the two pools do not starve each other
+os.environ.setdefault("OMP_WAIT_POLICY", "PASSIVE")
+os.environ.setdefault("OPENBLAS_THREAD_TIMEOUT", "4")
+
 import argparse
 import json
-import os
 import subprocess
 import sys
 import threading
@@ -48,7 +66,7 @@ for _p in (ROOT, PKG):
 M_PAIRS = 12
 SEED = 20261205          # theta draws of the three-mode leaf workload
 NDRAWS = 64
-# ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch (profiles/*.md), N = 671,744: the
+# ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch, N = 671,744: the
 # FP32 16-column fused apply (written Y stays in L2: reads 45.7 MB, writes 9.9 MB); the pipelined
 # tcgen05 mode product, 256-point axis, 18 columns (reads 48.6 MB = X once, writes 1.9 MB: Y stays
 # in L2);
@@ -60,10 +78,39 @@ UPDATE_TRAFFIC_BYTES = 200817152   # ncu dram bytes read + written, one launch (
 GRAM_TC_TRAFFIC_BYTES = 145235200
 
 
+# the workload both arms report (the reference arm prints the same dict)
+CONFIG = {"workload": "three-mode leaf 41x256x64 (N=671,744): lowest 12 eigenpairs accepted at "
+                      "||Hx - lx|| <= 1e-8 ||H|| (Gershgorin) by a fresh FP64 apply; theta ~ U(ranges), "
+                      "numpy default_rng(20261205) draws W..W+K-1 of 64",
+          "inputs": "synthetic; larger than L2 (a 16-column FP32 block is 43 MB; a solve streams ~10 GB)"}
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+
+
 def thetas():
     from kfgpu import circuits
     rng = np.random.default_rng(SEED)
     return [circuits.three_mode_theta(rng) for _ in range(NDRAWS)]
+
+
+def fixture(name):
+    """A committed eigenvalue fixture (tests/golden/*_eigs.json, made by the FP64 CPU oracle), or {}."""
+    try:
+        with open(os.path.join(GOLDEN, name)) as f:
+            return json.load(f)
+    except OSError:
+        return {}
+
+
+def rel_err(E, Eref):
+    E, Eref = np.asarray(E, dtype=float), np.asarray(Eref, dtype=float)
+    return float(np.max(np.abs(E - Eref) / np.maximum(np.abs(Eref), 1e-300)))
+
+
+def leaf3_err(Es_by_draw):
+    """max relative eigenvalue error over the draws the oracle fixture holds, and how many it covered."""
+    fx = fixture("leaf3_eigs.json").get("draws", {})
+    errs = [rel_err(E, fx[str(d)]["E"]) for d, E in Es_by_draw if str(d) in fx]
+    return (max(errs) if errs else None), len(errs)
 
 
 def peaks():
@@ -173,7 +220,7 @@ def measure_apply(torch, H, f32, b=16, reps=20):
 
 def run_ours(args, D):
     import torch
-    from kfgpu import KronFreeOperator, LOBPCG, circuits, solve
+    from kfgpu import ConvergenceError, KronFreeOperator, LOBPCG, circuits, solve
     from kfgpu._abi import launch_count
     from kfgpu.build import build_library
 
@@ -191,72 +238,72 @@ def run_ours(args, D):
     ops = {}
     for i in sorted(set(idx) | set(range(W))):
         dims, terms = circuits.three_mode_leaf(ths[i])
-        H = KronFreeOperator(dims, terms)
-        ops[i] = (H, None)
+        ops[i] = KronFreeOperator(dims, terms)
     stream = torch.cuda.Stream()
-    for H, _ in ops.values():
+    for H in ops.values():
         H.set_stream(stream.cuda_stream)
 
     def one(i, precision, precond=None):
-        H, seedb = ops[i]
+        """(converged pairs, stats, E) of one solve; a solve that runs out of maxiter counts the
+        pairs it did converge."""
+        H = ops[i]
         tol = 1e-8 * H.gershgorin_bound()
         pc = precond or ("separable" if precision == "mixed" else "ritz")
         buf = args.buffer if precision == "mixed" else None
-        E, V, st = solve(LOBPCG(tol=tol, precision=precision, preconditioner=pc, buffer=buf), H, M_PAIRS,
-                         seed_block=seedb)
-        return st["converged"], st
+        try:
+            E, V, st = solve(LOBPCG(tol=tol, precision=precision, preconditioner=pc, buffer=buf), H, M_PAIRS)
+        except ConvergenceError as e:
+            st = e.stats
+            st["hit_maxiter"] = True
+            return st["converged"], st, None
+        st["hit_maxiter"] = False
+        return st["converged"], st, E
+
+    def timed(draws, precision, precond=None):
+        D.barrier()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        conv, stats, Es = 0, [], []
+        for i in draws:
+            c, st, E = one(i, precision, precond)
+            conv += c
+            stats.append(st)
+            Es.append((i, E))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return conv, stats, Es, D.max(e0.elapsed_time(e1) / 1e3)
 
     for w in range(W):
         one(w, "mixed")
     torch.cuda.synchronize()
     n0 = launch_count()
     clocks = Clocks(D.local).start()
-    D.barrier()
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    conv, stats = 0, []
-    for i in idx:
-        c, st = one(i, "mixed")
-        conv += c
-        stats.append(st)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    D.barrier()
+    conv, stats, Es, t_mixed = timed(idx, "mixed")
     clk = clocks.stop()
     # the job's time is the slowest replica's; its work is every replica's
-    t_mixed = D.max(e0.elapsed_time(e1) / 1e3)
     conv_all = D.sum(conv)
     launches = int(D.sum(launch_count() - n0))
     value = conv_all / t_mixed
-    # plain FP64 on a subset of the same draws (the metric's denominator)
+    err_mixed, n_err = leaf3_err([(i, E) for i, E in Es if E is not None])
+    # the same FP64 solver with the same (separable) preconditioner on the same draws: what
+    # precision alone buys
+    c_sep, st_sep, Es_sep, t_sep = timed(idx, "f64", "separable")
+    f64_sep = D.sum(c_sep) / t_sep
+    err_sep, _ = leaf3_err([(i, E) for i, E in Es_sep if E is not None])
+    # plain FP64 with the reference's default per-Ritz Jacobi preconditioner on the first draws
     kp = max(1, min(args.plain_steps, K))
-    D.barrier()
-    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    f0.record(stream)
-    conv64, st64 = 0, []
-    for i in idx[:kp]:
-        c, st = one(i, "f64")
-        conv64 += c
-        st64.append(st)
-    f1.record(stream)
-    torch.cuda.synchronize()
-    t64 = D.max(f0.elapsed_time(f1) / 1e3)
-    plain = D.sum(conv64) / t64
-    # the same FP64 solver with the separable preconditioner (what precision alone buys)
-    g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    g0.record(stream)
-    c_sep, st_sep = one(idx[0], "f64", "separable")
-    g1.record(stream)
-    torch.cuda.synchronize()
-    t_sep = g0.elapsed_time(g1) / 1e3
+    c64, st64, Es64, t64 = timed(idx[:kp], "f64")
+    plain = D.sum(c64) / t64
+    err64, _ = leaf3_err([(i, E) for i, E in Es64 if E is not None])
+    ok64 = [j for j, st in enumerate(st64) if not st["hit_maxiter"]]
     # end to end through the public API with host buffers
     ke = max(1, min(args.e2e_steps, K))
     h2d = d2h = 0
     torch.cuda.synchronize()
     D.barrier()
     t0 = time.perf_counter()
-    conv_e = 0
+    conv_e, Es_e = 0, []
     for i in idx[:ke]:
         dims, terms = circuits.three_mode_leaf(ths[i])
         H = KronFreeOperator(dims, terms)
@@ -264,16 +311,18 @@ def run_ours(args, D):
         E, V, st = solve(LOBPCG(tol=tol, precision="mixed", preconditioner="separable", buffer=args.buffer), H,
                          M_PAIRS)
         conv_e += st["converged"]
+        Es_e.append((i, E))
         h2d += H.N * 8 + sum(op.n * 8 * 5 for _, fs in terms for _, op in fs)
         d2h += V.nbytes + E.nbytes
         H.close()
     torch.cuda.synchronize()
     te = D.max(time.perf_counter() - t0)
     conv_e = D.sum(conv_e)
+    err_e, _ = leaf3_err(Es_e)
     # roofline of the dominant kernel of a warm solve (by the ncu launch list: the fused stencil
     # apply), of the tcgen05 block update on the fused X/P Rayleigh-Ritz shape, of the
     # preconditioner's mode product and of the tensor-core Gram
-    H0 = ops[idx[0]][0]
+    H0 = ops[idx[0]]
     peak, kind = peaks()
     t_upd = time_update(torch, 1, 18, 36, 36, H0.N)
     alg_upd = (18 + 36 + 36) * H0.N * 4
@@ -284,24 +333,34 @@ def run_ours(args, D):
     t_apply = measure_apply(torch, H0, True)
     alg = 2 * H0.N * 16 * 4
     achieved = alg / t_apply / 1e9
+    ms64 = [st["iterations"] for st in st64]
     line = {
         "metric": "converged eigenpairs/s at 1e-8 resid: warm-start mixed vs plain FP64, 1 GB300",
         "value": value, "unit": "eigenpairs/s", "n_gpus": D.world, "steps": K, "warmup": W,
         "ms_per_step": 1e3 * t_mixed / K, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 bulk + f64 refinement", "data": "synthetic",
-        "config": {"workload": "three-mode leaf 41x256x64 (N=671,744), LOBPCG m=12 block=16, product seed, "
-                               "tol 1e-8*||H||, theta ~ U(ranges) seed 20261205",
-                   "buffer_columns": "library default (2, mixed only)" if args.buffer is None else args.buffer,
-                   "l2": "inputs larger than L2 (a 16-column FP32 block is 43 MB; a solve streams ~10 GB)"},
-        "replicas": D.world,
-        "plain_f64": {"value": plain, "steps": kp, "ms_per_step": 1e3 * t64 / kp,
-                      "iterations": [s["iterations"] for s in st64]},
-        "speedup_mixed_vs_f64": value / plain if plain > 0 else None,
-        "f64_separable": {"value": c_sep / t_sep, "iterations": st_sep["iterations"], "ms_per_step": 1e3 * t_sep},
-        "iterations": [s["iterations"] for s in stats], "iterations_f64_phase": [s["iterations_f64"] for s in stats],
+        "config": dict(CONFIG),
+        "method": "value: mixed-precision LOBPCG (FP32 bulk, FP64 Rayleigh-Ritz, refinement and acceptance), "
+                  "separable preconditioner, product-seed start (the learned warm start is the two-transmon "
+                  "workload's, in `warmstart`), block 16 + "
+                  + ("2 buffer columns" if args.buffer is None else f"{args.buffer} buffer columns"),
+        "max_rel_eig_err": err_mixed, "eig_err_draws": n_err,
+        "eig_err_ref": "FP64 CPU oracle, tests/golden/leaf3_eigs.json (residuals <= 1e-10 ||H||)",
         "max_residual_rel": max(s["max_residual"] / s["hnorm"] for s in stats),
+        "replicas": D.world,
+        "f64_separable": {"value": f64_sep, "steps": K, "ms_per_step": 1e3 * t_sep / K,
+                          "iterations": [s["iterations"] for s in st_sep], "max_rel_eig_err": err_sep},
+        "plain_f64": {"value": plain, "steps": kp, "ms_per_step": 1e3 * t64 / kp, "iterations": ms64,
+                      "hit_maxiter": sum(1 for s in st64 if s["hit_maxiter"]), "maxiter": 1000,
+                      "max_rel_eig_err": err64,
+                      "value_without_maxiter_runs": (sum(st64[j]["converged"] for j in ok64) /
+                                                     sum(st64[j]["seconds"] for j in ok64)) if ok64 else None},
+        "speedup_mixed_vs_f64": value / plain if plain > 0 else None,
+        "speedup_precision_alone": value / f64_sep if f64_sep > 0 else None,
+        "speedup_preconditioner_alone": f64_sep / plain if plain > 0 else None,
+        "iterations": [s["iterations"] for s in stats], "iterations_f64_phase": [s["iterations_f64"] for s in stats],
         "e2e": {"value": conv_e / te, "unit": "eigenpairs/s", "h2d_bytes_per_step": int(h2d / ke),
-                "d2h_bytes_per_step": int(d2h / ke), "steps": ke},
+                "d2h_bytes_per_step": int(d2h / ke), "steps": ke, "max_rel_eig_err": err_e},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": APPLY_TRAFFIC_BYTES, "kernel": "k_apply_fused<float> (fused stencil apply, 16 columns, the tuned variant)",
                      "algorithmic_bytes": alg, "launch_us": t_apply * 1e6, "peak_kind": kind},
@@ -321,9 +380,14 @@ def run_ours(args, D):
                           "algorithmic_bytes": alg_gram, "launch_us": t_gram * 1e6, "peak_kind": kind},
         "clocks": clk, "gpu_launches": launches,
     }
+    for H in ops.values():
+        H.close()
+    if not args.no_subs and D.world == 1:
+        line["dense"] = sub_dense(torch, args)
+        line["batch"] = sub_batch(torch, args)
+        line["warmstart"] = sub_warmstart(torch, args)
     if not args.no_cpu and D.world == 1:
-        line["cpu_baseline"] = cpu_baseline(ths[idx[0]], bounded=True,
-                                            iters=int(round(np.mean([s["iterations"] for s in st64]))))
+        line["cpu_baseline"] = cpu_baseline(ths[idx[0]], idx[0], "separable")
     return line if D.rank == 0 else None
 
 
@@ -539,14 +603,9 @@ def run_mode_workload(args):
     return out
 
 
-def run_batch_workload(args):
-    """Batched theta sweep: 512 fluxonium leaves (n ~ U{200..1600} on [-5 pi, 5 pi], 5-point stencil,
-    keep 10) plus 64 chains of 2-4 leaves (g ~ U[0.01, 0.1] n_i n_{i+1}, parents keep 20), all leaves
-    in one persistent graph-captured launch (CTA size from the autotuner), then the parents."""
-    import torch
-    from kfgpu import KronFreeOperator, LOBPCG, circuits, ops as P, solve
-    from kfgpu.batch import autotune, batch_solve
-    from kfgpu.ops import PhaseGrid, localop
+def batch_draws():
+    """The batched sweep's leaves and chains (numpy default_rng(20261207)), in draw order."""
+    from kfgpu import circuits
     rng = np.random.default_rng(SEED + 2)
     leaves = []
     for _ in range(512):
@@ -557,6 +616,17 @@ def run_batch_workload(args):
         k = int(rng.integers(2, 5))
         chains.append(([(circuits.fluxonium_theta(rng), int(rng.integers(200, 1601))) for _ in range(k)],
                        [rng.uniform(0.01, 0.1) for _ in range(k - 1)]))
+    return leaves, chains
+
+
+def sub_batch(torch, args):
+    """Batched theta sweep: 512 fluxonium leaves (n ~ U{200..1600} on [-5 pi, 5 pi], 5-point stencil,
+    keep 10) plus 64 chains of 2-4 leaves (g ~ U[0.01, 0.1] n_i n_{i+1}, parents keep 20), all leaves
+    in one persistent graph-captured launch (CTA size from the autotuner), then the parents."""
+    from kfgpu import KronFreeOperator, LOBPCG, circuits, ops as P, solve
+    from kfgpu.batch import autotune, batch_solve
+    from kfgpu.ops import PhaseGrid, localop
+    leaves, chains = batch_draws()
     all_leaves = leaves + [lf for c, _ in chains for lf in c]
     ops = []
     for th, n in all_leaves:
@@ -565,18 +635,17 @@ def run_batch_workload(args):
     m = [10] * len(ops)
     tol = 1e-8 * 2e3            # 1e-8 ||H|| for the coarsest leaves' Gershgorin bound scale
     tile = autotune(ops[:64], m[:64], tol)
+    batch_solve(ops[:32], m[:32], tol)          # warm-up: the graph and module set-up
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     Es, Vs, iters, resid = batch_solve(ops, m, tol)
     t_leaves = time.perf_counter() - t0
-    # parents of the chains
     t1 = time.perf_counter()
     k0 = len(leaves)
-    nparent_pairs = 0
+    nparent_pairs, Ep_all = 0, []
     for c, gs in chains:
         idx = list(range(k0, k0 + len(c)))
         k0 += len(c)
-        dims = [10] * len(c)
         terms = [(1.0, [(a, P.DiagonalOp(Es[i]))]) for a, i in enumerate(idx)]
         ports = []
         for i in idx:
@@ -585,23 +654,46 @@ def run_batch_workload(args):
             ports.append(Vs[i].T @ A @ Vs[i])
         for a in range(len(c) - 1):
             terms.append((-gs[a], [(a, P.DenseOp(ports[a])), (a + 1, P.DenseOp(ports[a + 1]))]))
-        H = KronFreeOperator(dims, terms, block_capacity=24)
+        H = KronFreeOperator([10] * len(c), terms, block_capacity=24)
         Ep, Vp, st = solve(LOBPCG(tol=1e-8 * H.gershgorin_bound(), precision="mixed"), H, 20)
+        Ep_all.append(Ep)
         nparent_pairs += 20
         H.close()
     t_parents = time.perf_counter() - t1
-    return {"workload": "batched theta sweep: 512 fluxonium leaves + 64 chains of 2-4 (704 leaves in one launch)",
-            "leaves": len(ops), "leaf_pairs_per_s": 10 * len(ops) / t_leaves, "leaf_seconds": t_leaves,
+    fx = fixture("batch_eigs.json")
+    err_leaf = max(rel_err(E, R) for E, R in zip(Es, fx["leaf_E"])) if fx else None
+    err_par = max(rel_err(E, R) for E, R in zip(Ep_all, fx["parent_E"])) if fx else None
+    # the batched launch's unavoidable HBM traffic: every leaf's operator data in (diagonal and 5
+    # band weights, FP64) and its 10 eigenpairs out; the filter's blocks stay in L2 / shared memory
+    by = sum(n * 6 * 8 + n * 10 * 8 + 80 for _, n in all_leaves)
+    peak, kind = peaks()
+    return {"workload": "batched theta sweep: 512 fluxonium leaves + 64 chains of 2-4 "
+                        f"({len(ops)} leaves in one launch), numpy default_rng(20261207)",
+            "value": (10 * len(ops) + nparent_pairs) / (t_leaves + t_parents), "unit": "eigenpairs/s",
+            "leaf_pairs_per_s": 10 * len(ops) / t_leaves, "leaf_seconds": t_leaves,
             "parents": len(chains), "parent_seconds": t_parents,
-            "pairs_per_s_total": (10 * len(ops) + nparent_pairs) / (t_leaves + t_parents),
+            "max_rel_eig_err": max(err_leaf, err_par) if fx else None, "max_rel_eig_err_leaves": err_leaf,
+            "max_rel_eig_err_parents": err_par, "eig_err_ref": "FP64 CPU oracle, tests/golden/batch_eigs.json",
             "tuned_threads_per_cta": tile, "max_leaf_iterations": int(iters.max()),
-            "mean_leaf_iterations": float(iters.mean()), "max_residual": float(resid.max())}
+            "mean_leaf_iterations": float(iters.mean()), "max_residual": float(resid.max()),
+            "roofline": {"bound": "hbm", "achieved": by / t_leaves / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": by / t_leaves / 1e9 / peak, "traffic": None, "algorithmic_bytes": by,
+                         "kernel": "k_batch_chfsi (one persistent launch over all leaves)", "peak_kind": kind,
+                         "note": "algorithmic bytes = each leaf's operator data in and eigenpairs out; the "
+                                 "filter blocks live in L2 and shared memory, so the launch is bound by its "
+                                 "per-leaf dependency chain, not by HBM"}}
 
 
-def run_warmstart_workload(args):
+def run_batch_workload(args):
+    import torch
+    return sub_batch(torch, args)
+
+
+def sub_warmstart(torch, args):
     """Learned warm start on the two-transmon circuit (flat 61 x 61): label n_train theta with the
     plain solver, POD 128, train 7 -> 256 -> 256 -> 1536 with the library's kernels, then LOBPCG on
-    n_test held-out theta: warm-started vs random start."""
+    n_test held-out theta: warm-started vs the product seed (the method without the network) vs a
+    random start, all with the separable preconditioner."""
     from kfgpu import warmstart as W
     t0 = time.perf_counter()
     train = W.sample_thetas(args.n_train, seed=SEED + 3)
@@ -609,102 +701,149 @@ def run_warmstart_workload(args):
     t_label = time.perf_counter() - t0
     POD = W.pod_basis(Vs, k=128)
     ws = W.WarmStart(POD, 12, hidden=256, seed=1)
+    torch.cuda.synchronize()
     t1 = time.perf_counter()
     losses = ws.fit(train, W.targets(Vs, POD), epochs=args.epochs, batch=256, lr=1e-3)
+    torch.cuda.synchronize()
     t_train = time.perf_counter() - t1
-    rows = W.evaluate(ws, W.sample_thetas(args.n_test, seed=SEED + 4))
+    test = W.sample_thetas(args.n_test, seed=SEED + 4)
+    rows = W.evaluate(ws, test, product_arm=True)
     wi = np.array([r["warm_iters"] for r in rows]); ri = np.array([r["random_iters"] for r in rows])
+    pi = np.array([r["product_iters"] for r in rows])
     wt = np.array([r["warm_s"] for r in rows]); rt = np.array([r["random_s"] for r in rows])
-    return {"workload": "learned warm start, two transmons flat 61x61 (N=3,721), m=12",
-            "n_train": args.n_train, "n_test": args.n_test, "label_seconds": t_label, "train_seconds": t_train,
+    pt = np.array([r["product_s"] for r in rows])
+    fx = fixture("warm_eigs.json")
+    err = None
+    if fx:
+        nchk = min(len(fx["E"]), len(rows))
+        assert all(abs(fx["theta"][j][k] - test[j][k]) < 1e-15 for j in range(nchk) for k in fx["theta"][j])
+        err = max(rel_err(rows[j]["E_warm"], fx["E"][j]) for j in range(nchk))
+    # training arithmetic: forward 2 B (7*256 + 256*256 + 256*1536) flops per batch, backward twice that
+    nb = -(-args.n_train // 256)
+    flops = 3 * 2 * 256 * (7 * 256 + 256 * 256 + 256 * 1536) * nb * args.epochs
+    peak_tc = float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["bf16_tflops"]) \
+        if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else 1900.0
+    return {"workload": "learned warm start, two transmons flat 61x61 (N=3,721), m=12; train "
+                        f"{args.n_train} theta, evaluate {args.n_test} held-out theta",
+            "value": 12 / float(wt.mean()), "unit": "eigenpairs/s (warm-started solve)",
+            "product_seed_pairs_per_s": 12 / float(pt.mean()), "random_pairs_per_s": 12 / float(rt.mean()),
+            "warm_mean_iterations": float(wi.mean()), "product_mean_iterations": float(pi.mean()),
+            "random_mean_iterations": float(ri.mean()),
+            "label_seconds": t_label, "train_seconds": t_train,
             "loss_first_last": [float(losses[0]), float(losses[-1])],
-            "warm_mean_iterations": float(wi.mean()), "random_mean_iterations": float(ri.mean()),
-            "warm_mean_seconds": float(wt.mean()), "random_mean_seconds": float(rt.mean()),
-            "warm_pairs_per_s": 12 / float(wt.mean()), "random_pairs_per_s": 12 / float(rt.mean()),
             "fell_back": int(sum(r["fell_back"] for r in rows)),
-            "max_abs_dE": float(max(r["max_dE"] for r in rows))}
+            "max_rel_eig_err": err, "eig_err_ref": "FP64 CPU oracle (LAPACK), tests/golden/warm_eigs.json, "
+                                                   "the first held-out theta",
+            "roofline": {"bound": "tensor", "achieved": flops / t_train / 1e12, "peak": peak_tc, "unit": "TFLOP/s",
+                         "frac": flops / t_train / 1e12 / peak_tc, "traffic": None,
+                         "kernel": "k_gemm forward / backward + Adam (BF16 weights, FP32 accumulation on the SIMT "
+                                   "pipes): the whole training loop, host steps included",
+                         "peak_kind": "measured bf16 burst"}}
 
 
-def run_dense_workload(args):
-    """Three children of 48 kept states (N = 110,592) with dense pairwise port couplings; the lowest
-    30 pairs, mixed vs FP64 (eigenvalue differences and FP64 residuals)."""
+def run_warmstart_workload(args):
     import torch
+    return sub_warmstart(torch, args)
+
+
+def sub_dense(torch, args):
+    """Three children of 48 kept states (N = 110,592) with dense pairwise port couplings; the lowest
+    30 pairs by mixed-precision and FP64 LOBPCG (block 32), eigenvalues against the FP64 oracle."""
     from kfgpu import KronFreeOperator, LOBPCG, circuits, solve
-    out = {"workload": "dense parent 48^3 (N=110,592), 3 dense pair couplings, m=30 block 32"}
     rng = np.random.default_rng(SEED + 5)
     dims, terms = circuits.dense_parent(rng, d=48)
     H = KronFreeOperator(dims, terms, block_capacity=32)
     tol = 1e-8 * H.gershgorin_bound()
+    solve(LOBPCG(tol=tol, precision="mixed", guard=2), H, 30)         # warm-up (kernel tuning)
     res = {}
-    for prec in ("mixed", "f64"):
+    for prec, reps in (("mixed", 3), ("f64", 1)):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        E, V, st = solve(LOBPCG(tol=tol, precision=prec, guard=2), H, 30)
-        res[prec] = (E, time.perf_counter() - t0, st)
-    out.update({"mixed_pairs_per_s": 30 / res["mixed"][1], "f64_pairs_per_s": 30 / res["f64"][1],
-                "mixed_iterations": res["mixed"][2]["iterations"], "f64_iterations": res["f64"][2]["iterations"],
-                "max_rel_dE_mixed_vs_f64": float(np.max(np.abs(res["mixed"][0] - res["f64"][0]) / np.abs(res["f64"][0]))),
-                "max_residual_rel": float(res["mixed"][2]["max_residual"] / H.gershgorin_bound())})
-    # the dense apply alone (32 columns, FP32 and FP64): flops counted as 6 mode products per column
-    for f32 in (True, False):
-        t = measure_apply(torch, H, f32, b=32)
-        flops = 6 * 2 * 48 * H.N * 32
-        out["apply_%s_us" % ("f32" if f32 else "f64")] = t * 1e6
-        out["apply_%s_tflops" % ("f32" if f32 else "f64")] = flops / t / 1e12
+        for _ in range(reps):
+            E, V, st = solve(LOBPCG(tol=tol, precision=prec, guard=2), H, 30)
+        res[prec] = (E, (time.perf_counter() - t0) / reps, st)
+    fx = fixture("dense48_eigs.json")
+    peak, kind = peaks()
+    t = measure_apply(torch, H, True, b=32)
+    by = 2 * H.N * 32 * 4
+    flops = 6 * 2 * 48 * H.N * 32
+    out = {"workload": "dense parent 48^3 (N=110,592), 3 dense pair couplings, m=30 block 32, "
+                       "numpy default_rng(20261210)",
+           "value": 30 / res["mixed"][1], "unit": "eigenpairs/s", "f64_pairs_per_s": 30 / res["f64"][1],
+           "mixed_iterations": res["mixed"][2]["iterations"], "f64_iterations": res["f64"][2]["iterations"],
+           "max_rel_eig_err": rel_err(res["mixed"][0], fx["E"]) if fx else None,
+           "max_rel_eig_err_f64": rel_err(res["f64"][0], fx["E"]) if fx else None,
+           "eig_err_ref": "FP64 CPU oracle (ARPACK), tests/golden/dense48_eigs.json",
+           "max_residual_rel": float(res["mixed"][2]["max_residual"] / H.gershgorin_bound()),
+           "roofline": {"bound": "hbm", "achieved": by / t / 1e9, "peak": peak, "unit": "GB/s",
+                        "frac": by / t / 1e9 / peak, "traffic": None, "algorithmic_bytes": by,
+                        "kernel": "FP32 apply of the three dense pair terms, 32 columns", "launch_us": t * 1e6,
+                        "tflops_counted_as_6_mode_products": flops / t / 1e12, "peak_kind": kind}}
+    t64 = measure_apply(torch, H, False, b=32)
+    out["apply_f64_us"] = t64 * 1e6
+    H.close()
     return out
 
 
-def cpu_baseline(theta, bounded=True, iters=None):
-    """The oracle's restatement of the reference CPU path on the host cores: a bounded sample of
-    LOBPCG iterations of the same solve (C/OpenMP mul! + NumPy LOBPCG), extrapolated to the
-    iteration count the same algorithm needs (measured here on the GPU's FP64 run when given,
-    else the sample's own count)."""
-    from oracle import capply, circuits as oc, solvers as osol
+def run_dense_workload(args):
+    import torch
+    return sub_dense(torch, args)
+
+
+def cpu_baseline(theta, draw, precond):
+    """One complete solve of the draw on the host cores, measured to convergence: the oracle's
+    restatement of the reference CPU path (C/OpenMP mul!, LOBPCG with the reference's policy, FP64,
+    product seed, maxiter 1000), with the given preconditioner."""
+    from oracle import circuits as oc, solvers as osol
     H = oc.three_mode_operator(theta)
-    CA = capply.CApply(H)
-
-    class Fast:
-        N, dtype = H.N, H.dtype
-
-        def matvec(self, X):
-            return CA.matvec(X)
-
-        def full_diagonal(self):
-            return H.full_diagonal()
-
     tol = 1e-8 * H.gershgorin_bound()
-    X0 = osol.perturbed_seed(H.product_seed(M_PAIRS + 4))
-    D = H.full_diagonal()
-    n_it = 8 if bounded else 100000
     t0 = time.perf_counter()
-    r = osol.lobpcg_core(Fast(), X0, D, tol, n_it, "ritz", 0.01)
+    try:
+        E, V, r = osol.lobpcg_solve(osol.LOBPCG(tol=tol, preconditioner=precond, maxiter=1000), H, M_PAIRS)
+        conv, err = M_PAIRS, None
+        fx = fixture("leaf3_eigs.json").get("draws", {})
+        if str(draw) in fx:
+            err = rel_err(E, fx[str(draw)]["E"])
+    except osol.NotConverged as e:
+        r, E = e.res, None
+        conv, err = int(np.sum(r["resid"][:M_PAIRS] <= tol)), None
     dt = time.perf_counter() - t0
-    per_it = dt / max(r["iters"], 1)
-    need = iters if iters else r["iters"]
     cores = os.cpu_count()
-    return {"value": M_PAIRS / (per_it * need), "unit": "eigenpairs/s", "cores": cores, "kind": "port",
-            "sample": f"{r['iters']} LOBPCG iterations of the N=671,744 solve in {dt:.1f} s "
-                      f"({per_it:.2f} s/iteration, OpenMP threads={cores}), extrapolated to {need} iterations"}
+    return {"value": conv / dt, "unit": "eigenpairs/s", "cores": cores, "kind": "port",
+            "sample": f"one complete solve of draw {draw} measured to convergence: {r['iters']} LOBPCG iterations "
+                      f"({precond} preconditioner, FP64, C/OpenMP mul! + threaded BLAS, {cores} threads), "
+                      f"{conv} of {M_PAIRS} pairs converged in {dt:.1f} s",
+            "iterations": int(r["iters"]), "seconds": dt, "max_rel_eig_err": err, "preconditioner": precond}
 
 
 def run_reference(args):
+    """The reference's CPU path (the oracle port: the reference is Julia and cannot run here) on the
+    host cores, on the first draw the repository's arm times: one complete solve with the
+    reference's default per-Ritz Jacobi preconditioner (the value), and one with the separable
+    preconditioner the repository's arm uses (so the algorithm's and the hardware's gains can be
+    read apart).  Warm-up: the oracle's C library is built and applied before timing."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return None
+    from oracle import capply, circuits as oc
     ths = thetas()
     K, W = args.steps, args.warmup
-    vals = []
-    for k in range(W + K):
-        cb = cpu_baseline(ths[k % NDRAWS], bounded=True, iters=args.ref_iters)
-        if k >= W:
-            vals.append(cb)
-    v = float(np.mean([c["value"] for c in vals]))
+    d = W % NDRAWS
+    Hw = oc.three_mode_operator(ths[d])
+    CA = capply.CApply(Hw)
+    X = np.asfortranarray(np.random.default_rng(0).standard_normal((Hw.N, 16)))
+    for _ in range(W):
+        CA.matvec(X)
+    ritz = cpu_baseline(ths[d], d, "ritz")
+    sep = cpu_baseline(ths[d], d, "separable")
+    v = ritz["value"]
     return {"metric": "converged eigenpairs/s at 1e-8 resid: warm-start mixed vs plain FP64, 1 GB300",
             "impl": "reference", "value": v, "unit": "eigenpairs/s", "n_gpus": 0, "steps": K, "warmup": W,
-            "higher_is_better": True, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "three-mode leaf 41x256x64 (N=671,744), LOBPCG m=12 block=16, product seed"},
-            "cpu_baseline": {"value": v, "unit": "eigenpairs/s", "cores": vals[0]["cores"], "kind": "port",
-                             "sample": vals[0]["sample"]},
+            "solves": 1, "higher_is_better": True, "dtype": "f64", "data": "synthetic", "config": dict(CONFIG),
+            "cpu_baseline": {"value": v, "unit": "eigenpairs/s", "cores": ritz["cores"], "kind": "port",
+                             "sample": ritz["sample"]},
+            "max_rel_eig_err": ritz["max_rel_eig_err"],
+            "cpu_separable": sep,
             "e2e": {"value": v, "unit": "eigenpairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
@@ -716,10 +855,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--plain-steps", type=int, default=2)
     ap.add_argument("--e2e-steps", type=int, default=2)
-    ap.add_argument("--ref-iters", type=int, default=868,
-                    help="LOBPCG iterations the plain FP64 solve of this workload takes, for the reference arm's "
-                         "extrapolation (868: the mean over the first two timed draws measured on GB300)")
-    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline solve in the repository's arm")
+    ap.add_argument("--no-subs", action="store_true",
+                    help="skip the batched-sweep, warm-start and dense-parent sub-measurements")
     ap.add_argument("--buffer", type=int, default=None,
                     help="unchecked LOBPCG columns beyond the guards in the mixed solves (default: the library's)")
     ap.add_argument("--workload", default="leaf3",

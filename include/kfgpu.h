@@ -111,10 +111,13 @@ int kf_op_apply_axpby(kf_op *op, const void *X, void *Y, const void *Z, int64_t 
  * have memory allocated behind its back, and a tight solver loop cannot take the device
  * synchronisation of a cudaMalloc.  This entry point computes the same Y = H X (device pointers
  * only; KF_F64 or KF_F32) and allocates nothing: its scratch is a static device array of
- * KF_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until exit.  Blocks whose
+ * KF_NOALLOC_SCRATCH_BYTES that each device holds from its first call until exit.  Blocks whose
  * dense-factor chains need more than that (2 N b elements) are rejected with KF_EINVAL.  All calls
- * on a device share the array, so calls that overlap on the GPU race; the first call on each
- * device looks up the array's address and should come before any stream capture. */
+ * on a device share the array, so calls that overlap on the GPU race.  The array is reserved when
+ * the library's module holding it loads, at the first call on each device (CUDA loads modules
+ * lazily), so a caller that must see no allocation later makes one set-up call per device first:
+ * b = 0 on an operator with dense-factor terms reserves the array, and a b > 0 call also loads the
+ * kernels.  Make the set-up call before any stream capture. */
 #define KF_NOALLOC_SCRATCH_BYTES (8u << 20)
 int kf_op_apply_noalloc(kf_op *op, const void *X, void *Y, int64_t ldx, int64_t ldy, int64_t b, int32_t flags);
 

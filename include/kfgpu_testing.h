@@ -111,6 +111,12 @@ int kf_test_update(int path, float *Y, int64_t ldy, int ky, const float *X0, int
 int kf_test_apply_variant(kf_op *op, int variant, const void *X, void *Y, int64_t ld, int64_t b, int32_t flags,
                           int reps, float *ms_per_launch);
 
+/*
+ * The bytes of chain scratch the operator has allocated for kf_op_apply so far (0 until a block
+ * with dense-factor terms is applied through kf_op_apply).  Returns a KF_* status.
+ */
+int kf_test_op_scratch_bytes(const struct kf_op *op, uint64_t *bytes);
+
 #ifdef __cplusplus
 }
 #endif

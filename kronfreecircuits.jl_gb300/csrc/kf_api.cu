@@ -392,6 +392,13 @@ int kf_test_sym_eig(int n, const double *A, int lda, double *w, double *V, int l
     });
 }
 
+int kf_test_op_scratch_bytes(const kf_op *op, uint64_t *bytes) {
+    return guarded([&] {
+        KF_REQUIRE(op && bytes, KF_EINVAL, "kf_test_op_scratch_bytes: NULL argument");
+        *bytes = (uint64_t)op->scratch_bytes;
+    });
+}
+
 int kf_test_chol2(const double *G, int wx, int r, double *C_out, int *status_out) {
     return guarded([&] {
         KF_REQUIRE(G && C_out && status_out && wx >= 0 && r >= 1 && r <= kf::CHOL2_MAX_R, KF_EINVAL,

@@ -10,13 +10,23 @@
 // the same application with no allocation at all: its chain scratch is one fixed array in device
 // global memory, declared here with static storage, sized KF_NOALLOC_SCRATCH_BYTES.
 //
-// Costs and rules.  Every GPU that loads this library holds the array until the process exits.
+// Costs and rules.  Each device holds the array from its first call until the process exits.
 // All calls on a device share the one array, and it keeps whatever the last call left in it
 // (nothing here needs it zeroed: each chain pass writes its scratch block in full before any pass
 // reads it); calls whose executions overlap on the GPU (different streams, or different host
-// threads with no ordering between their streams) race on it and give wrong results.  The first
-// call on each device looks up the array's device address (cudaGetSymbolAddress) with that device
-// current; make that first call before any stream capture begins.
+// threads with no ordering between their streams) race on it and give wrong results.
+//
+// Set-up.  The array belongs to this file's device module, and with CUDA's lazy module loading
+// (the default) the driver loads a module -- reserving its static arrays in device memory -- the
+// first time it is used.  So the first call on each device, which looks up the array's device
+// address (cudaGetSymbolAddress) with that device current, is where the array's 8 MiB are taken,
+// and the first launch of each kernel the call uses loads that kernel's module too.  A caller that
+// must see no device allocation once it runs makes one warm-up call per device at set-up: a call
+// with b = 0 on an operator with dense-factor terms does the address lookup and loads this module;
+// one with b > 0 also loads the kernels (make it with the precision the caller will use), and
+// every later call allocates nothing.  Make the set-up call before any stream capture begins.
+// After cudaDeviceReset the looked-up addresses (and every kf_op) are invalid: the library must
+// not be used across a reset.
 #include <mutex>
 
 #include "kf_internal.h"
@@ -60,7 +70,10 @@ extern "C" int kf_op_apply_noalloc(kf_op *op, const void *X, void *Y, int64_t ld
                    "kf_op_apply_noalloc: device pointers only (the host path needs staging buffers)");
         const int64_t N = op->N;
         KF_REQUIRE(b >= 0 && ldx >= N && ldy >= N, KF_EDIM, "kf_op_apply_noalloc: bad block shape");
-        if (b == 0) return KF_OK;
+        if (b == 0) {
+            if (!op->chains.empty()) (void)scratch_address();   // the set-up call (see above)
+            return KF_OK;
+        }
         KF_REQUIRE(X && Y, KF_EINVAL, "kf_op_apply_noalloc: NULL block");
         const bool f32 = (flags & KF_F32) != 0;
         const size_t es = f32 ? 4 : 8;

@@ -105,8 +105,11 @@ class WarmStart:
         return [self.POD @ c.reshape(k, self.m, order="F") for c in C]
 
 
-def evaluate(ws, thetas, m=12, ncut=30, fallback_resid=1e-2, fallback_iters=3, preconditioner="separable"):
-    """LOBPCG iterations and wall time per theta: warm-started by the network vs a random start."""
+def evaluate(ws, thetas, m=12, ncut=30, fallback_resid=1e-2, fallback_iters=3, preconditioner="separable",
+             product_arm=False):
+    """LOBPCG iterations and wall time per theta: warm-started by the network vs a random start and,
+    with `product_arm`, vs the solver's default start without the network (the product seed,
+    src/lobpcg.jl:247), all with the same preconditioner."""
     X0s = ws.blocks(thetas) if ws is not None else [None] * len(thetas)
     rows = []
     for th, X0 in zip(thetas, X0s):
@@ -116,6 +119,10 @@ def evaluate(ws, thetas, m=12, ncut=30, fallback_resid=1e-2, fallback_iters=3, p
         Er, _, sr = solve(LOBPCG(tol=tol, seed="random", preconditioner=preconditioner), H, m)
         tr = time.perf_counter() - t0
         row = {"random_iters": sr["iterations"], "random_s": tr, "E": Er}
+        if product_arm:
+            t0 = time.perf_counter()
+            Ep, _, sp = solve(LOBPCG(tol=tol, seed="product", preconditioner=preconditioner), H, m)
+            row.update({"product_iters": sp["iterations"], "product_s": time.perf_counter() - t0, "E_product": Ep})
         if X0 is not None:
             t0 = time.perf_counter()
             # guards from the product seed, as the reference's warm starts take them (src/lobpcg.jl:182-190)
@@ -123,7 +130,7 @@ def evaluate(ws, thetas, m=12, ncut=30, fallback_resid=1e-2, fallback_iters=3, p
                                      fallback_iters=fallback_iters, fallback_resid=fallback_resid), H, m, X0=X0)
             tw = time.perf_counter() - t0
             row.update({"warm_iters": sw["iterations"], "warm_s": tw, "fell_back": sw["fell_back"],
-                        "max_dE": float(np.max(np.abs(Ew - Er)))})
+                        "max_dE": float(np.max(np.abs(Ew - Er))), "E_warm": Ew})
         rows.append(row)
         H.close()
     return rows

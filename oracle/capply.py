@@ -41,7 +41,77 @@ def lib():
     if _lib is None:
         _lib = C.CDLL(build())
         _lib.kf_ref_apply.restype = C.c_int
+        _lib.kf_ref_resid.restype = C.c_int
+        _lib.kf_ref_scale.restype = C.c_int
+        _lib.kf_ref_gram.restype = C.c_int
+        _lib.kf_ref_update.restype = C.c_int
     return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _ld(a):
+    """Leading dimension of an F-contiguous (N, k) block (or of a column slice of one)."""
+    return a.strides[1] // 8 if a.ndim == 2 and a.shape[1] > 1 else a.shape[0]
+
+
+def resid(X, HX, lam, R):
+    """R = HX - X diag(lam) into the F-ordered R (threaded); returns the squared column norms."""
+    N, k = X.shape
+    n2 = np.empty(max(k, 1))
+    for a in (X, HX, R):
+        assert a.flags.f_contiguous or k == 1
+    lam = np.ascontiguousarray(lam, dtype=np.float64)
+    rc = lib().kf_ref_resid(C.c_int64(N), k, _dp(X), C.c_int64(_ld(X)), _dp(HX), C.c_int64(_ld(HX)), _dp(lam),
+                            _dp(R), C.c_int64(_ld(R)), _dp(n2))
+    if rc:
+        raise RuntimeError("kf_ref_resid failed")
+    return n2[:k]
+
+
+def _fcols(a):
+    """True when a is a column-major (N, k) block whose columns may be strided by a leading dimension."""
+    return a.ndim == 2 and a.strides[0] == 8 and (a.shape[1] <= 1 or a.strides[1] >= 8 * a.shape[0])
+
+
+def gram(A, B):
+    """A' B for tall column-major blocks (threaded, fixed-order partial sums)."""
+    N, ka = A.shape
+    kb = B.shape[1]
+    G = np.empty((ka, kb), order="F")
+    rc = lib().kf_ref_gram(C.c_int64(N), ka, _dp(A), C.c_int64(_ld(A)), kb, _dp(B), C.c_int64(_ld(B)), _dp(G))
+    if rc:
+        raise RuntimeError("kf_ref_gram failed")
+    return G
+
+
+def update(X, Cm, alpha=1.0, beta=0.0, Y=None):
+    """Y = alpha X Cm + beta Y for a tall column-major X (threaded); a new F block when Y is None."""
+    N, kx = X.shape
+    Cm = np.asfortranarray(Cm, dtype=np.float64)
+    ky = Cm.shape[1]
+    if Y is None:
+        Y = np.empty((N, ky), order="F")
+        beta = 0.0
+    rc = lib().kf_ref_update(C.c_int64(N), kx, _dp(X), C.c_int64(_ld(X)), ky, _dp(Cm), C.c_int64(max(Cm.shape[0], 1)),
+                             C.c_double(alpha), C.c_double(beta), _dp(Y), C.c_int64(_ld(Y)))
+    if rc:
+        raise RuntimeError("kf_ref_update failed")
+    return Y
+
+
+def scale(R, S, thp, eta, mode, W):
+    """W[:, j] = R[:, j] / hypot(S - thp[j], eta) (mode 0) or / (S - thp[0]) (mode 1); W may be R."""
+    N, k = R.shape
+    thp = np.ascontiguousarray(thp, dtype=np.float64)
+    S = np.ascontiguousarray(S, dtype=np.float64)
+    rc = lib().kf_ref_scale(C.c_int64(N), k, _dp(R), C.c_int64(_ld(R)), _dp(S), _dp(thp), C.c_double(eta), mode,
+                            _dp(W), C.c_int64(_ld(W)))
+    if rc:
+        raise RuntimeError("kf_ref_scale failed")
+    return W
 
 
 class CApply:

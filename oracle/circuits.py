@@ -97,3 +97,35 @@ def _merge(terms):
         else:
             out.append((c, fs))
     return [(c, fs) for c, fs in out if c != 0]
+
+
+def dense_parent_operator(rng, d=48):
+    """The parent-level dense contraction workload: three children keeping d states each,
+    H = diag(E_a + E_b + E_c) + sum_{i<j} g_ij P_i (x) P_j with per-child energies sorted U[0, 20],
+    P_i = sym(N(0, 1)) / sqrt(d) and g_ij ~ U[0.05, 0.5], drawn from `rng` in that order (the
+    energies of all three children, then the three port matrices, then each coupling as its term
+    is formed).  Returns the oracle operator (dims d^3, N = d^3)."""
+    Es = [np.sort(rng.uniform(0, 20, d)) for _ in range(3)]
+    Ps = []
+    for _ in range(3):
+        A = rng.standard_normal((d, d))
+        Ps.append((A + A.T) / 2 / np.sqrt(d))
+    terms = [(1.0, [(a, kfref.DiagonalOp(Es[a]))]) for a in range(3)]
+    for i, j in ((0, 1), (0, 2), (1, 2)):
+        terms.append((rng.uniform(0.05, 0.5), [(i, kfref.DenseOp(Ps[i])), (j, kfref.DenseOp(Ps[j]))]))
+    return kfref.KronFreeOperator([d, d, d], terms)
+
+
+def real_three_oscillators(d):
+    """Three truncated oscillators with real cos(0.5 (a + a')) pairwise couplings, restating the
+    reference's test helper (test/helpers.jl:27-60): H = sum_i w_i n_i + 0.2 sum_{i<j} C_i C_j,
+    w = (1.0, 1.1, 1.2), n = diag(0..d-1).  Returns (dims, terms with kfref ops)."""
+    a = np.diag(np.sqrt(np.arange(1.0, d)), 1)
+    X = a + a.T
+    lam, V = np.linalg.eigh(X)
+    cos_op = (V * np.cos(0.5 * lam)[None, :]) @ V.T
+    nvec = np.arange(d, dtype=float)
+    terms = [(w, [(i, kfref.DiagonalOp(nvec))]) for i, w in enumerate((1.0, 1.1, 1.2))]
+    for i, j in ((0, 1), (1, 2), (0, 2)):
+        terms.append((0.2, [(i, kfref.DenseOp(cos_op)), (j, kfref.DenseOp(cos_op))]))
+    return [d, d, d], terms

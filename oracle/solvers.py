@@ -68,43 +68,131 @@ def perturbed_seed(X0, key=0x4B46):
     return X
 
 
+def _blas():
+    from scipy.linalg import blas
+    return blas
+
+
+def _gemm(A, B, trans_a=False, alpha=1.0, beta=0.0, C=None):
+    """alpha op(A) B + beta C on F-ordered blocks; returns an F array.  Tall-skinny products (A'B and
+    X C with many rows) go to the threaded C helpers (oracle/kf_apply_ref.c), the rest to BLAS
+    dgemm.  A column slice of an F-ordered block is passed without a copy."""
+    from . import capply
+    tall = A.shape[0] >= 4096 and A.shape[1] <= 256 and B.shape[1] <= 256 and capply._fcols(A)
+    if tall and trans_a and capply._fcols(B):
+        G = capply.gram(A, B)
+        if C is None:
+            return G if alpha == 1.0 else alpha * G
+        C *= beta
+        C += alpha * G
+        return C
+    if tall and not trans_a and (C is None or (capply._fcols(C) and not np.shares_memory(C, A))):
+        return capply.update(A, B, alpha, beta, C)
+    blas = _blas()
+    A = A if A.flags.f_contiguous else np.asfortranarray(A)
+    B = B if B.flags.f_contiguous else np.asfortranarray(B)
+    if C is None:
+        return blas.dgemm(alpha, A, B, trans_a=int(trans_a))
+    return blas.dgemm(alpha, A, B, beta=beta, c=C, trans_a=int(trans_a), overwrite_c=True)
+
+
+def _fblock(N, k):
+    return np.empty((N, k), order="F")
+
+
 def svqb(M, cutoff):
     """Orthonormal basis of range(M) by the unit-diagonal Gram eigen-decomposition; drops small directions."""
     if M.shape[1] == 0:
         return M
-    G = M.T @ M
+    G = _gemm(M, M, trans_a=True)
     d = 1.0 / np.sqrt(np.maximum(np.diag(G), np.finfo(float).tiny))
     lam, U = np.linalg.eigh(d[:, None] * G * d[None, :])
     top = lam[-1]
     keep = lam > cutoff * top if top > 0 else np.zeros_like(lam, dtype=bool)
     T = (d[:, None] * U[:, keep]) / np.sqrt(lam[keep])[None, :]
-    return M @ T
+    return _gemm(M, np.asfortranarray(T))
 
 
-def lobpcg_core(H, X, D, tol, maxiter, precond="ritz", eta=0.01, n_conv_check=None, cutoff=1e-12):
+class SeparablePrecond:
+    """The separable (fast-diagonalization) preconditioner on the host, restating the library's
+    LOBPCG option: the reference's per-axis eigenbases of the single-axis terms
+    (separable_eigenbases, src/apply.jl:606-642) give
+        W_j = U diag(1 / hypot(S(p) - theta_j, eta_s)) U' R_j,   U = (x)_a U_a,
+    S(p) the sum of the per-axis eigenvalues, eta_s = max(eta, 1e-3 ||H||)."""
+
+    def __init__(self, H, eta, hbound):
+        self.dims = list(H.dims)
+        self.U, lam = H.separable_eigenbases()
+        S = lam[0]
+        for a in range(1, len(self.dims)):
+            S = (S[:, None] + lam[a][None, :]).reshape(-1, order="F")
+        self.S = np.ascontiguousarray(S)
+        self.eta = max(eta, 1e-3 * abs(hbound))
+        self.Ut = [None if u is None else np.ascontiguousarray(u.T) for u in self.U]
+        self.Uc = [None if u is None else np.ascontiguousarray(u) for u in self.U]
+
+    def _mode(self, X, a, A):
+        """Y[l, i, r] = sum_j A[i, j] X[l, j, r] along axis a of the F-ordered (N, k) block X."""
+        N, k = X.shape
+        n = self.dims[a]
+        L = int(np.prod(self.dims[:a]))
+        R = N * k // (L * n)
+        Xc = X.reshape(-1, order="F")
+        if L == 1:
+            Y = _gemm(A, Xc.reshape(n, R, order="F"))
+            return Y.reshape(N, k, order="F")
+        v = Xc.reshape(R, n, L)                       # C-order view of the F-ordered block
+        Y = np.matmul(A, v)                           # batched over R, each an n x n by n x L product
+        return np.asfortranarray(Y.reshape(-1).reshape(N, k, order="F"))
+
+    def __call__(self, Rb, thp):
+        from . import capply
+        Y = Rb if Rb.flags.f_contiguous else np.asfortranarray(Rb)
+        for a, ut in enumerate(self.Ut):
+            if ut is not None:
+                Y = self._mode(Y, a, ut)
+        if Y is Rb:
+            Y = Y.copy(order="F")
+        capply.scale(Y, self.S, thp, self.eta, 0, Y)
+        for a, u in enumerate(self.Uc):
+            if u is not None:
+                Y = self._mode(Y, a, u)
+        return Y
+
+
+def lobpcg_core(H, X, D, tol, maxiter, precond="ritz", eta=0.01, n_conv_check=None, cutoff=1e-12, sep=None,
+                trace=None):
     """Block LOBPCG for the lowest columns of X's width.  Returns dict(lam, X, resid, iters, n_matvec).
 
-    Raises RuntimeError on breakdown (an empty [W P] basis with unconverged columns).
+    Every block is F-ordered and every tall product goes through BLAS; the residuals and the
+    per-Ritz Jacobi scaling run in the C helpers (threaded).  `sep` is a SeparablePrecond for
+    precond="separable".  Raises RuntimeError on breakdown (an empty [W P] basis with unconverged
+    columns).
     """
+    from . import capply
     N, w = X.shape
     n_conv_check = w if n_conv_check is None else n_conv_check
-    X = svqb(X, cutoff)
+    X = svqb(np.asfortranarray(X), cutoff)
     if X.shape[1] < w:
         raise RuntimeError("LOBPCG: the initial block is rank deficient")
     X = svqb(X, cutoff)
-    HX = H.matvec(X)
+    HX = np.asfortranarray(H.matvec(X))
     nmv = w
-    lam, Q = np.linalg.eigh(_sym(X.T @ HX))
-    X, HX = X @ Q, HX @ Q
+    lam, Q = np.linalg.eigh(_sym(_gemm(X, HX, trans_a=True)))
+    Q = np.asfortranarray(Q)
+    X, HX = _gemm(X, Q), _gemm(HX, Q)
     theta_prec = (np.sum(D[:, None] * X ** 2, axis=0) / np.sum(X ** 2, axis=0))
-    P = np.zeros((N, 0))
+    P = _fblock(N, 0)
+    Rb = _fblock(N, w)
     nl = 0
     res = np.full(w, np.inf)
     it = 0
     while True:
         act = slice(nl, w)
-        R = HX[:, act] - X[:, act] * lam[None, act]
-        res[act] = colnorms(R)
+        R = Rb[:, :w - nl]
+        res[act] = np.sqrt(capply.resid(X[:, act], HX[:, act], lam[act], R))
+        if trace is not None:
+            trace(it, res.copy())
         newly = 0
         while nl + newly < w and res[nl + newly] <= tol:
             newly += 1
@@ -117,36 +205,64 @@ def lobpcg_core(H, X, D, tol, maxiter, precond="ritz", eta=0.01, n_conv_check=No
         # precondition the residuals of the still-active columns
         R = R[:, newly:]
         thp = theta_prec[newly:] if it == 1 else lam[nl + newly:w]
+        na = w - nl - newly
+        np_ = P.shape[1] - newly if P.shape[1] else 0
+        Z = _fblock(N, na + np_)
         if precond == "ritz":
-            W = R / np.hypot(D[:, None] - thp[None, :], eta)
+            capply.scale(R, D, thp, eta, 0, Z[:, :na])
         elif precond == "jacobi":
-            sigma = D.min() - 1
-            W = R / (D - sigma)[:, None]
+            capply.scale(R, D, np.array([D.min() - 1]), eta, 1, Z[:, :na])
+        elif precond == "separable":
+            Z[:, :na] = sep(R, thp)
         else:
-            W = R.copy()
-        if P.shape[1]:
-            P = P[:, newly:]
+            Z[:, :na] = R
+        if np_:
+            Z[:, na:] = P[:, newly:]
         nl += newly
-        na = w - nl
         # orthogonalize [W P] against every column of X (one projection), then against itself (SVQB), twice
-        Z = np.hstack([W, P])
         for _ in range(2):
-            Z = Z - X @ (X.T @ Z)
+            Cx = _gemm(X, Z, trans_a=True)
+            Z = _gemm(X, Cx, alpha=-1.0, beta=1.0, C=Z)
             Z = svqb(Z, cutoff)
         if Z.shape[1] == 0:
             raise RuntimeError("LOBPCG: the search directions vanished")
-        HZ = H.matvec(Z)
+        HZ = np.asfortranarray(H.matvec(Z))
         nmv += Z.shape[1]
-        S = np.hstack([X[:, nl:], Z])
-        HS = np.hstack([HX[:, nl:], HZ])
-        th, C = np.linalg.eigh(_sym(S.T @ HS))
-        C = C[:, :na]
-        X[:, nl:] = S @ C
-        HX[:, nl:] = HS @ C
+        Xa, HXa = X[:, nl:], HX[:, nl:]
+        nz = Z.shape[1]
+        A = np.empty((na + nz, na + nz))
+        A[:na, :na] = _gemm(Xa, HXa, trans_a=True)
+        A[:na, na:] = _gemm(Xa, HZ, trans_a=True)
+        A[na:, :na] = A[:na, na:].T
+        A[na:, na:] = _gemm(Z, HZ, trans_a=True)
+        th, Cm = np.linalg.eigh(_sym(A))
+        Cx = np.asfortranarray(Cm[:na, :na])
+        Cz = np.asfortranarray(Cm[na:, :na])
+        Xn = _gemm(Z, Cz, C=_gemm(Xa, Cx), beta=1.0)
+        HXn = _gemm(HZ, Cz, C=_gemm(HXa, Cx), beta=1.0)
+        X[:, nl:] = Xn
+        HX[:, nl:] = HXn
         lam[nl:] = th[:na]
-        P = Z @ C[na:, :]
+        P = _gemm(Z, Cz)
     order = np.argsort(lam, kind="stable")
     return {"lam": lam[order], "X": X[:, order], "resid": res[order], "iters": it, "n_matvec": nmv}
+
+
+def _fast(H):
+    """H with its matvec through the C restatement of mul! (oracle/kf_apply_ref.c) when H is a real
+    `kfref.KronFreeOperator`, else H itself."""
+    from . import capply, kfref
+    if not isinstance(H, kfref.KronFreeOperator) or H.dtype != np.float64:
+        return H
+    CA = capply.CApply(H)
+
+    class _F:
+        N, dtype = H.N, H.dtype
+
+        def matvec(self, X):
+            return CA.matvec(X)
+
+    return _F()
 
 
 def _sym(A):
@@ -161,12 +277,20 @@ class LOBPCG:
             raise ValueError("LOBPCG: tol must be positive and finite")
         if maxiter < 1:
             raise ValueError("LOBPCG: maxiter must be at least 1")
-        if preconditioner not in ("ritz", "jacobi", "none"):
-            raise ValueError("LOBPCG: preconditioner must be ritz, jacobi or none")
+        if preconditioner not in ("ritz", "jacobi", "none", "separable"):
+            raise ValueError("LOBPCG: preconditioner must be ritz, jacobi, none or separable")
         if guard < 0:
             raise ValueError("LOBPCG: guard must be nonnegative")
         self.tol, self.maxiter, self.preconditioner, self.eta = tol, maxiter, preconditioner, eta
         self.guard, self.seed = guard, seed
+
+
+class NotConverged(RuntimeError):
+    """A solve that ran out of maxiter; `res` is the last iterate's record (lam, X, resid, iters)."""
+
+    def __init__(self, msg, res):
+        super().__init__(msg)
+        self.res = res
 
 
 def lobpcg_solve(s, H, m, X0=None):
@@ -190,12 +314,14 @@ def lobpcg_solve(s, H, m, X0=None):
     pseed = H.product_seed(w) if s.seed == "product" else None
     D = H.full_diagonal()
     rng = _rng(0x5EED)
+    sep = SeparablePrecond(H, s.eta, H.gershgorin_bound()) if s.preconditioner == "separable" else None
+    Hm = _fast(H)
 
     def attempt(first, guards):
-        X = np.empty((N, w))
+        X = np.empty((N, w), order="F")
         X[:, :m] = first
         X[:, m:] = rng.standard_normal((N, g)) if guards is None else guards
-        return lobpcg_core(H, X, D, s.tol, s.maxiter, s.preconditioner, s.eta, n_conv_check=w)
+        return lobpcg_core(Hm, X, D, s.tol, s.maxiter, s.preconditioner, s.eta, n_conv_check=w, sep=sep)
 
     if X0 is not None:
         first = perturbed_seed(X0)
@@ -214,7 +340,7 @@ def lobpcg_solve(s, H, m, X0=None):
     resid = res["resid"]
     bad = int(np.sum(~(resid[:m] <= s.tol)))
     if bad:
-        raise RuntimeError(f"LOBPCG: {bad} of {m} eigenpairs did not converge within {s.maxiter} iterations")
+        raise NotConverged(f"LOBPCG: {bad} of {m} eigenpairs did not converge within {s.maxiter} iterations", res)
     return res["lam"][:m], res["X"][:, :m], res
 
 

@@ -1,0 +1,348 @@
+"""Parity of the GPU solvers at the measured configurations' own sizes, against the FP64 oracle.
+
+The reference pins its solvers at the boundary (test/test_solvers.jl:4-14, test/cuda/test_device.jl:
+62-131): eigenvalues equal an independent solve's, every true residual is below tol, the vectors
+are orthonormal.  Here, per configuration:
+
+  Lanczos              kf_solve(LANCZOS) against the oracle's Dense on the reference's own test
+                       operator (three real-coupled oscillators, d = 6), a fluxonium leaf and the
+                       two-transmon flat space (3,721 states)
+  Cholesky-QR          the Chebyshev filter with ortho = :cholqr (src/chebyshev.jl:119-131)
+  three-mode leaf      N = 671,744, m = 12: FP64 and mixed LOBPCG and the degree-20 Chebyshev
+                       filter (block 16) against eigenvalues fixed by the oracle's FP64 solve to
+                       1e-10 ||H|| (tests/golden/leaf3_eigs.json, cross-checked there by an
+                       independent SciPy LOBPCG from a random start)
+  dense parent 48^3    N = 110,592, m = 30, block 32, mixed and FP64, against ARPACK's eigenvalues
+                       (tests/golden/dense48_eigs.json)
+  batched sweep        leaves across the whole 200-1600 point range, and chains of 3 and 4 leaves
+  port operators       one-term operators of kept-basis and leaf ports, single and joint,
+                       against the oracle's explicit Kronecker products
+
+Eigenvalues within 1e-9 relative; residuals recomputed by the oracle's own operator.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import capply, circuits as ocirc, kfref, solvers as osol
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _fixture(name):
+    with open(os.path.join(GOLDEN, name)) as f:
+        return json.load(f)
+
+
+def _resid(Ho, E, V):
+    R = capply.CApply(Ho).matvec(np.asfortranarray(V)) - V * E[None, :]
+    return np.sqrt(np.sum(R ** 2, axis=0))
+
+
+def _oracle_op(dims, terms, constant=0.0):
+    """The oracle operator of a kfgpu term list (the same factor data, the oracle's own mul!)."""
+    from kfgpu import ops as P
+    conv = []
+    for c, fs in terms:
+        g = []
+        for a, op in fs:
+            if isinstance(op, P.DiagonalOp):
+                g.append((a, kfref.DiagonalOp(op.d)))
+            elif isinstance(op, P.ShiftOp):
+                g.append((a, kfref.ShiftOp(op.n, op.s, op.factor)))
+            elif isinstance(op, P.BandedOp):
+                g.append((a, kfref.BandedOp(op.n, op.offsets, op.weights)))
+            else:
+                g.append((a, kfref.DenseOp(op.dense())))
+        conv.append((c, g))
+    return kfref.KronFreeOperator(dims, conv, constant=constant)
+
+
+def _gpu_terms(terms):
+    """kfref (oracle) factor ops -> kfgpu ops of the same data."""
+    from kfgpu import ops as P
+    out = []
+    for c, fs in terms:
+        g = []
+        for a, op in fs:
+            if isinstance(op, kfref.DenseOp):
+                g.append((a, P.DenseOp(np.real(op.M))))
+            elif isinstance(op, kfref.DiagonalOp):
+                g.append((a, P.DiagonalOp(np.real(op.d))))
+            else:
+                raise TypeError(type(op).__name__)
+        out.append((c, g))
+    return out
+
+
+# ---------------------------------------------------------------------------------------------
+# Lanczos (src/solvers.jl:85-106)
+
+def test_lanczos_three_oscillators_matches_dense(cuda):
+    """The reference's own Lanczos test operator (test/cuda/test_device.jl:79-87): six pairs, 1e-8."""
+    from kfgpu import KronFreeOperator, Lanczos, solve
+    dims, terms = ocirc.real_three_oscillators(6)
+    Ho = kfref.KronFreeOperator(dims, terms)
+    Ed, _ = osol.dense_solve(Ho, 6)
+    H = KronFreeOperator(dims, _gpu_terms(terms), block_capacity=8)
+    E, V, st = solve(Lanczos(tol=1e-11), H, 6)
+    assert np.all(np.diff(E) >= 0)
+    assert np.max(np.abs(E - Ed)) < 1e-8 and np.max(np.abs(E - Ed) / np.abs(Ed)) < 1e-9
+    assert np.max(_resid(Ho, E, V)) <= 1e-8
+    assert np.linalg.norm(V.T @ V - np.eye(6)) < 1e-10
+    assert st["n_matvec"] > 0 and st["converged"] == 6
+
+
+@pytest.mark.parametrize("case", ["fluxonium", "two_transmons"])
+def test_lanczos_matches_dense(cuda, case):
+    from kfgpu import KronFreeOperator, Lanczos, circuits, solve
+    if case == "fluxonium":
+        th = circuits.fluxonium_theta(np.random.default_rng(31))
+        dims, terms = circuits.fluxonium_leaf(th, 400)
+        H = KronFreeOperator(dims, terms)
+        Ho = ocirc.fluxonium_operator(th, 400)
+        m = 8
+    else:
+        from kfgpu import warmstart as W
+        th = W.sample_thetas(1, seed=41)[0]
+        dims, terms, const = circuits.two_transmon_flat(th)
+        H = KronFreeOperator(dims, terms, constant=const)
+        Ho = _oracle_op(dims, terms, const)
+        m = 6
+    Ed, _ = osol.dense_solve(Ho, m)
+    tol = 1e-9 * H.gershgorin_bound()
+    E, V, st = solve(Lanczos(tol=tol), H, m)
+    assert np.max(np.abs(E - Ed) / np.maximum(1.0, np.abs(Ed))) < 1e-9, np.abs(E - Ed)
+    assert np.max(_resid(Ho, E, V)) <= tol
+    assert np.linalg.norm(V.T @ V - np.eye(m)) < 1e-10
+
+
+def test_lanczos_argument_errors(cuda):
+    from kfgpu import ArgumentError, KronFreeOperator, Lanczos, solve, ops as P
+    H = KronFreeOperator([10], [(1.0, [(0, P.DiagonalOp(np.arange(10.0)))])])
+    with pytest.raises(ArgumentError, match="Lanczos requires m >= 1"):
+        solve(Lanczos(), H, 0)
+    with pytest.raises(ArgumentError, match="exceeds the operator dimension"):
+        solve(Lanczos(), H, 11)
+
+
+# ---------------------------------------------------------------------------------------------
+# Chebyshev filter with Cholesky-QR (src/chebyshev.jl:119-131)
+
+@pytest.mark.parametrize("precision", ["f64", "mixed"])
+def test_chebyshev_cholqr_matches_dense(cuda, precision):
+    from kfgpu import ChebyshevFilter, KronFreeOperator, circuits, solve
+    th = ocirc.three_mode_theta(np.random.default_rng(12))
+    kw = dict(ncut=5, n2=24, n3=12)
+    dims, terms = circuits.three_mode_leaf(th, **kw)
+    Ho = ocirc.three_mode_operator(th, **kw)
+    Eref, _ = osol.dense_solve(Ho, 12)
+    H = KronFreeOperator(dims, terms)
+    tol = 1e-8 * H.gershgorin_bound()
+    E, V, st = solve(ChebyshevFilter(tol=tol, degree=20, extra=8, ortho="cholqr", precision=precision), H, 12)
+    assert np.max(np.abs(E - Eref) / np.maximum(1.0, np.abs(Eref))) < 1e-9
+    assert np.max(_resid(Ho, E, V)) <= tol * 1.0001
+    assert np.linalg.norm(V.T @ V - np.eye(12)) < 1e-10
+
+
+# ---------------------------------------------------------------------------------------------
+# the three-mode leaf at full size (N = 671,744)
+
+@pytest.fixture(scope="module")
+def leaf3():
+    return _fixture("leaf3_eigs.json")
+
+
+def _leaf3_case(leaf3, draw):
+    from kfgpu import KronFreeOperator, circuits
+    rec = leaf3["draws"][str(draw)]
+    th = rec["theta"]
+    # the fixture's theta is the benchmark's draw (numpy default_rng(20261205), in draw order)
+    rng = np.random.default_rng(leaf3["seed"])
+    for _ in range(draw + 1):
+        th_b = circuits.three_mode_theta(rng)
+    assert all(abs(th_b[k] - th[k]) < 1e-15 for k in th)
+    dims, terms = circuits.three_mode_leaf(th)
+    return KronFreeOperator(dims, terms), ocirc.three_mode_operator(th), np.array(rec["E"])
+
+
+@pytest.mark.parametrize("draw", [5, 6])
+def test_leaf3_lobpcg_full_size_vs_oracle(cuda, leaf3, draw):
+    """Draw 6 is the one where plain FP64 LOBPCG with per-Ritz Jacobi runs out of maxiter; both the
+    FP64 and the mixed solve (separable preconditioner) must reach the oracle's eigenvalues."""
+    from kfgpu import LOBPCG, solve
+    H, Ho, Eref = _leaf3_case(leaf3, draw)
+    tol = 1e-8 * H.gershgorin_bound()
+    for precision in ("f64", "mixed"):
+        E, V, st = solve(LOBPCG(tol=tol, precision=precision, preconditioner="separable"), H, 12)
+        assert np.max(np.abs(E - Eref) / np.abs(Eref)) < 1e-9, (precision, np.abs(E - Eref) / np.abs(Eref))
+        assert np.max(_resid(Ho, E, V)) <= tol
+        assert np.linalg.norm(V.T @ V - np.eye(12)) < 1e-9
+
+
+def test_leaf3_chebyshev_full_size_vs_oracle(cuda, leaf3):
+    """The degree-20 Chebyshev filter with block 16 (extra = 4) on the full leaf, mixed precision."""
+    from kfgpu import ChebyshevFilter, solve
+    H, Ho, Eref = _leaf3_case(leaf3, 5)
+    tol = 1e-8 * H.gershgorin_bound()
+    E, V, st = solve(ChebyshevFilter(tol=tol, degree=20, extra=4, maxiter=2000, precision="mixed"), H, 12)
+    assert np.max(np.abs(E - Eref) / np.abs(Eref)) < 1e-9, np.abs(E - Eref) / np.abs(Eref)
+    assert np.max(_resid(Ho, E, V)) <= tol * 1.0001
+
+
+def test_leaf3_fixture_cross_checked(leaf3):
+    """The fixture's draws were solved twice by unrelated iterations that agree."""
+    for d, x in leaf3["xcheck"].items():
+        assert x["max_rel_diff_vs_oracle_lobpcg"] < 1e-10, d
+
+
+# ---------------------------------------------------------------------------------------------
+# the dense parent (48^3 = 110,592)
+
+def test_dense48_lobpcg_vs_oracle(cuda):
+    from kfgpu import KronFreeOperator, LOBPCG, solve
+    fx = _fixture("dense48_eigs.json")
+    Ho = ocirc.dense_parent_operator(np.random.default_rng(fx["seed"]), d=48)
+    H = KronFreeOperator(Ho.dims, _gpu_terms(Ho.terms + [t for t in Ho.diagterms if t[1]]), block_capacity=32)
+    Eref = np.array(fx["E"])
+    tol = 1e-8 * H.gershgorin_bound()
+    for precision in ("f64", "mixed"):
+        E, V, st = solve(LOBPCG(tol=tol, precision=precision, guard=2), H, 30)
+        assert np.max(np.abs(E - Eref) / np.abs(Eref)) < 1e-9, (precision, np.abs(E - Eref))
+        assert np.max(_resid(Ho, E, V)) <= tol
+        assert np.linalg.norm(V.T @ V - np.eye(30)) < 1e-9
+
+
+# ---------------------------------------------------------------------------------------------
+# the batched sweep: the whole leaf size range, and chains of 3 and 4 leaves
+
+def _flux_leaves(sizes, seed):
+    from kfgpu import circuits
+    rng = np.random.default_rng(seed)
+    return [(circuits.fluxonium_theta(rng), n) for n in sizes]
+
+
+def test_batched_leaves_full_size_range(cuda):
+    from kfgpu import circuits
+    from kfgpu.batch import batch_solve
+    rng = np.random.default_rng(77)
+    sizes = [200, 1600, 201, 1599] + [int(x) for x in rng.integers(200, 1601, 20)]
+    leaves = _flux_leaves(sizes, 78)
+    ops = [(*circuits.fluxonium_leaf(th, n), 0.0) for th, n in leaves]
+    tol = 1e-9
+    Es, Vs, iters, resid = batch_solve(ops, [10] * len(ops), tol)
+    for (th, n), E, V in zip(leaves, Es, Vs):
+        Ho = ocirc.fluxonium_operator(th, n)
+        Eref, _ = osol.dense_solve(Ho, 10)
+        assert np.max(np.abs(E - Eref) / np.maximum(np.abs(Eref), 1.0)) < 1e-9, n
+        thr = max(tol, 10 * np.finfo(float).eps * Ho.gershgorin_bound())
+        assert np.max(_resid(Ho, E, V)) <= thr * 1.0001, n
+        assert np.linalg.norm(V.T @ V - np.eye(10)) < 1e-9
+
+
+@pytest.mark.parametrize("nleaf", [3, 4])
+def test_batched_chain_parents(cuda, nleaf):
+    """A chain of nleaf fluxonium leaves coupled by g n_i n_{i+1}: batched leaves, then the parent
+    (10^nleaf states, keep 20) by mixed LOBPCG, against ARPACK on the oracle's parent operator."""
+    import scipy.sparse.linalg as sla
+    from kfgpu import KronFreeOperator, LOBPCG, circuits, solve, ops as P
+    from kfgpu.batch import batch_solve
+    from kfgpu.ops import PhaseGrid, localop
+    rng = np.random.default_rng(90 + nleaf)
+    leaves = _flux_leaves([int(x) for x in rng.integers(200, 1601, nleaf)], 91 + nleaf)
+    gs = rng.uniform(0.01, 0.1, nleaf - 1)
+    ops = [(*circuits.fluxonium_leaf(th, n), 0.0) for th, n in leaves]
+    Es, Vs, _, _ = batch_solve(ops, [10] * nleaf, 1e-9)
+    ports = []
+    for (th, n), V in zip(leaves, Vs):
+        A = localop(PhaseGrid(-5 * np.pi, 5 * np.pi, n, 4), "n", part="im").dense()   # n = i A
+        ports.append(V.T @ A @ V)
+    terms = [(1.0, [(a, P.DiagonalOp(Es[a]))]) for a in range(nleaf)]
+    for a in range(nleaf - 1):
+        terms.append((-gs[a], [(a, P.DenseOp(ports[a])), (a + 1, P.DenseOp(ports[a + 1]))]))
+    H = KronFreeOperator([10] * nleaf, terms, block_capacity=24)
+    tol = 1e-9
+    E, V, _ = solve(LOBPCG(tol=tol, precision="mixed"), H, 20)
+    oterms = [(1.0, [(a, kfref.DiagonalOp(Es[a]))]) for a in range(nleaf)]
+    for a in range(nleaf - 1):
+        oterms.append((-gs[a], [(a, kfref.DenseOp(ports[a])), (a + 1, kfref.DenseOp(ports[a + 1]))]))
+    Ho = kfref.KronFreeOperator([10] * nleaf, oterms)
+    if Ho.N <= 1000:
+        Eref = np.linalg.eigvalsh(Ho.to_matrix())[:20]
+    else:
+        A = sla.LinearOperator((Ho.N, Ho.N), matvec=lambda x: Ho.matvec(x), dtype=np.float64)
+        Eref = np.sort(sla.eigsh(A, k=20, which="SA", tol=1e-14, ncv=80,
+                                 v0=np.random.default_rng(5).standard_normal(Ho.N))[0])
+    assert np.max(np.abs(E - Eref) / np.maximum(np.abs(Eref), 1.0)) < 1e-9
+    assert np.max(_resid(Ho, E, V)) <= tol
+
+
+# ---------------------------------------------------------------------------------------------
+# port operators (src/portoperator.jl:18-39)
+
+def test_port_operators_match_explicit_products(cuda):
+    from kfgpu import ArgumentError, ops as P
+    from kfgpu.ports import port_operator
+    from kfgpu import warmstart as W
+    th = W.sample_thetas(1, seed=3)[0]
+    # kept-basis ports of the two-transmon leaves: n in each leaf's lowest 8 states
+    n = np.arange(-30.0, 31.0)
+    ports = []
+    for EJ, EC, ng in ((th["E_J1"], th["E_C1"], th["n_g1"]), (th["E_J2"], th["E_C2"], th["n_g2"])):
+        Hl = kfref.KronFreeOperator([61], [(4 * EC, [(0, kfref.DiagonalOp((n - ng) ** 2))]),
+                                           (-EJ / 2, [(0, kfref.ShiftOp(61, 1, 1.0))]),
+                                           (-EJ / 2, [(0, kfref.ShiftOp(61, -1, 1.0))])])
+        w, V = np.linalg.eigh(Hl.to_matrix())
+        ports.append(V[:, :8].T @ (n[:, None] * V[:, :8]))
+    rng = np.random.default_rng(0)
+    cases = [
+        ([8, 8], [(0, P.DenseOp(ports[0]))], np.kron(np.eye(8), ports[0]), True),
+        ([8, 8], [(1, P.DenseOp(ports[1])), (0, P.DenseOp(ports[0]))], np.kron(ports[1], ports[0]), True),
+        ([61, 61], [(1, P.DiagonalOp(n))], np.kron(np.diag(n), np.eye(61)), True),
+        ([61, 61], [(0, P.ShiftOp(61, 1))], np.kron(np.eye(61), P.ShiftOp(61, 1).dense()), False),
+        ([61, 8], [(0, P.ShiftOp(61, -1)), (1, P.DenseOp(ports[1]))],
+         np.kron(ports[1], P.ShiftOp(61, -1).dense()), False),
+    ]
+    for dims, key, M, herm in cases:
+        H = port_operator(dims, key, block_capacity=4)
+        assert H.hermitian == herm
+        X = rng.standard_normal((H.N, 4))
+        Y = H.apply(X)
+        assert np.max(np.abs(Y - M @ X)) < 1e-12 * max(1.0, np.max(np.abs(M @ X)))
+        Y32 = H.apply(X.astype(np.float32), f32=True)
+        assert np.max(np.abs(Y32 - M @ X)) < 2e-6 * max(1.0, np.max(np.abs(M @ X)))
+    with pytest.raises(ArgumentError, match="distinct modes"):
+        port_operator([8, 8], [(0, P.DenseOp(ports[0])), (0, P.DenseOp(ports[0]))])
+
+
+# ---------------------------------------------------------------------------------------------
+# the learned warm start against the oracle's Dense (two transmons, 3,721 states)
+
+def test_warm_start_eigenvalues_vs_oracle_dense(cuda):
+    """A network trained on a few hundred labelled theta proposes the block; the warm-started solve,
+    the product-seed solve and the random-start solve all reach the oracle's Dense eigenvalues
+    (1e-9 relative), with residuals recomputed by the oracle's operator."""
+    from kfgpu import LOBPCG, circuits, solve
+    from kfgpu import warmstart as W
+    train = W.sample_thetas(256, seed=21)
+    Vs, _ = W.label(train)
+    POD = W.pod_basis(Vs, k=128)
+    ws = W.WarmStart(POD, 12, hidden=256, seed=1)
+    ws.fit(train, W.targets(Vs, POD), epochs=150, batch=128, lr=1e-3)
+    test = W.sample_thetas(3, seed=22)
+    rows = W.evaluate(ws, test, product_arm=True)
+    for th, r in zip(test, rows):
+        dims, terms, const = circuits.two_transmon_flat(th)
+        Ho = _oracle_op(dims, terms, const)
+        Ed, _ = osol.dense_solve(Ho, 12)
+        for key in ("E", "E_warm", "E_product"):
+            assert np.max(np.abs(r[key] - Ed) / np.maximum(1.0, np.abs(Ed))) < 1e-9, key
+        H = W.operator(th)
+        E, V, _ = solve(LOBPCG(tol=W.tolerance(H), preconditioner="separable", seed="product"), H, 12,
+                        X0=ws.blocks([th])[0])
+        assert np.max(_resid(Ho, E, V)) <= W.tolerance(H)
+        H.close()
