@@ -117,6 +117,18 @@ int kf_test_apply_variant(kf_op *op, int variant, const void *X, void *Y, int64_
  */
 int kf_test_op_scratch_bytes(const struct kf_op *op, uint64_t *bytes);
 
+/*
+ * Whether the plane-marching fused apply (forced-variant 5) applies to this operator for a block of
+ * b columns (FP32 when f32 != 0, else FP64) on a device with `sms` multiprocessors (0: ask the
+ * op's device); *eligible 1 or 0.  geom (may be NULL) receives 16 values: plane size P,
+ * march-axis length, outer count, halo H, in-plane reach R, tile TQ, tiles per plane, persistent
+ * CTAs, ring slots, slot X and diagonal lengths, shared entries, their register class (6, 8 or 16),
+ * points per thread, 1 when every shared entry reads the current plane, the dynamic shared memory
+ * bytes.  Returns a KF_* status.
+ */
+int kf_test_march_plan(const struct kf_op *op, int64_t b, int32_t f32, int32_t sms, int32_t *eligible,
+                       int32_t *geom);
+
 #ifdef __cplusplus
 }
 #endif

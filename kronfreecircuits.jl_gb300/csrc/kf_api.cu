@@ -399,6 +399,23 @@ int kf_test_op_scratch_bytes(const kf_op *op, uint64_t *bytes) {
     });
 }
 
+int kf_test_march_plan(const kf_op *op, int64_t b, int32_t f32, int32_t sms, int32_t *eligible, int32_t *geom) {
+    return guarded([&] {
+        KF_REQUIRE(op && eligible && b >= 1 && sms >= 0, KF_EINVAL, "kf_test_march_plan: bad argument");
+        if (sms == 0) KF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, op->device));
+        kf::MarchPlan mp;
+        const size_t es = f32 ? 4 : 8;
+        const bool ok = kf::march_plan(op, b, es, sms, mp);
+        *eligible = ok ? 1 : 0;
+        if (geom && ok) {
+            const int32_t g[16] = {mp.P, mp.nm, mp.nouter, mp.H, mp.R, mp.TQ, mp.ntile, mp.grid, mp.NR, mp.SLX,
+                                   mp.SLD, mp.nsm, mp.ms, mp.pt, mp.flat,
+                                   (int32_t)kf::march_smem_bytes(mp, es, 2 * mp.H + 1, mp.ms)};
+            for (int i = 0; i < 16; ++i) geom[i] = g[i];
+        }
+    });
+}
+
 int kf_test_chol2(const double *G, int wx, int r, double *C_out, int *status_out) {
     return guarded([&] {
         KF_REQUIRE(G && C_out && status_out && wx >= 0 && r >= 1 && r <= kf::CHOL2_MAX_R, KF_EINVAL,

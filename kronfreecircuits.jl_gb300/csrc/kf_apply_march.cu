@@ -1,0 +1,603 @@
+// The fused stencil apply, marching along the slowest stencil axis with a register window.
+//
+// Y = D X + sum_e w_e(p) X[p + delta_e] for the entry table of k_apply_fused (the diagonal, banded
+// and shift terms of src/apply.jl:370-432 fused into one pass), organised around the slowest axis m
+// that carries an offset: the state index splits as
+//     p = q + P (k + n_m o),   q in [0, P) (the axes before m), k in [0, n_m), o (the axes after m),
+// every entry's offset as delta_e = r_e + P o_e (|r_e| <= R, |o_e| <= H), and every entry's weight as
+// w_e(p) = w_in(q) w_plane(k) w_out(o).  The entries fall into three classes:
+//   window   r_e = 0 and no factor on the axes before m: X[q, k + o_e] comes from a per-thread
+//            register window of 2H + 1 planes, the weights summed per (plane, o) in a table;
+//   centre   r_e = 0, o_e = 0, factors on the axes before m only: one per-thread weight on X[q, k];
+//   shared   everything else: X[q + r_e, k + o_e] read from the shared-memory copy of plane k + o_e.
+// So every X element is read from global memory once per tile (plus the in-plane halo, from L2),
+// the slow axis' neighbours never leave registers, and only in-plane neighbours cost a
+// shared-memory load.
+//
+// Work split.  The kernel is persistent: one CTA per SM.  A CTA owns one tile of TQ consecutive q
+// (of one outer index) for its lifetime -- its per-point weights and the per-plane weight tables
+// are formed once -- and marches a contiguous range of the tile's (column, plane) pairs, split
+// evenly among the CTAs of the tile, column by column (each column's run with its plane halo).
+//
+// Pipeline.  A producer warp copies, for every plane the CTA touches, the column's slice
+// X[q0 - R .. q0 + TQ + R) and the diagonal's slice D[q0 .. q0 + TQ) into the next slot of a ring
+// in shared memory with cp.async.bulk (1-D bulk copies, completion counted in bytes on the slot's
+// "full" mbarrier).  The 12 consumer warps wait on "full" for the plane entering their window and,
+// when a plane leaves it (or a column's run ends), arrive on that slot's "empty" mbarrier, which the
+// producer waits on before reusing the slot.  No CTA-wide barrier inside the march.
+//
+// Every wait is bounded (a clock64 budget of about two seconds): a role whose wait ran out records
+// KF_ETIMEOUT in the host-mapped error word and raises the CTA's abort flag, which every other wait
+// loop checks; the producer then waits (bounded) for its copies still in flight before the CTA exits.
+#include <algorithm>
+#include <cstring>
+
+#include "kf_internal.h"
+
+namespace kf {
+
+namespace {
+
+constexpr int MCW = 12;                     // consumer warps
+constexpr int MCT = MCW * 32;               // consumer threads
+constexpr int MTHREADS = MCT + 32;          // + one producer warp
+constexpr long long M_WAIT_CYCLES = 4000000000LL;
+constexpr int M_SMEM_BUDGET = 200 * 1024;   // one CTA per SM
+
+__device__ __forceinline__ uint32_t msu32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void m_bar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(msu32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void m_expect(uint64_t *bar, uint32_t bytes) {
+    asm volatile(
+        "{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}\n" ::"r"(msu32(bar)),
+        "r"(bytes)
+        : "memory");
+}
+
+__device__ __forceinline__ void m_arrive(uint64_t *bar) {
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}\n" ::"r"(msu32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void m_bulk(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(msu32(dst)),
+        "l"(src), "r"(bytes), "r"(msu32(bar))
+        : "memory");
+}
+
+// wait for the phase with the given parity to complete; false when the budget ran out or another
+// role aborted
+__device__ __forceinline__ bool m_wait(uint64_t *bar, uint32_t parity, volatile int *abort_flag) {
+    const long long t0 = clock64();
+    for (;;) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.b32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(done)
+            : "r"(msu32(bar)), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (*abort_flag) return false;
+        if (clock64() - t0 > M_WAIT_CYCLES) return false;
+    }
+}
+
+__device__ __forceinline__ int64_t floor_to(int64_t x, int g) { return x >= 0 ? x / g * g : -((-x + g - 1) / g * g); }
+__device__ __forceinline__ int64_t ceil_to(int64_t x, int g) { return (x + g - 1) / g * g; }
+
+// one factor's weight at coordinate i (0 where the neighbour i + o leaves the axis)
+template <typename T>
+__device__ __forceinline__ T fac_w(const T *W, int w, int nb, int n, int o, int i) {
+    return ((unsigned)(i + o) < (unsigned)n) ? __ldg(W + w + i * nb) : T(0);
+}
+
+// the part of entry E's weight from the factors on the axes of class `sel` (0: before m, 1: m,
+// 2: after m); idx[a] is the coordinate on axis a
+template <typename T>
+__device__ __forceinline__ T entry_part(const Entry &E, const T *W, int m, const int *idx, int sel) {
+    T w = T(1);
+    {
+        const int s = E.a0 < m ? 0 : (E.a0 == m ? 1 : 2);
+        if (s == sel) w *= fac_w(W, E.w0, E.nb0, E.n0, E.o0, idx[E.a0]);
+    }
+    if (E.nf == 2) {
+        const int s = E.a1 < m ? 0 : (E.a1 == m ? 1 : 2);
+        if (s == sel) w *= fac_w(W, E.w1, E.nb1, E.n1, E.o1, idx[E.a1]);
+    }
+    return w;
+}
+
+// this CTA's tile group and its range [f0, f1) of (column, plane) pairs f = col * n_m + k
+struct Work {
+    int tile, outer;
+    int64_t f0, f1;
+};
+__device__ __forceinline__ Work cta_work(const MarchPlan &mp, int b) {
+    const int G = mp.ntile * mp.nouter;
+    const int g = blockIdx.x % G, r = blockIdx.x / G;
+    const int ng = ((int)gridDim.x - g + G - 1) / G;       // CTAs of this group
+    const int64_t tot = (int64_t)b * mp.nm;
+    Work w;
+    w.tile = g % mp.ntile;
+    w.outer = g / mp.ntile;
+    w.f0 = tot * r / ng;
+    w.f1 = tot * (r + 1) / ng;
+    return w;
+}
+
+// the end of the column run that starts at f: the column's last plane or the range's end
+__device__ __forceinline__ int run_end(int64_t f, int k0, int64_t f1, int nm) {
+    const int64_t e = k0 + (f1 - f);
+    return e < (int64_t)nm ? (int)e : nm;
+}
+
+template <typename T, int H, int MS, int PT>
+__global__ void __launch_bounds__(MTHREADS, 1)
+    k_apply_march(const ApplyPlan plan, const MarchPlan mp, const T *__restrict__ D, const T *__restrict__ W,
+                  const T *__restrict__ X, T *__restrict__ Y, int64_t ldx, int64_t ldy, int b, T alpha, T beta,
+                  const T *__restrict__ Z, int64_t ldz, T gamma, int epi, int *err) {
+    constexpr int G = 16 / (int)sizeof(T);
+    constexpr int WN = 2 * H + 1;
+    extern __shared__ __align__(128) unsigned char m_smem[];
+    const int SL = mp.SLX + mp.SLD;
+    const int NR = mp.NR;
+    T *ring = reinterpret_cast<T *>(m_smem);                      // [NR][SLX + SLD]
+    T *wm = ring + (size_t)NR * SL;                              // [nm][WN] window weights per plane
+    T *wp = wm + (size_t)mp.nm * WN;                             // [nm][MS] plane weights of the shared entries
+    uint64_t *full = reinterpret_cast<uint64_t *>(
+        ((uintptr_t)(wp + (size_t)mp.nm * MS + 2) + 7) & ~(uintptr_t)7);
+    uint64_t *empty = full + NR;
+    __shared__ int s_abort;
+
+    const int tid = threadIdx.x;
+    const int warp = tid >> 5, lane = tid & 31;
+    const Work wk = cta_work(mp, b);
+    const int q0 = wk.tile * mp.TQ, qn = min(mp.TQ, mp.P - q0);
+    const int64_t obase = (int64_t)wk.outer * mp.P * mp.nm;
+    // the plane size is a multiple of 16 bytes, so every plane's slice has the same alignment shift
+    const int misx = (int)((obase + q0 - mp.R) - floor_to(obase + q0 - mp.R, G));
+    const int misd = (int)((obase + q0) - floor_to(obase + q0, G));
+
+    // coordinates of the outer index (axes after m)
+    int idx_out[MAXDIMS_F];
+    {
+        int rem = wk.outer;
+#pragma unroll
+        for (int a = 0; a < MAXDIMS_F; ++a) {
+            idx_out[a] = 0;
+            if (a > mp.m && a < plan.ndims) {
+                idx_out[a] = rem % plan.dims[a];
+                rem /= plan.dims[a];
+            }
+        }
+    }
+
+    // the ring starts zeroed: a slice clamped at the ends of the column leaves its halo unwritten,
+    // and zero weights must meet finite values there
+    for (int e = tid; e < NR * SL; e += MTHREADS) ring[e] = T(0);
+    if (tid == 0) {
+        s_abort = 0;
+        for (int s = 0; s < NR; ++s) {
+            m_bar_init(full + s, 1);
+            m_bar_init(empty + s, MCW);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    // per-plane tables for every plane: the window weights (summed per plane offset) and the plane
+    // weights of the shared entries (1 without a factor on axis m, 0 for the padding entries); the
+    // outer weights folded in
+    for (int t = tid; t < mp.nm * (WN + MS); t += MTHREADS) {
+        int idx[MAXDIMS_F];
+#pragma unroll
+        for (int a = 0; a < MAXDIMS_F; ++a) idx[a] = idx_out[a];
+        T v = T(0);
+        if (t < mp.nm * WN) {
+            const int o = t % WN - H;
+            idx[mp.m] = t / WN;
+            for (int q = 0; q < mp.nwin; ++q) {
+                if (mp.wino[q] != o) continue;
+                const Entry &E = plan.e[mp.win[q]];
+                v += entry_part<T>(E, W, mp.m, idx, 1) * entry_part<T>(E, W, mp.m, idx, 2);
+            }
+            wm[t] = v;
+        } else {
+            const int t2 = t - mp.nm * WN, e = t2 % MS;
+            idx[mp.m] = t2 / MS;
+            if (e < mp.nsm1) v = T(1);
+            else if (e < mp.nsm) v = entry_part<T>(plan.e[mp.sm[e]], W, mp.m, idx, 1);
+            wp[t2] = v;
+        }
+    }
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    __syncthreads();
+
+    if (warp == MCW) {
+        // ---- producer: one lane issues every plane's two bulk copies, in load order
+        if (lane == 0) {
+            int s = 0, use = 0, issued = 0;   // load t goes to slot t % NR, as use t / NR
+            bool ok = true;
+            for (int64_t f = wk.f0; f < wk.f1 && ok;) {
+                const int col = (int)(f / mp.nm), k0 = (int)(f % mp.nm);
+                const int k1 = run_end(f, k0, wk.f1, mp.nm);
+                f += k1 - k0;
+                const T *Xc = X + (int64_t)col * ldx;
+                const int jfirst = max(0, k0 - H), jlast = min(mp.nm - 1, k1 - 1 + H);
+                for (int j = jfirst; j <= jlast; ++j) {
+                    if (use > 0 && !m_wait(empty + s, (uint32_t)((use - 1) & 1), &s_abort)) {
+                        ok = false;
+                        break;
+                    }
+                    T *slot = ring + (size_t)s * SL;
+                    const int64_t xs = obase + (int64_t)j * mp.P + q0 - mp.R, xb = xs - misx;
+                    int64_t xlo = xb, xhi = ceil_to(xs + qn + 2 * mp.R, G);
+                    if (xlo < 0) xlo = 0;
+                    if (xhi > mp.N) xhi = mp.N;
+                    const int64_t ds = obase + (int64_t)j * mp.P + q0, db = ds - misd;
+                    int64_t dhi = ceil_to(ds + qn, G);
+                    if (dhi > mp.N) dhi = mp.N;
+                    const uint32_t bx = xhi > xlo ? (uint32_t)((xhi - xlo) * (int64_t)sizeof(T)) : 0u;
+                    const uint32_t bd = dhi > db ? (uint32_t)((dhi - db) * (int64_t)sizeof(T)) : 0u;
+                    m_expect(full + s, bx + bd);
+                    if (bx) m_bulk(slot + (xlo - xb), Xc + xlo, bx, full + s);
+                    if (bd) m_bulk(slot + mp.SLX, D + db, bd, full + s);
+                    ++issued;
+                    if (++s == NR) { s = 0; ++use; }
+                }
+            }
+            if (!ok) {
+                s_abort = 1;
+                *(volatile int *)err = KF_ETIMEOUT;
+                __threadfence_system();
+                // copies still in flight write this CTA's shared memory: wait (bounded) for the
+                // latest use of every slot before leaving
+                volatile int never = 0;
+                for (int t = max(0, issued - NR); t < issued; ++t)
+                    (void)m_wait(full + t % NR, (uint32_t)((t / NR) & 1), &never);
+            }
+        }
+    } else {
+        // ---- consumers: thread tid owns points q0 + tid + MCT j, j < PT
+        bool valid[PT];
+        T wcen[PT];                   // centre weights (factors before m, times the outer ones)
+        T wsm[PT][MS];                // weights of the shared entries on the axes before m and after m
+#pragma unroll
+        for (int j = 0; j < PT; ++j) {
+            const int qi = tid + j * MCT;
+            valid[j] = qi < qn;
+            int idx[MAXDIMS_F];
+            int rem = valid[j] ? q0 + qi : q0;
+#pragma unroll
+            for (int a = 0; a < MAXDIMS_F; ++a) {
+                idx[a] = idx_out[a];
+                if (a < mp.m) {
+                    idx[a] = rem % plan.dims[a];
+                    rem /= plan.dims[a];
+                }
+            }
+            T c = T(0);
+            for (int q = 0; q < mp.ncen; ++q) {
+                const Entry &E = plan.e[mp.cen[q]];
+                c += entry_part<T>(E, W, mp.m, idx, 0) * entry_part<T>(E, W, mp.m, idx, 2);
+            }
+            wcen[j] = c;
+#pragma unroll
+            for (int e = 0; e < MS; ++e) {
+                T w = T(0);
+                if (e < mp.nsm) {
+                    const Entry &E = plan.e[mp.sm[e]];
+                    w = entry_part<T>(E, W, mp.m, idx, 0) * entry_part<T>(E, W, mp.m, idx, 2);
+                }
+                wsm[j][e] = w;
+            }
+        }
+        auto wrap = [&](int s) { return s >= NR ? s - NR : (s < 0 ? s + NR : s); };
+        // offset, within a slot, of this thread's first point in the X slice
+        const int xoff0 = mp.R + misx + tid;
+        const bool plain_sm = mp.nsm1 == mp.nsm;
+        int64_t t0 = 0;               // load index of the current run's first plane
+        bool ok = true;
+        for (int64_t f = wk.f0; f < wk.f1 && ok;) {
+            const int col = (int)(f / mp.nm), k0 = (int)(f % mp.nm);
+            const int k1 = run_end(f, k0, wk.f1, mp.nm);
+            f += k1 - k0;
+            const int jfirst = max(0, k0 - H), jlast = min(mp.nm - 1, k1 - 1 + H);
+            T xw[PT][WN];
+#pragma unroll
+            for (int j = 0; j < PT; ++j)
+#pragma unroll
+                for (int o = 0; o < WN; ++o) xw[j][o] = T(0);
+            // the window's first 2H planes
+#pragma unroll
+            for (int o = 0; o < 2 * H; ++o) {
+                const int jj = k0 - H + o;
+                if (!ok || jj < 0 || jj >= mp.nm) continue;
+                const int64_t t = t0 + (jj - jfirst);
+                if (!m_wait(full + (int)(t % NR), (uint32_t)((t / NR) & 1), &s_abort)) {
+                    ok = false;
+                    continue;
+                }
+                const T *sx = ring + (int)(t % NR) * SL + xoff0;
+#pragma unroll
+                for (int j = 0; j < PT; ++j) xw[j][o] = sx[j * MCT];
+            }
+            const int64_t tk0 = t0 + (k0 - jfirst);
+            int sk = (int)(tk0 % NR);                    // slot of plane k
+            int sn = (int)((tk0 + H) % NR);              // slot of plane k + H
+            int usen = (int)((tk0 + H) / NR);            // and its use index
+            T *ycol = Y + (int64_t)col * ldy + obase + q0 + tid;
+            const T *zcol = Z != nullptr ? Z + (int64_t)col * ldz + obase + q0 + tid : nullptr;
+            for (int k = k0; k < k1 && ok; ++k) {
+                if (k + H <= jlast) {
+                    if (!m_wait(full + sn, (uint32_t)(usen & 1), &s_abort)) {
+                        ok = false;
+                        break;
+                    }
+                    const T *sx = ring + sn * SL + xoff0;
+#pragma unroll
+                    for (int j = 0; j < PT; ++j) xw[j][2 * H] = sx[j * MCT];
+                } else {
+#pragma unroll
+                    for (int j = 0; j < PT; ++j) xw[j][2 * H] = T(0);
+                }
+                T wmk[WN];
+#pragma unroll
+                for (int o = 0; o < WN; ++o) wmk[o] = wm[k * WN + o];
+                // one ring offset per shared entry (its plane's slot, its in-plane offset); the
+                // entries past nsm carry weight 0 and offset 0
+                int pe[MS];
+                const int base = sk * SL + xoff0;
+                if (mp.flat) {
+#pragma unroll
+                    for (int e = 0; e < MS; ++e) pe[e] = base + mp.smr[e];
+                } else {
+#pragma unroll
+                    for (int e = 0; e < MS; ++e) pe[e] = wrap(sk + mp.smo[e]) * SL + xoff0 + mp.smr[e];
+                }
+                const int sdi = base - xoff0 + mp.SLX + misd + tid;
+                T *yk = ycol + (int64_t)k * mp.P;
+                if (plain_sm) {
+#pragma unroll
+                    for (int j = 0; j < PT; ++j) {
+                        const T xc = xw[j][H];
+                        T a0 = ring[sdi + j * MCT] * xc;
+                        a0 = fma(wcen[j], xc, a0);
+                        T a1 = wmk[0] * xw[j][0];
+#pragma unroll
+                        for (int o = 1; o < WN; ++o) a1 = fma(wmk[o], xw[j][o], a1);
+#pragma unroll
+                        for (int e = 0; e < MS; e += 2) {
+                            a0 = fma(wsm[j][e], ring[pe[e] + j * MCT], a0);
+                            if (e + 1 < MS) a1 = fma(wsm[j][e + 1], ring[pe[e + 1] + j * MCT], a1);
+                        }
+                        const T acc = a0 + a1;
+                        if (valid[j]) {
+                            T r = acc;
+                            if (epi) {
+                                r = alpha * acc + beta * xc;
+                                if (zcol != nullptr) r += gamma * zcol[(int64_t)k * mp.P + j * MCT];
+                            }
+                            yk[j * MCT] = r;
+                        }
+                    }
+                } else {
+                    T wpk[MS];
+#pragma unroll
+                    for (int e = 0; e < MS; ++e) wpk[e] = wp[k * MS + e];
+#pragma unroll
+                    for (int j = 0; j < PT; ++j) {
+                        const T xc = xw[j][H];
+                        T a0 = ring[sdi + j * MCT] * xc;
+                        a0 = fma(wcen[j], xc, a0);
+                        T a1 = wmk[0] * xw[j][0];
+#pragma unroll
+                        for (int o = 1; o < WN; ++o) a1 = fma(wmk[o], xw[j][o], a1);
+#pragma unroll
+                        for (int e = 0; e < MS; e += 2) {
+                            a0 = fma(wsm[j][e] * wpk[e], ring[pe[e] + j * MCT], a0);
+                            if (e + 1 < MS) a1 = fma(wsm[j][e + 1] * wpk[e + 1], ring[pe[e + 1] + j * MCT], a1);
+                        }
+                        const T acc = a0 + a1;
+                        if (valid[j]) {
+                            T r = acc;
+                            if (epi) {
+                                r = alpha * acc + beta * xc;
+                                if (zcol != nullptr) r += gamma * zcol[(int64_t)k * mp.P + j * MCT];
+                            }
+                            yk[j * MCT] = r;
+                        }
+                    }
+                }
+                // plane k - H leaves the window: release its slot
+                __syncwarp();
+                if (k - H >= jfirst && lane == 0) m_arrive(empty + wrap(sk - H));
+#pragma unroll
+                for (int j = 0; j < PT; ++j)
+#pragma unroll
+                    for (int o = 0; o < 2 * H; ++o) xw[j][o] = xw[j][o + 1];
+                if (++sk == NR) sk = 0;
+                if (++sn == NR) { sn = 0; ++usen; }
+            }
+            // the run ends: release its planes still in the window
+            if (ok) {
+                __syncwarp();
+                if (lane == 0)
+                    for (int jj = max(jfirst, k1 - H); jj <= jlast; ++jj)
+                        m_arrive(empty + (int)((t0 + (jj - jfirst)) % NR));
+            }
+            t0 += jlast - jfirst + 1;
+        }
+        if (!ok && lane == 0) {
+            s_abort = 1;
+            *(volatile int *)err = KF_ETIMEOUT;
+            __threadfence_system();
+        }
+    }
+    __syncthreads();
+}
+
+template <typename T, int H, int MS, int PT>
+void launch_k(const kf_op *op, const MarchPlan &mp, const T *D, const T *W, const T *X, T *Y, int64_t ldx,
+              int64_t ldy, int64_t b, T alpha, T beta, const T *Z, int64_t ldz, T gamma, int epi, cudaStream_t s) {
+    const size_t smem = march_smem_bytes(mp, sizeof(T), 2 * H + 1, MS);
+    static bool attr = false;   // per instantiation
+    if (!attr) {
+        KF_CUDA(cudaFuncSetAttribute(k_apply_march<T, H, MS, PT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     M_SMEM_BUDGET + 16384));
+        attr = true;
+    }
+    KF_REQUIRE(smem <= (size_t)M_SMEM_BUDGET + 16384, KF_EINVAL, "apply: plane ring too large");
+    k_apply_march<T, H, MS, PT><<<mp.grid, MTHREADS, smem, s>>>(op->plan, mp, D, W, X, Y, ldx, ldy, (int)b, alpha,
+                                                                beta, Z, ldz, gamma, epi, tc_error_word());
+    KF_LAUNCH_CHECK();
+}
+
+template <typename T, int H>
+void launch_h(const kf_op *op, const MarchPlan &mp, const T *D, const T *W, const T *X, T *Y, int64_t ldx,
+              int64_t ldy, int64_t b, T alpha, T beta, const T *Z, int64_t ldz, T gamma, int epi, cudaStream_t s) {
+    // points per thread: what fits 128 registers without spilling (13 warps on one SM)
+    constexpr int P8 = sizeof(T) == 4 ? 4 : 2, P16 = sizeof(T) == 4 ? 2 : 1;
+    if (mp.ms == 6)
+        launch_k<T, H, 6, P8>(op, mp, D, W, X, Y, ldx, ldy, b, alpha, beta, Z, ldz, gamma, epi, s);
+    else if (mp.ms == 8)
+        launch_k<T, H, 8, P8>(op, mp, D, W, X, Y, ldx, ldy, b, alpha, beta, Z, ldz, gamma, epi, s);
+    else
+        launch_k<T, H, 16, P16>(op, mp, D, W, X, Y, ldx, ldy, b, alpha, beta, Z, ldz, gamma, epi, s);
+}
+
+}  // namespace
+
+size_t march_smem_bytes(const MarchPlan &mp, size_t elem, int wn, int ms) {
+    size_t b = (size_t)mp.NR * (mp.SLX + mp.SLD) * elem + (size_t)mp.nm * (wn + ms) * elem + 2 * elem;
+    b = (b + 7) / 8 * 8 + 8;
+    return b + (size_t)2 * mp.NR * 8;
+}
+
+// The march plan of this operator for a block of b columns of element size `elem`, or false when
+// the kernel does not apply (no axis with an offset beyond the first, a plane or column length that
+// is not a multiple of 16 bytes, too wide a halo or too many shared entries).
+bool march_plan(const kf_op *op, int64_t b, size_t elem, int num_sms, MarchPlan &mp) {
+    const ApplyPlan &P = op->plan;
+    if (P.ne < 1 || P.ndims > MAXDIMS_F || b < 1) return false;
+    std::memset(&mp, 0, sizeof(mp));
+    int m = -1;
+    for (int e = 0; e < P.ne; ++e) {
+        const Entry &E = P.e[e];
+        if (E.o0 != 0) m = std::max(m, E.a0);
+        if (E.nf == 2 && E.o1 != 0) m = std::max(m, E.a1);
+    }
+    if (m < 1) return false;
+    int64_t st = 1;
+    for (int a = 0; a < m; ++a) st *= P.dims[a];
+    mp.m = m;
+    mp.P = (int)st;
+    mp.nm = P.dims[m];
+    mp.N = P.N;
+    mp.nouter = (int)(P.N / ((int64_t)mp.P * mp.nm));
+    if (mp.P < 128 || mp.nm < 4) return false;
+    const int G = 16 / (int)elem;
+    if (P.N % G != 0 || mp.P % G != 0) return false;
+    mp.H = 0;
+    mp.R = 0;
+    for (int e = 0; e < P.ne; ++e) {
+        const Entry &E = P.e[e];
+        int o = 0;
+        bool fin = false, fpl = false;
+        auto cls = [&](int a, int off) {
+            if (a == m) { o = off; fpl = true; }
+            else if (a < m) fin = true;
+        };
+        cls(E.a0, E.o0);
+        if (E.nf == 2) cls(E.a1, E.o1);
+        const int r = E.delta - o * mp.P;
+        mp.H = std::max(mp.H, std::abs(o));
+        mp.R = std::max(mp.R, std::abs(r));
+        if (r == 0 && !fin) {
+            if (mp.nwin >= MARCH_MAXW) return false;
+            mp.win[mp.nwin] = e;
+            mp.wino[mp.nwin++] = o;
+        } else if (r == 0 && o == 0 && !fpl) {
+            if (mp.ncen >= MARCH_MAXC) return false;
+            mp.cen[mp.ncen++] = e;
+        } else {
+            if (mp.nsm >= MARCH_MAXS) return false;
+            mp.sm[mp.nsm] = e;
+            mp.smr[mp.nsm] = r;
+            mp.smo[mp.nsm] = o;
+            mp.smpl[mp.nsm++] = fpl ? 1 : 0;
+        }
+    }
+    if (mp.H < 1 || mp.H > 4 || mp.R > 1024) return false;
+    // shared entries without a plane factor first; the entries past nsm stay 0 (offset 0, weight 0)
+    {
+        int ord[MARCH_MAXS], n1 = 0;
+        for (int e = 0; e < mp.nsm; ++e) if (!mp.smpl[e]) ord[n1++] = e;
+        mp.nsm1 = n1;
+        for (int e = 0; e < mp.nsm; ++e) if (mp.smpl[e]) ord[n1++] = e;
+        int sm[MARCH_MAXS], smr[MARCH_MAXS], smo[MARCH_MAXS], spl[MARCH_MAXS];
+        for (int e = 0; e < mp.nsm; ++e) {
+            sm[e] = mp.sm[ord[e]]; smr[e] = mp.smr[ord[e]]; smo[e] = mp.smo[ord[e]]; spl[e] = mp.smpl[ord[e]];
+        }
+        for (int e = 0; e < mp.nsm; ++e) {
+            mp.sm[e] = sm[e]; mp.smr[e] = smr[e]; mp.smo[e] = smo[e]; mp.smpl[e] = spl[e];
+        }
+    }
+    // register budget (128 per thread): up to 8 shared entries (padded to 6 or 8 with zero weights)
+    // with 4 FP32 or 2 FP64 points per thread, up to 16 with half as many
+    mp.ms = mp.nsm <= 6 ? 6 : mp.nsm <= 8 ? 8 : 16;
+    const int pt = (elem == 4 ? 4 : 2) / (mp.ms <= 8 ? 1 : 2);
+    const int tqmax = MCT * pt;
+    // tiles: at most tqmax points, balanced over the plane, a multiple of 16 bytes
+    mp.ntile = (mp.P + tqmax - 1) / tqmax;
+    mp.TQ = (mp.P + mp.ntile - 1) / mp.ntile;
+    mp.TQ = (mp.TQ + G - 1) / G * G;
+    if (mp.TQ > tqmax) { ++mp.ntile; mp.TQ = ((mp.P + mp.ntile - 1) / mp.ntile + G - 1) / G * G; }
+    if (mp.TQ > tqmax) return false;
+    // a slot spans every point a thread indexes (MCT pt, beyond TQ when the tiles are balanced
+    // below it), so the loads of a thread's unused points stay inside the slot
+    mp.pt = pt;
+    mp.SLX = (tqmax + 2 * mp.R + 2 * G + G - 1) / G * G;
+    mp.SLD = (tqmax + 2 * G + G - 1) / G * G;
+    // persistent CTAs: one per SM, at least one per (tile, outer) group
+    const int64_t groups = (int64_t)mp.ntile * mp.nouter;
+    if (groups > (1 << 20)) return false;
+    mp.grid = (int)std::max<int64_t>(groups, std::max(num_sms, 1));
+    // ring slots within the budget (at least the window and one plane ahead)
+    const size_t slot_b = (size_t)(mp.SLX + mp.SLD) * elem;
+    const size_t tab = (size_t)mp.nm * (2 * mp.H + 1 + mp.ms) * elem + 64;
+    if (tab >= (size_t)M_SMEM_BUDGET) return false;
+    int nr = (int)((M_SMEM_BUDGET - tab) / (slot_b + 16));
+    nr = std::min(nr, 24);
+    if (nr < 2 * mp.H + 2) return false;
+    mp.NR = nr;
+    mp.flat = 1;
+    for (int e = 0; e < mp.nsm; ++e) mp.flat = mp.flat && mp.smo[e] == 0;
+    mp.nseg = 1;
+    mp.L = mp.nm;
+    return true;
+}
+
+template <typename T>
+void launch_apply_march(const kf_op *op, const MarchPlan &mp, const T *D, const T *W, const T *X, T *Y, int64_t ldx,
+                        int64_t ldy, int64_t b, T alpha, T beta, const T *Z, int64_t ldz, T gamma, int epi,
+                        cudaStream_t s) {
+    switch (mp.H) {
+        case 1: launch_h<T, 1>(op, mp, D, W, X, Y, ldx, ldy, b, alpha, beta, Z, ldz, gamma, epi, s); break;
+        case 2: launch_h<T, 2>(op, mp, D, W, X, Y, ldx, ldy, b, alpha, beta, Z, ldz, gamma, epi, s); break;
+        case 3: launch_h<T, 3>(op, mp, D, W, X, Y, ldx, ldy, b, alpha, beta, Z, ldz, gamma, epi, s); break;
+        default: launch_h<T, 4>(op, mp, D, W, X, Y, ldx, ldy, b, alpha, beta, Z, ldz, gamma, epi, s); break;
+    }
+}
+
+template void launch_apply_march<float>(const kf_op *, const MarchPlan &, const float *, const float *, const float *,
+                                        float *, int64_t, int64_t, int64_t, float, float, const float *, int64_t,
+                                        float, int, cudaStream_t);
+template void launch_apply_march<double>(const kf_op *, const MarchPlan &, const double *, const double *,
+                                         const double *, double *, int64_t, int64_t, int64_t, double, double,
+                                         const double *, int64_t, double, int, cudaStream_t);
+
+}  // namespace kf

@@ -49,8 +49,8 @@ extern std::atomic<uint64_t> g_launches;
 
 constexpr int MAXDIMS = 8;     // axes of a state tensor
 constexpr int MAXB = 24;       // bands of one banded factor (a periodic order-8 stencil has 16)
-// five (columns per thread, unroll) shapes, the plane-marching kernel, 36 columns per thread (a
-// 36-column block in one pass instead of 32 + 4)
+// five (columns per thread, unroll) shapes of the point kernel, the plane-marching kernel (5), 36
+// columns per thread (a 36-column block in one pass instead of 32 + 4)
 constexpr int KF_APPLY_VARIANTS = 7;
 constexpr int MAXE = 48;       // stencil entries (products of bands) over all fused terms
 
@@ -181,22 +181,25 @@ struct kf_op {
 
 namespace kf {
 
-// plane-marching fused apply (kf_apply_tiled.cu): the slowest axis m with an offset is walked
-// plane by plane, plane slices staged in shared memory by TMA bulk copies
-struct TiledGeom {
-    int m;          // march axis
-    int P;          // plane size (product of the axes before m)
-    int nm;         // planes (length of axis m)
-    int N;          // column length
-    int H;          // largest |offset| along m
-    int R;          // largest |in-plane offset|
-    int SL;         // ring slot length per column, elements
-    int L;          // planes per CTA
-    int nseg, ntile, nouter;
+// plane-marching fused apply (kf_apply_march.cu): the slowest axis m with an offset is walked plane by
+// plane; its neighbours come from a per-thread register window, in-plane neighbours from plane
+// slices staged in shared memory by bulk copies
+constexpr int MARCH_MAXW = 24;   // window entries (r = 0, no factor before m)
+constexpr int MARCH_MAXC = 16;   // centre entries
+constexpr int MARCH_MAXS = 16;   // shared-memory entries
+struct MarchPlan {
+    int m, P, nm, nouter, N, H, R;
+    int nwin, win[MARCH_MAXW], wino[MARCH_MAXW];
+    int ncen, cen[MARCH_MAXC];
+    int nsm, nsm1, ms, sm[MARCH_MAXS], smr[MARCH_MAXS], smo[MARCH_MAXS], smpl[MARCH_MAXS];
+    int TQ, ntile, nseg, L, NR, SLX, SLD, pt;
+    int flat;       // every shared entry reads the current plane (o_e = 0)
+    int grid;       // persistent CTAs
 };
-bool tiled_geometry(const kf_op *op, int64_t b, size_t elem, TiledGeom &g);
+bool march_plan(const kf_op *op, int64_t b, size_t elem, int num_sms, MarchPlan &mp);
+size_t march_smem_bytes(const MarchPlan &mp, size_t elem, int wn, int ms);
 template <typename T>
-void launch_apply_tiled(const kf_op *op, const TiledGeom &g, const T *D, const T *W, const T *X, T *Y, int64_t ldx,
+void launch_apply_march(const kf_op *op, const MarchPlan &mp, const T *D, const T *W, const T *X, T *Y, int64_t ldx,
                         int64_t ldy, int64_t b, T alpha, T beta, const T *Z, int64_t ldz, T gamma, int epi,
                         cudaStream_t s);
 

@@ -202,6 +202,19 @@ static std::string tune_key(const kf_op *op, int slot) {
     return k;
 }
 
+// streaming multiprocessors of a device (cached per device)
+static int num_sms(int dev) {
+    static std::mutex mu;
+    static std::map<int, int> cache;
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find(dev);
+    if (it != cache.end()) return it->second;
+    int v = 0;
+    KF_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev));
+    cache[dev] = v;
+    return v;
+}
+
 template <typename T>
 static void apply_t(kf_op *op, const T *X, T *Y, int64_t ldx, int64_t ldy, int64_t b, double alpha, double beta,
                     const T *Z, int64_t ldz, double gamma, cudaStream_t s) {
@@ -214,12 +227,13 @@ static void apply_t(kf_op *op, const T *X, T *Y, int64_t ldx, int64_t ldy, int64
     const int epi = (!chains && !trivial_epi) ? 1 : 0;
     const int ne = op->plan.ne;
     // the plane-marching kernel (variant 5) where its geometry applies and X is 16-byte aligned
-    TiledGeom tg;
+    MarchPlan mp;
     const int G = 16 / (int)sizeof(T);
-    const bool tiled_ok = tiled_geometry(op, b, sizeof(T), tg) && ldx % G == 0 && (uintptr_t)X % 16 == 0;
+    const bool march_ok = ldx % G == 0 && (uintptr_t)X % 16 == 0 && (uintptr_t)D % 16 == 0 &&
+                          march_plan(op, b, sizeof(T), num_sms(op->device), mp);
     auto run = [&](int variant) {
-        if (variant == 5 && tiled_ok) {
-            launch_apply_tiled<T>(op, tg, D, W, X, Y, ldx, ldy, b, (T)alpha, (T)beta, Z, ldz, (T)gamma, epi, s);
+        if (variant == 5 && march_ok) {
+            launch_apply_march<T>(op, mp, D, W, X, Y, ldx, ldy, b, (T)alpha, (T)beta, Z, ldz, (T)gamma, epi, s);
             return;
         }
 #define KF_FUSED(CPT, U, ME)                                                                                  \
@@ -263,7 +277,7 @@ static void apply_t(kf_op *op, const T *X, T *Y, int64_t ldx, int64_t ldy, int64
         float best = 1e30f;
         int bestv = 0;
         for (int v = 0; v < KF_APPLY_VARIANTS; ++v) {
-            if (v == 5 && !tiled_ok) continue;
+            if (v == 5 && !march_ok) continue;
             run(v);                                   // warm
             float vbest = 1e30f;
             for (int batch = 0; batch < 3; ++batch) {

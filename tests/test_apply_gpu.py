@@ -201,12 +201,26 @@ def test_errors(cuda):
     H.apply_device(X.data_ptr(), X.data_ptr() + 8 * 12, 0)
 
 
+def _march_eligible(H, b, f32):
+    import ctypes as C
+    from kfgpu import _abi
+    ok, g = C.c_int32(), (C.c_int32 * 16)()
+    _abi.check(_abi.lib().kf_test_march_plan(H.handle, b, 1 if f32 else 0, 0, C.byref(ok), g))
+    return ok.value == 1, list(g)
+
+
+MARCH_SHAPES = ["three_mode", "wide", "outer", "mixed", "stencil3", "stencil9", "axes4"]
+
+
 @pytest.mark.parametrize("f32", [False, True])
-@pytest.mark.parametrize("shape", ["three_mode", "wide", "outer_axes"])
+@pytest.mark.parametrize("shape", MARCH_SHAPES)
 def test_plane_marching_apply(cuda, f32, shape):
-    """The plane-marching kernel (variant 5: plane slices staged in shared memory by TMA bulk
-    copies) against the point-per-thread kernel and the oracle, forced past the autotuner: the
-    three-mode structure, a plane wider than a tile, and axes after the marching axis."""
+    """The plane-marching kernel (variant 5: the slowest stencil axis from a register window, plane
+    slices staged in shared memory by bulk copies, persistent CTAs) against the point-per-thread
+    kernel and the oracle, forced past the autotuner: the three-mode structure, a plane wider than a
+    tile, axes after the marching axis, entries with offsets on both the marching axis and an
+    in-plane axis (and plane-dependent weights), 3- and 9-point stencils along the marching axis,
+    and a 4-axis operator whose marching axis has nothing to march over (the point kernel runs)."""
     import ctypes as C
     torch = cuda
     from kfgpu import _abi, circuits, ops as P
@@ -215,6 +229,7 @@ def test_plane_marching_apply(cuda, f32, shape):
     def banded(n, offs):
         return P.BandedOp(n, list(offs), [rng.standard_normal(n) for _ in offs])
 
+    expect = True
     if shape == "three_mode":
         th = circuits.three_mode_theta(rng)
         dims, terms = circuits.three_mode_leaf(th, ncut=6, n2=48, n3=20)
@@ -222,12 +237,35 @@ def test_plane_marching_apply(cuda, f32, shape):
         dims = [41, 300, 5]
         terms = [(1.0, [(0, P.ShiftOp(41, 1, 1.0))]), (0.7, [(1, banded(300, (-2, -1, 0, 1, 2)))]),
                  (0.3, [(2, banded(5, (-1, 1)))]), (0.5, [(0, P.DiagonalOp(rng.standard_normal(41)))])]
+    elif shape == "outer":
+        dims = [41, 32, 20, 3]
+        terms = [(1.0, [(1, banded(32, (-2, -1, 0, 1, 2)))]), (0.6, [(2, banded(20, (-2, -1, 0, 1, 2)))]),
+                 (0.4, [(3, P.DiagonalOp(rng.standard_normal(3)))]),
+                 (0.8, [(0, P.ShiftOp(41, -1, 1.0)), (3, P.DiagonalOp(rng.standard_normal(3)))]),
+                 (0.2, [(2, banded(20, (-1, 1))), (3, P.DiagonalOp(rng.standard_normal(3)))])]
+    elif shape == "mixed":
+        dims = [24, 16, 30]
+        terms = [(1.0, [(0, P.ShiftOp(24, 1, 1.0)), (2, banded(30, (-1, 0, 1)))]),
+                 (0.5, [(0, P.DiagonalOp(rng.standard_normal(24))), (2, banded(30, (-2, 2)))]),
+                 (0.7, [(1, banded(16, (-1, 1))), (2, P.DiagonalOp(rng.standard_normal(30)))]),
+                 (0.3, [(2, banded(30, (-2, -1, 0, 1, 2)))]), (1.2, [(0, P.DiagonalOp(rng.standard_normal(24)))])]
+    elif shape == "stencil3":
+        dims = [33, 40, 24]
+        terms = [(1.0, [(1, banded(40, (-1, 0, 1)))]), (0.9, [(2, banded(24, (-1, 0, 1)))]),
+                 (0.5, [(0, P.ShiftOp(33, 1, 1.0))])]
+    elif shape == "stencil9":
+        dims = [64, 9, 30]
+        terms = [(1.0, [(2, banded(30, tuple(range(-4, 5))))]), (0.5, [(1, banded(9, (-1, 1)))]),
+                 (0.2, [(0, P.DiagonalOp(rng.standard_normal(64)))])]
     else:
         dims = [8, 20, 12, 3]
         terms = [(1.0, [(0, P.ShiftOp(8, -1, 2.0)), (1, banded(20, (-2, 0, 1)))]),
                  (0.4, [(3, P.DiagonalOp(rng.standard_normal(3)))]), (0.9, [(2, P.DiagonalOp(rng.standard_normal(12)))])]
+        expect = False
     H, Ho = _pair(dims, terms)
     N, b = H.N, 5
+    ok, geom = _march_eligible(H, b, f32)
+    assert ok == expect, (shape, geom)
     dt = torch.float32 if f32 else torch.float64
     X = torch.as_tensor(rng.standard_normal((b, N)), dtype=dt, device="cuda")
     Ys = []
@@ -242,6 +280,42 @@ def test_plane_marching_apply(cuda, f32, shape):
     tol = TOL32 if f32 else TOL64
     assert np.max(np.abs(Ys[1] - R)) / scale < tol
     assert np.max(np.abs(Ys[1] - Ys[0])) / scale < tol
+
+
+@pytest.mark.parametrize("f32", [False, True])
+def test_plane_marching_full_size(cuda, f32):
+    """The marching kernel on the full three-mode leaf (41 x 256 x 64, 16 columns) against the
+    oracle's C mul!, and with the Chebyshev epilogue Y = alpha H X + beta X + gamma Z through the
+    tuned path."""
+    import ctypes as C
+    torch = cuda
+    from kfgpu import _abi, circuits
+    from oracle import capply
+    rng = np.random.default_rng(5)
+    th = circuits.three_mode_theta(rng)
+    dims, terms = circuits.three_mode_leaf(th)
+    H, Ho = _pair(dims, terms)
+    N, b = H.N, 16
+    ok, geom = _march_eligible(H, b, f32)
+    assert ok and geom[:5] == [41 * 256, 64, 1, 2, 82], geom
+    dt = torch.float32 if f32 else torch.float64
+    X = torch.as_tensor(rng.standard_normal((b, N)), dtype=dt, device="cuda")
+    flags = _abi.KF_DEVICE | (_abi.KF_F32 if f32 else _abi.KF_F64)
+    Y = torch.full_like(X, float("nan"))
+    _abi.check(_abi.lib().kf_test_apply_variant(H.handle, 5, C.c_void_p(X.data_ptr()), C.c_void_p(Y.data_ptr()), N,
+                                                b, flags, 1, None))
+    Xh = np.asfortranarray(X.double().cpu().numpy().T)
+    R = capply.CApply(Ho).matvec(Xh)
+    scale = max(1.0, np.max(np.abs(R)))
+    tol = TOL32 if f32 else TOL64
+    assert np.max(np.abs(Y.double().cpu().numpy().T - R)) / scale < tol
+    # the epilogue, through the tuned kernel
+    Zt = torch.as_tensor(rng.standard_normal((b, N)), dtype=dt, device="cuda")
+    Y2 = torch.full_like(X, float("nan"))
+    H.apply_axpby_device(X.data_ptr(), Y2.data_ptr(), Zt.data_ptr(), b, 0.5, -0.25, 2.0, f32=f32)
+    H.sync()
+    R2 = 0.5 * R - 0.25 * Xh + 2.0 * Zt.double().cpu().numpy().T
+    assert np.max(np.abs(Y2.double().cpu().numpy().T - R2)) / max(1.0, np.max(np.abs(R2))) < tol
 
 
 @pytest.mark.parametrize("f32", [False, True])
