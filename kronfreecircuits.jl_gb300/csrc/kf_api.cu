@@ -410,7 +410,7 @@ int kf_test_march_plan(const kf_op *op, int64_t b, int32_t f32, int32_t sms, int
         if (geom && ok) {
             const int32_t g[16] = {mp.P, mp.nm, mp.nouter, mp.H, mp.R, mp.TQ, mp.ntile, mp.grid, mp.NR, mp.SLX,
                                    mp.SLD, mp.nsm, mp.ms, mp.pt, mp.flat,
-                                   (int32_t)kf::march_smem_bytes(mp, es, 2 * mp.H + 1, mp.ms)};
+                                   (int32_t)kf::march_smem_bytes(mp, es, mp.wn, mp.ms)};
             for (int i = 0; i < 16; ++i) geom[i] = g[i];
         }
     });

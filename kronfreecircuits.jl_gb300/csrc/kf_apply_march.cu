@@ -14,10 +14,16 @@
 // the slow axis' neighbours never leave registers, and only in-plane neighbours cost a
 // shared-memory load.
 //
+// Weights.  They depend on the operator only, so a small kernel evaluates them once per operator and
+// precision into a table in device memory: per outer index, the shared entries' and the centre's
+// weights of every in-plane point (w_in w_out) and, per plane, the window weights summed per plane
+// offset and the shared entries' plane weights (w_plane).  The march reads a thread's point weights
+// with a few coalesced loads and copies its outer index's plane rows into shared memory.
+//
 // Work split.  The kernel is persistent: one CTA per SM.  A CTA owns one tile of TQ consecutive q
-// (of one outer index) for its lifetime -- its per-point weights and the per-plane weight tables
-// are formed once -- and marches a contiguous range of the tile's (column, plane) pairs, split
-// evenly among the CTAs of the tile, column by column (each column's run with its plane halo).
+// (of one outer index) for its lifetime and marches a contiguous range of the tile's (column, plane)
+// pairs, split evenly among the CTAs of the tile, column by column (each column's run with its plane
+// halo).
 //
 // Pipeline.  A producer warp copies, for every plane the CTA touches, the column's slice
 // X[q0 - R .. q0 + TQ + R) and the diagonal's slice D[q0 .. q0 + TQ) into the next slot of a ring
@@ -96,20 +102,35 @@ __device__ __forceinline__ T fac_w(const T *W, int w, int nb, int n, int o, int 
     return ((unsigned)(i + o) < (unsigned)n) ? __ldg(W + w + i * nb) : T(0);
 }
 
+// idx[a] for a runtime axis a, by a chain of selects (the array stays in registers)
+__device__ __forceinline__ int coord(const int (&idx)[MAXDIMS_F], int a) {
+    int v = idx[0];
+#pragma unroll
+    for (int k = 1; k < MAXDIMS_F; ++k) v = (a == k) ? idx[k] : v;
+    return v;
+}
+
 // the part of entry E's weight from the factors on the axes of class `sel` (0: before m, 1: m,
 // 2: after m); idx[a] is the coordinate on axis a
 template <typename T>
-__device__ __forceinline__ T entry_part(const Entry &E, const T *W, int m, const int *idx, int sel) {
+__device__ __forceinline__ T entry_part(const Entry &E, const T *W, int m, const int (&idx)[MAXDIMS_F], int sel) {
     T w = T(1);
     {
         const int s = E.a0 < m ? 0 : (E.a0 == m ? 1 : 2);
-        if (s == sel) w *= fac_w(W, E.w0, E.nb0, E.n0, E.o0, idx[E.a0]);
+        if (s == sel) w *= fac_w(W, E.w0, E.nb0, E.n0, E.o0, coord(idx, E.a0));
     }
     if (E.nf == 2) {
         const int s = E.a1 < m ? 0 : (E.a1 == m ? 1 : 2);
-        if (s == sel) w *= fac_w(W, E.w1, E.nb1, E.n1, E.o1, idx[E.a1]);
+        if (s == sel) w *= fac_w(W, E.w1, E.nb1, E.n1, E.o1, coord(idx, E.a1));
     }
     return w;
+}
+
+// idx with axis a set to v (static indexing)
+__device__ __forceinline__ void set_coord(int (&idx)[MAXDIMS_F], int a, int v) {
+#pragma unroll
+    for (int k = 0; k < MAXDIMS_F; ++k)
+        if (a == k) idx[k] = v;
 }
 
 // this CTA's tile group and its range [f0, f1) of (column, plane) pairs f = col * n_m + k
@@ -136,11 +157,74 @@ __device__ __forceinline__ int run_end(int64_t f, int k0, int64_t f1, int nm) {
     return e < (int64_t)nm ? (int)e : nm;
 }
 
-template <typename T, int H, int MS, int PT>
+// The weight table of a march plan (layout per outer index o: [MS + 1][P] point weights -- the
+// shared entries', then the centre's -- followed by [nm][wn + MS] plane rows -- the window weights
+// per plane offset, then the shared entries' plane weights, 1 without a factor on axis m, 0 past
+// nsm).  One thread per table element.
+template <typename T>
+__global__ void k_march_table(const ApplyPlan plan, const MarchPlan mp, const T *__restrict__ W, T *__restrict__ tab,
+                              int64_t total) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= total) return;
+    const int MS = mp.ms, WN = mp.wn, H = (mp.wn - 1) / 2;
+    const int64_t per = (int64_t)(MS + 1) * mp.P + (int64_t)mp.nm * (WN + MS);
+    const int o = (int)(t / per);
+    const int64_t r = t % per;
+    int idx[MAXDIMS_F];
+    {
+        int rem = o;
+#pragma unroll
+        for (int a = 0; a < MAXDIMS_F; ++a) {
+            idx[a] = 0;
+            if (a > mp.m && a < plan.ndims) {
+                idx[a] = rem % plan.dims[a];
+                rem /= plan.dims[a];
+            }
+        }
+    }
+    T v = T(0);
+    if (r < (int64_t)(MS + 1) * mp.P) {
+        const int e = (int)(r / mp.P), q = (int)(r % mp.P);
+        int rem = q;
+#pragma unroll
+        for (int a = 0; a < MAXDIMS_F; ++a)
+            if (a < mp.m) {
+                idx[a] = rem % plan.dims[a];
+                rem /= plan.dims[a];
+            }
+        if (e < mp.nsm) {
+            const Entry &E = plan.e[mp.sm[e]];
+            v = entry_part<T>(E, W, mp.m, idx, 0) * entry_part<T>(E, W, mp.m, idx, 2);
+        } else if (e == MS) {
+            for (int c = 0; c < mp.ncen; ++c) {
+                const Entry &E = plan.e[mp.cen[c]];
+                v += entry_part<T>(E, W, mp.m, idx, 0) * entry_part<T>(E, W, mp.m, idx, 2);
+            }
+        }
+    } else {
+        const int64_t r2 = r - (int64_t)(MS + 1) * mp.P;
+        const int k = (int)(r2 / (WN + MS)), c = (int)(r2 % (WN + MS));
+        set_coord(idx, mp.m, k);
+        if (c < WN) {
+            for (int q = 0; q < mp.nwin; ++q) {
+                if (mp.wino[q] != c - H) continue;
+                const Entry &E = plan.e[mp.win[q]];
+                v += entry_part<T>(E, W, mp.m, idx, 1) * entry_part<T>(E, W, mp.m, idx, 2);
+            }
+        } else {
+            const int e = c - WN;
+            if (e < mp.nsm1) v = T(1);
+            else if (e < mp.nsm) v = entry_part<T>(plan.e[mp.sm[e]], W, mp.m, idx, 1);
+        }
+    }
+    tab[t] = v;
+}
+
+template <typename T, int H, int MS, int PT, bool EPI>
 __global__ void __launch_bounds__(MTHREADS, 1)
     k_apply_march(const ApplyPlan plan, const MarchPlan mp, const T *__restrict__ D, const T *__restrict__ W,
                   const T *__restrict__ X, T *__restrict__ Y, int64_t ldx, int64_t ldy, int b, T alpha, T beta,
-                  const T *__restrict__ Z, int64_t ldz, T gamma, int epi, int *err) {
+                  const T *__restrict__ Z, int64_t ldz, T gamma, int epi, const T *__restrict__ tab, int *err) {
     constexpr int G = 16 / (int)sizeof(T);
     constexpr int WN = 2 * H + 1;
     extern __shared__ __align__(128) unsigned char m_smem[];
@@ -177,9 +261,10 @@ __global__ void __launch_bounds__(MTHREADS, 1)
         }
     }
 
-    // the ring starts zeroed: a slice clamped at the ends of the column leaves its halo unwritten,
-    // and zero weights must meet finite values there
+    // the ring starts zeroed: a shared entry whose neighbour plane lies outside the axis reads a slot
+    // no copy has filled yet, and its zero weight must meet a finite value there
     for (int e = tid; e < NR * SL; e += MTHREADS) ring[e] = T(0);
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
     if (tid == 0) {
         s_abort = 0;
         for (int s = 0; s < NR; ++s) {
@@ -188,55 +273,41 @@ __global__ void __launch_bounds__(MTHREADS, 1)
         }
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
-    // per-plane tables for every plane: the window weights (summed per plane offset) and the plane
-    // weights of the shared entries (1 without a factor on axis m, 0 for the padding entries); the
-    // outer weights folded in
-    for (int t = tid; t < mp.nm * (WN + MS); t += MTHREADS) {
-        int idx[MAXDIMS_F];
-#pragma unroll
-        for (int a = 0; a < MAXDIMS_F; ++a) idx[a] = idx_out[a];
-        T v = T(0);
-        if (t < mp.nm * WN) {
-            const int o = t % WN - H;
-            idx[mp.m] = t / WN;
-            for (int q = 0; q < mp.nwin; ++q) {
-                if (mp.wino[q] != o) continue;
-                const Entry &E = plan.e[mp.win[q]];
-                v += entry_part<T>(E, W, mp.m, idx, 1) * entry_part<T>(E, W, mp.m, idx, 2);
-            }
-            wm[t] = v;
-        } else {
-            const int t2 = t - mp.nm * WN, e = t2 % MS;
-            idx[mp.m] = t2 / MS;
-            if (e < mp.nsm1) v = T(1);
-            else if (e < mp.nsm) v = entry_part<T>(plan.e[mp.sm[e]], W, mp.m, idx, 1);
-            wp[t2] = v;
-        }
-    }
-    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
     __syncthreads();
 
     if (warp == MCW) {
-        // ---- producer: one lane issues every plane's two bulk copies, in load order
-        if (lane == 0) {
-            int s = 0, use = 0, issued = 0;   // load t goes to slot t % NR, as use t / NR
-            bool ok = true;
-            for (int64_t f = wk.f0; f < wk.f1 && ok;) {
-                const int col = (int)(f / mp.nm), k0 = (int)(f % mp.nm);
-                const int k1 = run_end(f, k0, wk.f1, mp.nm);
-                f += k1 - k0;
-                const T *Xc = X + (int64_t)col * ldx;
-                const int jfirst = max(0, k0 - H), jlast = min(mp.nm - 1, k1 - 1 + H);
-                for (int j = jfirst; j <= jlast; ++j) {
-                    if (use > 0 && !m_wait(empty + s, (uint32_t)((use - 1) & 1), &s_abort)) {
-                        ok = false;
-                        break;
-                    }
-                    T *slot = ring + (size_t)s * SL;
-                    const int64_t xs = obase + (int64_t)j * mp.P + q0 - mp.R, xb = xs - misx;
-                    int64_t xlo = xb, xhi = ceil_to(xs + qn + 2 * mp.R, G);
-                    if (xlo < 0) xlo = 0;
-                    if (xhi > mp.N) xhi = mp.N;
+        // ---- producer: lane 0 issues every plane's two bulk copies, in load order; a slice clamped at
+        // an end of the column leaves part of its slot unwritten, which the warp zeroes first (the
+        // slot may hold an earlier plane's values; zero keeps the halo of the column's end exact)
+        int s = 0, use = 0, issued = 0;   // load t goes to slot t % NR, as use t / NR
+        bool ok = true;
+        for (int64_t f = wk.f0; f < wk.f1 && ok;) {
+            const int col = (int)(f / mp.nm), k0 = (int)(f % mp.nm);
+            const int k1 = run_end(f, k0, wk.f1, mp.nm);
+            f += k1 - k0;
+            const T *Xc = X + (int64_t)col * ldx;
+            const int jfirst = max(0, k0 - H), jlast = min(mp.nm - 1, k1 - 1 + H);
+            for (int j = jfirst; j <= jlast; ++j) {
+                int good = 1;
+                if (use > 0 && lane == 0) good = m_wait(empty + s, (uint32_t)((use - 1) & 1), &s_abort) ? 1 : 0;
+                good = __shfl_sync(0xffffffffu, good, 0);
+                if (!good) {
+                    ok = false;
+                    break;
+                }
+                T *slot = ring + (size_t)s * SL;
+                const int64_t xs = obase + (int64_t)j * mp.P + q0 - mp.R, xb = xs - misx;
+                const int64_t xend = ceil_to(xs + qn + 2 * mp.R, G);
+                int64_t xlo = xb, xhi = xend;
+                if (xlo < 0) xlo = 0;
+                if (xhi > mp.N) xhi = mp.N;
+                if (xlo > xb || xhi < xend) {
+                    for (int e = lane; e < (int)(xlo - xb); e += 32) slot[e] = T(0);
+                    for (int e = (int)(xhi - xb) + lane; e < (int)(xend - xb); e += 32) slot[e] = T(0);
+                    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+                }
+                __syncwarp();
+                if (lane == 0) {
                     const int64_t ds = obase + (int64_t)j * mp.P + q0, db = ds - misd;
                     int64_t dhi = ceil_to(ds + qn, G);
                     if (dhi > mp.N) dhi = mp.N;
@@ -245,23 +316,31 @@ __global__ void __launch_bounds__(MTHREADS, 1)
                     m_expect(full + s, bx + bd);
                     if (bx) m_bulk(slot + (xlo - xb), Xc + xlo, bx, full + s);
                     if (bd) m_bulk(slot + mp.SLX, D + db, bd, full + s);
-                    ++issued;
-                    if (++s == NR) { s = 0; ++use; }
                 }
-            }
-            if (!ok) {
-                s_abort = 1;
-                *(volatile int *)err = KF_ETIMEOUT;
-                __threadfence_system();
-                // copies still in flight write this CTA's shared memory: wait (bounded) for the
-                // latest use of every slot before leaving
-                volatile int never = 0;
-                for (int t = max(0, issued - NR); t < issued; ++t)
-                    (void)m_wait(full + t % NR, (uint32_t)((t / NR) & 1), &never);
+                ++issued;
+                if (++s == NR) { s = 0; ++use; }
             }
         }
+        if (!ok && lane == 0) {
+            s_abort = 1;
+            *(volatile int *)err = KF_ETIMEOUT;
+            __threadfence_system();
+            // copies still in flight write this CTA's shared memory: wait (bounded) for the latest
+            // use of every slot before leaving
+            volatile int never = 0;
+            for (int t = max(0, issued - NR); t < issued; ++t)
+                (void)m_wait(full + t % NR, (uint32_t)((t / NR) & 1), &never);
+        }
     } else {
-        // ---- consumers: thread tid owns points q0 + tid + MCT j, j < PT
+        // ---- consumers: this outer index's plane rows into shared memory, the points' weights into
+        // registers, from the operator's weight table
+        const T *tab_o = tab + (int64_t)wk.outer * ((int64_t)(MS + 1) * mp.P + (int64_t)mp.nm * (WN + MS));
+        const T *rows = tab_o + (int64_t)(MS + 1) * mp.P;
+        for (int t = tid; t < mp.nm * (WN + MS); t += MCT) {
+            const int k = t / (WN + MS), c = t % (WN + MS);
+            if (c < WN) wm[k * WN + c] = rows[t];
+            else wp[k * MS + (c - WN)] = rows[t];
+        }
         bool valid[PT];
         T wcen[PT];                   // centre weights (factors before m, times the outer ones)
         T wsm[PT][MS];                // weights of the shared entries on the axes before m and after m
@@ -269,32 +348,12 @@ __global__ void __launch_bounds__(MTHREADS, 1)
         for (int j = 0; j < PT; ++j) {
             const int qi = tid + j * MCT;
             valid[j] = qi < qn;
-            int idx[MAXDIMS_F];
-            int rem = valid[j] ? q0 + qi : q0;
+            const T *pt = tab_o + q0 + qi;
 #pragma unroll
-            for (int a = 0; a < MAXDIMS_F; ++a) {
-                idx[a] = idx_out[a];
-                if (a < mp.m) {
-                    idx[a] = rem % plan.dims[a];
-                    rem /= plan.dims[a];
-                }
-            }
-            T c = T(0);
-            for (int q = 0; q < mp.ncen; ++q) {
-                const Entry &E = plan.e[mp.cen[q]];
-                c += entry_part<T>(E, W, mp.m, idx, 0) * entry_part<T>(E, W, mp.m, idx, 2);
-            }
-            wcen[j] = c;
-#pragma unroll
-            for (int e = 0; e < MS; ++e) {
-                T w = T(0);
-                if (e < mp.nsm) {
-                    const Entry &E = plan.e[mp.sm[e]];
-                    w = entry_part<T>(E, W, mp.m, idx, 0) * entry_part<T>(E, W, mp.m, idx, 2);
-                }
-                wsm[j][e] = w;
-            }
+            for (int e = 0; e < MS; ++e) wsm[j][e] = valid[j] ? __ldg(pt + (int64_t)e * mp.P) : T(0);
+            wcen[j] = valid[j] ? __ldg(pt + (int64_t)MS * mp.P) : T(0);
         }
+        asm volatile("bar.sync 1, %0;\n" ::"r"(MCT) : "memory");   // the consumer warps only
         auto wrap = [&](int s) { return s >= NR ? s - NR : (s < 0 ? s + NR : s); };
         // offset, within a slot, of this thread's first point in the X slice
         const int xoff0 = mp.R + misx + tid;
@@ -374,15 +433,12 @@ __global__ void __launch_bounds__(MTHREADS, 1)
                             a0 = fma(wsm[j][e], ring[pe[e] + j * MCT], a0);
                             if (e + 1 < MS) a1 = fma(wsm[j][e + 1], ring[pe[e + 1] + j * MCT], a1);
                         }
-                        const T acc = a0 + a1;
-                        if (valid[j]) {
-                            T r = acc;
-                            if (epi) {
-                                r = alpha * acc + beta * xc;
-                                if (zcol != nullptr) r += gamma * zcol[(int64_t)k * mp.P + j * MCT];
-                            }
-                            yk[j * MCT] = r;
+                        T r = a0 + a1;
+                        if (EPI) {
+                            r = alpha * r + beta * xc;
+                            if (zcol != nullptr && valid[j]) r += gamma * zcol[(int64_t)k * mp.P + j * MCT];
                         }
+                        if (valid[j]) yk[j * MCT] = r;
                     }
                 } else {
                     T wpk[MS];
@@ -401,15 +457,12 @@ __global__ void __launch_bounds__(MTHREADS, 1)
                             a0 = fma(wsm[j][e] * wpk[e], ring[pe[e] + j * MCT], a0);
                             if (e + 1 < MS) a1 = fma(wsm[j][e + 1] * wpk[e + 1], ring[pe[e + 1] + j * MCT], a1);
                         }
-                        const T acc = a0 + a1;
-                        if (valid[j]) {
-                            T r = acc;
-                            if (epi) {
-                                r = alpha * acc + beta * xc;
-                                if (zcol != nullptr) r += gamma * zcol[(int64_t)k * mp.P + j * MCT];
-                            }
-                            yk[j * MCT] = r;
+                        T r = a0 + a1;
+                        if (EPI) {
+                            r = alpha * r + beta * xc;
+                            if (zcol != nullptr && valid[j]) r += gamma * zcol[(int64_t)k * mp.P + j * MCT];
                         }
+                        if (valid[j]) yk[j * MCT] = r;
                     }
                 }
                 // plane k - H leaves the window: release its slot
@@ -440,33 +493,40 @@ __global__ void __launch_bounds__(MTHREADS, 1)
     __syncthreads();
 }
 
-template <typename T, int H, int MS, int PT>
+template <typename T, int H, int MS, int PT, bool EPI>
 void launch_k(const kf_op *op, const MarchPlan &mp, const T *D, const T *W, const T *X, T *Y, int64_t ldx,
-              int64_t ldy, int64_t b, T alpha, T beta, const T *Z, int64_t ldz, T gamma, int epi, cudaStream_t s) {
+              int64_t ldy, int64_t b, T alpha, T beta, const T *Z, int64_t ldz, T gamma, int epi, const T *tab,
+              cudaStream_t s) {
     const size_t smem = march_smem_bytes(mp, sizeof(T), 2 * H + 1, MS);
     static bool attr = false;   // per instantiation
     if (!attr) {
-        KF_CUDA(cudaFuncSetAttribute(k_apply_march<T, H, MS, PT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        KF_CUDA(cudaFuncSetAttribute(k_apply_march<T, H, MS, PT, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      M_SMEM_BUDGET + 16384));
         attr = true;
     }
     KF_REQUIRE(smem <= (size_t)M_SMEM_BUDGET + 16384, KF_EINVAL, "apply: plane ring too large");
-    k_apply_march<T, H, MS, PT><<<mp.grid, MTHREADS, smem, s>>>(op->plan, mp, D, W, X, Y, ldx, ldy, (int)b, alpha,
-                                                                beta, Z, ldz, gamma, epi, tc_error_word());
+    k_apply_march<T, H, MS, PT, EPI><<<mp.grid, MTHREADS, smem, s>>>(op->plan, mp, D, W, X, Y, ldx, ldy, (int)b, alpha,
+                                                                beta, Z, ldz, gamma, epi, tab, tc_error_word());
     KF_LAUNCH_CHECK();
 }
 
 template <typename T, int H>
 void launch_h(const kf_op *op, const MarchPlan &mp, const T *D, const T *W, const T *X, T *Y, int64_t ldx,
-              int64_t ldy, int64_t b, T alpha, T beta, const T *Z, int64_t ldz, T gamma, int epi, cudaStream_t s) {
+              int64_t ldy, int64_t b, T alpha, T beta, const T *Z, int64_t ldz, T gamma, int epi, const T *tab,
+              cudaStream_t s) {
     // points per thread: what fits 128 registers without spilling (13 warps on one SM)
     constexpr int P8 = sizeof(T) == 4 ? 4 : 2, P16 = sizeof(T) == 4 ? 2 : 1;
-    if (mp.ms == 6)
-        launch_k<T, H, 6, P8>(op, mp, D, W, X, Y, ldx, ldy, b, alpha, beta, Z, ldz, gamma, epi, s);
-    else if (mp.ms == 8)
-        launch_k<T, H, 8, P8>(op, mp, D, W, X, Y, ldx, ldy, b, alpha, beta, Z, ldz, gamma, epi, s);
-    else
-        launch_k<T, H, 16, P16>(op, mp, D, W, X, Y, ldx, ldy, b, alpha, beta, Z, ldz, gamma, epi, s);
+#define KF_MARCH(MS_, PT_)                                                                                   \
+    do {                                                                                                     \
+        if (epi)                                                                                             \
+            launch_k<T, H, MS_, PT_, true>(op, mp, D, W, X, Y, ldx, ldy, b, alpha, beta, Z, ldz, gamma, epi, tab, s); \
+        else                                                                                                 \
+            launch_k<T, H, MS_, PT_, false>(op, mp, D, W, X, Y, ldx, ldy, b, alpha, beta, Z, ldz, gamma, epi, tab, s); \
+    } while (0)
+    if (mp.ms == 6) KF_MARCH(6, P8);
+    else if (mp.ms == 8) KF_MARCH(8, P8);
+    else KF_MARCH(16, P16);
+#undef KF_MARCH
 }
 
 }  // namespace
@@ -568,11 +628,13 @@ bool march_plan(const kf_op *op, int64_t b, size_t elem, int num_sms, MarchPlan 
     mp.grid = (int)std::max<int64_t>(groups, std::max(num_sms, 1));
     // ring slots within the budget (at least the window and one plane ahead)
     const size_t slot_b = (size_t)(mp.SLX + mp.SLD) * elem;
-    const size_t tab = (size_t)mp.nm * (2 * mp.H + 1 + mp.ms) * elem + 64;
+    const int hk = mp.H == 3 ? 4 : mp.H;      // the kernel's window half-width
+    mp.wn = 2 * hk + 1;
+    const size_t tab = (size_t)mp.nm * (2 * hk + 1 + mp.ms) * elem + 64;
     if (tab >= (size_t)M_SMEM_BUDGET) return false;
     int nr = (int)((M_SMEM_BUDGET - tab) / (slot_b + 16));
     nr = std::min(nr, 24);
-    if (nr < 2 * mp.H + 2) return false;
+    if (nr < 2 * 4 + 2) return false;        // a halo of 3 runs on the kernel for 4
     mp.NR = nr;
     mp.flat = 1;
     for (int e = 0; e < mp.nsm; ++e) mp.flat = mp.flat && mp.smo[e] == 0;
@@ -582,21 +644,30 @@ bool march_plan(const kf_op *op, int64_t b, size_t elem, int num_sms, MarchPlan 
 }
 
 template <typename T>
-void launch_apply_march(const kf_op *op, const MarchPlan &mp, const T *D, const T *W, const T *X, T *Y, int64_t ldx,
+void launch_apply_march(kf_op *op, const MarchPlan &mp, const T *D, const T *W, const T *X, T *Y, int64_t ldx,
                         int64_t ldy, int64_t b, T alpha, T beta, const T *Z, int64_t ldz, T gamma, int epi,
                         cudaStream_t s) {
-    switch (mp.H) {
-        case 1: launch_h<T, 1>(op, mp, D, W, X, Y, ldx, ldy, b, alpha, beta, Z, ldz, gamma, epi, s); break;
-        case 2: launch_h<T, 2>(op, mp, D, W, X, Y, ldx, ldy, b, alpha, beta, Z, ldz, gamma, epi, s); break;
-        case 3: launch_h<T, 3>(op, mp, D, W, X, Y, ldx, ldy, b, alpha, beta, Z, ldz, gamma, epi, s); break;
-        default: launch_h<T, 4>(op, mp, D, W, X, Y, ldx, ldy, b, alpha, beta, Z, ldz, gamma, epi, s); break;
+    const int slot = sizeof(T) == 4 ? 1 : 0;
+    if (op->d_march[slot] == nullptr) {
+        const int64_t total = (int64_t)mp.nouter * ((int64_t)(mp.ms + 1) * mp.P + (int64_t)mp.nm * (mp.wn + mp.ms));
+        void *p = nullptr;
+        KF_CUDA(cudaMalloc(&p, (size_t)total * sizeof(T)));
+        k_march_table<T><<<(unsigned)((total + 255) / 256), 256, 0, s>>>(op->plan, mp, W, (T *)p, total);
+        KF_LAUNCH_CHECK();
+        op->d_march[slot] = p;
+    }
+    const T *tab = (const T *)op->d_march[slot];
+    switch (mp.wn) {
+        case 3: launch_h<T, 1>(op, mp, D, W, X, Y, ldx, ldy, b, alpha, beta, Z, ldz, gamma, epi, tab, s); break;
+        case 5: launch_h<T, 2>(op, mp, D, W, X, Y, ldx, ldy, b, alpha, beta, Z, ldz, gamma, epi, tab, s); break;
+        default: launch_h<T, 4>(op, mp, D, W, X, Y, ldx, ldy, b, alpha, beta, Z, ldz, gamma, epi, tab, s); break;
     }
 }
 
-template void launch_apply_march<float>(const kf_op *, const MarchPlan &, const float *, const float *, const float *,
+template void launch_apply_march<float>(kf_op *, const MarchPlan &, const float *, const float *, const float *,
                                         float *, int64_t, int64_t, int64_t, float, float, const float *, int64_t,
                                         float, int, cudaStream_t);
-template void launch_apply_march<double>(const kf_op *, const MarchPlan &, const double *, const double *,
+template void launch_apply_march<double>(kf_op *, const MarchPlan &, const double *, const double *,
                                          const double *, double *, int64_t, int64_t, int64_t, double, double,
                                          const double *, int64_t, double, int, cudaStream_t);
 

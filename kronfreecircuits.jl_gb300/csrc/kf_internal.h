@@ -148,6 +148,8 @@ struct kf_op {
     std::vector<kf::TcMatrix> chain_tc;   // tensor-core images of dense chain factors (FP32 applies)
     double *d_chain64 = nullptr;
     float *d_chain32 = nullptr;
+    // the plane-marching apply's weight tables (FP64, FP32), built on its first use
+    void *d_march[2] = {nullptr, nullptr};
     // scratch for chains: two buffers of N * cap doubles
     int64_t cap = 0;
     void *d_scratch = nullptr;
@@ -195,11 +197,12 @@ struct MarchPlan {
     int TQ, ntile, nseg, L, NR, SLX, SLD, pt;
     int flat;       // every shared entry reads the current plane (o_e = 0)
     int grid;       // persistent CTAs
+    int wn;         // the kernel's window length (2H + 1; a halo of 3 runs on the kernel for 4)
 };
 bool march_plan(const kf_op *op, int64_t b, size_t elem, int num_sms, MarchPlan &mp);
 size_t march_smem_bytes(const MarchPlan &mp, size_t elem, int wn, int ms);
 template <typename T>
-void launch_apply_march(const kf_op *op, const MarchPlan &mp, const T *D, const T *W, const T *X, T *Y, int64_t ldx,
+void launch_apply_march(kf_op *op, const MarchPlan &mp, const T *D, const T *W, const T *X, T *Y, int64_t ldx,
                         int64_t ldy, int64_t b, T alpha, T beta, const T *Z, int64_t ldz, T gamma, int epi,
                         cudaStream_t s);
 

@@ -899,6 +899,8 @@ void free_op(kf_op *op) {
     cudaFree(op->d_chain64);
     cudaFree(op->d_chain32);
     cudaFree(op->d_scratch);
+    cudaFree(op->d_march[0]);
+    cudaFree(op->d_march[1]);
     for (float *p : op->sep.dU) cudaFree(p);
     for (float *p : op->sep.dUt) cudaFree(p);
     for (double *p : op->sep.dU64) cudaFree(p);

@@ -209,7 +209,7 @@ def _march_eligible(H, b, f32):
     return ok.value == 1, list(g)
 
 
-MARCH_SHAPES = ["three_mode", "wide", "outer", "mixed", "stencil3", "stencil9", "axes4"]
+MARCH_SHAPES = ["three_mode", "wide", "outer", "mixed", "stencil3", "stencil7", "stencil9", "axes4"]
 
 
 @pytest.mark.parametrize("f32", [False, True])
@@ -219,7 +219,7 @@ def test_plane_marching_apply(cuda, f32, shape):
     slices staged in shared memory by bulk copies, persistent CTAs) against the point-per-thread
     kernel and the oracle, forced past the autotuner: the three-mode structure, a plane wider than a
     tile, axes after the marching axis, entries with offsets on both the marching axis and an
-    in-plane axis (and plane-dependent weights), 3- and 9-point stencils along the marching axis,
+    in-plane axis (and plane-dependent weights), 3-, 7- and 9-point stencils along the marching axis,
     and a 4-axis operator whose marching axis has nothing to march over (the point kernel runs)."""
     import ctypes as C
     torch = cuda
@@ -253,6 +253,10 @@ def test_plane_marching_apply(cuda, f32, shape):
         dims = [33, 40, 24]
         terms = [(1.0, [(1, banded(40, (-1, 0, 1)))]), (0.9, [(2, banded(24, (-1, 0, 1)))]),
                  (0.5, [(0, P.ShiftOp(33, 1, 1.0))])]
+    elif shape == "stencil7":
+        dims = [20, 12, 40]
+        terms = [(1.0, [(2, banded(40, tuple(range(-3, 4))))]), (0.5, [(0, banded(20, (-1, 1)))]),
+                 (0.3, [(0, P.ShiftOp(20, 1, 1.0)), (2, banded(40, (-3, 3)))])]
     elif shape == "stencil9":
         dims = [64, 9, 30]
         terms = [(1.0, [(2, banded(30, tuple(range(-4, 5))))]), (0.5, [(1, banded(9, (-1, 1)))]),
