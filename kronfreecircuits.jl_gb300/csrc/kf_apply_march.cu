@@ -93,6 +93,23 @@ __device__ __forceinline__ bool m_wait(uint64_t *bar, uint32_t parity, volatile 
     }
 }
 
+// a load from shared memory at a 32-bit shared-window address (ordered after the mbarrier waits,
+// which are volatile asm too)
+template <typename T>
+__device__ __forceinline__ T lds(uint32_t a);
+template <>
+__device__ __forceinline__ float lds<float>(uint32_t a) {
+    float v;
+    asm volatile("ld.shared.f32 %0, [%1];\n" : "=f"(v) : "r"(a));
+    return v;
+}
+template <>
+__device__ __forceinline__ double lds<double>(uint32_t a) {
+    double v;
+    asm volatile("ld.shared.f64 %0, [%1];\n" : "=d"(v) : "r"(a));
+    return v;
+}
+
 __device__ __forceinline__ int64_t floor_to(int64_t x, int g) { return x >= 0 ? x / g * g : -((-x + g - 1) / g * g); }
 __device__ __forceinline__ int64_t ceil_to(int64_t x, int g) { return (x + g - 1) / g * g; }
 
@@ -358,6 +375,8 @@ __global__ void __launch_bounds__(MTHREADS, 1)
         // offset, within a slot, of this thread's first point in the X slice
         const int xoff0 = mp.R + misx + tid;
         const bool plain_sm = mp.nsm1 == mp.nsm;
+        const bool fast = plain_sm && mp.flat;
+        const uint32_t ring_s = msu32(ring), wm_s = msu32(wm);
         int64_t t0 = 0;               // load index of the current run's first plane
         bool ok = true;
         for (int64_t f = wk.f0; f < wk.f1 && ok;) {
@@ -390,7 +409,73 @@ __global__ void __launch_bounds__(MTHREADS, 1)
             int usen = (int)((tk0 + H) / NR);            // and its use index
             T *ycol = Y + (int64_t)col * ldy + obase + q0 + tid;
             const T *zcol = Z != nullptr ? Z + (int64_t)col * ldz + obase + q0 + tid : nullptr;
-            for (int k = k0; k < k1 && ok; ++k) {
+            // the march, WN planes per block: at step r of a block, window position o (plane k - H + o)
+            // lives in register xw[j][(o + r) % WN], so the window rotates without moves
+            if (fast) {
+                // every shared entry reads the current plane with in-plane weights only (the
+                // three-mode leaf's stencil): 32-bit shared addresses, no per-entry plane weights
+                for (int kb = k0; kb < k1 && ok; kb += WN) {
+#pragma unroll
+                    for (int r = 0; r < WN; ++r) {
+                        const int k = kb + r;
+                        if (k >= k1 || !ok) break;
+                        if (k + H <= jlast) {
+                            if (!m_wait(full + sn, (uint32_t)(usen & 1), &s_abort)) {
+                                ok = false;
+                                break;
+                            }
+                            const uint32_t ax = ring_s + (uint32_t)(sn * SL + xoff0) * (uint32_t)sizeof(T);
+#pragma unroll
+                            for (int j = 0; j < PT; ++j)
+                                xw[j][(2 * H + r) % WN] = lds<T>(ax + (uint32_t)(j * MCT * sizeof(T)));
+                        } else {
+#pragma unroll
+                            for (int j = 0; j < PT; ++j) xw[j][(2 * H + r) % WN] = T(0);
+                        }
+                        T wmk[WN];
+                        const uint32_t aw = wm_s + (uint32_t)(k * WN) * (uint32_t)sizeof(T);
+#pragma unroll
+                        for (int o = 0; o < WN; ++o) wmk[o] = lds<T>(aw + (uint32_t)(o * sizeof(T)));
+                        const uint32_t ab = ring_s + (uint32_t)(sk * SL + xoff0) * (uint32_t)sizeof(T);
+                        uint32_t pa[MS];
+#pragma unroll
+                        for (int e = 0; e < MS; ++e) pa[e] = ab + (uint32_t)(mp.smr[e] * (int)sizeof(T));
+                        const uint32_t ad = ring_s + (uint32_t)(sk * SL + mp.SLX + misd + tid) * (uint32_t)sizeof(T);
+                        T *yk = ycol + (int64_t)k * mp.P;
+#pragma unroll
+                        for (int j = 0; j < PT; ++j) {
+                            constexpr uint32_t JB = MCT * sizeof(T);
+                            const T xc = xw[j][(H + r) % WN];
+                            T a0 = lds<T>(ad + j * JB) * xc;
+                            a0 = fma(wcen[j], xc, a0);
+                            T a1 = wmk[0] * xw[j][r % WN];
+#pragma unroll
+                            for (int o = 1; o < WN; ++o) a1 = fma(wmk[o], xw[j][(o + r) % WN], a1);
+#pragma unroll
+                            for (int e = 0; e < MS; e += 2) {
+                                a0 = fma(wsm[j][e], lds<T>(pa[e] + j * JB), a0);
+                                if (e + 1 < MS) a1 = fma(wsm[j][e + 1], lds<T>(pa[e + 1] + j * JB), a1);
+                            }
+                            T out = a0 + a1;
+                            if (EPI) {
+                                out = alpha * out + beta * xc;
+                                if (zcol != nullptr && valid[j]) out += gamma * zcol[(int64_t)k * mp.P + j * MCT];
+                            }
+                            if (valid[j]) yk[j * MCT] = out;
+                        }
+                        // plane k - H leaves the window: release its slot
+                        __syncwarp();
+                        if (k - H >= jfirst && lane == 0) m_arrive(empty + wrap(sk - H));
+                        if (++sk == NR) sk = 0;
+                        if (++sn == NR) { sn = 0; ++usen; }
+                    }
+                }
+            } else {
+            for (int kb = k0; kb < k1 && ok; kb += WN) {
+#pragma unroll
+            for (int r = 0; r < WN; ++r) {
+                const int k = kb + r;
+                if (k >= k1 || !ok) break;
                 if (k + H <= jlast) {
                     if (!m_wait(full + sn, (uint32_t)(usen & 1), &s_abort)) {
                         ok = false;
@@ -398,10 +483,10 @@ __global__ void __launch_bounds__(MTHREADS, 1)
                     }
                     const T *sx = ring + sn * SL + xoff0;
 #pragma unroll
-                    for (int j = 0; j < PT; ++j) xw[j][2 * H] = sx[j * MCT];
+                    for (int j = 0; j < PT; ++j) xw[j][(2 * H + r) % WN] = sx[j * MCT];
                 } else {
 #pragma unroll
-                    for (int j = 0; j < PT; ++j) xw[j][2 * H] = T(0);
+                    for (int j = 0; j < PT; ++j) xw[j][(2 * H + r) % WN] = T(0);
                 }
                 T wmk[WN];
 #pragma unroll
@@ -422,23 +507,23 @@ __global__ void __launch_bounds__(MTHREADS, 1)
                 if (plain_sm) {
 #pragma unroll
                     for (int j = 0; j < PT; ++j) {
-                        const T xc = xw[j][H];
+                        const T xc = xw[j][(H + r) % WN];
                         T a0 = ring[sdi + j * MCT] * xc;
                         a0 = fma(wcen[j], xc, a0);
-                        T a1 = wmk[0] * xw[j][0];
+                        T a1 = wmk[0] * xw[j][r % WN];
 #pragma unroll
-                        for (int o = 1; o < WN; ++o) a1 = fma(wmk[o], xw[j][o], a1);
+                        for (int o = 1; o < WN; ++o) a1 = fma(wmk[o], xw[j][(o + r) % WN], a1);
 #pragma unroll
                         for (int e = 0; e < MS; e += 2) {
                             a0 = fma(wsm[j][e], ring[pe[e] + j * MCT], a0);
                             if (e + 1 < MS) a1 = fma(wsm[j][e + 1], ring[pe[e + 1] + j * MCT], a1);
                         }
-                        T r = a0 + a1;
+                        T out = a0 + a1;
                         if (EPI) {
-                            r = alpha * r + beta * xc;
-                            if (zcol != nullptr && valid[j]) r += gamma * zcol[(int64_t)k * mp.P + j * MCT];
+                            out = alpha * out + beta * xc;
+                            if (zcol != nullptr && valid[j]) out += gamma * zcol[(int64_t)k * mp.P + j * MCT];
                         }
-                        if (valid[j]) yk[j * MCT] = r;
+                        if (valid[j]) yk[j * MCT] = out;
                     }
                 } else {
                     T wpk[MS];
@@ -446,34 +531,32 @@ __global__ void __launch_bounds__(MTHREADS, 1)
                     for (int e = 0; e < MS; ++e) wpk[e] = wp[k * MS + e];
 #pragma unroll
                     for (int j = 0; j < PT; ++j) {
-                        const T xc = xw[j][H];
+                        const T xc = xw[j][(H + r) % WN];
                         T a0 = ring[sdi + j * MCT] * xc;
                         a0 = fma(wcen[j], xc, a0);
-                        T a1 = wmk[0] * xw[j][0];
+                        T a1 = wmk[0] * xw[j][r % WN];
 #pragma unroll
-                        for (int o = 1; o < WN; ++o) a1 = fma(wmk[o], xw[j][o], a1);
+                        for (int o = 1; o < WN; ++o) a1 = fma(wmk[o], xw[j][(o + r) % WN], a1);
 #pragma unroll
                         for (int e = 0; e < MS; e += 2) {
                             a0 = fma(wsm[j][e] * wpk[e], ring[pe[e] + j * MCT], a0);
                             if (e + 1 < MS) a1 = fma(wsm[j][e + 1] * wpk[e + 1], ring[pe[e + 1] + j * MCT], a1);
                         }
-                        T r = a0 + a1;
+                        T out = a0 + a1;
                         if (EPI) {
-                            r = alpha * r + beta * xc;
-                            if (zcol != nullptr && valid[j]) r += gamma * zcol[(int64_t)k * mp.P + j * MCT];
+                            out = alpha * out + beta * xc;
+                            if (zcol != nullptr && valid[j]) out += gamma * zcol[(int64_t)k * mp.P + j * MCT];
                         }
-                        if (valid[j]) yk[j * MCT] = r;
+                        if (valid[j]) yk[j * MCT] = out;
                     }
                 }
                 // plane k - H leaves the window: release its slot
                 __syncwarp();
                 if (k - H >= jfirst && lane == 0) m_arrive(empty + wrap(sk - H));
-#pragma unroll
-                for (int j = 0; j < PT; ++j)
-#pragma unroll
-                    for (int o = 0; o < 2 * H; ++o) xw[j][o] = xw[j][o + 1];
                 if (++sk == NR) sk = 0;
                 if (++sn == NR) { sn = 0; ++usen; }
+            }
+            }
             }
             // the run ends: release its planes still in the window
             if (ok) {
