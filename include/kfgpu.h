@@ -183,9 +183,9 @@ typedef struct {
     double mixed_switch;       /* MIXED: FP32 phase stops when every active residual is below
                                   mixed_switch * ||H|| (||H|| = gershgorin bound)              */
     int32_t fallback_iters;    /* warm start judge: after this many iterations ...             */
-    double fallback_resid;     /* ... a largest residual above this (absolute, energy units)
-                                  restarts a warm-started solve from a random block (0
-                                  disables); the judge of a learned warm start                 */
+    double fallback_resid;     /* ... a largest residual of the m warm-start columns above this
+                                  (absolute, energy units) restarts a warm-started solve from a
+                                  random block (0 disables); the judge of a learned warm start */
     int32_t seed_kind;         /* LOBPCG / Chebyshev `seed` (src/tree.jl:66-87, 293-321):
                                   KF_SEED_PRODUCT (default) or KF_SEED_RANDOM; used when
                                   kf_solve's seed argument is NULL                             */

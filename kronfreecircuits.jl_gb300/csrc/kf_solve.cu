@@ -197,6 +197,7 @@ struct LobParams {
     bool stall_exit;        // FP32 phase: leave when the residuals stop falling
     int judge_iters;        // warm-start judge: iteration at which ...
     double judge_resid;     // ... a largest residual above this aborts (0 = off)
+    int judge_cols = 0;     // ... among the first judge_cols columns (the warm block's m; 0: all checked)
 };
 
 struct LobOut {
@@ -508,7 +509,12 @@ static LobOut lobpcg_run(kf_op *op, LobWork<T> &Wk, const double *D, const LobPa
             std::fprintf(stderr, "kf lobpcg %s it=%d locked=%d(+%d) active_resid=[%.3e, %.3e]\n", sizeof(T) == 4 ? "f32" : "f64",
                          it, nl, newly, bestr, worst);
         if (!std::isfinite(worst)) throw Error(KF_ENOTFINITE, "LOBPCG: the residual block is not finite");
-        if (prm.judge_resid > 0 && it == prm.judge_iters && worst > prm.judge_resid) {
+        double judged = worst;
+        if (prm.judge_cols > 0) {
+            judged = 0;
+            for (int j = nl; j < std::min(prm.judge_cols, ncc); ++j) judged = std::max(judged, res[j]);
+        }
+        if (prm.judge_resid > 0 && it == prm.judge_iters && judged > prm.judge_resid) {
             out.judged_bad = true;
             break;
         }
@@ -1049,6 +1055,9 @@ static void solve_lobpcg(kf_op *op, const kf_solver_opts &o, int m, const double
     if (X0) st.warm = 1;
     LobParams p64{o.tol, o.maxiter, o.preconditioner, o.eta, w, 1e-12, false, o.fallback_iters,
                   o.fallback_resid > 0 ? o.fallback_resid : 0.0};
+    // the judge looks at the warm block's m columns: the guards and buffers come from the product
+    // seed, the method without the warm start
+    p64.judge_cols = m;
     std::vector<double> theta;
     LobOut r;
     const double t0 = now_s();

@@ -38,6 +38,21 @@ def test_warm_start_beats_random_start(trained):
     assert warm < rand, (warm, rand)
 
 
+def test_warm_start_against_the_product_seed(trained):
+    """The solver's default start, the product seed, is the other baseline: on this weakly coupled
+    circuit its product states are already close to the eigenvectors (3-5 iterations), closer
+    than the network's block, so the learned start does not beat it; pinned here: the same
+    eigenvalues, and the learned start within one and a half iterations of the product seed on
+    average."""
+    W, ws, _ = trained
+    rows = W.evaluate(ws, W.sample_thetas(24, seed=98), product_arm=True)
+    warm = np.mean([r["warm_iters"] for r in rows])
+    prod = np.mean([r["product_iters"] for r in rows])
+    assert warm <= prod + 1.5, (warm, prod)
+    for r in rows:
+        assert np.max(np.abs(r["E_warm"] - r["E_product"])) < 1e-9 * np.max(np.abs(r["E"]))
+
+
 def test_untrained_network_is_judged_and_replaced(cuda):
     from kfgpu import warmstart as W
     th = W.sample_thetas(4, seed=5)
