@@ -10,6 +10,7 @@
 #include <stdexcept>
 #include <string>
 #include <future>
+#include <map>
 #include <vector>
 
 #include "../../include/kfgpu.h"
@@ -92,6 +93,17 @@ struct ChainTerm {
     std::vector<ChainFactor> f;
 };
 
+// Dense pairwise couplings on a three-axis basis (kf_pairs.cu): pairs (0,1), (0,2), (1,2), each
+// g A (x) B with the factors' data at off[pair][0 / 1] in the chain pools
+struct PairPlan {
+    int ok;
+    int d[3];
+    int has[3];
+    double g[3];
+    size_t off[3][2];
+    int share0, share1, share2;   // the axis-0 matrices of (0,1), (0,2) equal; axis 1 of (0,1), (1,2); axis 2 of (0,2), (1,2)
+};
+
 // tensor-core mode products (kf_tc.cu): a d x d operator (d <= 256) as a BF16 image in the
 // tcgen05 K-major shared-memory layout, rows padded to Mp (128 or 256), columns to Kp
 struct TcMatrix {
@@ -131,9 +143,8 @@ struct kf_op {
     cudaStream_t stream = nullptr;
     bool own_stream = true;
     kf::ApplyPlan plan{};
-    int apply_variant[16] = {-1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1};
+    std::map<int, int> apply_tuned;    // fused-apply variant per (precision, block width)
     int force_variant = -1;   // test-only: run this fused-apply variant instead of the tuned one
-    float apply_variant_ms[16] = {};
     int64_t N = 0;
     std::vector<int64_t> dims;
     std::vector<int64_t> strides;
@@ -145,6 +156,7 @@ struct kf_op {
     float *d_w32 = nullptr;
     // dense-chain terms and their data (FP64 and FP32 copies)
     std::vector<kf::ChainTerm> chains;
+    kf::PairPlan pairs{};                  // the chains as dense pairwise couplings, when they are
     std::vector<kf::TcMatrix> chain_tc;   // tensor-core images of dense chain factors (FP32 applies)
     double *d_chain64 = nullptr;
     float *d_chain32 = nullptr;
@@ -205,6 +217,13 @@ template <typename T>
 void launch_apply_march(kf_op *op, const MarchPlan &mp, const T *D, const T *W, const T *X, T *Y, int64_t ldx,
                         int64_t ldy, int64_t b, T alpha, T beta, const T *Z, int64_t ldz, T gamma, int epi,
                         cudaStream_t s);
+
+// dense pairwise couplings (kf_pairs.cu)
+void pairs_plan(kf_op *op, const std::vector<std::vector<double>> &hdata);
+size_t pairs_smem_bytes(const PairPlan &pp, size_t elem);
+template <typename T>
+void apply_pairs(const kf_op *op, const T *X, int64_t ldx, T *Y, int64_t ldy, int64_t b, const T *D, int accumulate,
+                 T *scratch, cudaStream_t s);
 
 // kernels of kf_op.cu
 void launch_apply(kf_op *op, bool f32, const void *X, void *Y, int64_t ldx, int64_t ldy, int64_t b,

@@ -189,9 +189,9 @@ __global__ void k_axpby_cols(T *__restrict__ Y, int64_t ldy, const T *__restrict
 static std::mutex g_tune_mu;
 static std::map<std::string, int> g_tune;
 
-static std::string tune_key(const kf_op *op, int slot) {
+static std::string tune_key(const kf_op *op, int width) {
     const ApplyPlan &P = op->plan;
-    std::string k = std::to_string(op->device) + ":" + std::to_string(slot) + ":" + std::to_string(P.N) + ":" +
+    std::string k = std::to_string(op->device) + ":" + std::to_string(width) + ":" + std::to_string(P.N) + ":" +
                     std::to_string(P.ne);
     for (int a = 0; a < P.ndims; ++a) k += "," + std::to_string(P.dims[a]);
     for (int e = 0; e < P.ne; ++e) {
@@ -225,6 +225,29 @@ static void apply_t(kf_op *op, const T *X, T *Y, int64_t ldx, int64_t ldy, int64
     const bool chains = !op->chains.empty();
     const bool trivial_epi = alpha == 1.0 && beta == 0.0 && (Z == nullptr || gamma == 0.0);
     const int epi = (!chains && !trivial_epi) ? 1 : 0;
+    // dense pairwise couplings: two passes (kf_pairs.cu) instead of the chains; without banded or
+    // shift terms the pair kernel also forms D X, so the fused pass is skipped
+    const bool pairs = chains && op->pairs.ok && pairs_smem_bytes(op->pairs, sizeof(T)) <= 200 * 1024;
+    auto chain_scratch = [&]() -> T * {
+        const size_t need = (size_t)2 * op->N * b * sizeof(T);
+        if (op->scratch_bytes < need) {
+            if (op->d_scratch) KF_CUDA(cudaFree(op->d_scratch));
+            op->d_scratch = nullptr;
+            op->scratch_bytes = 0;
+            KF_CUDA(cudaMalloc(&op->d_scratch, need));
+            op->scratch_bytes = need;
+        }
+        return (T *)op->d_scratch;
+    };
+    if (pairs && op->plan.ne == 0 && op->force_variant < 0) {
+        apply_pairs<T>(op, X, ldx, Y, ldy, b, D, 0, chain_scratch(), s);
+        if (!trivial_epi) {
+            const unsigned g2 = (unsigned)((N * b + 255) / 256);
+            k_axpby_cols<T><<<g2, 256, 0, s>>>(Y, ldy, X, ldx, Z, ldz, N, (int)b, (T)alpha, (T)beta, (T)gamma);
+            KF_LAUNCH_CHECK();
+        }
+        return;
+    }
     const int ne = op->plan.ne;
     // the plane-marching kernel (variant 5) where its geometry applies and X is 16-byte aligned
     MarchPlan mp;
@@ -253,64 +276,72 @@ static void apply_t(kf_op *op, const T *X, T *Y, int64_t ldx, int64_t ldy, int64
 #undef KF_FUSED
         KF_LAUNCH_CHECK();
     };
-    // autotune: on the first apply of a block this wide (per precision), time every variant on the
-    // caller's own buffers (each overwrites Y completely with the same result) and keep the fastest;
-    // each variant's time is the best of three batches of four launches (one batch of three picked
-    // differently from process to process)
-    const int slot = (f32 ? 1 : 0) * 8 + (b >= 32 ? 3 : b >= 16 ? 2 : b >= 4 ? 1 : 0);
-    // operators of the same stencil shape (a parameter sweep rebuilds the same structure with new
-    // coefficients) share one tuning per process and device
-    const std::string key = tune_key(op, slot);
+    // autotune: on the first apply of a block this wide (per precision; widths above 64 share one
+    // choice), time every variant on the caller's own buffers (each overwrites Y completely with the
+    // same result) and keep the fastest; each variant's time is the best of three batches of four
+    // launches (one batch of three picked differently from process to process)
+    const int wkey = (f32 ? 1 << 20 : 0) | (int)std::min<int64_t>(b, 65);
     if (op->force_variant >= 0) {
         run(op->force_variant);
         goto chained;
     }
-    if (op->apply_variant[slot] < 0) {
-        std::lock_guard<std::mutex> lk(g_tune_mu);
-        auto it = g_tune.find(key);
-        if (it != g_tune.end()) op->apply_variant[slot] = it->second;
-    }
-    if (op->apply_variant[slot] < 0) {
-        cudaEvent_t e0, e1;
-        KF_CUDA(cudaEventCreate(&e0));
-        KF_CUDA(cudaEventCreate(&e1));
-        float best = 1e30f;
-        int bestv = 0;
-        for (int v = 0; v < KF_APPLY_VARIANTS; ++v) {
-            if (v == 5 && !march_ok) continue;
-            run(v);                                   // warm
-            float vbest = 1e30f;
-            for (int batch = 0; batch < 3; ++batch) {
-                KF_CUDA(cudaEventRecord(e0, s));
-                for (int r = 0; r < 4; ++r) run(v);
-                KF_CUDA(cudaEventRecord(e1, s));
-                KF_CUDA(cudaEventSynchronize(e1));
-                float ms = 0;
-                KF_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-                vbest = std::min(vbest, ms);
+    {
+        auto hit = op->apply_tuned.find(wkey);
+        int chosen = hit != op->apply_tuned.end() ? hit->second : -1;
+        if (chosen < 0) {
+            // operators of the same stencil shape (a parameter sweep rebuilds the same structure
+            // with new coefficients) share one tuning per process and device
+            const std::string key = tune_key(op, wkey);
+            {
+                std::lock_guard<std::mutex> lk(g_tune_mu);
+                auto it = g_tune.find(key);
+                if (it != g_tune.end()) chosen = it->second;
             }
-            if (vbest < best) { best = vbest; bestv = v; }
+            if (chosen < 0) {
+                cudaEvent_t e0, e1;
+                KF_CUDA(cudaEventCreate(&e0));
+                KF_CUDA(cudaEventCreate(&e1));
+                float best = 1e30f;
+                int bestv = 0;
+                for (int v = 0; v < KF_APPLY_VARIANTS; ++v) {
+                    if (v == 5 && !march_ok) continue;
+                    run(v);                                   // warm
+                    float vbest = 1e30f;
+                    for (int batch = 0; batch < 3; ++batch) {
+                        KF_CUDA(cudaEventRecord(e0, s));
+                        for (int r = 0; r < 4; ++r) run(v);
+                        KF_CUDA(cudaEventRecord(e1, s));
+                        KF_CUDA(cudaEventSynchronize(e1));
+                        float ms = 0;
+                        KF_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+                        vbest = std::min(vbest, ms);
+                    }
+                    if (vbest < best) { best = vbest; bestv = v; }
+                }
+                cudaEventDestroy(e0);
+                cudaEventDestroy(e1);
+                chosen = bestv;
+                std::lock_guard<std::mutex> lk(g_tune_mu);
+                g_tune[key] = bestv;
+            }
+            op->apply_tuned[wkey] = chosen;
         }
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
-        op->apply_variant[slot] = bestv;
-        op->apply_variant_ms[slot] = best / 4;
-        std::lock_guard<std::mutex> lk(g_tune_mu);
-        g_tune[key] = bestv;
+        run(chosen);
     }
-    run(op->apply_variant[slot]);
 chained:
     if (!chains) return;
-    // dense-containing terms: chain through scratch, one contiguous (N x b) block per buffer
-    const size_t need = (size_t)2 * N * b * sizeof(T);
-    if (op->scratch_bytes < need) {
-        if (op->d_scratch) KF_CUDA(cudaFree(op->d_scratch));
-        op->d_scratch = nullptr;
-        op->scratch_bytes = 0;
-        KF_CUDA(cudaMalloc(&op->d_scratch, need));
-        op->scratch_bytes = need;
+    if (pairs) {
+        apply_pairs<T>(op, X, ldx, Y, ldy, b, nullptr, 1, chain_scratch(), s);
+        if (!trivial_epi) {
+            const unsigned g3 = (unsigned)((N * b + 255) / 256);
+            k_axpby_cols<T><<<g3, 256, 0, s>>>(Y, ldy, X, ldx, Z, ldz, N, (int)b, (T)alpha, (T)beta, (T)gamma);
+            KF_LAUNCH_CHECK();
+        }
+        return;
     }
-    T *buf[2] = {(T *)op->d_scratch, (T *)op->d_scratch + N * b};
+    // dense-containing terms: chain through scratch, one contiguous (N x b) block per buffer
+    T *sbuf = chain_scratch();
+    T *buf[2] = {sbuf, sbuf + N * b};
     const T *cdata = f32 ? (const T *)op->d_chain32 : (const T *)op->d_chain64;
     const int64_t total = N * b;
     const unsigned g2 = (unsigned)((total + 255) / 256);
@@ -856,6 +887,7 @@ void build_op(const kf_op_desc *desc, kf_op *op) {
                 ++q;
             }
     }
+    pairs_plan(op, chain_data);
     // host-side derived quantities
     op->h_diag = D;
     double dmax = -INFINITY;

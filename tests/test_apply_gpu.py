@@ -346,3 +346,52 @@ def test_every_point_variant_agrees(cuda, f32):
         _abi.check(_abi.lib().kf_test_apply_variant(H.handle, v, C.c_void_p(X.data_ptr()), C.c_void_p(Y.data_ptr()), N,
                                                     b, flags, 1, None))
         assert np.max(np.abs(Y.double().cpu().numpy() - R)) / scale < tol, v
+
+
+@pytest.mark.parametrize("f32", [False, True])
+@pytest.mark.parametrize("case", ["parent48", "distinct", "only02", "only12", "p01_p12", "banded", "d12"])
+def test_dense_pair_terms(cuda, f32, case):
+    """Dense pairwise couplings g A (x) B on a three-axis basis (the two-pass pair path: a mode
+    product along the last axis, then per-slab register-blocked products) against the oracle's
+    term-by-term mul!: shared and distinct factor matrices, every subset of pairs, an extra banded
+    term (the fused pass first, the pairs accumulated), and the Chebyshev epilogue."""
+    torch = cuda
+    from kfgpu import ops as P
+    rng = np.random.default_rng(101)
+    d = 12 if case == "d12" else 48
+    dims = [d, d, d]
+
+    def sym(n):
+        A = rng.standard_normal((n, n))
+        return (A + A.T) / 2 / np.sqrt(n)
+
+    Ps = [sym(d) for _ in range(3)]
+    diag = [(1.0, [(a, P.DiagonalOp(np.sort(rng.uniform(0, 20, d))))]) for a in range(3)]
+    pairs = {"01": (0.3, [(0, P.DenseOp(Ps[0])), (1, P.DenseOp(Ps[1]))]),
+             "02": (0.2, [(0, P.DenseOp(Ps[0])), (2, P.DenseOp(Ps[2]))]),
+             "12": (0.4, [(1, P.DenseOp(Ps[1])), (2, P.DenseOp(Ps[2]))])}
+    if case == "distinct":
+        pairs["02"] = (0.2, [(0, P.DenseOp(sym(d))), (2, P.DenseOp(Ps[2]))])
+        pairs["12"] = (0.4, [(1, P.DenseOp(sym(d))), (2, P.DenseOp(sym(d)))])
+    keys = {"only02": ["02"], "only12": ["12"], "p01_p12": ["01", "12"]}.get(case, ["01", "02", "12"])
+    terms = diag + [pairs[k] for k in keys]
+    if case == "banded":
+        terms.append((0.7, [(1, P.BandedOp(d, [-1, 1], [rng.standard_normal(d), rng.standard_normal(d)]))]))
+    H, Ho = _pair(dims, terms, cap=8)
+    N, b = H.N, 6
+    dt = torch.float32 if f32 else torch.float64
+    X = torch.as_tensor(rng.standard_normal((b, N)), dtype=dt, device="cuda")
+    Y = torch.full_like(X, float("nan"))
+    H.apply_device(X.data_ptr(), Y.data_ptr(), b, f32=f32)
+    H.sync()
+    Xh = X.double().cpu().numpy().T
+    R = Ho.matvec(Xh)
+    tol = TOL32 if f32 else TOL64
+    scale = max(1.0, np.max(np.abs(R)))
+    assert np.max(np.abs(Y.double().cpu().numpy().T - R)) / scale < tol
+    Zt = torch.as_tensor(rng.standard_normal((b, N)), dtype=dt, device="cuda")
+    Y2 = torch.full_like(X, float("nan"))
+    H.apply_axpby_device(X.data_ptr(), Y2.data_ptr(), Zt.data_ptr(), b, 0.5, -0.25, 2.0, f32=f32)
+    H.sync()
+    R2 = 0.5 * R - 0.25 * Xh + 2.0 * Zt.double().cpu().numpy().T
+    assert np.max(np.abs(Y2.double().cpu().numpy().T - R2)) / max(1.0, np.max(np.abs(R2))) < tol
