@@ -121,6 +121,17 @@ int kf_op_apply_axpby(kf_op *op, const void *X, void *Y, const void *Z, int64_t 
 #define KF_NOALLOC_SCRATCH_BYTES (8u << 20)
 int kf_op_apply_noalloc(kf_op *op, const void *X, void *Y, int64_t ldx, int64_t ldy, int64_t b, int32_t flags);
 
+/* The port matrix W' H V (kw x kv, column-major, FP64, caller-owned HOST memory) of an operator H
+ * on a node's product basis, for column blocks V (N x kv) and W (N x kw; NULL: W = V), FP64, host
+ * (KF_HOST) or device pointers with leading dimensions ldv, ldw.  Replaces the formation of ports
+ * and joint ports on a node's kept vectors, V' (x)_a O_a V, in _assemble_node (src/materialize.jl:
+ * 426-441 _apply_ops / _port_matrix, :463-467 _node_port, :490-495 _joint_port, :505-517
+ * _real_sandwich): H is the port's one-term operator (port_operator, src/portoperator.jl:18-39) or,
+ * for a real expansion's component, the sum of its terms with their coefficients; the caller keeps
+ * the port's character (real, imaginary or both components) and phase fixing. */
+int kf_op_sandwich(kf_op *op, const double *W, int64_t ldw, int32_t kw, const double *V, int64_t ldv, int32_t kv,
+                   double *P_out, int32_t flags);
+
 /* diagonal(H) real part (src/apply.jl:455-478, _full_diagonal), N values into host memory. */
 int kf_op_diagonal(kf_op *op, double *out);
 

@@ -163,6 +163,63 @@ int kf_op_apply_axpby(kf_op *op, const void *X, void *Y, const void *Z, int64_t 
     });
 }
 
+int kf_op_sandwich(kf_op *op, const double *W, int64_t ldw, int32_t kw, const double *V, int64_t ldv, int32_t kv,
+                   double *P_out, int32_t flags) {
+    return guarded([&] {
+        KF_REQUIRE(op && V && P_out, KF_EINVAL, "kf_op_sandwich: NULL argument");
+        const int64_t N = op->N;
+        if (W == nullptr) {
+            W = V;
+            ldw = ldv;
+            kw = kv;
+        }
+        KF_REQUIRE(kv >= 1 && kw >= 1 && kv <= 4096 && kw <= 4096, KF_EINVAL,
+                   "kf_op_sandwich: the blocks must have 1..4096 columns");
+        KF_REQUIRE(ldv >= N && ldw >= N, KF_EDIM, "kf_op_sandwich: leading dimensions must be >= N");
+        cudaStream_t s = op->stream;
+        const bool host = (flags & KF_HOST) != 0;
+        double *dV = nullptr, *dW = nullptr, *dY = nullptr, *dG = nullptr, *dpart = nullptr;
+        auto cleanup = [&]() {
+            if (host) {
+                cudaFreeAsync(dV, s);
+                if (dW != dV) cudaFreeAsync(dW, s);
+            }
+            cudaFreeAsync(dY, s);
+            cudaFreeAsync(dG, s);
+            cudaFreeAsync(dpart, s);
+        };
+        try {
+            const double *Vd = V, *Wd = W;
+            int64_t lv = ldv, lw = ldw;
+            if (host) {
+                KF_CUDA(cudaMallocAsync((void **)&dV, (size_t)N * kv * 8, s));
+                KF_CUDA(cudaMemcpy2DAsync(dV, N * 8, V, ldv * 8, N * 8, kv, cudaMemcpyHostToDevice, s));
+                Vd = dV;
+                lv = N;
+                if (W == V) {
+                    dW = dV;
+                } else {
+                    KF_CUDA(cudaMallocAsync((void **)&dW, (size_t)N * kw * 8, s));
+                    KF_CUDA(cudaMemcpy2DAsync(dW, N * 8, W, ldw * 8, N * 8, kw, cudaMemcpyHostToDevice, s));
+                }
+                Wd = dW;
+                lw = N;
+            }
+            KF_CUDA(cudaMallocAsync((void **)&dY, (size_t)N * kv * 8, s));
+            KF_CUDA(cudaMallocAsync((void **)&dG, (size_t)kw * kv * 8, s));
+            KF_CUDA(cudaMallocAsync((void **)&dpart, kf::gram_partials_size(kw, kv, N), s));
+            kf::launch_apply(op, false, Vd, dY, lv, N, kv, 1.0, 0.0, nullptr, 0, 0.0, s);
+            kf::gram<double>(Wd, lw, kw, dY, N, kv, N, dG, dpart, s);
+            KF_CUDA(cudaMemcpyAsync(P_out, dG, (size_t)kw * kv * 8, cudaMemcpyDeviceToHost, s));
+            KF_CUDA(cudaStreamSynchronize(s));
+        } catch (...) {
+            cleanup();
+            throw;
+        }
+        cleanup();
+    });
+}
+
 int kf_op_diagonal(kf_op *op, double *out) {
     return guarded([&] {
         KF_REQUIRE(op && out, KF_EINVAL, "kf_op_diagonal: NULL argument");

@@ -1,6 +1,8 @@
 """Ports as operators on a node's product basis.
 
   port_operator(sys, key, node)        src/portoperator.jl:18-39
+  port_matrix(H, V, W)                 src/materialize.jl:426-517 (_apply_ops, _port_matrix,
+                                       _node_port, _joint_port, _real_sandwich): W' H V on the GPU
 
 The reference's `port_operator` returns a one-term `KronFreeOperator` (coefficient 1, one factor
 per keyed mode, identity on the other axes) on the product basis of `node`; each factor is the
@@ -11,6 +13,8 @@ application is the same fused / chained `mul!`.  Real factors only (diagonal, ba
 dense real matrices): every configuration measured here is real by structure.
 """
 from __future__ import annotations
+
+import ctypes as C
 
 import numpy as np
 
@@ -44,3 +48,20 @@ def port_operator(dims, key, block_capacity=1):
     H = KronFreeOperator(dims, [(1.0, key)], block_capacity=block_capacity)
     H.hermitian = all(_hermitian(op) for _, op in key)
     return H
+
+
+def port_matrix(H, V, W=None):
+    """W' H V (host FP64, kw x kv) for host blocks V (N x kv) and W (N x kw, default V): a port or
+    joint port of a node's kept vectors V when H is its port operator, one component of a real
+    expansion when H carries that component's terms (kf_op_sandwich)."""
+    Vf = np.asfortranarray(V, dtype=np.float64)
+    if Vf.ndim != 2 or Vf.shape[0] != H.N:
+        raise _abi.DimensionMismatch(_abi.KF_EDIM, f"port_matrix: V has shape {Vf.shape}, expected ({H.N}, k)")
+    Wf = None if W is None else np.asfortranarray(W, dtype=np.float64)
+    if Wf is not None and (Wf.ndim != 2 or Wf.shape[0] != H.N):
+        raise _abi.DimensionMismatch(_abi.KF_EDIM, f"port_matrix: W has shape {Wf.shape}, expected ({H.N}, k)")
+    kw = Vf.shape[1] if Wf is None else Wf.shape[1]
+    P = np.empty((kw, Vf.shape[1]), order="F")
+    _abi.check(_abi.lib().kf_op_sandwich(H.handle, None if Wf is None else Wf.ctypes.data, H.N, kw, Vf.ctypes.data,
+                                         H.N, Vf.shape[1], P.ctypes.data, _abi.KF_HOST))
+    return P

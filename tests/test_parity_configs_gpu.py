@@ -196,6 +196,7 @@ def test_leaf3_chebyshev_full_size_vs_oracle(cuda, leaf3):
 
 def test_leaf3_fixture_cross_checked(leaf3):
     """The fixture's draws were solved twice by unrelated iterations that agree."""
+    assert len(leaf3["xcheck"]) >= 1
     for d, x in leaf3["xcheck"].items():
         assert x["max_rel_diff_vs_oracle_lobpcg"] < 1e-10, d
 
@@ -346,3 +347,52 @@ def test_warm_start_eigenvalues_vs_oracle_dense(cuda):
                         X0=ws.blocks([th])[0])
         assert np.max(_resid(Ho, E, V)) <= W.tolerance(H)
         H.close()
+
+
+# ---------------------------------------------------------------------------------------------
+# port and joint-port formation on kept vectors (src/materialize.jl:426-517)
+
+def test_port_formation_matches_oracle(goldens, cuda):
+    """kf_op_sandwich: V' (x)_a O_a V for the kept vectors of the two-transmon leaves (the port n
+    and the non-Hermitian e^{i phi} shift port) and of a three-mode leaf (a banded port, and a joint
+    port on two axes), and W' H V with another block, against the oracle's explicit products
+    (oracle/tree.py _kept_port)."""
+    from kfgpu import circuits
+    from kfgpu.ports import port_matrix, port_operator
+    from kfgpu.ops import localop
+    from oracle import tree
+    th = goldens["goldens"]["two_transmons"]["params"]
+    for EJ, EC, ng in ((th["E_J1"], th["E_C1"], th["n_g1"]), (th["E_J2"], th["E_C2"], th["n_g2"])):
+        bases = {"varphi_1": kfref.ChargeBasis(30)}
+        Hl = kfref.KronFreeOperator([61], kfref.leaf_terms(goldens["specs"]["transmon"],
+                                                           dict(E_J=EJ, E_C=EC, n_g=ng), bases))
+        _, V = np.linalg.eigh(np.real(Hl.to_matrix()))
+        child = {"bases": bases, "vectors": V[:, :8]}
+        for kind, k in (("n", 0.0), ("expiphi", 1), ("expiphi", -1)):
+            Po = tree._kept_port(child, [("varphi_1", kind, k)])
+            assert np.max(np.abs(Po.imag)) == 0.0
+            Pg = port_matrix(port_operator([61], [(0, localop(circuits.ChargeBasis(30), kind, k))]), V[:, :8])
+            assert np.max(np.abs(Pg - Po.real)) < 1e-12 * max(1.0, np.max(np.abs(Po)))
+    # a small three-mode leaf (9 x 16 x 10): its lowest 10 states by the oracle's Dense
+    rng = np.random.default_rng(3)
+    kw = dict(ncut=4, n2=16, n3=10)
+    dims, terms = circuits.three_mode_leaf(circuits.three_mode_theta(rng), **kw)
+    _, Vm = osol.dense_solve(_oracle_op(dims, terms), 10)
+    Vm = np.ascontiguousarray(np.real(Vm))
+    b1, b2, b3 = circuits.three_mode_bases(**kw)
+    obases = {"q": kfref.ChargeBasis(4), "x": kfref.PhaseGrid(-4 * np.pi, 4 * np.pi, 16, 4),
+              "y": kfref.PhaseGrid(-3 * np.pi, 3 * np.pi, 10, 4)}
+    child = {"bases": obases, "vectors": Vm}
+    cases = [([("x", "n2", 0.0)], [(1, localop(b2, "n2"))]),
+             ([("q", "n", 0.0), ("y", "phi2", 0.0)], [(0, localop(b1, "n")), (2, localop(b3, "phi2"))]),
+             ([("q", "expiphi", 1), ("x", "phi", 0.0)], [(0, localop(b1, "expiphi", 1)), (1, localop(b2, "phi"))])]
+    for ofactors, key in cases:
+        Po = tree._kept_port(child, ofactors)
+        assert np.max(np.abs(Po.imag)) < 1e-13
+        Pg = port_matrix(port_operator(dims, key), Vm)
+        assert np.max(np.abs(Pg - Po.real)) < 1e-12 * max(1.0, np.max(np.abs(Po)))
+    # W' H V with a different left block, device-side blocks through the same entry point
+    W = rng.standard_normal((Vm.shape[0], 4))
+    Hp = port_operator(dims, cases[1][1])
+    ref = W.T @ _oracle_op(dims, [(1.0, cases[1][1])]).matvec(Vm)
+    assert np.max(np.abs(port_matrix(Hp, Vm, W) - ref)) < 1e-11 * max(1.0, np.max(np.abs(ref)))
