@@ -7,9 +7,10 @@
 // src/chebyshev.jl:68-81) are tall-skinny: N rows, a few dozen columns.  On the SIMT pipes they are
 // FMA-bound and their cost grows with the output; here every element is read from memory once.
 //
-// What bounds this kernel is the number of MMAs, not their width: a kind::tf32 MMA consumes K = 8
-// rows and, measured, costs about the same at N = 16 as at N = 112 (about 100 cycles).  So the
-// images are laid out to let one wide MMA carry several of the split products:
+// A kind::tf32 MMA (M = 128, K = 8) costs 44.5 cycles at N = 16, 48 at N = 64 and 64 at N = 128
+// (measured alone on GB300: the tensor core reads its operands at about 128 bytes per cycle), so
+// one wide MMA that carries several of the split products is cheaper than several narrow ones, and
+// the images are laid out for that:
 //   the pool (up to four source blocks, each starting at a multiple of 8 rows) puts the sources
 //   that only give rows of G first and the B sources (the columns of G) last, ending at row RB of
 //   the hi image; the lo image follows it and starts with the B rows (then the others).  The B
@@ -26,11 +27,13 @@
 // The epilogue adds hi*hi + hi*lo on the lanes of the hi rows and lo*hi on the lanes of the lo
 // rows into two FP32 partial sets per CTA; the reduction sums both.
 //
-// Measured on GB300, a kind::tf32 MMA with M = 128 occupies the tensor core for a fixed ~150 ns
-// whatever its N (16 .. 256): this kernel is bound by the count of MMAs, one per 8 rows (RB = 64) or
-// two (RB = 128), about 80 us per 671,744 rows for the one-MMA layout.  Two accumulator slots and
-// producers that refill the stage of chunk t - 2 keep the tensor core fed (four slots and a refill
-// distance of four measured slower).
+// The MMAs are not what bounds it: a 32-row chunk takes ~1,100 cycles per SM against ~200 for its
+// MMAs.  A clock64 timeline of one CTA shows the producers waiting for data requested several
+// microseconds earlier: the loads deliver well under the 4.8-5.0 TB/s that a plain cp.async stream
+// of the same column pieces reaches.  In timing-only copies, dropping the split, the MMAs, the
+// epilogue's loads or the proxy fence each changed the time by under 10%, and so did a variant with
+// 128-byte-swizzled images, 256-byte column runs, four accumulator slots, one barrier arrival per
+// warp, suspended waits and other ring depths.
 //
 // One persistent CTA per SM (or per chunk when there are fewer), warp-specialised:
 //   warps 0-7   producers: 16-byte cp.async copies of their pieces of the chunk straight into the
@@ -158,7 +161,7 @@ struct GtArgs {
     int nsrc;
     int64_t N;
     int64_t nchunks;
-    int b_off, nbr;                // B rows: hi rows [b_off, RB) = lo rows [0, nbr); nbr % 16 == 0
+    int b_off, nbr;                // B rows: hi rows [b_off, RB) = lo rows [0, nbr); nbr % 8 == 0
                                    // (SPLIT: stage rows RB + [0, nbr) and RB + nbr + [0, nbr))
     int nr, nc;                    // output entries (nr x nc, column-major)
     uint8_t rinv_hi[128];          // hi image row -> output row (255: not wanted)
@@ -481,7 +484,9 @@ bool gram_tc(const GramTcSrc *src, int nsrc, int r0, int r1, int c0, int c1, int
         cspan = (cspan + src[q].k + 7) / 8 * 8;
         order.push_back(q);
     }
-    const int nbr = (cspan + 15) / 16 * 16;
+    // B columns in whole 8-row groups (the MMA's N = 2 nbr stays a multiple of 16): [X Z]'Z at
+    // block 18 (24 + 40 pool rows) then fits the one-MMA layout
+    const int nbr = cspan;
     if (nbr > GT_NBR_MAX) return false;
     const int RB = aspan + nbr <= 64 ? 64 : aspan + nbr <= 128 ? 128 : 0;
     if (!RB) return false;

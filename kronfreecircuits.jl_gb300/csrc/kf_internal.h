@@ -143,7 +143,7 @@ struct kf_op {
     cudaStream_t stream = nullptr;
     bool own_stream = true;
     kf::ApplyPlan plan{};
-    std::map<int, int> apply_tuned;    // fused-apply variant per (precision, block width)
+    std::map<int, int> apply_tuned;    // fused-apply variant per (precision, 4-column width class)
     int force_variant = -1;   // test-only: run this fused-apply variant instead of the tuned one
     int64_t N = 0;
     std::vector<int64_t> dims;
@@ -228,6 +228,10 @@ void apply_pairs(const kf_op *op, const T *X, int64_t ldx, T *Y, int64_t ldy, in
 // kernels of kf_op.cu
 void launch_apply(kf_op *op, bool f32, const void *X, void *Y, int64_t ldx, int64_t ldy, int64_t b,
                   double alpha, double beta, const void *Z, int64_t ldz, double gamma, cudaStream_t s);
+
+// run the fused apply's tuner now for every width class up to maxb columns not yet tuned for this
+// operator's stencil shape (X, Y: N x maxb device blocks, leading dimension ld, contents unused)
+void pretune_apply(kf_op *op, bool f32, const void *X, void *Y, int64_t ld, int maxb, cudaStream_t s);
 
 // dense linear algebra on tall-skinny blocks (kf_blas.cu); T = float or double.
 // Column-major blocks with leading dimension ld.

@@ -202,6 +202,9 @@ static std::string tune_key(const kf_op *op, int width) {
     return k;
 }
 
+// the tuner's width class of a block of b columns (classes of four columns; widths above 64 share one)
+static int tune_class(bool f32, int64_t b) { return (f32 ? 1 << 20 : 0) | (int)((std::min<int64_t>(b, 65) + 3) / 4); }
+
 // streaming multiprocessors of a device (cached per device)
 static int num_sms(int dev) {
     static std::mutex mu;
@@ -276,11 +279,12 @@ static void apply_t(kf_op *op, const T *X, T *Y, int64_t ldx, int64_t ldy, int64
 #undef KF_FUSED
         KF_LAUNCH_CHECK();
     };
-    // autotune: on the first apply of a block this wide (per precision; widths above 64 share one
-    // choice), time every variant on the caller's own buffers (each overwrites Y completely with the
-    // same result) and keep the fastest; each variant's time is the best of three batches of four
-    // launches (one batch of three picked differently from process to process)
-    const int wkey = (f32 ? 1 << 20 : 0) | (int)std::min<int64_t>(b, 65);
+    // autotune: on the first apply of a block in this width class (per precision; classes of four
+    // columns, widths above 64 share one), time every variant on the caller's own buffers (each
+    // overwrites Y completely with the same result) and keep the fastest; each variant's time is the
+    // best of three batches of four launches.  Classes rather than exact widths: locking shrinks
+    // the active block one column at a time, and a tuning costs about 80 launches
+    const int wkey = tune_class(f32, b);
     if (op->force_variant >= 0) {
         run(op->force_variant);
         goto chained;
@@ -454,6 +458,27 @@ void launch_apply(kf_op *op, bool f32, const void *X, void *Y, int64_t ldx, int6
         apply_t<float>(op, (const float *)X, (float *)Y, ldx, ldy, b, alpha, beta, (const float *)Z, ldz, gamma, s);
     else
         apply_t<double>(op, (const double *)X, (double *)Y, ldx, ldy, b, alpha, beta, (const double *)Z, ldz, gamma, s);
+}
+
+void pretune_apply(kf_op *op, bool f32, const void *X, void *Y, int64_t ld, int maxb, cudaStream_t s) {
+    if (op->force_variant >= 0 || op->N == 0) return;
+    const bool pairs = !op->chains.empty() && op->pairs.ok &&
+                       pairs_smem_bytes(op->pairs, f32 ? 4 : 8) <= 200 * 1024;
+    if (pairs && op->plan.ne == 0) return;   // the pair kernel is not tuned
+    for (int b = 4; b < maxb + 4; b += 4) {
+        const int bb = std::min(b, maxb);
+        const int wkey = tune_class(f32, bb);
+        if (op->apply_tuned.count(wkey)) continue;
+        {
+            std::lock_guard<std::mutex> lk(g_tune_mu);
+            auto it = g_tune.find(tune_key(op, wkey));
+            if (it != g_tune.end()) {
+                op->apply_tuned[wkey] = it->second;
+                continue;
+            }
+        }
+        launch_apply(op, f32, X, Y, ld, ld, bb, 1, 0, nullptr, 0, 0, s);
+    }
 }
 
 // ------------------------------------------------------------------------------------------

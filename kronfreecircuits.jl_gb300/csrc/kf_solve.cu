@@ -1068,6 +1068,10 @@ static void solve_lobpcg(kf_op *op, const kf_solver_opts &o, int m, const double
         int64_t nmv32 = 0;
         if (o.precision == KF_PREC_MIXED) {
             LobWork<float> W32(N, wi);
+            // every width class the solve applies H to is tuned here, not in the middle of the
+            // iteration (the active block narrows one column at a time as columns lock)
+            pretune_apply(op, true, W32.Z.p, W32.HZ.p, N, 2 * wi, s);
+            pretune_apply(op, false, W64.Z.p, W64.HZ.p, N, wi, s);
             convert<double, float>(W64.X.as<double>(), N, W32.X.as<float>(), N, wi, N, s);
             LobParams p32 = q;
             p32.lock_tol = std::max(o.tol, o.mixed_switch * hn);
@@ -1093,6 +1097,7 @@ static void solve_lobpcg(kf_op *op, const kf_solver_opts &o, int m, const double
             r.nmv += nmv32;
             return;
         }
+        pretune_apply(op, false, W64.Z.p, W64.HZ.p, N, 2 * wi, s);
         const double tf = now_s();
         r = lobpcg_run<double>(op, W64, dD.as<double>(), q, s, theta);
         st.seconds_f64 = now_s() - tf;

@@ -52,9 +52,11 @@ def _blocks(torch, widths, N, ld=None, seed=0):
 
 
 POOLS = [
-    # (widths, r0, r1, c0, c1, N); the pools up to 64 rows take one MMA per K step, the others two
+    # (widths, r0, r1, c0, c1, N); the pools up to 64 rows (sources in 8-row groups) take one MMA per
+    # K step, the others two
     ((16, 32), 0, 2, 1, 2, 671744),              # [X Z]'Z, block 16 (64-row pool)
-    ((20, 40), 0, 2, 1, 2, 671744),              # [X Z]'Z, block 20 (128-row pool)
+    ((20, 40), 0, 2, 1, 2, 671744),              # [X Z]'Z, block 20 (24 + 40 rows: one MMA)
+    ((20, 44), 0, 2, 1, 2, 131072),              # 24 + 48 rows: two MMAs per K step
     ((16, 32, 16, 32), 0, 2, 2, 4, 671744),      # [X_a Q]'[HX_a HZ]
     ((20, 40, 20, 40), 0, 2, 2, 4, 671744),      # also the refinement's [X_a Q]'[R HZ]
     ((8, 16, 24), 0, 2, 1, 3, 131072),           # a source both in the rows and the columns
