@@ -19,14 +19,15 @@ fresh FP64 application.
   e2e              the public API end to end with host buffers: kf_op_create from the host term
                    list, solve (product seed built by the library), host eigenpairs out, kf_op_destroy,
                    every step
-  roofline         the dominant kernel of a warm solve by the ncu launch list (its template
-                   instantiations summed), the fused stencil apply: algorithmic bytes 2 N b 4 per
-                   launch (16 columns) over its CUDA-event time, against the measured HBM copy
-                   bandwidth; roofline_update / roofline_mode / roofline_gram: the tcgen05 FP32 block
-                   update on the fused X/P Rayleigh-Ritz shape ([X_a Q] C, 18 + 36 -> 36 columns,
-                   (54 + 36) N 4), the separable preconditioner's tcgen05 mode product (256-point
-                   axis, 18 columns, 2 N b 4) and the tensor-core Gram of the orthogonalisation
-                   ([X Z]'Z, 18 + 36 columns, N b 4)
+  roofline         the kernel with the largest share of a warm solve's ncu launch list (its
+                   template instantiations summed): the tensor-core FP32 Gram, on the
+                   orthogonalisation's [X Z]'Z (18 + 36 columns): algorithmic bytes (18 + 36) N 4 per
+                   launch over its CUDA-event time, against the measured HBM copy bandwidth;
+                   roofline_apply / roofline_update / roofline_mode: the fused stencil apply
+                   (16 FP32 columns, 2 N b 4), the tcgen05 FP32 block update on the fused X/P
+                   Rayleigh-Ritz shape ([X_a Q] C, 18 + 36 -> 36 columns, (54 + 36) N 4) and the
+                   separable preconditioner's tcgen05 mode product (256-point axis, 18 columns,
+                   2 N b 4)
   dense / batch / warmstart
                    the other configurations, each with its own value, eigenvalue error against the
                    oracle's fixture and roofline: the 48^3 dense parent, the batched sweep of 704
@@ -72,10 +73,10 @@ NDRAWS = 64
 # in L2);
 # the tensor-core Gram of [X Z]'Z at 18 + 36 columns (reads 145.2 MB = every element once, writes
 # 0.1 MB of partials)
-APPLY_TRAFFIC_BYTES = 55641088
+APPLY_TRAFFIC_BYTES = 47563520     # ncu dram bytes read + written, one 16-column k_apply_march launch
 MODE_TRAFFIC_BYTES = 50463488
 UPDATE_TRAFFIC_BYTES = 200817152   # ncu dram bytes read + written, one launch (the rest of Y stays in L2)
-GRAM_TC_TRAFFIC_BYTES = 145235200
+GRAM_TC_TRAFFIC_BYTES = 145209856   # ncu dram bytes, one [X Z]'Z launch (one-MMA layout)
 
 
 # the workload both arms report (the reference arm prints the same dict)
@@ -319,9 +320,9 @@ def run_ours(args, D):
     te = D.max(time.perf_counter() - t0)
     conv_e = D.sum(conv_e)
     err_e, _ = leaf3_err(Es_e)
-    # roofline of the dominant kernel of a warm solve (by the ncu launch list: the fused stencil
-    # apply), of the tcgen05 block update on the fused X/P Rayleigh-Ritz shape, of the
-    # preconditioner's mode product and of the tensor-core Gram
+    # roofline of the dominant kernel of a warm solve (by the ncu launch list: the tensor-core Gram),
+    # of the fused stencil apply, of the tcgen05 block update on the fused X/P Rayleigh-Ritz shape and
+    # of the preconditioner's mode product
     H0 = ops[idx[0]]
     peak, kind = peaks()
     t_upd = time_update(torch, 1, 18, 36, 36, H0.N)
@@ -361,9 +362,16 @@ def run_ours(args, D):
         "iterations": [s["iterations"] for s in stats], "iterations_f64_phase": [s["iterations_f64"] for s in stats],
         "e2e": {"value": conv_e / te, "unit": "eigenpairs/s", "h2d_bytes_per_step": int(h2d / ke),
                 "d2h_bytes_per_step": int(d2h / ke), "steps": ke, "max_rel_eig_err": err_e},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": APPLY_TRAFFIC_BYTES, "kernel": "k_apply_fused<float> (fused stencil apply, 16 columns, the tuned variant)",
-                     "algorithmic_bytes": alg, "launch_us": t_apply * 1e6, "peak_kind": kind},
+        "roofline": {"bound": "hbm", "achieved": alg_gram / t_gram / 1e9, "peak": peak, "unit": "GB/s",
+                     "frac": alg_gram / t_gram / 1e9 / peak, "traffic": GRAM_TC_TRAFFIC_BYTES,
+                     "kernel": "k_gram_tc<64> + k_reduce_partials_f32 (tensor-core FP32 Gram, one-MMA layout: "
+                               "[X Z]'Z, 18 + 36 FP32 columns)",
+                     "algorithmic_bytes": alg_gram, "launch_us": t_gram * 1e6, "peak_kind": kind},
+        "roofline_apply": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                           "traffic": APPLY_TRAFFIC_BYTES,
+                           "kernel": "k_apply_march<float> (plane-marching fused stencil apply, 16 columns, the "
+                                     "tuned variant)",
+                           "algorithmic_bytes": alg, "launch_us": t_apply * 1e6, "peak_kind": kind},
         "roofline_update": {"bound": "hbm", "achieved": alg_upd / t_upd / 1e9, "peak": peak, "unit": "GB/s",
                             "frac": alg_upd / t_upd / 1e9 / peak, "traffic": UPDATE_TRAFFIC_BYTES,
                             "kernel": "k_update_tc<3> (tcgen05 FP32 block update, TF32 hi / lo, 3-tile staging ring: "
@@ -374,10 +382,6 @@ def run_ours(args, D):
                           "kernel": f"k_mode_pipe<64> (pipelined tcgen05 BF16 mode product, 256-point axis, "
                                     f"{MODE_COLS} columns)",
                           "algorithmic_bytes": alg_mode, "launch_us": t_mode * 1e6, "peak_kind": kind},
-        "roofline_gram": {"bound": "hbm", "achieved": alg_gram / t_gram / 1e9, "peak": peak, "unit": "GB/s",
-                          "frac": alg_gram / t_gram / 1e9 / peak, "traffic": GRAM_TC_TRAFFIC_BYTES,
-                          "kernel": "k_gram_tc + k_reduce_partials_f32 ([X Z]'Z, 18 + 36 FP32 columns)",
-                          "algorithmic_bytes": alg_gram, "launch_us": t_gram * 1e6, "peak_kind": kind},
         "clocks": clk, "gpu_launches": launches,
     }
     for H in ops.values():

@@ -132,6 +132,24 @@ int kf_op_apply_noalloc(kf_op *op, const void *X, void *Y, int64_t ldx, int64_t 
 int kf_op_sandwich(kf_op *op, const double *W, int64_t ldw, int32_t kw, const double *V, int64_t ldv, int32_t kv,
                    double *P_out, int32_t flags);
 
+/* The linear solve on the complement of a node's known states (src/resolvent.jl:146-252,
+ * _complement_solve; the Sternheimer solves of the reference's derivatives): X[:, j] solves
+ * Q (H - shifts[j]) Q x = Q B[:, j] with x orthogonal to the nbasis orthonormal columns of basis,
+ * Q = 1 - basis basis', by a conjugate gradient on all n columns in lockstep, each with its own
+ * scalars, preconditioned by 1 / hypot(diagonal(H) - shifts[j], eta).  FP64.  basis (N x nbasis),
+ * B (N x n) and X (N x n) are host (KF_HOST) or device pointers with leading dimensions >= N;
+ * shifts (n) and scale (n, or NULL: the column norms of B) are host arrays.  Stopping rule, round-off
+ * floor (1000 eps scale_j, five checks of the true residual without halving), positivity check and
+ * final acceptance are the reference's.  Outputs (host, each may be NULL): iterations; per column
+ * state (0 met its tolerance tol ||Q B_j||, 1 converged from the start with x = 0, 2 stopped at the
+ * round-off floor), residuals (true residual / ||Q B_j|| for state 0) and floor_residuals (true
+ * residual / scale_j for state 2).  KF_EBREAKDOWN: "not positive on the complement";
+ * KF_ENOCONV: "did not converge". */
+int kf_complement_solve(kf_op *op, const double *basis, int64_t ldbasis, int32_t nbasis, const double *B, int64_t ldb,
+                        int32_t n, const double *shifts, const double *scale, double tol, int32_t maxiter, double eta,
+                        double *X, int64_t ldx, int32_t *iterations, int32_t *state, double *residuals,
+                        double *floor_residuals, int32_t flags);
+
 /* diagonal(H) real part (src/apply.jl:455-478, _full_diagonal), N values into host memory. */
 int kf_op_diagonal(kf_op *op, double *out);
 

@@ -220,6 +220,67 @@ int kf_op_sandwich(kf_op *op, const double *W, int64_t ldw, int32_t kw, const do
     });
 }
 
+int kf_complement_solve(kf_op *op, const double *basis, int64_t ldbasis, int32_t nbasis, const double *B, int64_t ldb,
+                        int32_t n, const double *shifts, const double *scale, double tol, int32_t maxiter, double eta,
+                        double *X, int64_t ldx, int32_t *iterations, int32_t *state, double *residuals,
+                        double *floor_residuals, int32_t flags) {
+    return guarded([&] {
+        KF_REQUIRE(op && B && shifts && X, KF_EINVAL, "kf_complement_solve: NULL argument");
+        KF_REQUIRE(n >= 1 && n <= 4096, KF_EINVAL, "kf_complement_solve: 1..4096 right-hand sides");
+        KF_REQUIRE(nbasis >= 0 && nbasis <= 4096 && (nbasis == 0 || basis), KF_EINVAL,
+                   "kf_complement_solve: the basis must have 0..4096 columns");
+        KF_REQUIRE(tol > 0 && maxiter >= 0 && eta >= 0, KF_EINVAL, "kf_complement_solve: tol > 0, maxiter >= 0, eta >= 0");
+        const int64_t N = op->N;
+        KF_REQUIRE(ldb >= N && ldx >= N && (nbasis == 0 || ldbasis >= N), KF_EDIM,
+                   "kf_complement_solve: leading dimensions must be >= N");
+        KF_REQUIRE(nbasis < N, KF_EDIM, "kf_complement_solve: the basis must leave a complement");
+        cudaStream_t s = op->stream;
+        const bool host = (flags & KF_HOST) != 0;
+        double *dB = nullptr, *dV = nullptr, *dX = nullptr;
+        auto cleanup = [&]() {
+            cudaFreeAsync(dB, s);
+            cudaFreeAsync(dV, s);
+            cudaFreeAsync(dX, s);
+        };
+        kf::CgResult r;
+        try {
+            const double *Bd = B, *Vd = basis;
+            double *Xd = X;
+            int64_t lb = ldb, lv = ldbasis, lx = ldx;
+            if (host) {
+                KF_CUDA(cudaMallocAsync((void **)&dB, (size_t)N * n * 8, s));
+                KF_CUDA(cudaMemcpy2DAsync(dB, N * 8, B, ldb * 8, N * 8, n, cudaMemcpyHostToDevice, s));
+                Bd = dB;
+                lb = N;
+                if (nbasis > 0) {
+                    KF_CUDA(cudaMallocAsync((void **)&dV, (size_t)N * nbasis * 8, s));
+                    KF_CUDA(cudaMemcpy2DAsync(dV, N * 8, basis, ldbasis * 8, N * 8, nbasis, cudaMemcpyHostToDevice, s));
+                    Vd = dV;
+                    lv = N;
+                }
+                KF_CUDA(cudaMallocAsync((void **)&dX, (size_t)N * n * 8, s));
+                Xd = dX;
+                lx = N;
+            }
+            kf::complement_solve(op, Vd, lv, nbasis, Bd, lb, n, shifts, scale, tol, maxiter, eta, Xd, lx, r, s);
+            if (host) {
+                KF_CUDA(cudaMemcpy2DAsync(X, ldx * 8, dX, N * 8, N * 8, n, cudaMemcpyDeviceToHost, s));
+                KF_CUDA(cudaStreamSynchronize(s));
+            }
+        } catch (...) {
+            cleanup();
+            throw;
+        }
+        cleanup();
+        if (iterations) *iterations = r.iterations;
+        for (int j = 0; j < n; ++j) {
+            if (state) state[j] = r.state[j];
+            if (residuals) residuals[j] = r.residuals[j];
+            if (floor_residuals) floor_residuals[j] = r.floor_residuals[j];
+        }
+    });
+}
+
 int kf_op_diagonal(kf_op *op, double *out) {
     return guarded([&] {
         KF_REQUIRE(op && out, KF_EINVAL, "kf_op_diagonal: NULL argument");

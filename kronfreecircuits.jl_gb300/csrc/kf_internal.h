@@ -229,6 +229,19 @@ void apply_pairs(const kf_op *op, const T *X, int64_t ldx, T *Y, int64_t ldy, in
 void launch_apply(kf_op *op, bool f32, const void *X, void *Y, int64_t ldx, int64_t ldy, int64_t b,
                   double alpha, double beta, const void *Z, int64_t ldz, double gamma, cudaStream_t s);
 
+// the linear solve on the complement of known states (kf_cg.cu; src/resolvent.jl:146-252): per
+// column, state 0 met its tolerance, 1 converged from the start (x = 0), 2 stopped at the round-off
+// floor; residuals[j] the true residual relative to ||Q B_j|| (state 0), floor_residuals[j] relative
+// to scale_j (state 2)
+struct CgResult {
+    int iterations = 0;
+    std::vector<int> state;
+    std::vector<double> residuals, floor_residuals;
+};
+void complement_solve(kf_op *op, const double *basis, int64_t ldbs, int nb, const double *B, int64_t ldb, int n,
+                      const double *shifts, const double *scale, double tol, int maxiter, double eta, double *X_out,
+                      int64_t ldx, CgResult &res, cudaStream_t s);
+
 // run the fused apply's tuner now for every width class up to maxb columns not yet tuned for this
 // operator's stencil shape (X, Y: N x maxb device blocks, leading dimension ld, contents unused)
 void pretune_apply(kf_op *op, bool f32, const void *X, void *Y, int64_t ld, int maxb, cudaStream_t s);
