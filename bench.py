@@ -390,6 +390,7 @@ def run_ours(args, D):
         line["dense"] = sub_dense(torch, args)
         line["batch"] = sub_batch(torch, args)
         line["warmstart"] = sub_warmstart(torch, args)
+        line["complement"] = sub_complement(torch, args)
     if not args.no_cpu and D.world == 1:
         line["cpu_baseline"] = cpu_baseline(ths[idx[0]], idx[0], "separable")
     return line if D.rank == 0 else None
@@ -791,6 +792,65 @@ def sub_dense(torch, args):
     return out
 
 
+def sub_complement(torch, args):
+    """The linear solve on the complement of the three-mode leaf's 12 lowest states (N = 671,744):
+    12 seeded right-hand sides, every shift at the lowest energy, tol 1e-9, FP64 conjugate gradient
+    (kf_complement_solve); beside it the oracle's restatement of the reference CPU path (C/OpenMP
+    apply + NumPy BLAS) timed over a bounded number of iterations."""
+    from kfgpu import KronFreeOperator, LOBPCG, circuits, solve
+    from kfgpu.resolvent import complement_solve
+    th = thetas()[0]
+    dims, terms = circuits.three_mode_leaf(th)
+    H = KronFreeOperator(dims, terms)
+    E, V, _ = solve(LOBPCG(tol=1e-9 * H.gershgorin_bound(), precision="mixed", preconditioner="separable"), H, 12)
+    rng = np.random.default_rng(SEED + 6)
+    B = rng.standard_normal((H.N, 12))
+    shifts = np.full(12, E[0])
+    complement_solve(H, V, B, shifts, tol=1e-9, maxiter=20000)          # warm-up (kernel tuning)
+    reps = 2
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        X, it, res, fs, af, fres = complement_solve(H, V, B, shifts, tol=1e-9, maxiter=20000)
+    t = (time.perf_counter() - t0) / reps
+    peak, kind = peaks()
+    ta = measure_apply(torch, H, False, b=12)
+    by = 2 * H.N * 12 * 8
+    out = {"workload": "complement solve, three-mode leaf 41x256x64 (N=671,744), basis = its 12 lowest states, "
+                       "12 right-hand sides (numpy default_rng(20261211)), shifts at the lowest energy, tol 1e-9",
+           "value": 12 / t, "unit": "right-hand sides solved/s", "seconds": t, "iterations": it,
+           "ms_per_iteration": 1e3 * t / max(it, 1), "max_true_residual_rel": float(np.max(res)),
+           "at_floor": len(af), "from_start": len(fs),
+           "roofline": {"bound": "hbm", "achieved": by / ta / 1e9, "peak": peak, "unit": "GB/s",
+                        "frac": by / ta / 1e9 / peak, "traffic": None, "algorithmic_bytes": by,
+                        "kernel": "FP64 fused stencil apply, 12 columns (one per iteration)", "launch_us": ta * 1e6,
+                        "peak_kind": kind}}
+    if not args.no_cpu:
+        out["cpu_baseline"] = cpu_complement(th, V, B, shifts, it)
+    H.close()
+    return out
+
+
+def cpu_complement(theta, V, B, shifts, gpu_iters, k=6):
+    """The oracle's complement solve on the host cores for k iterations (C/OpenMP apply, threaded
+    BLAS), extrapolated to the GPU solve's iteration count."""
+    from oracle import capply, circuits as ocirc, resolvent as ores
+    Hr = ocirc.three_mode_operator(theta)
+    Ho = capply.CApply(Hr)
+    D = Hr.diagonal().real
+    t0 = time.perf_counter()
+    try:
+        ores.complement_solve(Ho, D, V, B, shifts, tol=1e-9, maxiter=k)
+    except ores.ComplementError:
+        pass
+    t = time.perf_counter() - t0
+    per = t / k
+    return {"value": B.shape[1] / (per * gpu_iters), "unit": "right-hand sides solved/s", "cores": os.cpu_count(),
+            "kind": "port", "sample": f"{k} iterations of the oracle's complement solve (C/OpenMP apply + threaded "
+                                      f"NumPy BLAS, FP64), {t:.2f} s, extrapolated to the GPU solve's {gpu_iters}",
+            "seconds_per_iteration": per}
+
+
 def run_dense_workload(args):
     import torch
     return sub_dense(torch, args)
@@ -867,7 +927,7 @@ def main():
     ap.add_argument("--buffer", type=int, default=None,
                     help="unchecked LOBPCG columns beyond the guards in the mixed solves (default: the library's)")
     ap.add_argument("--workload", default="leaf3",
-                    choices=["leaf3", "batch", "warmstart", "dense", "apply", "mode", "gram", "update"],
+                    choices=["leaf3", "batch", "warmstart", "dense", "apply", "mode", "gram", "update", "complement"],
                     help="leaf3 (the benchmarked workload) or one of the other measured configurations")
     ap.add_argument("--n-train", type=int, default=4096)
     ap.add_argument("--n-test", type=int, default=1024)
@@ -881,7 +941,7 @@ def main():
     if args.workload != "leaf3":
         fn = {"batch": run_batch_workload, "warmstart": run_warmstart_workload, "dense": run_dense_workload,
               "apply": run_apply_workload, "mode": run_mode_workload, "gram": run_gram_workload,
-              "update": run_update_workload}
+              "update": run_update_workload, "complement": lambda a: sub_complement(__import__("torch"), a)}
         print(json.dumps(fn[args.workload](args)), flush=True)
         return
     if args.warmup < 3:
