@@ -251,8 +251,9 @@ def run_ours(args, D):
         tol = 1e-8 * H.gershgorin_bound()
         pc = precond or ("separable" if precision == "mixed" else "ritz")
         buf = args.buffer if precision == "mixed" else None
+        kw = {"mixed_switch": args.mixed_switch} if args.mixed_switch is not None else {}
         try:
-            E, V, st = solve(LOBPCG(tol=tol, precision=precision, preconditioner=pc, buffer=buf), H, M_PAIRS)
+            E, V, st = solve(LOBPCG(tol=tol, precision=precision, preconditioner=pc, buffer=buf, **kw), H, M_PAIRS)
         except ConvergenceError as e:
             st = e.stats
             st["hit_maxiter"] = True
@@ -309,7 +310,8 @@ def run_ours(args, D):
         dims, terms = circuits.three_mode_leaf(ths[i])
         H = KronFreeOperator(dims, terms)
         tol = 1e-8 * H.gershgorin_bound()
-        E, V, st = solve(LOBPCG(tol=tol, precision="mixed", preconditioner="separable", buffer=args.buffer), H,
+        kw = {"mixed_switch": args.mixed_switch} if args.mixed_switch is not None else {}
+        E, V, st = solve(LOBPCG(tol=tol, precision="mixed", preconditioner="separable", buffer=args.buffer, **kw), H,
                          M_PAIRS)
         conv_e += st["converged"]
         Es_e.append((i, E))
@@ -926,6 +928,8 @@ def main():
                     help="skip the batched-sweep, warm-start and dense-parent sub-measurements")
     ap.add_argument("--buffer", type=int, default=None,
                     help="unchecked LOBPCG columns beyond the guards in the mixed solves (default: the library's)")
+    ap.add_argument("--mixed-switch", type=float, default=None,
+                    help="FP32 phase of the mixed solves stops below this times ||H|| (default: the library's)")
     ap.add_argument("--workload", default="leaf3",
                     choices=["leaf3", "batch", "warmstart", "dense", "apply", "mode", "gram", "update", "complement"],
                     help="leaf3 (the benchmarked workload) or one of the other measured configurations")

@@ -55,8 +55,11 @@ template <typename T>
 __device__ void leaf_apply(const LeafDesc &L, const T *D, const T *W, const T *X, T *Y, int nb, T alpha, T beta,
                            const T *Z, T gamma) {
     const int N = L.N;
+    // element e = (column c, row r); one division per thread, then (c, r) advance by the block's
+    // stride without dividing (each element's arithmetic is unchanged)
+    const int sc = (int)blockDim.x / N, sr = (int)blockDim.x % N;
+    int c = (int)threadIdx.x / N, r = (int)threadIdx.x % N;
     for (int e = threadIdx.x; e < N * nb; e += blockDim.x) {
-        const int c = e / N, r = e % N;
         const T *x = X + (int64_t)c * N;
         T acc = D[r] * x[r];
         for (int b = 0; b < L.nbands; ++b) {
@@ -66,6 +69,12 @@ __device__ void leaf_apply(const LeafDesc &L, const T *D, const T *W, const T *X
         T v = alpha * acc + beta * x[r];
         if (Z) v += gamma * Z[(int64_t)c * N + r];
         Y[(int64_t)c * N + r] = v;
+        c += sc;
+        r += sr;
+        if (r >= N) {
+            r -= N;
+            ++c;
+        }
     }
     __syncthreads();
 }
@@ -86,11 +95,18 @@ __device__ void leaf_gram(const T *A, const T *B, int N, int nb, double *G) {
 // Y (N x k) = X (N x kk) C (kk x k, FP64 shared, column-major ldc)
 template <typename T>
 __device__ void leaf_update(T *Y, const T *X, int N, int kk, int k, const double *C, int ldc) {
+    const int sc = (int)blockDim.x / N, sr = (int)blockDim.x % N;
+    int c = (int)threadIdx.x / N, r = (int)threadIdx.x % N;
     for (int e = threadIdx.x; e < N * k; e += blockDim.x) {
-        const int c = e / N, r = e % N;
         double s = 0;
         for (int q = 0; q < kk; ++q) s += (double)X[(int64_t)q * N + r] * C[q + ldc * c];
         Y[(int64_t)c * N + r] = (T)s;
+        c += sc;
+        r += sr;
+        if (r >= N) {
+            r -= N;
+            ++c;
+        }
     }
     __syncthreads();
 }
