@@ -129,6 +129,13 @@ int kf_test_op_scratch_bytes(const struct kf_op *op, uint64_t *bytes);
 int kf_test_march_plan(const struct kf_op *op, int64_t b, int32_t f32, int32_t sms, int32_t *eligible,
                        int32_t *geom);
 
+/* The device Rayleigh-Ritz eigensolver of the FP32 LOBPCG phase (FP32 Jacobi, one CTA): G on the
+ * host in the merged (ldg x ldg, rows [X_a; Q], columns [H X_a, H Z]) or packed layout; writes
+ * C (ns x 2 na: [C_x | [0; C_z]]) and the na lowest Ritz values into theta_out (in / out).  status
+ * != 0 takes the path of a failed device Cholesky (C keeps X, drops P; theta_out comes back as given). */
+int kf_test_rr_eig(const double *G, int32_t ldg, int32_t packed, int32_t na, int32_t k, int32_t status, double *C_out,
+                   double *theta_out);
+
 #ifdef __cplusplus
 }
 #endif

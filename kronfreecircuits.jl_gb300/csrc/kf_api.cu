@@ -220,6 +220,41 @@ int kf_op_sandwich(kf_op *op, const double *W, int64_t ldw, int32_t kw, const do
     });
 }
 
+int kf_test_rr_eig(const double *G, int32_t ldg, int32_t packed, int32_t na, int32_t k, int32_t status, double *C_out,
+                   double *theta_out) {
+    return guarded([&] {
+        KF_REQUIRE(G && C_out && theta_out && na >= 1 && k >= 0 && na + k <= 64, KF_EINVAL,
+                   "kf_test_rr_eig: 1 <= na, na + k <= 64");
+        const int ns = na + k;
+        const size_t gn = packed ? (size_t)na * na + (size_t)na * k + (size_t)k * k : (size_t)ldg * ns;
+        KF_REQUIRE(packed || ldg >= ns, KF_EDIM, "kf_test_rr_eig: ldg >= na + k");
+        double *dG = nullptr, *dC = nullptr, *dth = nullptr;
+        int *dst = nullptr;
+        auto cleanup = [&]() {
+            cudaFree(dG);
+            cudaFree(dC);
+            cudaFree(dth);
+            cudaFree(dst);
+        };
+        try {
+            KF_CUDA(cudaMalloc(&dG, gn * 8));
+            KF_CUDA(cudaMalloc(&dC, (size_t)ns * 2 * na * 8));
+            KF_CUDA(cudaMalloc(&dth, (size_t)na * 8));
+            KF_CUDA(cudaMalloc(&dst, sizeof(int)));
+            KF_CUDA(cudaMemcpy(dG, G, gn * 8, cudaMemcpyHostToDevice));
+            KF_CUDA(cudaMemcpy(dst, &status, sizeof(int), cudaMemcpyHostToDevice));
+            KF_CUDA(cudaMemcpy(dth, theta_out, (size_t)na * 8, cudaMemcpyHostToDevice));   // in / out
+            KF_REQUIRE(kf::rr_eig_device(dG, ldg, packed != 0, na, k, dC, dth, dst, 0), KF_EINVAL, "rr_eig_device refused");
+            KF_CUDA(cudaMemcpy(C_out, dC, (size_t)ns * 2 * na * 8, cudaMemcpyDeviceToHost));
+            KF_CUDA(cudaMemcpy(theta_out, dth, (size_t)na * 8, cudaMemcpyDeviceToHost));
+        } catch (...) {
+            cleanup();
+            throw;
+        }
+        cleanup();
+    });
+}
+
 int kf_complement_solve(kf_op *op, const double *basis, int64_t ldbasis, int32_t nbasis, const double *B, int64_t ldb,
                         int32_t n, const double *shifts, const double *scale, double tol, int32_t maxiter, double eta,
                         double *X, int64_t ldx, int32_t *iterations, int32_t *state, double *residuals,

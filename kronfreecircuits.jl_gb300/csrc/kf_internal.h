@@ -229,6 +229,13 @@ void apply_pairs(const kf_op *op, const T *X, int64_t ldx, T *Y, int64_t ldy, in
 void launch_apply(kf_op *op, bool f32, const void *X, void *Y, int64_t ldx, int64_t ldy, int64_t b,
                   double alpha, double beta, const void *Z, int64_t ldz, double gamma, cudaStream_t s);
 
+// the Rayleigh-Ritz eigenproblem of an FP32 LOBPCG iteration on the device (kf_rr.cu): from the
+// Gram blocks G (merged ld x ld layout, or packed [X_a'HX_a | X_a'HZ | Q'HZ]), writes the update
+// coefficients C (ns x 2 na, column-major) and the na lowest Ritz values to theta; false (nothing
+// launched) when na + k > 64.  `status`: the device Cholesky's word; nonzero -> C keeps X, drops P
+bool rr_eig_device(const double *G, int ldg, bool packed, int na, int k, double *C, double *theta, const int *status,
+                   cudaStream_t s);
+
 // the linear solve on the complement of known states (kf_cg.cu; src/resolvent.jl:146-252): per
 // column, state 0 met its tolerance, 1 converged from the start (x = 0), 2 stopped at the round-off
 // floor; residuals[j] the true residual relative to ||Q B_j|| (state 0), floor_residuals[j] relative

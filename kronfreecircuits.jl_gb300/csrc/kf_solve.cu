@@ -19,7 +19,8 @@
 // [X_active, W, P] gives the new active Ritz pairs; P is the [W P] part of the update.
 //
 // Precision (KF_PREC_MIXED): the bulk of the iterations run with FP32 blocks (FP32 applies,
-// FP32 Gram products accumulated in FP64 across CTAs, FP64 Rayleigh-Ritz on the host); when
+// FP32 Gram products accumulated in FP64 across CTAs, FP64 Rayleigh-Ritz on the host, or with
+// KF_DEVICE_RR=1 by FP32 Jacobi on the device, kf_rr.cu, so that an iteration waits once); when
 // every active residual is below mixed_switch * ||H|| (or the FP32 residuals stop falling),
 // the block is widened to FP64 and the same iteration finishes in FP64 with FP64 residuals,
 // the last sweep being the FP64 refinement that the acceptance test measures.
@@ -215,7 +216,7 @@ template <typename T>
 struct LobWork {
     int64_t N;
     int w;
-    DevMem X, HX, Xn, HXn, Z, HZ, Zt, Pn, F1, F2, dG, dC, dpart, dth, dthp, dnorm, dD, dstat;
+    DevMem X, HX, Xn, HXn, Z, HZ, Zt, Pn, F1, F2, dG, dC, dpart, dth, dthp, dnorm, dD, dstat, dtheta;
     HostMem hG, hC, hv, hstat;
     size_t part_bytes;
     LobWork(int64_t N_, int w_)
@@ -226,7 +227,7 @@ struct LobWork {
           F1((size_t)N_ * w_ * sizeof(float)), F2((size_t)N_ * w_ * sizeof(float)),
           dG((size_t)9 * w_ * w_ * sizeof(double)), dC((size_t)9 * w_ * w_ * sizeof(double)),
           dpart(gram_partials_size(3 * w_, 3 * w_, N_)), dth(w_ * sizeof(double)), dthp(w_ * sizeof(double)),
-          dnorm(2 * w_ * sizeof(double)), dD(0), dstat(16),
+          dnorm(2 * w_ * sizeof(double)), dD(0), dstat(16), dtheta(w_ * sizeof(double)),
           hG((size_t)9 * w_ * w_ * sizeof(double)), hC((size_t)9 * w_ * w_ * sizeof(double)),
           hv((size_t)4 * w_ * sizeof(double)), hstat(16), part_bytes(gram_partials_size(3 * w_, 3 * w_, N_)) {}
 };
@@ -350,7 +351,7 @@ static void merged_gram_sync(LobWork<float> &W, const float *X, int wx, const fl
 
 // returns k (columns of Q, in W.Z) or 0 when the directions vanished
 static int merged_finish(kf_op *op, LobWork<float> &W, const float *X, int wx, float *Zb, int na, int np, int newly,
-                         double cutoff, cudaStream_t s) {
+                         double cutoff, cudaStream_t s, bool host_second = false) {
     const int64_t N = W.N;
     const int nz = na + np, ld = wx + nz;
     const double *hG = W.hG.as<double>();
@@ -386,8 +387,9 @@ static int merged_finish(kf_op *op, LobWork<float> &W, const float *X, int wx, f
     h2d(C, hC, (size_t)lc * r1, s);
     float *Z1 = W.Zt.as<float>();
     update2<float>(Z1, N, r1, Zb, N, nz, X, N, wx, C, lc, 1.0, 0.0, N, s);
-    if (r1 > CHOL2_MAX_R) {
-        // wider than the device Cholesky takes: the second pass on the host, result in W.Z
+    if (r1 > CHOL2_MAX_R || host_second) {
+        // wider than the device Cholesky takes (or its previous attempt failed): the second pass on
+        // the host, result in W.Z
         float *Q = nullptr;
         const int r2 = ortho_against<float>(op, W, Z1, r1, X, wx, Zb, Q, cutoff, s, 1);
         KF_CUDA(cudaMemsetAsync(W.dstat.as<int>(), 0, sizeof(int), s));
@@ -420,6 +422,16 @@ static LobOut lobpcg_run(kf_op *op, LobWork<T> &Wk, const double *D, const LobPa
     // FP32 blocks: norms and the first Gram of [W P] share one wait, the second orthogonalisation
     // pass runs on the device (merged_gram_sync / merged_finish); FP64 keeps the plain sequence
     constexpr bool merged = sizeof(T) == 4;
+    // FP32 blocks with KF_DEVICE_RR=1 (read per solve): the Rayleigh-Ritz eigenproblem on the device
+    // (kf_rr.cu) -- the Ritz values live in Wk.dtheta and come back with the next residual norms --
+    // except with the fixed Jacobi preconditioner (its shift travels in the theta buffer).  Off by
+    // default: on GB300 the one-CTA FP32 Jacobi takes longer than the host round trip it saves
+    // (111.9 against 122.8 eigenpairs/s on the three-mode leaf)
+    const char *dev_rr_env = std::getenv("KF_DEVICE_RR");
+    const bool dev_rr = merged && prm.precond != KF_PRECOND_JACOBI && dev_rr_env && dev_rr_env[0] &&
+                        dev_rr_env[0] != '0';
+    double *dtheta = Wk.dtheta.template as<double>();
+    bool host_second = false;   // the previous device Cholesky failed: host second pass this time
     LobOut out;
     T *X = Wk.X.template as<T>(), *HX = Wk.HX.template as<T>();
     T *Xn = Wk.Xn.template as<T>(), *HXn = Wk.HXn.template as<T>();
@@ -448,6 +460,10 @@ static LobOut lobpcg_run(kf_op *op, LobWork<T> &Wk, const double *D, const LobPa
             throw Error(KF_EBREAKDOWN, "LOBPCG: Rayleigh-Ritz eigenproblem did not converge");
         std::memcpy(hC, V.data(), sizeof(double) * w * w);
         h2d(C, hC, (size_t)w * w, s);
+        if (dev_rr) {
+            std::memcpy(hv + 2 * w, theta.data(), sizeof(double) * w);
+            h2d(dtheta, hv + 2 * w, w, s);
+        }
         update<T>(Xn, N, w, X, N, w, C, w, 1.0, 0.0, N, s);
         update<T>(HXn, N, w, HX, N, w, C, w, 1.0, 0.0, N, s);
         std::swap(X, Xn);
@@ -461,10 +477,16 @@ static LobOut lobpcg_run(kf_op *op, LobWork<T> &Wk, const double *D, const LobPa
     int since_best = 0;
     for (int it = 0;; ++it) {
         const int na = w - nl;
-        // residuals of the active columns, preconditioned into Z[:, 0:na]
-        std::memcpy(hv, theta.data() + nl, sizeof(double) * na);
-        h2d(dth, hv, na, s);
-        h2d(dthp, hv, na, s);
+        // residuals of the active columns, preconditioned into Z[:, 0:na]; with the device
+        // Rayleigh-Ritz the Ritz values are read where it wrote them
+        double *dth_it = dth, *dthp_it = dthp;
+        if (dev_rr) {
+            dth_it = dthp_it = dtheta + nl;
+        } else {
+            std::memcpy(hv, theta.data() + nl, sizeof(double) * na);
+            h2d(dth, hv, na, s);
+            h2d(dthp, hv, na, s);
+        }
         if (prm.precond == KF_PRECOND_JACOBI) {
             // fixed Jacobi: sigma = min(D) - 1, passed in thetap[0]
             double dmin = op->h_fulldiag.empty() ? 0.0
@@ -473,13 +495,28 @@ static LobOut lobpcg_run(kf_op *op, LobWork<T> &Wk, const double *D, const LobPa
             h2d(dthp, &sig, 1, s);
         }
         const int mode = prm.precond == KF_PRECOND_RITZ ? 0 : prm.precond == KF_PRECOND_JACOBI ? 1 : 2;  // separable: 2, then below
-        residual_precond<T>(X + (int64_t)nl * N, HX + (int64_t)nl * N, N, na, N, dth, dthp, D, prm.eta, mode, Z, N,
-                            dnorm, part, s);
+        residual_precond<T>(X + (int64_t)nl * N, HX + (int64_t)nl * N, N, na, N, dth_it, dthp_it, D, prm.eta, mode, Z,
+                            N, dnorm, part, s);
         if constexpr (merged) {
             // W for every active column (those that lock now get zero weight later), P after it
-            precondition_f32(op, Wk, prm, (float *)Z, na, dth, s);
+            precondition_f32(op, Wk, prm, (float *)Z, na, dth_it, s);
             if (np > 0) copy_block<float>((const float *)Pn, N, (float *)Z + (int64_t)na * N, N, np, N, s);
+            if (dev_rr) {
+                // the Ritz values and the last device Cholesky's status ride on the same wait
+                KF_CUDA(cudaMemcpyAsync(hv + 2 * w, dtheta, sizeof(double) * w, cudaMemcpyDeviceToHost, s));
+                KF_CUDA(cudaMemcpyAsync(Wk.hstat.template as<int>(), Wk.dstat.template as<int>(), sizeof(int),
+                                        cudaMemcpyDeviceToHost, s));
+            }
             merged_gram_sync(Wk, (const float *)X, w, (const float *)Z, na + np, dnorm, na, hv + w, s);
+            if (dev_rr) {
+                std::memcpy(theta.data(), hv + 2 * w, sizeof(double) * w);
+                if (it > 0 && *Wk.hstat.template as<int>() != 0) {
+                    // the previous iteration's device Cholesky met a nearly dependent direction: that
+                    // iteration kept X and dropped P; the host takes the second pass this time
+                    ++out.ortho_fallbacks;
+                    host_second = true;
+                }
+            }
         } else {
             d2h_sync<T>(hv + w, dnorm, na, s);
         }
@@ -536,7 +573,8 @@ static LobOut lobpcg_run(kf_op *op, LobWork<T> &Wk, const double *D, const LobPa
         T *Qc = nullptr;
         int k = 0, r1 = 0;
         if constexpr (merged) {
-            k = r1 = merged_finish(op, Wk, (const float *)X, w, (float *)Z, na, np, newly, prm.cutoff, s);
+            k = r1 = merged_finish(op, Wk, (const float *)X, w, (float *)Z, na, np, newly, prm.cutoff, s, host_second);
+            host_second = false;
             Qc = Z;
             nl += newly;
         } else {
@@ -568,6 +606,9 @@ static LobOut lobpcg_run(kf_op *op, LobWork<T> &Wk, const double *D, const LobPa
         // Rayleigh-Ritz on S = [X_act, Q]: A = S' H S assembled from three Gram blocks
         const int na3 = w - nl;
         T *Xa = X + (int64_t)nl * N, *HXa = HX + (int64_t)nl * N;
+        // the device Rayleigh-Ritz takes this iteration when its eigenproblem fits one CTA
+        const bool dev_it = dev_rr && na3 + k <= 64;
+        bool rr_done_on_device = false;
         auto apply_rr = [&]() {
             launch_apply(op, f32, Qc, HZ, N, N, k, 1, 0, nullptr, 0, 0, s);
             out.nmv += k;
@@ -580,6 +621,11 @@ static LobOut lobpcg_run(kf_op *op, LobWork<T> &Wk, const double *D, const LobPa
                 gram<T>(Xa, N, na3, HXa, N, na3, N, G, part, s);
                 gram<T>(Xa, N, na3, HZ, N, k, N, G2, part, s);
                 gram<T>(Qc, N, k, HZ, N, k, N, G3, part, s);
+            }
+            if (dev_it) {
+                // eigenpairs, C and the Ritz values on the device; no host wait
+                rr_done_on_device = rr_eig_device(G, na3 + k, !one, na3, k, C, dtheta + nl, Wk.dstat.template as<int>(), s);
+                if (rr_done_on_device) return;
             }
             if (merged)
                 KF_CUDA(cudaMemcpyAsync(Wk.hstat.template as<int>(), Wk.dstat.template as<int>(), sizeof(int),
@@ -600,7 +646,7 @@ static LobOut lobpcg_run(kf_op *op, LobWork<T> &Wk, const double *D, const LobPa
         };
         apply_rr();
         if constexpr (merged) {
-            if (*Wk.hstat.template as<int>() != 0) {
+            if (!rr_done_on_device && *Wk.hstat.template as<int>() != 0) {
                 // the device Cholesky met a nearly dependent direction: the host SVQB pass from Z1
                 ++out.ortho_fallbacks;
                 T *Q2 = nullptr;
@@ -611,25 +657,34 @@ static LobOut lobpcg_run(kf_op *op, LobWork<T> &Wk, const double *D, const LobPa
             }
         }
         const int ns = na3 + k;
-        std::vector<double> A((size_t)ns * ns);
-        const double *h1 = hG, *h2 = hG + (size_t)na3 * na3, *h3 = h2 + (size_t)na3 * k;
-        for (int j = 0; j < na3; ++j)
-            for (int i = 0; i < na3; ++i) A[i + (size_t)ns * j] = h1[i + (size_t)na3 * j];
-        for (int j = 0; j < k; ++j)
-            for (int i = 0; i < na3; ++i) {
-                A[i + (size_t)ns * (na3 + j)] = h2[i + (size_t)na3 * j];
-                A[(na3 + j) + (size_t)ns * i] = h2[i + (size_t)na3 * j];
+        std::vector<double> A, lam, V;
+        if (!rr_done_on_device) {
+            A.assign((size_t)ns * ns, 0.0);
+            const double *h1 = hG, *h2 = hG + (size_t)na3 * na3, *h3 = h2 + (size_t)na3 * k;
+            for (int j = 0; j < na3; ++j)
+                for (int i = 0; i < na3; ++i) A[i + (size_t)ns * j] = h1[i + (size_t)na3 * j];
+            for (int j = 0; j < k; ++j)
+                for (int i = 0; i < na3; ++i) {
+                    A[i + (size_t)ns * (na3 + j)] = h2[i + (size_t)na3 * j];
+                    A[(na3 + j) + (size_t)ns * i] = h2[i + (size_t)na3 * j];
+                }
+            for (int j = 0; j < k; ++j)
+                for (int i = 0; i < k; ++i) A[(na3 + i) + (size_t)ns * (na3 + j)] = h3[i + (size_t)k * j];
+            lam.resize(ns);
+            V.resize((size_t)ns * ns);
+            if (timed_sym_eig(ns, A.data(), ns, lam.data(), V.data(), ns) != 0)
+                throw Error(KF_EBREAKDOWN, "LOBPCG: Rayleigh-Ritz eigenproblem did not converge");
+            // C = V[:, 0:na3] (ns x na3), then [0; C_z] beside it: [X_new P_new] = [X_a Q] [C | [0; C_z]]
+            std::memcpy(hC, V.data(), sizeof(double) * (size_t)ns * na3);
+            for (int j = 0; j < na3; ++j)
+                for (int i = 0; i < ns; ++i) hC[(size_t)ns * (na3 + j) + i] = i < na3 ? 0.0 : V[i + (size_t)ns * j];
+            h2d(C, hC, (size_t)ns * 2 * na3, s);
+            if (dev_rr) {
+                // keep the device copy of the Ritz values current for the next iteration's kernels
+                std::memcpy(hv + 2 * w + nl, lam.data(), sizeof(double) * na3);
+                h2d(dtheta + nl, hv + 2 * w + nl, na3, s);
             }
-        for (int j = 0; j < k; ++j)
-            for (int i = 0; i < k; ++i) A[(na3 + i) + (size_t)ns * (na3 + j)] = h3[i + (size_t)k * j];
-        std::vector<double> lam(ns), V((size_t)ns * ns);
-        if (timed_sym_eig(ns, A.data(), ns, lam.data(), V.data(), ns) != 0)
-            throw Error(KF_EBREAKDOWN, "LOBPCG: Rayleigh-Ritz eigenproblem did not converge");
-        // C = V[:, 0:na3] (ns x na3), then [0; C_z] beside it: [X_new P_new] = [X_a Q] [C | [0; C_z]]
-        std::memcpy(hC, V.data(), sizeof(double) * (size_t)ns * na3);
-        for (int j = 0; j < na3; ++j)
-            for (int i = 0; i < ns; ++i) hC[(size_t)ns * (na3 + j) + i] = i < na3 ? 0.0 : V[i + (size_t)ns * j];
-        h2d(C, hC, (size_t)ns * 2 * na3, s);
+        }
         // X_act <- Xa Cx + Q Cz ; HX likewise ; P <- Q Cz
         T *Xna = Xn + (int64_t)nl * N, *HXna = HXn + (int64_t)nl * N;
         bool fused = false;
@@ -649,7 +704,8 @@ static LobOut lobpcg_run(kf_op *op, LobWork<T> &Wk, const double *D, const LobPa
         np = na3;
         std::swap(X, Xn);
         std::swap(HX, HXn);
-        for (int j = 0; j < na3; ++j) theta[nl + j] = lam[j];
+        if (!rr_done_on_device)
+            for (int j = 0; j < na3; ++j) theta[nl + j] = lam[j];
         na_prev = na3;
     }
     (void)na_prev;

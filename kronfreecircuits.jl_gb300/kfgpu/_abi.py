@@ -135,6 +135,7 @@ def lib():
                                         C.POINTER(C.c_float), P]),
         "kf_test_chol2": (C.c_int, [P, C.c_int32, C.c_int32, P, P]),
         "kf_test_op_scratch_bytes": (C.c_int, [P, P]),
+        "kf_test_rr_eig": (C.c_int, [P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, P, P]),
         "kf_test_march_plan": (C.c_int, [P, C.c_int64, C.c_int32, C.c_int32, P, P]),
         "kf_test_sym_eig": (C.c_int, [C.c_int32, P, C.c_int32, P, P, C.c_int32]),
         "kf_test_update_split": (C.c_int, [C.c_int32, P, C.c_int32, P, C.c_int32, P, C.c_int32, P, C.c_int32, P, C.c_double,
