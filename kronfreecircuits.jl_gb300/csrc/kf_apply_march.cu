@@ -32,6 +32,11 @@
 // when a plane leaves it (or a column's run ends), arrive on that slot's "empty" mbarrier, which the
 // producer waits on before reusing the slot.  No CTA-wide barrier inside the march.
 //
+// KF_CHECK builds test every slice, ring, weight and output index first (sites 101-109: X slice fits
+// its slot, diagonal slice fits, window reads, window reads on the fast path, shared-entry reads,
+// diagonal reads, window weights, output stores, table reads) and record a failure instead of the
+// access.
+//
 // Every wait is bounded (a clock64 budget of about two seconds): a role whose wait ran out records
 // KF_ETIMEOUT in the host-mapped error word and raises the CTA's abort flag, which every other wait
 // loop checks; the producer then waits (bounded) for its copies still in flight before the CTA exits.
@@ -318,7 +323,11 @@ __global__ void __launch_bounds__(MTHREADS, 1)
                 int64_t xlo = xb, xhi = xend;
                 if (xlo < 0) xlo = 0;
                 if (xhi > mp.N) xhi = mp.N;
-                if (xlo > xb || xhi < xend) {
+                const bool xfit = KF_CHK(xend - xb <= mp.SLX && col < b, err, 101);
+                if (!xfit) {
+                    xlo = xb;
+                    xhi = xb;   // nothing copied, nothing zeroed
+                } else if (xlo > xb || xhi < xend) {
                     for (int e = lane; e < (int)(xlo - xb); e += 32) slot[e] = T(0);
                     for (int e = (int)(xhi - xb) + lane; e < (int)(xend - xb); e += 32) slot[e] = T(0);
                     asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
@@ -329,7 +338,8 @@ __global__ void __launch_bounds__(MTHREADS, 1)
                     int64_t dhi = ceil_to(ds + qn, G);
                     if (dhi > mp.N) dhi = mp.N;
                     const uint32_t bx = xhi > xlo ? (uint32_t)((xhi - xlo) * (int64_t)sizeof(T)) : 0u;
-                    const uint32_t bd = dhi > db ? (uint32_t)((dhi - db) * (int64_t)sizeof(T)) : 0u;
+                    uint32_t bd = dhi > db ? (uint32_t)((dhi - db) * (int64_t)sizeof(T)) : 0u;
+                    if (!KF_CHK(db >= 0 && mp.SLX + (dhi - db) <= SL, err, 102)) bd = 0u;
                     m_expect(full + s, bx + bd);
                     if (bx) m_bulk(slot + (xlo - xb), Xc + xlo, bx, full + s);
                     if (bd) m_bulk(slot + mp.SLX, D + db, bd, full + s);
@@ -367,8 +377,9 @@ __global__ void __launch_bounds__(MTHREADS, 1)
             valid[j] = qi < qn;
             const T *pt = tab_o + q0 + qi;
 #pragma unroll
-            for (int e = 0; e < MS; ++e) wsm[j][e] = valid[j] ? __ldg(pt + (int64_t)e * mp.P) : T(0);
-            wcen[j] = valid[j] ? __ldg(pt + (int64_t)MS * mp.P) : T(0);
+            const bool tin = !valid[j] || KF_CHK(q0 + qi < mp.P, err, 109);
+            for (int e = 0; e < MS; ++e) wsm[j][e] = (valid[j] && tin) ? __ldg(pt + (int64_t)e * mp.P) : T(0);
+            wcen[j] = (valid[j] && tin) ? __ldg(pt + (int64_t)MS * mp.P) : T(0);
         }
         asm volatile("bar.sync 1, %0;\n" ::"r"(MCT) : "memory");   // the consumer warps only
         auto wrap = [&](int s) { return s >= NR ? s - NR : (s < 0 ? s + NR : s); };
@@ -401,7 +412,7 @@ __global__ void __launch_bounds__(MTHREADS, 1)
                 }
                 const T *sx = ring + (int)(t % NR) * SL + xoff0;
 #pragma unroll
-                for (int j = 0; j < PT; ++j) xw[j][o] = sx[j * MCT];
+                for (int j = 0; j < PT; ++j) xw[j][o] = KF_CHK(xoff0 + j * MCT < mp.SLX, err, 103) ? sx[j * MCT] : T(0);
             }
             const int64_t tk0 = t0 + (k0 - jfirst);
             int sk = (int)(tk0 % NR);                    // slot of plane k
@@ -427,7 +438,9 @@ __global__ void __launch_bounds__(MTHREADS, 1)
                             const uint32_t ax = ring_s + (uint32_t)(sn * SL + xoff0) * (uint32_t)sizeof(T);
 #pragma unroll
                             for (int j = 0; j < PT; ++j)
-                                xw[j][(2 * H + r) % WN] = lds<T>(ax + (uint32_t)(j * MCT * sizeof(T)));
+                                xw[j][(2 * H + r) % WN] = KF_CHK(sn < NR && xoff0 + j * MCT < mp.SLX, err, 104)
+                                                              ? lds<T>(ax + (uint32_t)(j * MCT * sizeof(T)))
+                                                              : T(0);
                         } else {
 #pragma unroll
                             for (int j = 0; j < PT; ++j) xw[j][(2 * H + r) % WN] = T(0);
@@ -435,7 +448,9 @@ __global__ void __launch_bounds__(MTHREADS, 1)
                         T wmk[WN];
                         const uint32_t aw = wm_s + (uint32_t)(k * WN) * (uint32_t)sizeof(T);
 #pragma unroll
-                        for (int o = 0; o < WN; ++o) wmk[o] = lds<T>(aw + (uint32_t)(o * sizeof(T)));
+                        for (int o = 0; o < WN; ++o)
+                            wmk[o] = KF_CHK(k * WN + o < mp.nm * WN, err, 107) ? lds<T>(aw + (uint32_t)(o * sizeof(T)))
+                                                                               : T(0);
                         const uint32_t ab = ring_s + (uint32_t)(sk * SL + xoff0) * (uint32_t)sizeof(T);
                         uint32_t pa[MS];
 #pragma unroll
@@ -446,22 +461,29 @@ __global__ void __launch_bounds__(MTHREADS, 1)
                         for (int j = 0; j < PT; ++j) {
                             constexpr uint32_t JB = MCT * sizeof(T);
                             const T xc = xw[j][(H + r) % WN];
-                            T a0 = lds<T>(ad + j * JB) * xc;
+                            T a0 = (KF_CHK(mp.SLX + misd + tid + j * MCT < SL, err, 106) ? lds<T>(ad + j * JB) : T(0)) * xc;
                             a0 = fma(wcen[j], xc, a0);
                             T a1 = wmk[0] * xw[j][r % WN];
 #pragma unroll
                             for (int o = 1; o < WN; ++o) a1 = fma(wmk[o], xw[j][(o + r) % WN], a1);
 #pragma unroll
                             for (int e = 0; e < MS; e += 2) {
-                                a0 = fma(wsm[j][e], lds<T>(pa[e] + j * JB), a0);
-                                if (e + 1 < MS) a1 = fma(wsm[j][e + 1], lds<T>(pa[e + 1] + j * JB), a1);
+                                const bool in0 = KF_CHK(xoff0 + mp.smr[e] + j * MCT >= 0 &&
+                                                            xoff0 + mp.smr[e] + j * MCT < mp.SLX, err, 105);
+                                a0 = fma(wsm[j][e], in0 ? lds<T>(pa[e] + j * JB) : T(0), a0);
+                                if (e + 1 < MS) {
+                                    const bool in1 = KF_CHK(xoff0 + mp.smr[e + 1] + j * MCT >= 0 &&
+                                                                xoff0 + mp.smr[e + 1] + j * MCT < mp.SLX, err, 105);
+                                    a1 = fma(wsm[j][e + 1], in1 ? lds<T>(pa[e + 1] + j * JB) : T(0), a1);
+                                }
                             }
                             T out = a0 + a1;
                             if (EPI) {
                                 out = alpha * out + beta * xc;
                                 if (zcol != nullptr && valid[j]) out += gamma * zcol[(int64_t)k * mp.P + j * MCT];
                             }
-                            if (valid[j]) yk[j * MCT] = out;
+                            if (valid[j] && KF_CHK(obase + q0 + tid + j * MCT + (int64_t)k * mp.P < mp.N, err, 108))
+                                yk[j * MCT] = out;
                         }
                         // plane k - H leaves the window: release its slot
                         __syncwarp();
@@ -483,14 +505,15 @@ __global__ void __launch_bounds__(MTHREADS, 1)
                     }
                     const T *sx = ring + sn * SL + xoff0;
 #pragma unroll
-                    for (int j = 0; j < PT; ++j) xw[j][(2 * H + r) % WN] = sx[j * MCT];
+                    for (int j = 0; j < PT; ++j)
+                        xw[j][(2 * H + r) % WN] = KF_CHK(xoff0 + j * MCT < mp.SLX, err, 103) ? sx[j * MCT] : T(0);
                 } else {
 #pragma unroll
                     for (int j = 0; j < PT; ++j) xw[j][(2 * H + r) % WN] = T(0);
                 }
                 T wmk[WN];
 #pragma unroll
-                for (int o = 0; o < WN; ++o) wmk[o] = wm[k * WN + o];
+                for (int o = 0; o < WN; ++o) wmk[o] = KF_CHK(k * WN + o < mp.nm * WN, err, 107) ? wm[k * WN + o] : T(0);
                 // one ring offset per shared entry (its plane's slot, its in-plane offset); the
                 // entries past nsm carry weight 0 and offset 0
                 int pe[MS];
@@ -504,26 +527,31 @@ __global__ void __launch_bounds__(MTHREADS, 1)
                 }
                 const int sdi = base - xoff0 + mp.SLX + misd + tid;
                 T *yk = ycol + (int64_t)k * mp.P;
+                // a ring read, checked in KF_CHECK builds
+                auto rd = [&](int idx, int site) -> T {
+                    return KF_CHK(idx >= 0 && idx < NR * SL, err, site) ? ring[idx] : T(0);
+                };
                 if (plain_sm) {
 #pragma unroll
                     for (int j = 0; j < PT; ++j) {
                         const T xc = xw[j][(H + r) % WN];
-                        T a0 = ring[sdi + j * MCT] * xc;
+                        T a0 = rd(sdi + j * MCT, 106) * xc;
                         a0 = fma(wcen[j], xc, a0);
                         T a1 = wmk[0] * xw[j][r % WN];
 #pragma unroll
                         for (int o = 1; o < WN; ++o) a1 = fma(wmk[o], xw[j][(o + r) % WN], a1);
 #pragma unroll
                         for (int e = 0; e < MS; e += 2) {
-                            a0 = fma(wsm[j][e], ring[pe[e] + j * MCT], a0);
-                            if (e + 1 < MS) a1 = fma(wsm[j][e + 1], ring[pe[e + 1] + j * MCT], a1);
+                            a0 = fma(wsm[j][e], rd(pe[e] + j * MCT, 105), a0);
+                            if (e + 1 < MS) a1 = fma(wsm[j][e + 1], rd(pe[e + 1] + j * MCT, 105), a1);
                         }
                         T out = a0 + a1;
                         if (EPI) {
                             out = alpha * out + beta * xc;
                             if (zcol != nullptr && valid[j]) out += gamma * zcol[(int64_t)k * mp.P + j * MCT];
                         }
-                        if (valid[j]) yk[j * MCT] = out;
+                        if (valid[j] && KF_CHK(obase + q0 + tid + j * MCT + (int64_t)k * mp.P < mp.N, err, 108))
+                            yk[j * MCT] = out;
                     }
                 } else {
                     T wpk[MS];
@@ -532,22 +560,23 @@ __global__ void __launch_bounds__(MTHREADS, 1)
 #pragma unroll
                     for (int j = 0; j < PT; ++j) {
                         const T xc = xw[j][(H + r) % WN];
-                        T a0 = ring[sdi + j * MCT] * xc;
+                        T a0 = rd(sdi + j * MCT, 106) * xc;
                         a0 = fma(wcen[j], xc, a0);
                         T a1 = wmk[0] * xw[j][r % WN];
 #pragma unroll
                         for (int o = 1; o < WN; ++o) a1 = fma(wmk[o], xw[j][(o + r) % WN], a1);
 #pragma unroll
                         for (int e = 0; e < MS; e += 2) {
-                            a0 = fma(wsm[j][e] * wpk[e], ring[pe[e] + j * MCT], a0);
-                            if (e + 1 < MS) a1 = fma(wsm[j][e + 1] * wpk[e + 1], ring[pe[e + 1] + j * MCT], a1);
+                            a0 = fma(wsm[j][e] * wpk[e], rd(pe[e] + j * MCT, 105), a0);
+                            if (e + 1 < MS) a1 = fma(wsm[j][e + 1] * wpk[e + 1], rd(pe[e + 1] + j * MCT, 105), a1);
                         }
                         T out = a0 + a1;
                         if (EPI) {
                             out = alpha * out + beta * xc;
                             if (zcol != nullptr && valid[j]) out += gamma * zcol[(int64_t)k * mp.P + j * MCT];
                         }
-                        if (valid[j]) yk[j * MCT] = out;
+                        if (valid[j] && KF_CHK(obase + q0 + tid + j * MCT + (int64_t)k * mp.P < mp.N, err, 108))
+                            yk[j * MCT] = out;
                     }
                 }
                 // plane k - H leaves the window: release its slot

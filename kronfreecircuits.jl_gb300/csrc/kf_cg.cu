@@ -6,7 +6,7 @@
 //
 // Per iteration, in FP64 on the device: AP = H P (the fused apply), AP -= s o P, AP = Q AP (a Gram
 // basis' AP and an update), kappa = <P, AP>, alpha = rho / kappa on the active columns, X += alpha P,
-// R -= alpha AP, ||R||, Z = Q (Minv o R), rho' = <R, Z>.  One host wait brings kappa, ||R|| and rho'
+// R -= alpha AP, ||R||, Z = Q (Minv o R) with Minv formed once per solve, rho' = <R, Z>.  One host wait brings kappa, ||R|| and rho'
 // back; the host applies the reference's column rules -- the positivity check, the per-column
 // target tol ||Q B_j||, the round-off cap 1000 eps scale_j with true residuals recomputed (a fresh
 // apply) for the columns below it and the five-check patience, the final true-residual acceptance --
@@ -95,15 +95,23 @@ __global__ void k_cg_reduce(const double *__restrict__ partials, int nblk, int n
     out[j] = s;
 }
 
-// Z_j = R_j / hypot(D - s_j, eta)
-__global__ void k_cg_precond(double *__restrict__ Z, const double *__restrict__ R, const double *__restrict__ D,
-                             const double *__restrict__ s, double eta, int64_t N, int n) {
+// Minv[:, j] = 1 / hypot(D - s_j, eta), once per solve (src/resolvent.jl:156, `Minv = 1 ./ hypot.(D .- S,
+// eta)`): the FP64 hypot is costly on this GPU's FP64 pipe, the per-iteration step is then a product
+__global__ void k_cg_minv(double *__restrict__ Minv, const double *__restrict__ D, const double *__restrict__ s,
+                          double eta, int64_t N, int n) {
     const int64_t tot = N * n;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < tot; i += (int64_t)gridDim.x * blockDim.x) {
         const int j = (int)(i / N);
         const int64_t r = i - (int64_t)j * N;
-        Z[i] = R[i] / hypot(D[r] - s[j], eta);
+        Minv[i] = 1.0 / hypot(D[r] - s[j], eta);
     }
+}
+
+// Z = Minv o R
+__global__ void k_cg_precond(double *__restrict__ Z, const double *__restrict__ R, const double *__restrict__ Minv,
+                             int64_t tot) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < tot; i += (int64_t)gridDim.x * blockDim.x)
+        Z[i] = Minv[i] * R[i];
 }
 
 // P = Z + beta_j P
@@ -147,7 +155,7 @@ void complement_solve(kf_op *op, const double *basis, int64_t ldbs, int nb, cons
                       int64_t ldx, CgResult &res, cudaStream_t s) {
     const int64_t N = op->N;
     const size_t blk = (size_t)N * n * sizeof(double);
-    double *QB, *X, *R, *Z, *P, *AP, *T, *D, *sm, *part, *C;
+    double *QB, *X, *R, *Z, *P, *AP, *T, *Mi, *D, *sm, *part, *C;
     const CgRed rd = cg_red(N, n);
     const size_t part_bytes = std::max(gram_partials_size(std::max(nb, 1), n, N), (size_t)rd.nblk * n * sizeof(double));
     std::vector<void *> owned;
@@ -167,6 +175,7 @@ void complement_solve(kf_op *op, const double *basis, int64_t ldbs, int nb, cons
         dalloc(P, blk);
         dalloc(AP, blk);
         dalloc(T, blk);
+        dalloc(Mi, blk);
         dalloc(D, (size_t)N * sizeof(double));
         dalloc(sm, (size_t)8 * n * sizeof(double));   // s, alpha, beta, rho, active, kappa, rn2, rho'
         dalloc(part, part_bytes);
@@ -175,6 +184,8 @@ void complement_solve(kf_op *op, const double *basis, int64_t ldbs, int nb, cons
         double *d_kappa = sm + 5 * n, *d_rn2 = sm + 6 * n, *d_rhon = sm + 7 * n;
         KF_CUDA(cudaMemcpyAsync(D, op->h_fulldiag.data(), (size_t)N * sizeof(double), cudaMemcpyHostToDevice, s));
         KF_CUDA(cudaMemcpyAsync(d_s, shifts, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, s));
+        k_cg_minv<<<ew_grid(N * n), CG_THREADS, 0, s>>>(Mi, D, d_s, eta, N, n);
+        KF_LAUNCH_CHECK();
         KF_CUDA(cudaMemcpy2DAsync(QB, N * sizeof(double), B, ldb * sizeof(double), N * sizeof(double), n,
                                   cudaMemcpyDeviceToDevice, s));
         auto project = [&](double *Y) {
@@ -220,7 +231,7 @@ void complement_solve(kf_op *op, const double *basis, int64_t ldbs, int nb, cons
         scale_columns<double>(QB, N, n, N, d_beta, s);
         KF_CUDA(cudaMemsetAsync(X, 0, blk, s));
         KF_CUDA(cudaMemcpyAsync(R, QB, blk, cudaMemcpyDeviceToDevice, s));
-        k_cg_precond<<<ew_grid(N * n), CG_THREADS, 0, s>>>(Z, R, D, d_s, eta, N, n);
+        k_cg_precond<<<ew_grid(N * n), CG_THREADS, 0, s>>>(Z, R, Mi, N * n);
         KF_LAUNCH_CHECK();
         project(Z);
         KF_CUDA(cudaMemcpyAsync(P, Z, blk, cudaMemcpyDeviceToDevice, s));
@@ -265,7 +276,7 @@ void complement_solve(kf_op *op, const double *basis, int64_t ldbs, int nb, cons
             KF_LAUNCH_CHECK();
             k_cg_reduce<<<(n + 127) / 128, 128, 0, s>>>(part, rd.nblk, n, d_rn2);
             KF_LAUNCH_CHECK();
-            k_cg_precond<<<ew_grid(N * n), CG_THREADS, 0, s>>>(Z, R, D, d_s, eta, N, n);
+            k_cg_precond<<<ew_grid(N * n), CG_THREADS, 0, s>>>(Z, R, Mi, N * n);
             KF_LAUNCH_CHECK();
             project(Z);
             coldot(R, Z, d_rhon);

@@ -43,6 +43,16 @@ extern std::atomic<uint64_t> g_launches;
         KF_CUDA(cudaGetLastError());                                                           \
     } while (0)
 
+// Bounds-recording builds (-DKF_CHECK, kfgpu.build.build_library(check=True)): a kernel tests an
+// index before an access, writes the failing site's number into the second word of the host-mapped
+// error allocation (tc_error_word() + 1) and skips the access; it never traps.  In normal builds the
+// test is the constant true.
+#ifdef KF_CHECK
+#define KF_CHK(cond, err, site) ((cond) ? true : ((*(volatile int *)((err) + 1) = (site)), false))
+#else
+#define KF_CHK(cond, err, site) true
+#endif
+
 #define KF_REQUIRE(cond, code, msg)                                                            \
     do {                                                                                       \
         if (!(cond)) throw ::kf::Error((code), (msg));                                         \

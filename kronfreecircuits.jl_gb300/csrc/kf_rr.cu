@@ -7,7 +7,7 @@
 // the kernel costs more GPU time per iteration (~150-200 us on one SM) than the host round trip it
 // removes (~65 us of idle GPU), 111.9 against 122.8 eigenpairs/s on the three-mode leaf.
 //
-// Why FP32 suffices here: the FP32 phase stops at residuals of 2e-6 ||H||; Jacobi in FP32 gives
+// Why FP32 suffices here: the FP32 phase stops at residuals of 1e-6 ||H||; Jacobi in FP32 gives
 // Ritz values to about 1e-7 of ||A|| <= ||H|| and eigenvectors orthonormal to about 1e-7, the
 // precision of the FP32 blocks they rotate.  The FP64 refinement keeps its FP64 Rayleigh-Ritz.
 //

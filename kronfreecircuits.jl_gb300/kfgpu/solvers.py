@@ -29,7 +29,7 @@ def _arg(cond, msg):
 
 class LOBPCG:
     def __init__(self, tol=1e-8, maxiter=1000, preconditioner="ritz", eta=0.01, guard=4, seed="product",
-                 precision="f64", mixed_switch=2e-6, fallback_iters=3, fallback_resid=0.0, rng_seed=0x4B46,
+                 precision="f64", mixed_switch=1e-6, fallback_iters=3, fallback_resid=0.0, rng_seed=0x4B46,
                  buffer=None):
         _arg(tol > 0 and math.isfinite(tol), f"LOBPCG: tol must be positive and finite, got {tol}")
         _arg(maxiter >= 1, f"LOBPCG: maxiter must be at least 1, got {maxiter}")

@@ -4,7 +4,7 @@ host path assembles it (upper triangle of the merged [X_a Q]'[HX_a HZ] layout, o
 [X_a'HX_a | X_a'HZ | Q'HZ] blocks), odd and even sizes up to 64 with clustered eigenvalues: Ritz
 values within 2e-6 ||A||, the coefficient layout [C_x | [0; C_z]], the retained eigenvectors
 orthonormal to 1e-5 and spanning the same invariant subspace; and the failed-Cholesky path (X kept,
-P dropped, theta untouched).  FP32 is the phase's own precision: it stops at 2e-6 ||H||.
+P dropped, theta untouched).  FP32 is the phase's own precision: it stops at 1e-6 ||H||.
 """
 import ctypes as C
 
