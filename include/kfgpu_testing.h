@@ -129,6 +129,11 @@ int kf_test_op_scratch_bytes(const struct kf_op *op, uint64_t *bytes);
 int kf_test_march_plan(const struct kf_op *op, int64_t b, int32_t f32, int32_t sms, int32_t *eligible,
                        int32_t *geom);
 
+/* Bounds-recording builds (-DKF_CHECK): the site number of the first failed bounds check since the
+ * last call (0: none; the word is reset), after a device synchronisation; check_build = 1 when the
+ * library was compiled with KF_CHECK. */
+int kf_test_check_word(int32_t *site, int32_t *check_build);
+
 /* The device Rayleigh-Ritz eigensolver of the FP32 LOBPCG phase (FP32 Jacobi, one CTA): G on the
  * host in the merged (ldg x ldg, rows [X_a; Q], columns [H X_a, H Z]) or packed layout; writes
  * C (ns x 2 na: [C_x | [0; C_z]]) and the na lowest Ritz values into theta_out (in / out).  status

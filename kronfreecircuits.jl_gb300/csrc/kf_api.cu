@@ -220,6 +220,19 @@ int kf_op_sandwich(kf_op *op, const double *W, int64_t ldw, int32_t kw, const do
     });
 }
 
+int kf_test_check_word(int32_t *site, int32_t *check_build) {
+    return guarded([&] {
+        KF_REQUIRE(site && check_build, KF_EINVAL, "kf_test_check_word: NULL argument");
+        KF_CUDA(cudaDeviceSynchronize());
+        *site = kf::check_take_site();
+#ifdef KF_CHECK
+        *check_build = 1;
+#else
+        *check_build = 0;
+#endif
+    });
+}
+
 int kf_test_rr_eig(const double *G, int32_t ldg, int32_t packed, int32_t na, int32_t k, int32_t status, double *C_out,
                    double *theta_out) {
     return guarded([&] {

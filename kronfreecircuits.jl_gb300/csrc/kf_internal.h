@@ -130,6 +130,7 @@ void tc_mode_product(float *Y, int64_t ldy, const float *X, int64_t ldx, const T
                      int64_t b, double alpha, double beta, cudaStream_t s);
 int tc_take_error();
 int *tc_error_word();  // the host-mapped word device-side waits report KF_ETIMEOUT in
+int check_take_site(); // KF_CHECK builds: the first failed bounds-check site since the last call (0: none)
 // FP32 block update on the tensor cores (kf_tcgemm.cu), TF32 hi / lo operands, kx <= 64, ky <= 80
 bool update_tc_ok(int kx, int ky);
 void update_tc(float *Y, int64_t ldy, int ky, const float *X0, int64_t ldx0, int kx0, const float *X1, int64_t ldx1,

@@ -565,7 +565,8 @@ static size_t mode_pipe_smem(const TcMatrix &m, int tn) {
     return (size_t)m.Mp * m.Kp * 2 + (size_t)2 * tn * m.Kp * 2 + (size_t)8 * 32 * MP_EPS * 4 + 10 * 8 + 16;
 }
 
-// host-mapped error word shared by every tensor-core launch
+// host-mapped error words shared by every tensor-core and bulk-copy launch: [0] a wait that ran out
+// (KF_ETIMEOUT), [1] in KF_CHECK builds the site of the first failed bounds check
 std::mutex g_tc_mu;
 int *g_tc_err_host = nullptr;
 int *g_tc_err_dev = nullptr;
@@ -575,8 +576,8 @@ int g_mp_attr_mask = 0;   // devices whose pipelined-kernel attributes are set
 int *tc_err_word() {
     std::lock_guard<std::mutex> lk(g_tc_mu);
     if (!g_tc_err_host) {
-        KF_CUDA(cudaHostAlloc(&g_tc_err_host, sizeof(int), cudaHostAllocMapped));
-        *g_tc_err_host = 0;
+        KF_CUDA(cudaHostAlloc(&g_tc_err_host, 2 * sizeof(int), cudaHostAllocMapped));
+        g_tc_err_host[0] = g_tc_err_host[1] = 0;
         KF_CUDA(cudaHostGetDevicePointer(&g_tc_err_dev, g_tc_err_host, 0));
     }
     return g_tc_err_dev;
@@ -757,6 +758,14 @@ void tc_mode_product(float *Y, int64_t ldy, const float *X, int64_t ldx, const T
 }
 
 int *tc_error_word() { return tc_err_word(); }
+
+int check_take_site() {
+    tc_err_word();   // allocates the words on first use
+    std::lock_guard<std::mutex> lk(g_tc_mu);
+    const int s = *(volatile int *)(g_tc_err_host + 1);
+    *(volatile int *)(g_tc_err_host + 1) = 0;
+    return s;
+}
 
 int tc_take_error() {
     std::lock_guard<std::mutex> lk(g_tc_mu);

@@ -10,7 +10,8 @@ import ctypes as C
 import os
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(_HERE, "libkfgpu.so")
+# KF_LIB selects another build of the library (the bounds-recording libkfgpu_check.so)
+LIB_PATH = os.environ.get("KF_LIB") or os.path.join(_HERE, "libkfgpu.so")
 
 KF_OK, KF_EINVAL, KF_EDIM, KF_EALIAS, KF_ECUDA, KF_ENOCONV, KF_EBREAKDOWN, KF_ENOMEM, KF_ETIMEOUT, KF_ENOTFINITE = range(10)
 KF_F64, KF_F32, KF_HOST = 0x0, 0x1, 0x2
@@ -135,6 +136,7 @@ def lib():
                                         C.POINTER(C.c_float), P]),
         "kf_test_chol2": (C.c_int, [P, C.c_int32, C.c_int32, P, P]),
         "kf_test_op_scratch_bytes": (C.c_int, [P, P]),
+        "kf_test_check_word": (C.c_int, [P, P]),
         "kf_test_rr_eig": (C.c_int, [P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, P, P]),
         "kf_test_march_plan": (C.c_int, [P, C.c_int64, C.c_int32, C.c_int32, P, P]),
         "kf_test_sym_eig": (C.c_int, [C.c_int32, P, C.c_int32, P, P, C.c_int32]),

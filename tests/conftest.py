@@ -14,6 +14,20 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300) and the built libkfgpu.so")
 
 
+def pytest_sessionfinish(session, exitstatus):
+    """With KF_CHECK_CLEAN=1 (a run against the bounds-recording library, KF_LIB): fail the session
+    when the library is not a KF_CHECK build or a kernel recorded a failed bounds check."""
+    if os.environ.get("KF_CHECK_CLEAN") != "1":
+        return
+    import ctypes as C
+    from kfgpu import _abi
+    site, chk = C.c_int32(0), C.c_int32(0)
+    _abi.check(_abi.lib().kf_test_check_word(C.byref(site), C.byref(chk)))
+    if chk.value != 1 or site.value != 0:
+        print(f"\nKF_CHECK: check build {chk.value}, first failed bounds-check site {site.value}")
+        session.exitstatus = 1
+
+
 @pytest.fixture(scope="session")
 def goldens():
     import json
