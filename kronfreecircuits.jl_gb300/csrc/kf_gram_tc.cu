@@ -27,15 +27,23 @@
 // The epilogue adds hi*hi + hi*lo on the lanes of the hi rows and lo*hi on the lanes of the lo
 // rows into two FP32 partial sets per CTA; the reduction sums both.
 //
-// The MMAs are not what bounds it: a 32-row chunk takes ~1,100 cycles per SM against ~200 for its
-// MMAs.  A clock64 timeline of one CTA shows the producers waiting for data requested several
-// microseconds earlier: the loads deliver well under the 4.8-5.0 TB/s that a plain cp.async stream
-// of the same column pieces reaches.  In timing-only copies, dropping the split, the MMAs, the
-// epilogue's loads or the proxy fence each changed the time by under 10%, and so did a variant with
-// 128-byte-swizzled images, 256-byte column runs, four accumulator slots, one barrier arrival per
-// warp, suspended waits and other ring depths.
+// Two kernels share these layouts.  k_gram_tma (the default, below) loads with 2-D tensor copies
+// of 128 rows x k columns per source; k_gram_tc, the fallback where the driver gives no tensor-map
+// encoder, copies 16-byte pieces with cp.async.  What was measured on GB300 on the way there:
+//   - a stream of tensor copies over the solve's 54 columns reaches 1.4-2.0 TB/s with 32-row boxes
+//     (128-byte rows), 2.8 TB/s with 64-row, 5.0 TB/s with 128-row and 5.7 TB/s with 256-row boxes:
+//     the copy engine pays per box row, so the rows must be long;
+//   - a synchronisation per 32-row chunk (split -> issuer -> epilogue -> issuer) costs more than
+//     the chunk's loads, split and 4 MMAs together: timing-only copies that dropped the loads, the
+//     split, the MMAs or the epilogue's TMEM loads all stayed within 15% of the full kernel, and a
+//     clock64 timeline showed each barrier hop taking a few hundred cycles.  So the 64-row pools
+//     synchronise once per 4 chunks (two accumulator slots of 2 chunks each, double-buffered);
+//   - the split loads its pieces for a chunk before storing any (the loads and stores go to
+//     different buffers, which the compiler cannot tell apart).
+// [X Z]'Z at block 18 (18 + 36 columns, N = 671,744) went 94.5 -> 53.4 us with these, the
+// Rayleigh-Ritz pool (108 columns) 131.3 -> 106.7 us.
 //
-// One persistent CTA per SM (or per chunk when there are fewer), warp-specialised:
+// k_gram_tc: one persistent CTA per SM (or per chunk when there are fewer), warp-specialised:
 //   warps 0-7   producers: 16-byte cp.async copies of their pieces of the chunk straight into the
 //               core-matrix layout of the hi image of stage t % S (S - R chunks in flight ahead),
 //               then the split of their own pieces into hi (in place) and lo, arrive on full[s];
@@ -45,11 +53,15 @@
 //               / 4 the half of the B columns; adds slot t % 2 into FP32 registers (round to
 //               nearest), arrives on acce[t % 2]; at the end writes the CTA's FP32 partial sums.
 // The tensor cores' FP32 accumulation rounds toward zero, a bias of about 2^-24 of the running sum
-// per addition: accumulator chains of one chunk (4 MMAs per accumulator) keep it near 1e-7.
+// per addition: accumulator chains of one or two chunks (4 or 8 MMAs per accumulator) keep it near
+// 1e-7 or 2e-7 of an entry.
 // Every wait is an mbarrier wait with a cycle budget; when one runs out the CTA records
 // KF_ETIMEOUT in the host-mapped error word, every role leaves its loop at its next check, the
 // issuer waits (bounded) for its MMAs in flight, and TMEM is freed.
+#include <cuda.h>   // CUtensorMap and its enums (the encoder itself is taken from the driver at run time)
+
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -121,21 +133,37 @@ __device__ __forceinline__ void gt_arrive(uint64_t *bar) {
 }
 
 // completion number `n` (0-based) of the barrier's phases; false when the budget ran out or the
-// CTA is aborting
+// CTA is aborting.  The waiting thread is suspended inside try_wait until the phase completes (or
+// for at most the hint, 1 ms), so idle roles take no issue slots and no shared-memory bandwidth
+// from the ones working: with spinning waits, a wait on a barrier that had completed long before
+// took the MMA issuer 350-430 cycles.
 __device__ __forceinline__ bool gt_wait(uint64_t *bar, uint32_t n, volatile int *abort) {
     const uint32_t parity = n & 1u;
-    const long long t0 = clock64();
-    for (;;) {
+    {
+        // a phase that has completed already: the non-blocking test answers without the try_wait
         uint32_t done;
         asm volatile(
-            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "{\n\t.reg .pred p;\n\tmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
             "selp.b32 %0, 1, 0, p;\n\t}\n"
             : "=r"(done)
             : "r"(gsu32(bar)), "r"(parity)
             : "memory");
         if (done) return true;
+    }
+    long long t0 = -1;
+    for (;;) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+            "selp.b32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(done)
+            : "r"(gsu32(bar)), "r"(parity), "r"(1000000u)
+            : "memory");
+        if (done) return true;
         if (*abort) return false;
-        if (clock64() - t0 > GT_WAIT_CYCLES) return false;
+        const long long now = clock64();
+        if (t0 < 0) t0 = now;
+        else if (now - t0 > GT_WAIT_CYCLES) return false;
     }
 }
 
@@ -155,6 +183,10 @@ __device__ __forceinline__ void gt_ld16(uint32_t taddr, uint32_t (&r)[16]) {
 }
 
 struct GtArgs {
+    CUtensorMap tm[GT_MAX_SRC];    // TMA variant: per source, boxes of 128 rows x k columns
+    uint32_t roff[GT_MAX_SRC];     // TMA variant: byte offset of source q's box in a raw slot
+    uint32_t rslot, tx_bytes;      // TMA variant: bytes of a raw slot (one group, all sources)
+    int nraw;                      // TMA variant: raw slots
     const float *p[GT_MAX_SRC];
     int64_t ld[GT_MAX_SRC];
     int off[GT_MAX_SRC], k[GT_MAX_SRC];   // hi image rows [off, off + k) per source
@@ -405,6 +437,344 @@ __global__ void __launch_bounds__(GT_THREADS, 1) k_gram_tc(const GtArgs a) {
     if (warp == 8) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(512));
 }
 
+// ---- The TMA-fed variant (the default).  Same pool layouts, accumulator slots and epilogue as
+// k_gram_tc; the loads are 2-D tensor copies of 128 rows x k columns per source (512-byte rows:
+// measured on GB300, a stream of such boxes over the solve's 54 columns reaches 5.0 TB/s, one of
+// 32-row boxes -- 128-byte rows -- only 1.4-2.0 TB/s, whatever the ring depth), into a raw ring of
+// groups (per source, per column, 128 consecutive FP32 values).  Four 32-row chunks per group:
+//   warp 0      producer (one lane): one box per source per group into raw slot g % R,
+//               completing on rfull;
+//   warps 1-4   split: per chunk, the 16-byte pieces of the chunk's pool rows from the raw slot
+//               (eight threads read one column's 128 bytes) into hi and lo operand images of
+//               stage t % SO, K-major in the 128-byte-swizzled layout (piece j of image row r at
+//               position j ^ (r % 8), 8-row atoms 1024 bytes apart); one arrival per warp on
+//               ofull, and on rempty once the group's four chunks are done;
+//   warp 5      issuer, warps 6-13 epilogue: as in k_gram_tc (swizzled descriptors).
+// Rows past N read as zero (the tensor copy's fill), so a group is always four chunks.
+constexpr int GM_SPLITTERS = 128;                               // warps 1-4
+constexpr int GM_THREADS = 32 + GM_SPLITTERS + 32 + GT_EPI;     // 448
+constexpr int GM_GR = 128;                                      // data rows per group
+constexpr int GM_CPG = GM_GR / GT_KC;                           // chunks per group
+constexpr int GM_MAX_RAW = 8;                                   // raw slots at most
+
+template <int RB, int SO, int CPS>
+struct GmPlan {
+    static constexpr int IMG = RB * GT_KC * 4;
+    static constexpr int CHB = 2 * IMG;                         // hi + lo images of one chunk
+    static constexpr int STAGE = CPS * CHB;                     // one synchronisation unit
+    static constexpr int OPS = SO * STAGE;                      // operand stages
+    static constexpr int PPT = RB * 8 / GM_SPLITTERS;           // 16-byte pieces of the pool rows per thread
+    static constexpr int ASL = CPS == 4 ? 2 : 1;                // accumulator slots per unit
+    static constexpr int CPA = CPS / ASL;                       // chunks accumulated per slot
+    static constexpr size_t BARS = 8 * (2 * GM_MAX_RAW + 2 * SO + 2 * GT_MAX_SLOTS + 2);
+    static_assert(IMG % 1024 == 0, "swizzle atoms");
+    static_assert(CPS == 1 || CPS == 4, "chunks per unit");
+};
+
+// dynamic shared memory of a launch with R raw slots of `rslot` bytes
+template <int RB, int SO, int CPS>
+size_t gm_smem(int R, uint32_t rslot) {
+    return 1024 + (size_t)GmPlan<RB, SO, CPS>::OPS + (size_t)R * rslot + GmPlan<RB, SO, CPS>::BARS;
+}
+
+// K-major operand in the 128-byte-swizzled layout: rows of 128 bytes, 8-row atoms 1024 bytes apart
+__device__ __forceinline__ uint64_t gm_desc_sw128(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)1 << 16;                  // leading-dimension offset (unused for swizzled K-major)
+    d |= (uint64_t)(1024u >> 4) << 32;       // stride between 8-row atoms
+    d |= (uint64_t)1 << 46;                  // descriptor version (tcgen05)
+    d |= (uint64_t)2 << 61;                  // 128-byte swizzle
+    return d;
+}
+
+__device__ __forceinline__ void gm_expect(uint64_t *bar, uint32_t bytes) {
+    asm volatile(
+        "{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}\n" ::"r"(gsu32(bar)),
+        "r"(bytes)
+        : "memory");
+}
+
+// one 2-D box of the tensor map (a kernel parameter) at element coordinates (x, y)
+__device__ __forceinline__ void gm_tma2d(uint32_t dst, const CUtensorMap *tm, int x, int y, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+        "[%4];\n" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(gsu32(bar))
+        : "memory");
+}
+
+template <int RB, int SO, bool SPLIT, int CPS>
+__global__ void __launch_bounds__(GM_THREADS, 1) k_gram_tma(const __grid_constant__ GtArgs a) {
+    using P = GmPlan<RB, SO, CPS>;
+    static_assert(CPS == 1 || RB == 64 || SPLIT, "four chunks per unit need the one-MMA accumulator layout");
+    constexpr int UPG = GM_CPG / CPS;          // units per group
+    static_assert(!SPLIT || RB == 128, "the split layout fills two 128-row images");
+    constexpr bool ONE = RB == 64 || SPLIT;
+    constexpr uint32_t SLOT = ONE ? 128 : 256;
+    extern __shared__ unsigned char gm_smem_raw[];
+    unsigned char *ops = gm_smem_raw + ((1024u - (gsu32(gm_smem_raw) & 1023u)) & 1023u);
+    const int R = a.nraw;
+    unsigned char *raw = ops + P::OPS;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(raw + (size_t)R * a.rslot);
+    uint64_t *rfull = bars, *rempty = bars + GM_MAX_RAW, *ofull = bars + 2 * GM_MAX_RAW, *oempty = ofull + SO,
+             *accf = oempty + SO, *acce = accf + GT_MAX_SLOTS, *fin = acce + GT_MAX_SLOTS;
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(fin + 1);
+    __shared__ volatile int s_abort;
+
+    // zero the operand images once: rows that no source fills (alignment gaps) stay zero
+    for (size_t o = (size_t)tid * 16; o < (size_t)P::OPS; o += (size_t)GM_THREADS * 16)
+        *reinterpret_cast<uint4 *>(ops + o) = make_uint4(0u, 0u, 0u, 0u);
+    if (tid == 0) {
+        for (int q = 0; q < R; ++q) {
+            gt_bar_init(rfull + q, 1);
+            gt_bar_init(rempty + q, GM_SPLITTERS / 32);
+        }
+        for (int q = 0; q < SO; ++q) {
+            gt_bar_init(ofull + q, GM_SPLITTERS / 32);
+            gt_bar_init(oempty + q, 1);
+        }
+        for (int q = 0; q < GT_MAX_SLOTS; ++q) {
+            gt_bar_init(accf + q, 1);
+            gt_bar_init(acce + q, GT_EPI / 32);
+        }
+        gt_bar_init(fin, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        s_abort = 0;
+    }
+    if (warp == 5) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(gsu32(tslot)),
+                     "r"(512));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = *tslot;
+    // this CTA's groups: a contiguous range [gfirst, gfirst + myg)
+    const int64_t ngroups = a.nchunks;
+    const int64_t gper = ngroups / gridDim.x, grem = ngroups % gridDim.x;
+    const int64_t myg = gper + ((int64_t)blockIdx.x < grem ? 1 : 0);
+    const int64_t gfirst = (int64_t)blockIdx.x * gper + ((int64_t)blockIdx.x < grem ? (int64_t)blockIdx.x : grem);
+    const int64_t myu = myg * UPG;     // synchronisation units
+    const uint32_t obase = gsu32(ops), rbase = gsu32(raw);
+
+    if (warp == 0) {
+        // ---- producer (one lane)
+        if (lane == 0) {
+            int64_t issued = 0;
+            for (int64_t g = 0; g < myg; ++g) {
+                const int r = (int)(g % R);
+                // the slot held group g - R: its four chunks must have been split
+                if (g >= R && !gt_wait(rempty + r, (uint32_t)(g / R - 1), &s_abort)) { s_abort = 1; break; }
+                gm_expect(rfull + r, a.tx_bytes);
+                const int x = (int)((gfirst + g) * GM_GR);
+                const uint32_t slot = rbase + (uint32_t)r * a.rslot;
+                for (int q = 0; q < a.nsrc; ++q) gm_tma2d(slot + a.roff[q], &a.tm[q], x, 0, rfull + r);
+                ++issued;
+            }
+            if (s_abort) {
+                // copies still in flight write this CTA's shared memory: wait (bounded) for them
+                volatile int never = 0;
+                for (int64_t g = issued > R ? issued - R : 0; g < issued; ++g)
+                    (void)gt_wait(rfull + g % R, (uint32_t)(g / R), &never);
+            }
+        }
+    } else if (warp <= 4) {
+        // ---- split: piece e of a chunk's pool rows is row m = e / 8, K piece j = e % 8 (data rows
+        // 4 j .. 4 j + 3 of the chunk); eight consecutive threads read one column's 128 bytes and
+        // write one swizzled image row (conflict-free both ways)
+        const int ct = tid - 32;
+        uint32_t roff[P::PPT], hoff[P::PPT], loff[P::PPT];
+        bool has[P::PPT];
+#pragma unroll
+        for (int j = 0; j < P::PPT; ++j) {
+            const int e = ct + j * GM_SPLITTERS;
+            const int m = e >> 3, pj = e & 7;
+            int ph, pl;
+            if (SPLIT) {
+                ph = m < a.b_off ? m : RB + (m - a.b_off);
+                pl = m < a.b_off ? 64 + m : RB + a.nbr + (m - a.b_off);
+            } else {
+                ph = m;
+                pl = RB + (m >= a.b_off ? m - a.b_off : m + a.nbr);
+            }
+            hoff[j] = (uint32_t)(ph * 128 + ((pj ^ (ph & 7)) << 4));
+            loff[j] = (uint32_t)(pl * 128 + ((pj ^ (pl & 7)) << 4));
+            has[j] = false;
+            roff[j] = 0;
+            for (int q = 0; q < a.nsrc; ++q)
+                if (m >= a.off[q] && m < a.off[q] + a.k[q]) {
+                    has[j] = true;
+                    roff[j] = a.roff[q] + (uint32_t)(m - a.off[q]) * (GM_GR * 4) + (uint32_t)pj * 16;
+                }
+        }
+        bool ok = true;
+        for (int64_t g = 0; g < myg && ok; ++g) {
+            const int r = (int)(g % R);
+            ok = __all_sync(0xffffffffu, gt_wait(rfull + r, (uint32_t)(g / R), &s_abort));
+            if (!ok) break;
+            const unsigned char *slot = raw + (size_t)r * a.rslot;
+            for (int i = 0; i < UPG; ++i) {
+                const int64_t u = g * UPG + i;
+                const int o = (int)(u % SO);
+                // the stage held unit u - SO: its MMAs must have retired
+                if (u >= SO) {
+                    ok = __all_sync(0xffffffffu, gt_wait(oempty + o, (uint32_t)(u / SO - 1), &s_abort));
+                    if (!ok) break;
+                }
+                // the pieces of chunk cu + 1 are loaded before those of chunk cu are stored, so the
+                // loads of a chunk are in flight together (a piece without a source reads the slot's
+                // first bytes and is not stored)
+                uint4 v[P::PPT], w[P::PPT];
+#pragma unroll
+                for (int j = 0; j < P::PPT; ++j)
+                    v[j] = *reinterpret_cast<const uint4 *>(slot + roff[j] + (i * CPS) * 128);
+#pragma unroll
+                for (int cu = 0; cu < CPS; ++cu) {
+                    if (cu + 1 < CPS) {
+#pragma unroll
+                        for (int j = 0; j < P::PPT; ++j)
+                            w[j] = *reinterpret_cast<const uint4 *>(slot + roff[j] + (i * CPS + cu + 1) * 128);
+                    }
+                    unsigned char *st = ops + (size_t)o * P::STAGE + (size_t)cu * P::CHB;
+#pragma unroll
+                    for (int j = 0; j < P::PPT; ++j) {
+                        if (!has[j]) continue;
+                        const uint32_t x[4] = {v[j].x, v[j].y, v[j].z, v[j].w};
+                        uint32_t h[4], l[4];
+#pragma unroll
+                        for (int e = 0; e < 4; ++e) {
+                            h[e] = x[e] & 0xFFFFE000u;
+                            l[e] = __float_as_uint(__uint_as_float(x[e]) - __uint_as_float(h[e]));
+                        }
+                        *reinterpret_cast<uint4 *>(st + hoff[j]) = make_uint4(h[0], h[1], h[2], h[3]);
+                        *reinterpret_cast<uint4 *>(st + loff[j]) = make_uint4(l[0], l[1], l[2], l[3]);
+                    }
+#pragma unroll
+                    for (int j = 0; j < P::PPT; ++j) v[j] = w[j];
+                }
+                asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+                __syncwarp();
+                if (lane == 0) gt_arrive(ofull + o);
+            }
+            if (!ok) break;
+            // the group's raw slot is free for the producer
+            __syncwarp();
+            if (lane == 0) gt_arrive(rempty + r);
+        }
+        if (!ok) s_abort = 1;
+    } else if (warp == 5) {
+        // ---- MMA issuer (one lane)
+        if (lane == 0) {
+            const uint32_t n1 = (uint32_t)(2 * a.nbr);
+            const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((n1 >> 3) << 17) | ((128u >> 4) << 24);
+            const uint32_t boff = SPLIT ? (uint32_t)P::IMG : (uint32_t)a.b_off * 128u;   // [B_hi; B_lo]
+            int64_t issued = 0;
+            for (int64_t u = 0; u < myu; ++u) {
+                const int o = (int)(u % SO), sl = (int)(u & 1);
+                if (!gt_wait(ofull + o, (uint32_t)(u / SO), &s_abort)) { s_abort = 1; break; }
+                if (u >= 2 && !gt_wait(acce + sl, (uint32_t)(u / 2 - 1), &s_abort)) { s_abort = 1; break; }
+                asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+#pragma unroll
+                for (int cu = 0; cu < CPS; ++cu) {
+                    const uint32_t hi = obase + (uint32_t)o * P::STAGE + (uint32_t)cu * P::CHB, lo = hi + P::IMG;
+                    // unit u's slots: sl * ASL .. + ASL - 1, CPA chunks accumulated in each
+                    const uint32_t d = tmem + (uint32_t)(sl * P::ASL + cu / P::CPA) * SLOT;
+#pragma unroll
+                    for (int ks = 0; ks < GT_KC / 8; ++ks) {
+                        const uint32_t kb = (uint32_t)ks * 32;   // 8 TF32 values of every image row
+                        const uint32_t acc = (cu % P::CPA == 0 && ks == 0) ? 0u : 1u;
+                        const uint64_t db = gm_desc_sw128(hi + boff + kb);
+                        gt_mma(d, gm_desc_sw128(hi + kb), db, idesc, acc);
+                        if (!ONE) gt_mma(d + 128, gm_desc_sw128(lo + kb), db, idesc, acc);
+                    }
+                }
+                gt_commit(oempty + o);
+                gt_commit(accf + sl);
+                ++issued;
+            }
+            if (issued > 0 && s_abort) {
+                gt_commit(fin);
+                volatile int never = 0;
+                (void)gt_wait(fin, 0, &never);
+            }
+        }
+    } else {
+        // ---- epilogue (warps 6-13), as in k_gram_tc
+        const int q = warp & 3, m = q * 32 + lane, h = (warp - 6) >> 2;
+        const int h0 = min(a.nbr, (a.nbr / 2 + 15) / 16 * 16);
+        const int cb = h == 0 ? 0 : h0, ce = h == 0 ? h0 : a.nbr;
+        const uint32_t lb = (uint32_t)(q * 32) << 16;
+        const bool has_hi = !ONE || q < 2, has_lo = !ONE || q >= 2;
+        float acc_hi[GT_NBH], acc_lo[GT_NBH];
+#pragma unroll
+        for (int c = 0; c < GT_NBH; ++c) acc_hi[c] = acc_lo[c] = 0.f;
+        bool ok = true;
+        for (int64_t u = 0; u < myu; ++u) {
+            const int sl = (int)(u & 1);
+            ok = gt_wait(accf + sl, (uint32_t)(u / 2), &s_abort);
+            ok = __all_sync(0xffffffffu, ok);   // tcgen05.ld is warp-collective
+            if (!ok) { s_abort = 1; break; }
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+#pragma unroll
+            for (int as = 0; as < P::ASL; ++as) {
+            const uint32_t d = tmem + lb + (uint32_t)(sl * P::ASL + as) * SLOT;
+#pragma unroll
+            for (int c0 = 0; c0 < GT_NBH; c0 += 16) {
+                if (cb + c0 >= ce) break;
+                const uint32_t col = (uint32_t)(cb + c0);
+                uint32_t r1[16];
+                if (has_hi) {
+                    gt_ld16(d + col, r1);
+                    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+                    for (int w = 0; w < 16; ++w) acc_hi[c0 + w] += __uint_as_float(r1[w]);
+                    gt_ld16(d + (uint32_t)a.nbr + col, r1);
+                    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+                    for (int w = 0; w < 16; ++w) acc_hi[c0 + w] += __uint_as_float(r1[w]);
+                }
+                if (has_lo) {
+                    gt_ld16(d + (ONE ? 0u : 128u) + col, r1);
+                    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+                    for (int w = 0; w < 16; ++w) acc_lo[c0 + w] += __uint_as_float(r1[w]);
+                }
+            }
+            }
+            // the warp's loads have completed (tcgen05.wait::ld): one arrival per warp
+            asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+            __syncwarp();
+            if (lane == 0) gt_arrive(acce + sl);
+        }
+        if (ok) {
+            const size_t E = (size_t)a.nr * a.nc;
+            float *out = a.part + (size_t)blockIdx.x * 2 * E;
+            const int ih = has_hi ? a.rinv_hi[m] : 255;
+            const int il = has_lo ? a.rinv_lo[ONE ? m - 64 : m] : 255;
+#pragma unroll
+            for (int c = 0; c < GT_NBH; ++c) {
+                if (cb + c >= ce) break;
+                const int j = a.cinv[cb + c];
+                if (j == 255) continue;
+                if (ih != 255) out[ih + (size_t)a.nr * j] = acc_hi[c];
+                if (il != 255) out[E + il + (size_t)a.nr * j] = acc_lo[c];
+            }
+        }
+    }
+    if (s_abort && tid == 0) {
+        *(volatile int *)a.err = KF_ETIMEOUT;
+        __threadfence_system();
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    if (warp == 5) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(512));
+}
+
 // G[e] = sum over the CTAs' FP32 partials, in FP64, one warp per entry
 __global__ void k_reduce_partials_f32(const float *__restrict__ part, int nparts, int n, double *__restrict__ G) {
     const int e = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
@@ -417,17 +787,84 @@ __global__ void k_reduce_partials_f32(const float *__restrict__ part, int nparts
     if (lane == 0) G[e] = s;
 }
 
+std::mutex g_gt_mu;
 using GtKernel = void (*)(const GtArgs);
-const GtKernel g_gt_kern[3] = {k_gram_tc<64, 12, 2>, k_gram_tc<128, 6, 2>, k_gram_tc<128, 6, 2, true>};
-const size_t g_gt_smem[3] = {GtPlan<64, 12, 2>::SMEM, GtPlan<128, 6, 2>::SMEM, GtPlan<128, 6, 2>::SMEM};
+// plans 0-2: the cp.async kernel (RB 64, RB 128, split); 3-5: the TMA kernel (same order, its raw
+// ring sized per launch from what the device leaves after the operand stages)
+const GtKernel g_gt_kern[6] = {k_gram_tc<64, 12, 2>,         k_gram_tc<128, 6, 2>,
+                               k_gram_tc<128, 6, 2, true>,   k_gram_tma<64, 2, false, 4>,
+                               k_gram_tma<128, 2, false, 1>, k_gram_tma<128, 2, true, 1>};
+const size_t g_gt_smem[6] = {GtPlan<64, 12, 2>::SMEM,    GtPlan<128, 6, 2>::SMEM,       GtPlan<128, 6, 2>::SMEM,
+                             gm_smem<64, 2, 4>(0, 0),    gm_smem<128, 2, 1>(0, 0),      gm_smem<128, 2, 1>(0, 0)};
 
-// per device: SM count and, per plan, whether the kernel fits and its attribute is set
+// per device: SM count and, per plan, whether the kernel fits and the dynamic shared memory its
+// attribute allows
 struct GtDevice {
     bool ready = false;
     int sms = 0;
-    bool fits[3] = {false, false, false};
+    bool fits[6] = {false, false, false, false, false, false};
+    size_t dyn[6] = {0, 0, 0, 0, 0, 0};
 };
-std::mutex g_gt_mu;
+
+// the driver's tensor-map encoder (cuTensorMapEncodeTiled), looked up once through the runtime;
+// null when the driver does not provide it (the cp.async kernel is used then)
+using TmEncode = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                              const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                              CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+TmEncode tm_encoder() {
+    static std::once_flag once;
+    static TmEncode fn = nullptr;
+    std::call_once(once, [] {
+        const char *e = std::getenv("KF_GRAM_TMA");
+        if (e && e[0] == '0') return;   // the cp.async kernel only
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<TmEncode>(p);
+        else
+            (void)cudaGetLastError();
+    });
+    return fn;
+}
+
+// tensor maps of the column blocks the solvers pass (their workspaces are reused, so a small
+// direct-mapped cache saves most encodes): N rows x k columns, leading dimension ld, boxes of
+// 128 rows x k columns (unswizzled: per column 512 contiguous bytes), rows past N read as zero
+struct TmEntry {
+    const float *p = nullptr;
+    int64_t ld = 0, N = 0;
+    int k = 0;
+    CUtensorMap m;
+};
+TmEntry g_tm_cache[64];
+
+bool tm_for(const float *p, int64_t ld, int64_t N, int k, CUtensorMap *out) {
+    const TmEncode enc = tm_encoder();
+    if (!enc || N > ((int64_t)1 << 31) - GM_GR || k > 256) return false;
+    const size_t h = (((uintptr_t)p >> 8) ^ (size_t)ld * 31 ^ (size_t)N * 7 ^ (size_t)k) & 63;
+    std::lock_guard<std::mutex> lk(g_gt_mu);
+    TmEntry &c = g_tm_cache[h];
+    if (c.p != p || c.ld != ld || c.N != N || c.k != k) {
+        const cuuint64_t dims[2] = {(cuuint64_t)N, (cuuint64_t)k};
+        const cuuint64_t strides[1] = {(cuuint64_t)ld * sizeof(float)};
+        const cuuint32_t box[2] = {(cuuint32_t)GM_GR, (cuuint32_t)k};
+        const cuuint32_t es[2] = {1, 1};
+        if (enc(&c.m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float *>(p), dims, strides, box, es,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS) {
+            c.p = nullptr;
+            return false;
+        }
+        c.p = p;
+        c.ld = ld;
+        c.N = N;
+        c.k = k;
+    }
+    *out = c.m;
+    return true;
+}
 GtDevice g_gt_dev[32];
 
 const GtDevice &gt_device() {
@@ -440,13 +877,15 @@ const GtDevice &gt_device() {
         int optin = 0;
         KF_CUDA(cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, dev));
         KF_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-        for (int p = 0; p < 3; ++p) {
+        for (int p = 0; p < 6; ++p) {
             cudaFuncAttributes fa;
             KF_CUDA(cudaFuncGetAttributes(&fa, g_gt_kern[p]));
             d.fits[p] = g_gt_smem[p] + fa.sharedSizeBytes <= (size_t)optin;
+            // the TMA plans take all the device allows (their raw ring grows into it)
+            d.dyn[p] = p >= 3 ? (size_t)optin - fa.sharedSizeBytes : g_gt_smem[p];
             if (d.fits[p])
                 KF_CUDA(cudaFuncSetAttribute(g_gt_kern[p], cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)g_gt_smem[p]));
+                                             (int)d.dyn[p]));
         }
         d.ready = true;
     }
@@ -525,14 +964,34 @@ bool gram_tc(const GramTcSrc *src, int nsrc, int r0, int r1, int c0, int c1, int
     a.nr = nr;
     a.nc = nc;
     const GtDevice &dv = gt_device();
-    const int plan = RB == 64 ? 0 : split ? 2 : 1;
+    int plan = RB == 64 ? 0 : split ? 2 : 1;
+    size_t smem = g_gt_smem[plan];
+    if (dv.fits[plan + 3]) {
+        // the TMA kernel: one tensor map per source; a raw slot holds every source's 128 x k box
+        bool tma = true;
+        a.rslot = 0;
+        for (int i = 0; i < a.nsrc && tma; ++i) {
+            tma = tm_for(a.p[i], a.ld[i], N, a.k[i], &a.tm[i]);
+            a.roff[i] = a.rslot;
+            a.rslot += (uint32_t)a.k[i] * GM_GR * 4u;
+        }
+        a.tx_bytes = a.rslot;
+        const size_t fixed = g_gt_smem[plan + 3];
+        const int R = tma ? (int)std::min<size_t>(GM_MAX_RAW, (dv.dyn[plan + 3] - fixed) / a.rslot) : 0;
+        if (R >= 2) {
+            a.nraw = R;
+            plan += 3;
+            smem = fixed + (size_t)R * a.rslot;
+            a.nchunks = (N + GM_GR - 1) / GM_GR;   // groups of four chunks
+        }
+    }
     if (!dv.fits[plan]) return false;
     const int grid = (int)std::min<int64_t>(dv.sms, a.nchunks);
     if ((size_t)2 * grid * nr * nc * sizeof(float) > partial_bytes) return false;
     a.part = (float *)partials;
     a.err = tc_error_word();
 
-    g_gt_kern[plan]<<<grid, GT_THREADS, g_gt_smem[plan], s>>>(a);
+    g_gt_kern[plan]<<<grid, plan >= 3 ? GM_THREADS : GT_THREADS, smem, s>>>(a);
     KF_LAUNCH_CHECK();
     const int n = nr * nc;
     k_reduce_partials_f32<<<(n + 7) / 8, 256, 0, s>>>((const float *)partials, 2 * grid, n, G);

@@ -6,10 +6,17 @@ of the 32-row chunk (zero-filled tail copies), a leading dimension above N, disj
 sources of up to 64 rows each (one MMA per K step on [A_hi; A_lo] x [B_hi; B_lo]), and the shapes
 the kernel turns down (the solvers then keep the SIMT Gram).
 
+The default kernel loads with 2-D tensor copies (128 rows x k columns per source); the cp.async
+kernel, used where the driver gives no tensor-map encoder, runs the same pools in a subprocess with
+KF_GRAM_TMA=0.
+
 Tolerance: hi*hi + hi*lo + lo*hi drops lo*lo (2^-20 of a product) and TF32 keeps 10 mantissa bits
 of lo (2^-21): 2e-6 of sqrt(sum|a|^2 sum|b|^2) per entry, as for the SIMT FP32 Gram.
 """
 import ctypes as C
+import os
+import subprocess
+import sys
 
 import numpy as np
 import pytest
@@ -115,3 +122,15 @@ def test_gram_tc_repeated_launches_agree(cuda):
     _abi.check(st1)
     _abi.check(st2)
     assert np.array_equal(G1, G2)
+
+
+def test_gram_tc_cp_async_kernel(cuda):
+    """The pools and ragged row counts above on the cp.async kernel (KF_GRAM_TMA=0 at start-up)."""
+    if os.environ.get("KF_GRAM_TMA") == "0":
+        pytest.skip("this is the cp.async run")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, "-m", "pytest", "-x", "-q", "-p", "no:cacheprovider", os.path.abspath(__file__),
+                        "-k", "against_fp64 or ragged or repeated"],
+                       env={**os.environ, "KF_GRAM_TMA": "0"}, capture_output=True, text=True, cwd=root)
+    assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-3000:]
+    assert " passed" in r.stdout
