@@ -366,8 +366,8 @@ def run_ours(args, D):
                 "d2h_bytes_per_step": int(d2h / ke), "steps": ke, "max_rel_eig_err": err_e},
         "roofline": {"bound": "hbm", "achieved": alg_gram / t_gram / 1e9, "peak": peak, "unit": "GB/s",
                      "frac": alg_gram / t_gram / 1e9 / peak, "traffic": GRAM_TC_TRAFFIC_BYTES,
-                     "kernel": "k_gram_tc<64> + k_reduce_partials_f32 (tensor-core FP32 Gram, one-MMA layout: "
-                               "[X Z]'Z, 18 + 36 FP32 columns)",
+                     "kernel": "k_gram_tma<64> + k_reduce_partials_f32 (tensor-core FP32 Gram fed by 2-D tensor "
+                               "copies, one-MMA layout: [X Z]'Z, 18 + 36 FP32 columns)",
                      "algorithmic_bytes": alg_gram, "launch_us": t_gram * 1e6, "peak_kind": kind},
         "roofline_apply": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                            "traffic": APPLY_TRAFFIC_BYTES,
