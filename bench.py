@@ -439,7 +439,8 @@ def run_apply_workload(args):
         by = 2 * H.N * 16 * (4 if f32 else 8)
         out["apply_%s_us" % ("f32" if f32 else "f64")] = t * 1e6
         out["apply_%s_gbs" % ("f32" if f32 else "f64")] = by / t / 1e9
-    # every kernel variant forced (0-4, 6: point per thread, 5: plane-marching through shared memory)
+    # every kernel variant forced (0-4, 6: point per thread, 5 and 7: plane-marching through shared
+    # memory with 12 or 7 consumer warps)
     import ctypes as C
     from kfgpu import _abi
     for f32 in (True, False):
@@ -447,7 +448,7 @@ def run_apply_workload(args):
         X = torch.randn(16, H.N, dtype=dt, device="cuda")
         Y = torch.empty_like(X)
         flags = _abi.KF_DEVICE | (_abi.KF_F32 if f32 else _abi.KF_F64)
-        for v in range(7):
+        for v in range(8):
             ms = C.c_float(0)
             _abi.check(_abi.lib().kf_test_apply_variant(H.handle, v, C.c_void_p(X.data_ptr()), C.c_void_p(Y.data_ptr()),
                                                         H.N, 16, flags, 10, C.byref(ms)))

@@ -49,9 +49,11 @@ namespace kf {
 
 namespace {
 
-constexpr int MCW = 12;                     // consumer warps
-constexpr int MCT = MCW * 32;               // consumer threads
-constexpr int MTHREADS = MCT + 32;          // + one producer warp
+// consumer warps: 12 (4 FP32 / 2 FP64 points per thread at 128 registers), or 7 with more points
+// per thread (8 FP32 / 4 FP64: with the producer, two warps per SM sub-partition, so up to 255
+// registers; the per-plane work -- waits, weight loads, ring addresses, releases -- is spread over
+// twice the points)
+constexpr int MCW_STD = 12, MCW_WIDE = 7;
 constexpr long long M_WAIT_CYCLES = 4000000000LL;
 constexpr int M_SMEM_BUDGET = 200 * 1024;   // one CTA per SM
 
@@ -242,13 +244,15 @@ __global__ void k_march_table(const ApplyPlan plan, const MarchPlan mp, const T 
     tab[t] = v;
 }
 
-template <typename T, int H, int MS, int PT, bool EPI>
-__global__ void __launch_bounds__(MTHREADS, 1)
+template <typename T, int H, int MS, int PT, bool EPI, int MCW>
+__global__ void __launch_bounds__(MCW * 32 + 32, 1)
     k_apply_march(const ApplyPlan plan, const MarchPlan mp, const T *__restrict__ D, const T *__restrict__ W,
                   const T *__restrict__ X, T *__restrict__ Y, int64_t ldx, int64_t ldy, int b, T alpha, T beta,
                   const T *__restrict__ Z, int64_t ldz, T gamma, int epi, const T *__restrict__ tab, int *err) {
     constexpr int G = 16 / (int)sizeof(T);
     constexpr int WN = 2 * H + 1;
+    constexpr int MCT = MCW * 32;               // consumer threads
+    constexpr int MTHREADS = MCT + 32;          // + one producer warp
     extern __shared__ __align__(128) unsigned char m_smem[];
     const int SL = mp.SLX + mp.SLD;
     const int NR = mp.NR;
@@ -605,19 +609,19 @@ __global__ void __launch_bounds__(MTHREADS, 1)
     __syncthreads();
 }
 
-template <typename T, int H, int MS, int PT, bool EPI>
+template <typename T, int H, int MS, int PT, bool EPI, int MCW>
 void launch_k(const kf_op *op, const MarchPlan &mp, const T *D, const T *W, const T *X, T *Y, int64_t ldx,
               int64_t ldy, int64_t b, T alpha, T beta, const T *Z, int64_t ldz, T gamma, int epi, const T *tab,
               cudaStream_t s) {
     const size_t smem = march_smem_bytes(mp, sizeof(T), 2 * H + 1, MS);
     static bool attr = false;   // per instantiation
     if (!attr) {
-        KF_CUDA(cudaFuncSetAttribute(k_apply_march<T, H, MS, PT, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     M_SMEM_BUDGET + 16384));
+        KF_CUDA(cudaFuncSetAttribute(k_apply_march<T, H, MS, PT, EPI, MCW>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, M_SMEM_BUDGET + 16384));
         attr = true;
     }
     KF_REQUIRE(smem <= (size_t)M_SMEM_BUDGET + 16384, KF_EINVAL, "apply: plane ring too large");
-    k_apply_march<T, H, MS, PT, EPI><<<mp.grid, MTHREADS, smem, s>>>(op->plan, mp, D, W, X, Y, ldx, ldy, (int)b, alpha,
+    k_apply_march<T, H, MS, PT, EPI, MCW><<<mp.grid, MCW * 32 + 32, smem, s>>>(op->plan, mp, D, W, X, Y, ldx, ldy, (int)b, alpha,
                                                                 beta, Z, ldz, gamma, epi, tab, tc_error_word());
     KF_LAUNCH_CHECK();
 }
@@ -626,18 +630,25 @@ template <typename T, int H>
 void launch_h(const kf_op *op, const MarchPlan &mp, const T *D, const T *W, const T *X, T *Y, int64_t ldx,
               int64_t ldy, int64_t b, T alpha, T beta, const T *Z, int64_t ldz, T gamma, int epi, const T *tab,
               cudaStream_t s) {
-    // points per thread: what fits 128 registers without spilling (13 warps on one SM)
+    // points per thread: what fits 128 registers without spilling (13 warps on one SM), or, with 7
+    // consumer warps, 255 registers
     constexpr int P8 = sizeof(T) == 4 ? 4 : 2, P16 = sizeof(T) == 4 ? 2 : 1;
-#define KF_MARCH(MS_, PT_)                                                                                   \
-    do {                                                                                                     \
-        if (epi)                                                                                             \
-            launch_k<T, H, MS_, PT_, true>(op, mp, D, W, X, Y, ldx, ldy, b, alpha, beta, Z, ldz, gamma, epi, tab, s); \
-        else                                                                                                 \
-            launch_k<T, H, MS_, PT_, false>(op, mp, D, W, X, Y, ldx, ldy, b, alpha, beta, Z, ldz, gamma, epi, tab, s); \
+    constexpr int PW = sizeof(T) == 4 ? 8 : 4;
+#define KF_MARCH(MS_, PT_, MCW_)                                                                                   \
+    do {                                                                                                           \
+        if (epi)                                                                                                   \
+            launch_k<T, H, MS_, PT_, true, MCW_>(op, mp, D, W, X, Y, ldx, ldy, b, alpha, beta, Z, ldz, gamma, epi, tab, \
+                                                 s);                                                               \
+        else                                                                                                       \
+            launch_k<T, H, MS_, PT_, false, MCW_>(op, mp, D, W, X, Y, ldx, ldy, b, alpha, beta, Z, ldz, gamma, epi, \
+                                                  tab, s);                                                         \
     } while (0)
-    if (mp.ms == 6) KF_MARCH(6, P8);
-    else if (mp.ms == 8) KF_MARCH(8, P8);
-    else KF_MARCH(16, P16);
+    if (mp.mcw == MCW_WIDE) {
+        if (mp.ms == 6) KF_MARCH(6, PW, MCW_WIDE);
+        else KF_MARCH(8, PW, MCW_WIDE);
+    } else if (mp.ms == 6) KF_MARCH(6, P8, MCW_STD);
+    else if (mp.ms == 8) KF_MARCH(8, P8, MCW_STD);
+    else KF_MARCH(16, P16, MCW_STD);
 #undef KF_MARCH
 }
 
@@ -652,7 +663,7 @@ size_t march_smem_bytes(const MarchPlan &mp, size_t elem, int wn, int ms) {
 // The march plan of this operator for a block of b columns of element size `elem`, or false when
 // the kernel does not apply (no axis with an offset beyond the first, a plane or column length that
 // is not a multiple of 16 bytes, too wide a halo or too many shared entries).
-bool march_plan(const kf_op *op, int64_t b, size_t elem, int num_sms, MarchPlan &mp) {
+bool march_plan(const kf_op *op, int64_t b, size_t elem, int num_sms, MarchPlan &mp, int mcw) {
     const ApplyPlan &P = op->plan;
     if (P.ne < 1 || P.ndims > MAXDIMS_F || b < 1) return false;
     std::memset(&mp, 0, sizeof(mp));
@@ -719,10 +730,13 @@ bool march_plan(const kf_op *op, int64_t b, size_t elem, int num_sms, MarchPlan 
         }
     }
     // register budget (128 per thread): up to 8 shared entries (padded to 6 or 8 with zero weights)
-    // with 4 FP32 or 2 FP64 points per thread, up to 16 with half as many
+    // with 4 FP32 or 2 FP64 points per thread, up to 16 with half as many; with 7 consumer warps
+    // (255 registers) 8 FP32 or 4 FP64 points, up to 8 shared entries
     mp.ms = mp.nsm <= 6 ? 6 : mp.nsm <= 8 ? 8 : 16;
-    const int pt = (elem == 4 ? 4 : 2) / (mp.ms <= 8 ? 1 : 2);
-    const int tqmax = MCT * pt;
+    if (mcw != MCW_STD && (mcw != MCW_WIDE || mp.ms > 8)) return false;
+    mp.mcw = mcw;
+    const int pt = mcw == MCW_WIDE ? (elem == 4 ? 8 : 4) : (elem == 4 ? 4 : 2) / (mp.ms <= 8 ? 1 : 2);
+    const int tqmax = 32 * mcw * pt;
     // tiles: at most tqmax points, balanced over the plane, a multiple of 16 bytes
     mp.ntile = (mp.P + tqmax - 1) / tqmax;
     mp.TQ = (mp.P + mp.ntile - 1) / mp.ntile;

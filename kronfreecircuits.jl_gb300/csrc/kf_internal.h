@@ -62,7 +62,7 @@ constexpr int MAXDIMS = 8;     // axes of a state tensor
 constexpr int MAXB = 24;       // bands of one banded factor (a periodic order-8 stencil has 16)
 // five (columns per thread, unroll) shapes of the point kernel, the plane-marching kernel (5), 36
 // columns per thread (a 36-column block in one pass instead of 32 + 4)
-constexpr int KF_APPLY_VARIANTS = 7;
+constexpr int KF_APPLY_VARIANTS = 8;
 constexpr int MAXE = 48;       // stencil entries (products of bands) over all fused terms
 
 // The fused kernel's stencil entries.  Every term built only of diagonal, banded and shift
@@ -221,8 +221,9 @@ struct MarchPlan {
     int flat;       // every shared entry reads the current plane (o_e = 0)
     int grid;       // persistent CTAs
     int wn;         // the kernel's window length (2H + 1; a halo of 3 runs on the kernel for 4)
+    int mcw;        // consumer warps (12, or 7 with twice the points per thread)
 };
-bool march_plan(const kf_op *op, int64_t b, size_t elem, int num_sms, MarchPlan &mp);
+bool march_plan(const kf_op *op, int64_t b, size_t elem, int num_sms, MarchPlan &mp, int mcw = 12);
 size_t march_smem_bytes(const MarchPlan &mp, size_t elem, int wn, int ms);
 template <typename T>
 void launch_apply_march(kf_op *op, const MarchPlan &mp, const T *D, const T *W, const T *X, T *Y, int64_t ldx,

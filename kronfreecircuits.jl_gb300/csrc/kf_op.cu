@@ -252,14 +252,17 @@ static void apply_t(kf_op *op, const T *X, T *Y, int64_t ldx, int64_t ldy, int64
         return;
     }
     const int ne = op->plan.ne;
-    // the plane-marching kernel (variant 5) where its geometry applies and X is 16-byte aligned
-    MarchPlan mp;
+    // the plane-marching kernel where its geometry applies and X is 16-byte aligned: variant 5 with 12
+    // consumer warps, variant 7 with 7 and twice the points per thread
+    MarchPlan mp, mpw;
     const int G = 16 / (int)sizeof(T);
-    const bool march_ok = ldx % G == 0 && (uintptr_t)X % 16 == 0 && (uintptr_t)D % 16 == 0 &&
-                          march_plan(op, b, sizeof(T), num_sms(op->device), mp);
+    const bool aligned = ldx % G == 0 && (uintptr_t)X % 16 == 0 && (uintptr_t)D % 16 == 0;
+    const bool march_ok = aligned && march_plan(op, b, sizeof(T), num_sms(op->device), mp);
+    const bool march_wide_ok = march_ok && march_plan(op, b, sizeof(T), num_sms(op->device), mpw, 7);
     auto run = [&](int variant) {
-        if (variant == 5 && march_ok) {
-            launch_apply_march<T>(op, mp, D, W, X, Y, ldx, ldy, b, (T)alpha, (T)beta, Z, ldz, (T)gamma, epi, s);
+        if ((variant == 5 && march_ok) || (variant == 7 && march_wide_ok)) {
+            launch_apply_march<T>(op, variant == 7 ? mpw : mp, D, W, X, Y, ldx, ldy, b, (T)alpha, (T)beta, Z, ldz,
+                                  (T)gamma, epi, s);
             return;
         }
 #define KF_FUSED(CPT, U, ME)                                                                                  \
@@ -308,7 +311,7 @@ static void apply_t(kf_op *op, const T *X, T *Y, int64_t ldx, int64_t ldy, int64
                 float best = 1e30f;
                 int bestv = 0;
                 for (int v = 0; v < KF_APPLY_VARIANTS; ++v) {
-                    if (v == 5 && !march_ok) continue;
+                    if ((v == 5 && !march_ok) || (v == 7 && !march_wide_ok)) continue;
                     run(v);                                   // warm
                     float vbest = 1e30f;
                     for (int batch = 0; batch < 3; ++batch) {
