@@ -85,6 +85,17 @@ __device__ __forceinline__ void m_bulk(void *dst, const void *src, uint32_t byte
 // wait for the phase with the given parity to complete; false when the budget ran out or another
 // role aborted
 __device__ __forceinline__ bool m_wait(uint64_t *bar, uint32_t parity, volatile int *abort_flag) {
+    {
+        // the usual case, a plane that has landed already: one non-blocking test, no clock read
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.b32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(done)
+            : "r"(msu32(bar)), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
     const long long t0 = clock64();
     for (;;) {
         uint32_t done;
