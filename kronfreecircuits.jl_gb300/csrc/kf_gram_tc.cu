@@ -894,6 +894,10 @@ const GtDevice &gt_device() {
 
 }  // namespace
 
+bool tensor_map_cols(const float *p, int64_t ld, int64_t N, int k, void *map) {
+    return tm_for(p, ld, N, k, reinterpret_cast<CUtensorMap *>(map));
+}
+
 size_t gram_tc_partials_size(int nr, int nc) { return (size_t)2 * 256 * nr * nc * sizeof(float); }
 
 bool gram_tc(const GramTcSrc *src, int nsrc, int r0, int r1, int c0, int c1, int64_t N, double *G, void *partials,

@@ -27,6 +27,8 @@
 // issuer waits (bounded) for its MMAs in flight and TMEM is freed.  The only named barrier inside
 // a loop is the producers' own, a reduction that also carries the abort decision, so that all 256
 // producer threads leave at the same iteration and none is stranded.
+#include <cuda.h>   // CUtensorMap (the maps themselves come from tensor_map_cols)
+
 #include <cstring>
 #include <mutex>
 
@@ -117,6 +119,9 @@ __device__ __forceinline__ void ug_cp16(void *dst, const float *src, int bytes) 
 }
 
 struct UgArgs {
+    CUtensorMap ym[2];  // tstore: the output blocks Y0, Y1 as 128-row x k-column boxes
+    int tstore;         // 1: the epilogue stages a tile's outputs in shared memory and stores them with
+                        // 2-D tensor copies (beta = 0, aligned outputs); 0: per-element global stores
     float *Y, *Y1;
     const float *X0, *X1;
     const double *C;
@@ -128,8 +133,20 @@ struct UgArgs {
 };
 
 // NSTG: staging tiles of the cp.async ring (0: register gather)
+// named barrier 2 over the 256 epilogue threads, returning the OR of their flags (uniform)
+__device__ __forceinline__ bool ug_epi_sync_or(bool v) {
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\tsetp.ne.b32 q, %1, 0;\n\tbar.red.or.pred p, 2, 256, q;\n\t"
+        "selp.b32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(r)
+        : "r"((uint32_t)v)
+        : "memory");
+    return r != 0;
+}
+
 template <int NSTG>
-__global__ void __launch_bounds__(UG_THREADS, 1) k_update_tc(const UgArgs a) {
+__global__ void __launch_bounds__(UG_THREADS, 1) k_update_tc(const __grid_constant__ UgArgs a) {
     extern __shared__ __align__(16) unsigned char ug_smem[];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int Kp = a.Kp, Np = a.Np;
@@ -139,7 +156,11 @@ __global__ void __launch_bounds__(UG_THREADS, 1) k_update_tc(const UgArgs a) {
     unsigned char *Bsm = ug_smem;                           // B hi | B lo
     unsigned char *Asm = Bsm + 2 * bimg;                    // stage s: A hi | A lo at 2 s aimg
     float *Stg = reinterpret_cast<float *>(Asm + 4 * aimg);   // NSTG staging tiles of Kp x UG_SS floats
-    uint64_t *bars = reinterpret_cast<uint64_t *>(Asm + 4 * aimg + (size_t)NSTG * Kp * UG_SS * 4);
+    // tstore: the output tile [ky][128] (column-major, 128-byte aligned for the tensor copies)
+    unsigned char *Osm_raw = Asm + 4 * aimg + (size_t)NSTG * Kp * UG_SS * 4;
+    float *Osm = reinterpret_cast<float *>(Osm_raw + ((128u - (su32(Osm_raw) & 127u)) & 127u));
+    const size_t obytes = a.tstore ? (size_t)a.ky * UG_TM * 4 + 128 : 0;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(Osm_raw + obytes);
     uint64_t *full = bars, *empty = bars + 2, *accf = bars + 4, *acce = bars + 6, *fin = bars + 8;
     uint32_t *tslot = reinterpret_cast<uint32_t *>(bars + 9);
     __shared__ volatile int s_abort;
@@ -312,11 +333,7 @@ __global__ void __launch_bounds__(UG_THREADS, 1) k_update_tc(const UgArgs a) {
         // ---- epilogue: warp w (9-16) reads TMEM lanes 32 (w % 4) .. + 31 and the 16-column blocks
         // of parity (w - 9) / 4; the three partial products of a block are loaded before one wait
         const int q = warp & 3, h = (warp - 9) >> 2;
-        for (int k = 0; k < my; ++k) {
-            const int sl = k & 1;
-            if (!ug_wait(accf + sl, (uint32_t)(k / 2), &s_abort)) { s_abort = 1; break; }
-            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-            const int64_t row = (int64_t)(blockIdx.x + (int64_t)k * gridDim.x) * UG_TM + q * 32 + lane;
+        auto drain = [&](int k, int sl, auto &&put) {
             const uint32_t base = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)sl * slot_cols;
             for (int j0 = 16 * h; j0 < a.ky; j0 += 32) {
                 // hi*hi (column j), hi*lo (Np + j), lo*hi (2 Np + j)
@@ -332,23 +349,84 @@ __global__ void __launch_bounds__(UG_THREADS, 1) k_update_tc(const UgArgs a) {
                           "=r"(r[part][14]), "=r"(r[part][15])
                         : "r"(base + (uint32_t)(part * Np + j0)));
                 asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-                if (row < a.N) {
 #pragma unroll
-                    for (int t = 0; t < 16; ++t) {
-                        const int j = j0 + t;
-                        if (j < a.ky) {
-                            const float sum = (__uint_as_float(r[0][t]) + __uint_as_float(r[1][t])) +
-                                              __uint_as_float(r[2][t]);
-                            float *yp = j < a.ky0 ? a.Y + row + (int64_t)j * a.ldy
-                                                  : a.Y1 + row + (int64_t)(j - a.ky0) * a.ldy1;
-                            const float v = a.alpha * sum;
-                            *yp = a.beta == 0.f ? v : v + a.beta * *yp;
-                        }
-                    }
+                for (int t = 0; t < 16; ++t) {
+                    const int j = j0 + t;
+                    if (j < a.ky)
+                        put(j, a.alpha * ((__uint_as_float(r[0][t]) + __uint_as_float(r[1][t])) +
+                                          __uint_as_float(r[2][t])));
                 }
             }
-            asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-            ug_arrive(acce + sl);
+        };
+        if (a.tstore) {
+            // the tile's outputs go to shared memory ([j][row], conflict-free: consecutive lanes write
+            // consecutive rows), the accumulator slot is released at once, and one thread stores the
+            // tile with 2-D tensor copies (128 rows x ky0, x ky1 columns).  Before a tile writes the
+            // buffer, the previous tile's copies must have read it.  A last tile that ends past N
+            // is stored element by element: the copies' clipping at the tensor's end was seen to
+            // write the row just past N (N = 100,003, a 16-byte chunk across the end).
+            const int m = q * 32 + lane;
+            const bool leader = warp == 9 && lane == 0;
+            bool ok = true;
+            for (int k = 0; k < my; ++k) {
+                const int sl = k & 1;
+                const bool bad = !ug_wait(accf + sl, (uint32_t)(k / 2), &s_abort);
+                if (leader && k > 0) asm volatile("cp.async.bulk.wait_group.read 0;\n" ::: "memory");
+                if (ug_epi_sync_or(bad || s_abort)) { ok = false; break; }
+                asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                const int64_t row0 = (int64_t)(blockIdx.x + (int64_t)k * gridDim.x) * UG_TM;
+                const bool whole = row0 + UG_TM <= a.N;   // the same for every thread of the tile
+                if (whole) {
+                    drain(k, sl, [&](int j, float v) { Osm[j * UG_TM + m] = v; });
+                } else {
+                    const int64_t row = row0 + m;
+                    drain(k, sl, [&](int j, float v) {
+                        if (row < a.N) {
+                            float *yp = j < a.ky0 ? a.Y + row + (int64_t)j * a.ldy
+                                                  : a.Y1 + row + (int64_t)(j - a.ky0) * a.ldy1;
+                            *yp = v;
+                        }
+                    });
+                }
+                asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+                ug_arrive(acce + sl);
+                asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+                if (ug_epi_sync_or(false)) { ok = false; break; }
+                if (leader && whole) {
+                    const int x = (int)row0;
+                    asm volatile(
+                        "cp.async.bulk.tensor.2d.global.shared::cta.tile.bulk_group [%0, {%1, %2}], [%3];\n" ::"l"(
+                            reinterpret_cast<uint64_t>(&a.ym[0])),
+                        "r"(x), "r"(0), "r"(su32(Osm))
+                        : "memory");
+                    if (a.ky0 < a.ky)
+                        asm volatile(
+                            "cp.async.bulk.tensor.2d.global.shared::cta.tile.bulk_group [%0, {%1, %2}], [%3];\n" ::"l"(
+                                reinterpret_cast<uint64_t>(&a.ym[1])),
+                            "r"(x), "r"(0), "r"(su32(Osm + (size_t)a.ky0 * UG_TM))
+                            : "memory");
+                    asm volatile("cp.async.bulk.commit_group;\n" ::: "memory");
+                }
+            }
+            if (!ok) s_abort = 1;
+            // the copies must have completed before the CTA leaves
+            if (leader) asm volatile("cp.async.bulk.wait_group 0;\n" ::: "memory");
+        } else {
+            for (int k = 0; k < my; ++k) {
+                const int sl = k & 1;
+                if (!ug_wait(accf + sl, (uint32_t)(k / 2), &s_abort)) { s_abort = 1; break; }
+                asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                const int64_t row = (int64_t)(blockIdx.x + (int64_t)k * gridDim.x) * UG_TM + q * 32 + lane;
+                drain(k, sl, [&](int j, float v) {
+                    if (row < a.N) {
+                        float *yp = j < a.ky0 ? a.Y + row + (int64_t)j * a.ldy
+                                              : a.Y1 + row + (int64_t)(j - a.ky0) * a.ldy1;
+                        *yp = a.beta == 0.f ? v : v + a.beta * *yp;
+                    }
+                });
+                asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+                ug_arrive(acce + sl);
+            }
         }
     }
     if (s_abort && tid == 0) {
@@ -437,7 +515,21 @@ void update_tc2(float *Y0, int64_t ldy0, int ky0, float *Y1, int64_t ldy1, int k
                    KF_EINVAL, "update_tc: the requested staging ring does not fit");
         nstg = force_nstg;
     }
-    const size_t smem = base + nstg * stg;
+    // outputs by 2-D tensor copies where beta = 0, the output blocks are 16-byte aligned with a
+    // staging ring and the tile buffer [ky][128] fitting (the ring one tile shallower if need be)
+    a.tstore = 0;
+    const size_t obuf = (size_t)ky * UG_TM * 4 + 128;
+    if (beta == 0.0 && nstg > 0 && al(Y0, ldy0) && (ky1 == 0 || al(Y1, ldy1)) &&
+        tensor_map_cols(Y0, ldy0, N, a.ky0, &a.ym[0]) && (ky1 == 0 || tensor_map_cols(Y1, ldy1, N, ky1, &a.ym[1]))) {
+        for (int q : {3, 2}) {
+            if ((force_nstg < 0 || force_nstg == q) && base + q * stg + obuf <= dyn_max[q]) {
+                nstg = q;
+                a.tstore = 1;
+                break;
+            }
+        }
+    }
+    const size_t smem = base + nstg * stg + (a.tstore ? obuf : 0);
     KF_REQUIRE(smem <= dyn_max[nstg], KF_EINVAL, "update_tc: shared-memory stages too large");
     {
         std::lock_guard<std::mutex> lk(g_ug_mu);
