@@ -132,6 +132,25 @@ int kf_op_apply_noalloc(kf_op *op, const void *X, void *Y, int64_t ldx, int64_t 
 int kf_op_sandwich(kf_op *op, const double *W, int64_t ldw, int32_t kw, const double *V, int64_t ldv, int32_t kv,
                    double *P_out, int32_t flags);
 
+/* Matrix-free time evolution under port drives: the action of the drive Hamiltonian on a node's
+ * product basis, which QuantumToolbox's sesolve applies (src/quantumtoolbox.jl:84-99,
+ * drive_hamiltonian with basis = :free, batch = true: a QobjEvo around the KronFreeOperator H0 and
+ * the port operators of src/portoperator.jl:18-39).  Y = H(t) X with
+ *     H(t) = 2 pi [H0 - E0 + sum_k coef[k] O_k]     (rad/ns; coef[k] = f_k(t) in GHz),
+ * X and Y complex blocks of m columns stored as 2m FP64 columns: the real parts, then the imaginary
+ * parts (column j at X + j ldx, its imaginary part at X + (m + j) ldx).  omega != NULL: the
+ * interaction frame, Y = e^{i Omega t} (H(t) - diag Omega) e^{-i Omega t} X with Omega = omega (N
+ * values, rad/ns: the diagonal of 2 pi (H0 - E0), on the same side as X).  ports: nports operators on
+ * H0's product basis (KF_EDIM otherwise); coef: host array.  H0 and the ports are real operators.
+ * flags: KF_F64 with KF_DEVICE (H0's stream, asynchronous) or KF_HOST (returns when done). */
+int kf_drive_apply(kf_op *H0, double E0, int32_t nports, kf_op *const *ports, const double *coef, const double *omega,
+                   double t, const void *X, int64_t ldx, void *Y, int64_t ldy, int64_t m, int32_t flags);
+
+/* to_lab (src/quantumtoolbox.jl:25-37): the lab-frame state e^{-i Omega t} psi of an
+ * interaction-picture block, in place: X as in kf_drive_apply (2m FP64 columns), omega N values
+ * (rad/ns) on the same side as X.  KF_DEVICE: runs on the default stream and returns when done. */
+int kf_to_lab(const double *omega, int64_t N, double t, void *X, int64_t ldx, int64_t m, int32_t flags);
+
 /* The linear solve on the complement of a node's known states (src/resolvent.jl:146-252,
  * _complement_solve; the Sternheimer solves of the reference's derivatives): X[:, j] solves
  * Q (H - shifts[j]) Q x = Q B[:, j] with x orthogonal to the nbasis orthonormal columns of basis,

@@ -4,6 +4,8 @@
 #include <cstring>
 #include <limits>
 
+#include <cmath>
+
 #include "kf_internal.h"
 #include "../../include/kfgpu_testing.h"
 
@@ -160,6 +162,74 @@ int kf_op_apply_axpby(kf_op *op, const void *X, void *Y, const void *Z, int64_t 
         KF_REQUIRE(!ranges_overlap(X, bx, Y, bx), KF_EALIAS, "mul!: y must not alias x");
         KF_REQUIRE(Z == nullptr || !ranges_overlap(Z, bx, Y, bx), KF_EALIAS, "kf_op_apply_axpby: y must not alias z");
         launch_apply(op, (flags & KF_F32) != 0, X, Y, ld, ld, b, alpha, beta, Z, ld, Z ? gamma : 0.0, op->stream);
+    });
+}
+
+int kf_drive_apply(kf_op *H0, double E0, int32_t nports, kf_op *const *ports, const double *coef, const double *omega,
+                   double t, const void *X, int64_t ldx, void *Y, int64_t ldy, int64_t m, int32_t flags) {
+    return guarded([&] {
+        KF_REQUIRE(H0 != nullptr, KF_EINVAL, "kf_drive_apply: H0 is NULL");
+        KF_REQUIRE(!(flags & KF_F32), KF_EINVAL, "kf_drive_apply: time evolution runs in FP64");
+        KF_REQUIRE(nports >= 0 && (nports == 0 || (ports && coef)), KF_EINVAL, "kf_drive_apply: bad port list");
+        const int64_t N = H0->N;
+        for (int k = 0; k < nports; ++k) {
+            KF_REQUIRE(ports[k] != nullptr, KF_EINVAL, "kf_drive_apply: port operator " + std::to_string(k) + " is NULL");
+            KF_REQUIRE(ports[k]->N == N && ports[k]->dims == H0->dims, KF_EDIM,
+                       "drive_hamiltonian: port operator " + std::to_string(k) + " is not on H0's product basis");
+            KF_REQUIRE(std::isfinite(coef[k]), KF_EINVAL, "kf_drive_apply: coefficient " + std::to_string(k) +
+                                                              " is not finite");
+        }
+        KF_REQUIRE(m >= 0, KF_EDIM, "kf_drive_apply: negative block width");
+        KF_REQUIRE(ldx >= N && ldy >= N, KF_EDIM, "kf_drive_apply: leading dimension below the operator's size");
+        KF_REQUIRE(std::isfinite(E0) && std::isfinite(t), KF_EINVAL, "kf_drive_apply: E0 and t must be finite");
+        if (m == 0 || N == 0) return;
+        KF_REQUIRE(X && Y, KF_EINVAL, "kf_drive_apply: NULL block");
+        const size_t bx = ((size_t)(2 * m - 1) * ldx + N) * 8, by = ((size_t)(2 * m - 1) * ldy + N) * 8;
+        KF_REQUIRE(!ranges_overlap(X, bx, Y, by), KF_EALIAS, "kf_drive_apply: y must not alias x");
+        cudaStream_t s = H0->stream;
+        if (flags & KF_HOST) {
+            double *dX = nullptr, *dY = nullptr, *dW = nullptr;
+            KF_CUDA(cudaMallocAsync((void **)&dX, (size_t)N * 2 * m * 8, s));
+            KF_CUDA(cudaMallocAsync((void **)&dY, (size_t)N * 2 * m * 8, s));
+            if (omega) {
+                KF_CUDA(cudaMallocAsync((void **)&dW, (size_t)N * 8, s));
+                KF_CUDA(cudaMemcpyAsync(dW, omega, (size_t)N * 8, cudaMemcpyHostToDevice, s));
+            }
+            KF_CUDA(cudaMemcpy2DAsync(dX, N * 8, X, ldx * 8, N * 8, 2 * m, cudaMemcpyHostToDevice, s));
+            kf::drive_apply(H0, E0, nports, ports, coef, dW, t, dX, N, dY, N, m);
+            KF_CUDA(cudaMemcpy2DAsync(Y, ldy * 8, dY, N * 8, N * 8, 2 * m, cudaMemcpyDeviceToHost, s));
+            KF_CUDA(cudaFreeAsync(dX, s));
+            KF_CUDA(cudaFreeAsync(dY, s));
+            if (dW) KF_CUDA(cudaFreeAsync(dW, s));
+            KF_CUDA(cudaStreamSynchronize(s));
+        } else {
+            kf::drive_apply(H0, E0, nports, ports, coef, omega, t, (const double *)X, ldx, (double *)Y, ldy, m);
+        }
+    });
+}
+
+int kf_to_lab(const double *omega, int64_t N, double t, void *X, int64_t ldx, int64_t m, int32_t flags) {
+    return guarded([&] {
+        KF_REQUIRE(!(flags & KF_F32), KF_EINVAL, "kf_to_lab: time evolution runs in FP64");
+        KF_REQUIRE(N >= 0 && m >= 0 && ldx >= N, KF_EDIM, "to_lab: bad block shape");
+        KF_REQUIRE(std::isfinite(t), KF_EINVAL, "kf_to_lab: t must be finite");
+        if (N == 0 || m == 0) return;
+        KF_REQUIRE(omega && X, KF_EINVAL, "kf_to_lab: NULL argument");
+        cudaStream_t s = 0;
+        if (flags & KF_HOST) {
+            double *dX = nullptr, *dW = nullptr;
+            KF_CUDA(cudaMalloc((void **)&dX, (size_t)N * 2 * m * 8));
+            KF_CUDA(cudaMalloc((void **)&dW, (size_t)N * 8));
+            KF_CUDA(cudaMemcpy(dW, omega, (size_t)N * 8, cudaMemcpyHostToDevice));
+            KF_CUDA(cudaMemcpy2D(dX, N * 8, X, ldx * 8, N * 8, 2 * m, cudaMemcpyHostToDevice));
+            kf::rotate_rows(dW, N, t, -1.0, dX, N, m, s);
+            KF_CUDA(cudaMemcpy2D(X, ldx * 8, dX, N * 8, N * 8, 2 * m, cudaMemcpyDeviceToHost));
+            cudaFree(dX);
+            cudaFree(dW);
+        } else {
+            kf::rotate_rows(omega, N, t, -1.0, (double *)X, ldx, m, s);
+            KF_CUDA(cudaStreamSynchronize(s));
+        }
     });
 }
 

@@ -177,6 +177,9 @@ struct kf_op {
     int64_t cap = 0;
     void *d_scratch = nullptr;
     size_t scratch_bytes = 0;
+    // scratch of the drive apply (kf_drive.cu): the rotated block and one port's product
+    void *d_drive = nullptr;
+    size_t drive_bytes = 0;
     // host copies of derived data
     std::vector<double> h_diag;           // fused diagonal (real)
     double gershgorin = 0;
@@ -247,6 +250,16 @@ void launch_apply(kf_op *op, bool f32, const void *X, void *Y, int64_t ldx, int6
 // launched) when na + k > 64.  `status`: the device Cholesky's word; nonzero -> C keeps X, drops P
 bool rr_eig_device(const double *G, int ldg, bool packed, int na, int k, double *C, double *theta, const int *status,
                    cudaStream_t s);
+
+// time evolution under port drives (kf_drive.cu; src/quantumtoolbox.jl drive_hamiltonian with
+// basis = :free): Y = H(t) X, H(t) = 2 pi [H0 - E0 + sum_k coef_k O_k] (rad/ns), X a complex block of m
+// columns stored as 2m FP64 columns (real parts, then imaginary parts); omega != nullptr: the
+// interaction frame e^{i Omega t} (H(t) - diag Omega) e^{-i Omega t}.  Device pointers, H0's stream.
+void drive_apply(kf_op *H0, double E0, int nports, kf_op *const *ports, const double *coef, const double *omega,
+                 double t, const double *X, int64_t ldx, double *Y, int64_t ldy, int64_t m);
+// X <- e^{sign i Omega t} X in place (complex block of m columns as above)
+void rotate_rows(const double *omega, int64_t N, double t, double sign, double *X, int64_t ldx, int64_t m,
+                 cudaStream_t s);
 
 // the linear solve on the complement of known states (kf_cg.cu; src/resolvent.jl:146-252): per
 // column, state 0 met its tolerance, 1 converged from the start (x = 0), 2 stopped at the round-off

@@ -959,6 +959,7 @@ void free_op(kf_op *op) {
     cudaFree(op->d_chain64);
     cudaFree(op->d_chain32);
     cudaFree(op->d_scratch);
+    cudaFree(op->d_drive);
     cudaFree(op->d_march[0]);
     cudaFree(op->d_march[1]);
     for (float *p : op->sep.dU) cudaFree(p);
