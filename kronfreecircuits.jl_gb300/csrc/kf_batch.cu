@@ -46,6 +46,7 @@ struct BatchParams {
     int maxiter;
     int degree;
     int64_t scratch_per_cta;    // doubles
+    int *err;                   // the host-mapped error words (KF_CHECK builds record bounds-check sites)
 };
 
 // ---- block helpers (all threads of the CTA call them) ---------------------------------------
@@ -53,13 +54,15 @@ struct BatchParams {
 // Y = alpha H X + beta X + gamma Z on an N x nb block (column stride N); T = float or double
 template <typename T>
 __device__ void leaf_apply(const LeafDesc &L, const T *D, const T *W, const T *X, T *Y, int nb, T alpha, T beta,
-                           const T *Z, T gamma) {
+                           const T *Z, T gamma, int *err) {
     const int N = L.N;
     // element e = (column c, row r); one division per thread, then (c, r) advance by the block's
     // stride without dividing (each element's arithmetic is unchanged)
     const int sc = (int)blockDim.x / N, sr = (int)blockDim.x % N;
     int c = (int)threadIdx.x / N, r = (int)threadIdx.x % N;
     for (int e = threadIdx.x; e < N * nb; e += blockDim.x) {
+        // KF_CHECK site 201: the incremental decode stays inside the N x nb block
+        if (!KF_CHK(c < nb && r >= 0 && r < N, err, 201)) break;
         const T *x = X + (int64_t)c * N;
         T acc = D[r] * x[r];
         for (int b = 0; b < L.nbands; ++b) {
@@ -94,10 +97,12 @@ __device__ void leaf_gram(const T *A, const T *B, int N, int nb, double *G) {
 
 // Y (N x k) = X (N x kk) C (kk x k, FP64 shared, column-major ldc)
 template <typename T>
-__device__ void leaf_update(T *Y, const T *X, int N, int kk, int k, const double *C, int ldc) {
+__device__ void leaf_update(T *Y, const T *X, int N, int kk, int k, const double *C, int ldc, int *err) {
     const int sc = (int)blockDim.x / N, sr = (int)blockDim.x % N;
     int c = (int)threadIdx.x / N, r = (int)threadIdx.x % N;
     for (int e = threadIdx.x; e < N * k; e += blockDim.x) {
+        // KF_CHECK site 202: the element inside the N x k block, C's last entry inside its shared array
+        if (!KF_CHK(c < k && r >= 0 && r < N && (kk - 1) + ldc * c < BMAXNB * BMAXNB, err, 202)) break;
         double s = 0;
         for (int q = 0; q < kk; ++q) s += (double)X[(int64_t)q * N + r] * C[q + ldc * c];
         Y[(int64_t)c * N + r] = (T)s;
@@ -232,6 +237,12 @@ __global__ void k_batch_chfsi(const LeafDesc *__restrict__ leaves, const int *__
         // scratch: FP64 X, HX, A, B ; FP32 A32, B32, C32 (all N x nb)
         double *X = base, *HX = X + (int64_t)N * nb, *A = HX + (int64_t)N * nb, *B = A + (int64_t)N * nb;
         float *A32 = (float *)(B + (int64_t)N * nb), *B32 = A32 + (int64_t)N * nb, *C32 = B32 + (int64_t)N * nb;
+        // KF_CHECK site 203: the leaf's blocks fit this CTA's scratch and its block the shared arrays
+        // (the same for every thread: the leaf is skipped as a whole)
+        if (!KF_CHK(nb >= 1 && nb <= BMAXNB && N >= 1 &&
+                        (int64_t)N * nb * 4 + ((int64_t)N * nb * 3 + 1) / 2 <= P.scratch_per_cta,
+                    P.err, 203))
+            continue;
         // random start, orthonormalised
         for (int e = threadIdx.x; e < N * nb; e += blockDim.x) {
             const uint64_t h = bmix(bmix(0x4346ull + li) ^ (uint64_t)e);
@@ -264,9 +275,9 @@ __global__ void k_batch_chfsi(const LeafDesc *__restrict__ leaves, const int *__
                     for (int k = threadIdx.x; k < N * na; k += blockDim.x) A32[k] = (float)X[(int64_t)nlock * N + k];
                     __syncthreads();
                     float *a = A32, *b = B32, *cc = C32;
-                    leaf_apply<float>(L, D32, W32, a, b, na, (float)(1 / e), (float)(-c / e), nullptr, 0.f);
+                    leaf_apply<float>(L, D32, W32, a, b, na, (float)(1 / e), (float)(-c / e), nullptr, 0.f, P.err);
                     for (int k = 2; k <= deg; ++k) {
-                        leaf_apply<float>(L, D32, W32, b, cc, na, (float)(2 / e), (float)(-2 * c / e), a, -1.f);
+                        leaf_apply<float>(L, D32, W32, b, cc, na, (float)(2 / e), (float)(-2 * c / e), a, -1.f, P.err);
                         float *t = a; a = b; b = cc; cc = t;
                         if (k % 10 == 0) {   // rescale the live pair by the newer member's column norms
                             for (int col = threadIdx.x; col < na; col += blockDim.x) {
@@ -289,9 +300,9 @@ __global__ void k_batch_chfsi(const LeafDesc *__restrict__ leaves, const int *__
                     __syncthreads();
                     // FP64: reuse HX (free until Rayleigh-Ritz) and B as the recurrence buffers
                     double *a = A, *b = B, *cc = HX;
-                    leaf_apply<double>(L, D64, W64, a, b, na, 1 / e, -c / e, nullptr, 0.0);
+                    leaf_apply<double>(L, D64, W64, a, b, na, 1 / e, -c / e, nullptr, 0.0, P.err);
                     for (int k = 2; k <= deg; ++k) {
-                        leaf_apply<double>(L, D64, W64, b, cc, na, 2 / e, -2 * c / e, a, -1.0);
+                        leaf_apply<double>(L, D64, W64, b, cc, na, 2 / e, -2 * c / e, a, -1.0, P.err);
                         double *t = a; a = b; b = cc; cc = t;
                         if (k % 10 == 0) {
                             for (int col = threadIdx.x; col < na; col += blockDim.x) {
@@ -339,14 +350,14 @@ __global__ void k_batch_chfsi(const LeafDesc *__restrict__ leaves, const int *__
                 leaf_gram<double>(Xa, Xa, N, na, G);
                 ok = chol_inv(G, Vs, Us, na, &s_flag);
                 if (ok) {
-                    leaf_update<double>(A, Xa, N, na, na, Vs, na);
+                    leaf_update<double>(A, Xa, N, na, na, Vs, na, P.err);
                     for (int k = threadIdx.x; k < N * na; k += blockDim.x) Xa[k] = A[k];
                     __syncthreads();
                 }
             }
             if (!ok) break;   // rank-deficient block: reported as not converged
             // Rayleigh-Ritz on the active columns
-            leaf_apply<double>(L, D64, W64, Xa, HX, na, 1.0, 0.0, nullptr, 0.0);
+            leaf_apply<double>(L, D64, W64, Xa, HX, na, 1.0, 0.0, nullptr, 0.0, P.err);
             leaf_gram<double>(Xa, HX, N, na, G);
             if (threadIdx.x == 0)
                 for (int j = 0; j < na; ++j)
@@ -356,13 +367,13 @@ __global__ void k_batch_chfsi(const LeafDesc *__restrict__ leaves, const int *__
                     }
             __syncthreads();
             jacobi_eig(G, Vs, wv, na);
-            leaf_update<double>(A, Xa, N, na, na, Vs, na);
+            leaf_update<double>(A, Xa, N, na, na, Vs, na, P.err);
             for (int k = threadIdx.x; k < N * na; k += blockDim.x) Xa[k] = A[k];
             __syncthreads();
             if (threadIdx.x < na) theta[nlock + threadIdx.x] = wv[threadIdx.x];
             __syncthreads();
             // residual norms of the active columns (FP64)
-            leaf_apply<double>(L, D64, W64, Xa, HX, na, 1.0, 0.0, nullptr, 0.0);
+            leaf_apply<double>(L, D64, W64, Xa, HX, na, 1.0, 0.0, nullptr, 0.0, P.err);
             for (int col = threadIdx.x; col < na; col += blockDim.x) {
                 double s = 0;
                 const double th = theta[nlock + col];
@@ -526,7 +537,7 @@ float run_batch(const Prepared &P, double tol, int maxiter, int threads, int deg
     KF_CUDA(cudaMemcpyAsync(dO, P.order.data(), sizeof(int) * count, cudaMemcpyHostToDevice, s));
     KF_CUDA(cudaMemcpyAsync(d64, P.data.data(), sizeof(double) * P.data.size(), cudaMemcpyHostToDevice, s));
     KF_CUDA(cudaMemcpyAsync(df32, d32.data(), sizeof(float) * d32.size(), cudaMemcpyHostToDevice, s));
-    BatchParams bp{count, tol, maxiter, degree, per};
+    BatchParams bp{count, tol, maxiter, degree, per, tc_error_word()};
     // capture: reset the work counter, then the persistent kernel
     cudaGraph_t graph;
     cudaGraphExec_t exec;

@@ -58,6 +58,9 @@
 // Every wait is an mbarrier wait with a cycle budget; when one runs out the CTA records
 // KF_ETIMEOUT in the host-mapped error word, every role leaves its loop at its next check, the
 // issuer waits (bounded) for its MMAs in flight, and TMEM is freed.
+// KF_CHECK builds test, in k_gram_tma, every raw-slot piece read (site 301), every operand-image
+// store (302) and every tensor copy's box against its slot (303), and record a failure instead of
+// the access.
 #include <cuda.h>   // CUtensorMap and its enums (the encoder itself is taken from the driver at run time)
 
 #include <algorithm>
@@ -572,7 +575,10 @@ __global__ void __launch_bounds__(GM_THREADS, 1) k_gram_tma(const __grid_constan
                 gm_expect(rfull + r, a.tx_bytes);
                 const int x = (int)((gfirst + g) * GM_GR);
                 const uint32_t slot = rbase + (uint32_t)r * a.rslot;
-                for (int q = 0; q < a.nsrc; ++q) gm_tma2d(slot + a.roff[q], &a.tm[q], x, 0, rfull + r);
+                // KF_CHECK site 303: every source's box inside the raw slot
+                for (int q = 0; q < a.nsrc; ++q)
+                    if (KF_CHK(a.roff[q] + (uint32_t)a.k[q] * (GM_GR * 4) <= a.rslot, a.err, 303))
+                        gm_tma2d(slot + a.roff[q], &a.tm[q], x, 0, rfull + r);
                 ++issued;
             }
             if (s_abort) {
@@ -629,20 +635,28 @@ __global__ void __launch_bounds__(GM_THREADS, 1) k_gram_tma(const __grid_constan
                 // loads of a chunk are in flight together (a piece without a source reads the slot's
                 // first bytes and is not stored)
                 uint4 v[P::PPT], w[P::PPT];
+                // KF_CHECK site 301: a piece's 16 bytes inside the raw slot
 #pragma unroll
                 for (int j = 0; j < P::PPT; ++j)
-                    v[j] = *reinterpret_cast<const uint4 *>(slot + roff[j] + (i * CPS) * 128);
+                    v[j] = KF_CHK(roff[j] + (uint32_t)(i * CPS) * 128u + 16u <= a.rslot, a.err, 301)
+                               ? *reinterpret_cast<const uint4 *>(slot + roff[j] + (i * CPS) * 128)
+                               : make_uint4(0u, 0u, 0u, 0u);
 #pragma unroll
                 for (int cu = 0; cu < CPS; ++cu) {
                     if (cu + 1 < CPS) {
 #pragma unroll
                         for (int j = 0; j < P::PPT; ++j)
-                            w[j] = *reinterpret_cast<const uint4 *>(slot + roff[j] + (i * CPS + cu + 1) * 128);
+                            w[j] = KF_CHK(roff[j] + (uint32_t)(i * CPS + cu + 1) * 128u + 16u <= a.rslot, a.err, 301)
+                                       ? *reinterpret_cast<const uint4 *>(slot + roff[j] + (i * CPS + cu + 1) * 128)
+                                       : make_uint4(0u, 0u, 0u, 0u);
                     }
                     unsigned char *st = ops + (size_t)o * P::STAGE + (size_t)cu * P::CHB;
 #pragma unroll
                     for (int j = 0; j < P::PPT; ++j) {
-                        if (!has[j]) continue;
+                        // KF_CHECK site 302: the hi and lo pieces inside the chunk's images
+                        if (!has[j] || !KF_CHK(hoff[j] + 16u <= (uint32_t)P::CHB && loff[j] + 16u <= (uint32_t)P::CHB,
+                                               a.err, 302))
+                            continue;
                         const uint32_t x[4] = {v[j].x, v[j].y, v[j].z, v[j].w};
                         uint32_t h[4], l[4];
 #pragma unroll
