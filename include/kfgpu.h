@@ -233,7 +233,7 @@ typedef struct {
     int32_t fallback_iters;    /* warm start judge: after this many iterations ...             */
     double fallback_resid;     /* ... a largest residual of the m warm-start columns above this
                                   (absolute, energy units) restarts a warm-started solve from a
-                                  random block (0 disables); the judge of a learned warm start */
+                                  random block (0 disables); the check on a learned warm start */
     int32_t seed_kind;         /* LOBPCG / Chebyshev `seed` (src/tree.jl:66-87, 293-321):
                                   KF_SEED_PRODUCT (default) or KF_SEED_RANDOM; used when
                                   kf_solve's seed argument is NULL                             */

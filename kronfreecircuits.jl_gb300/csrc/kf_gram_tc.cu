@@ -28,7 +28,7 @@
 // rows into two FP32 partial sets per CTA; the reduction sums both.
 //
 // Two kernels share these layouts.  k_gram_tma (the default, below) loads with 2-D tensor copies
-// of 128 rows x k columns per source; k_gram_tc, the fallback where the driver gives no tensor-map
+// of 128 rows x k columns per source; k_gram_tc, the fallback where the CUDA driver gives no tensor-map
 // encoder, copies 16-byte pieces with cp.async.  What was measured on GB300 on the way there:
 //   - a stream of tensor copies over the solve's 54 columns reaches 1.4-2.0 TB/s with 32-row boxes
 //     (128-byte rows), 2.8 TB/s with 64-row, 5.0 TB/s with 128-row and 5.7 TB/s with 256-row boxes:
@@ -61,7 +61,7 @@
 // KF_CHECK builds test, in k_gram_tma, every raw-slot piece read (site 301), every operand-image
 // store (302) and every tensor copy's box against its slot (303), and record a failure instead of
 // the access.
-#include <cuda.h>   // CUtensorMap and its enums (the encoder itself is taken from the driver at run time)
+#include <cuda.h>   // CUtensorMap and its enums (the encoder itself is taken from the CUDA driver at run time)
 
 #include <algorithm>
 #include <cstdlib>
@@ -820,8 +820,8 @@ struct GtDevice {
     size_t dyn[6] = {0, 0, 0, 0, 0, 0};
 };
 
-// the driver's tensor-map encoder (cuTensorMapEncodeTiled), looked up once through the runtime;
-// null when the driver does not provide it (the cp.async kernel is used then)
+// the CUDA driver's tensor-map encoder (cuTensorMapEncodeTiled), looked up once through the runtime;
+// null when the CUDA driver does not provide it (the cp.async kernel is used then)
 using TmEncode = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
                               const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
                               CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);

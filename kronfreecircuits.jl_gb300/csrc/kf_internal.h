@@ -307,7 +307,7 @@ bool gram_tc(const GramTcSrc *src, int nsrc, int r0, int r1, int c0, int c1, int
 size_t gram_tc_partials_size(int nr, int nc);
 // a 2-D tensor map (a CUtensorMap, 64-byte aligned, 128 bytes) of an FP32 column block: N rows x k
 // columns, leading dimension ld, boxes of 128 rows x k columns, unswizzled, rows past N read as zero
-// and clipped on stores; false where the driver gives no encoder or k > 256 (the caller checks the
+// and clipped on stores; false where the CUDA driver gives no encoder or k > 256 (the caller checks the
 // base is 16-byte aligned and ld a multiple of 4); cached per (p, ld, N, k)
 bool tensor_map_cols(const float *p, int64_t ld, int64_t N, int k, void *map);
 // second orthogonalisation pass on the device: from G = [X Z]'Z, coefficients C ((r + wx) x r)

@@ -7,7 +7,7 @@ sources of up to 64 rows each (one MMA per K step on [A_hi; A_lo] x [B_hi; B_lo]
 the kernel turns down (the solvers then keep the SIMT Gram).
 
 The default kernel loads with 2-D tensor copies (128 rows x k columns per source); the cp.async
-kernel, used where the driver gives no tensor-map encoder, runs the same pools in a subprocess with
+kernel, used where the CUDA driver gives no tensor-map encoder, runs the same pools in a subprocess with
 KF_GRAM_TMA=0.
 
 Tolerance: hi*hi + hi*lo + lo*hi drops lo*lo (2^-20 of a product) and TF32 keeps 10 mantissa bits
