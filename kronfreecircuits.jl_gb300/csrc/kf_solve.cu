@@ -534,7 +534,7 @@ static LobOut lobpcg_run(kf_op *op, LobWork<T> &Wk, const double *D, const LobPa
             out.converged = true;
             break;
         }
-        // the checked columns (m + guards); buffer columns beyond them do not enter the judge,
+        // the checked columns (m + guards); buffer columns beyond them do not enter the warm-start check,
         // the stall test or the convergence count
         const int ncc = prm.n_conv_check;
         double worst = 0, bestr = INFINITY;
@@ -852,7 +852,7 @@ static LobOut lobpcg_refine(kf_op *op, RefineWork &Rw, LobWork<float> &Wk, const
             out.converged = true;
             break;
         }
-        // the checked columns (m + guards); buffer columns beyond them do not enter the judge,
+        // the checked columns (m + guards); buffer columns beyond them do not enter the warm-start check,
         // the stall test or the convergence count
         const int ncc = prm.n_conv_check;
         double worst = 0, bestr = INFINITY;
@@ -1111,7 +1111,7 @@ static void solve_lobpcg(kf_op *op, const kf_solver_opts &o, int m, const double
     if (X0) st.warm = 1;
     LobParams p64{o.tol, o.maxiter, o.preconditioner, o.eta, w, 1e-12, false, o.fallback_iters,
                   o.fallback_resid > 0 ? o.fallback_resid : 0.0};
-    // the judge looks at the warm block's m columns: the guards and buffers come from the product
+    // the warm-start check looks at the warm block's m columns: the guards and buffers come from the product
     // seed, the method without the warm start
     p64.judge_cols = m;
     std::vector<double> theta;

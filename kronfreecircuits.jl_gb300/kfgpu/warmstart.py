@@ -9,9 +9,9 @@ Pipeline (all GPU work through libkfgpu):
   4. train the din -> 256 -> 256 -> k m network with the library's own forward / backward / Adam
      kernels (kfgpu.mlp);
   5. warm start: X0 = POD C_pred(theta), handed to kf_solve as the warm-start block, with the
-     solver's judge: if the largest residual after `fallback_iters` iterations exceeds
+     solver's check: if the largest residual after `fallback_iters` iterations exceeds
      `fallback_resid`, the solve restarts from a random block (the plain method remains the
-     fallback and the judge).
+     fallback and the reference).
 
 The reference's warm start is the previous solution's vectors (src/materialize.jl:656-670,
 `_initial_block`); this is the learned extension of that hook for parameter sweeps.

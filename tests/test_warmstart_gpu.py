@@ -4,7 +4,7 @@ A network trained by the library's own kernels on the plain solver's eigenvector
 initial LOBPCG block for held-out theta.  Checked: the warm-started solves reach the same
 eigenvalues as random starts (1e-9 relative), need fewer iterations on average (what the network
 gains), and an untrained network's block is judged after 3 iterations and replaced by a random
-start without harming the result (the plain method stays the fallback and the judge).
+start without harming the result (the plain method stays the fallback and the reference).
 """
 import numpy as np
 import pytest
