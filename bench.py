@@ -73,9 +73,9 @@ NDRAWS = 64
 # in L2);
 # the tensor-core Gram of [X Z]'Z at 18 + 36 columns (reads 145.2 MB = every element once, writes
 # 0.1 MB of partials)
-APPLY_TRAFFIC_BYTES = 47563520     # ncu dram bytes read + written, one 16-column k_apply_march launch
+APPLY_TRAFFIC_BYTES = 47370624     # ncu dram bytes read + written, one 16-column k_apply_march launch (7 warps)
 MODE_TRAFFIC_BYTES = 50463488
-UPDATE_TRAFFIC_BYTES = 200817152   # ncu dram bytes read + written, one launch (the rest of Y stays in L2)
+UPDATE_TRAFFIC_BYTES = 201177600   # ncu dram bytes read + written, one 54 -> 36 launch (the rest of Y stays in L2)
 GRAM_TC_TRAFFIC_BYTES = 145209856   # ncu dram bytes, one [X Z]'Z launch (one-MMA layout)
 
 
