@@ -140,11 +140,14 @@ int kf_op_sandwich(kf_op *op, const double *W, int64_t ldw, int32_t kw, const do
  * X and Y complex blocks of m columns stored as 2m FP64 columns: the real parts, then the imaginary
  * parts (column j at X + j ldx, its imaginary part at X + (m + j) ldx).  omega != NULL: the
  * interaction frame, Y = e^{i Omega t} (H(t) - diag Omega) e^{-i Omega t} X with Omega = omega (N
- * values, rad/ns: the diagonal of 2 pi (H0 - E0), on the same side as X).  ports: nports operators on
- * H0's product basis (KF_EDIM otherwise); coef: host array.  H0 and the ports are real operators.
+ * values, rad/ns: the diagonal of 2 pi (H0 - E0), on the same side as X).  Port k is
+ * ports[k] + i ports_im[k]: its real and imaginary components as real operators on H0's product
+ * basis (KF_EDIM otherwise), either array or entry may be NULL (a real-character port has no
+ * imaginary component), not both entries of one port; coef: host array.  H0 is a real operator.
  * flags: KF_F64 with KF_DEVICE (H0's stream, asynchronous) or KF_HOST (returns when done). */
-int kf_drive_apply(kf_op *H0, double E0, int32_t nports, kf_op *const *ports, const double *coef, const double *omega,
-                   double t, const void *X, int64_t ldx, void *Y, int64_t ldy, int64_t m, int32_t flags);
+int kf_drive_apply(kf_op *H0, double E0, int32_t nports, kf_op *const *ports, kf_op *const *ports_im,
+                   const double *coef, const double *omega, double t, const void *X, int64_t ldx, void *Y, int64_t ldy,
+                   int64_t m, int32_t flags);
 
 /* to_lab (src/quantumtoolbox.jl:25-37): the lab-frame state e^{-i Omega t} psi of an
  * interaction-picture block, in place: X as in kf_drive_apply (2m FP64 columns), omega N values

@@ -165,17 +165,22 @@ int kf_op_apply_axpby(kf_op *op, const void *X, void *Y, const void *Z, int64_t 
     });
 }
 
-int kf_drive_apply(kf_op *H0, double E0, int32_t nports, kf_op *const *ports, const double *coef, const double *omega,
-                   double t, const void *X, int64_t ldx, void *Y, int64_t ldy, int64_t m, int32_t flags) {
+int kf_drive_apply(kf_op *H0, double E0, int32_t nports, kf_op *const *ports, kf_op *const *ports_im,
+                   const double *coef, const double *omega, double t, const void *X, int64_t ldx, void *Y, int64_t ldy,
+                   int64_t m, int32_t flags) {
     return guarded([&] {
         KF_REQUIRE(H0 != nullptr, KF_EINVAL, "kf_drive_apply: H0 is NULL");
         KF_REQUIRE(!(flags & KF_F32), KF_EINVAL, "kf_drive_apply: time evolution runs in FP64");
-        KF_REQUIRE(nports >= 0 && (nports == 0 || (ports && coef)), KF_EINVAL, "kf_drive_apply: bad port list");
+        KF_REQUIRE(nports >= 0 && (nports == 0 || ((ports || ports_im) && coef)), KF_EINVAL,
+                   "kf_drive_apply: bad port list");
         const int64_t N = H0->N;
         for (int k = 0; k < nports; ++k) {
-            KF_REQUIRE(ports[k] != nullptr, KF_EINVAL, "kf_drive_apply: port operator " + std::to_string(k) + " is NULL");
-            KF_REQUIRE(ports[k]->N == N && ports[k]->dims == H0->dims, KF_EDIM,
-                       "drive_hamiltonian: port operator " + std::to_string(k) + " is not on H0's product basis");
+            kf_op *re = ports ? ports[k] : nullptr, *im = ports_im ? ports_im[k] : nullptr;
+            KF_REQUIRE(re != nullptr || im != nullptr, KF_EINVAL,
+                       "kf_drive_apply: port operator " + std::to_string(k) + " has neither component");
+            for (kf_op *o : {re, im})
+                KF_REQUIRE(o == nullptr || (o->N == N && o->dims == H0->dims), KF_EDIM,
+                           "drive_hamiltonian: port operator " + std::to_string(k) + " is not on H0's product basis");
             KF_REQUIRE(std::isfinite(coef[k]), KF_EINVAL, "kf_drive_apply: coefficient " + std::to_string(k) +
                                                               " is not finite");
         }
@@ -196,14 +201,15 @@ int kf_drive_apply(kf_op *H0, double E0, int32_t nports, kf_op *const *ports, co
                 KF_CUDA(cudaMemcpyAsync(dW, omega, (size_t)N * 8, cudaMemcpyHostToDevice, s));
             }
             KF_CUDA(cudaMemcpy2DAsync(dX, N * 8, X, ldx * 8, N * 8, 2 * m, cudaMemcpyHostToDevice, s));
-            kf::drive_apply(H0, E0, nports, ports, coef, dW, t, dX, N, dY, N, m);
+            kf::drive_apply(H0, E0, nports, ports, ports_im, coef, dW, t, dX, N, dY, N, m);
             KF_CUDA(cudaMemcpy2DAsync(Y, ldy * 8, dY, N * 8, N * 8, 2 * m, cudaMemcpyDeviceToHost, s));
             KF_CUDA(cudaFreeAsync(dX, s));
             KF_CUDA(cudaFreeAsync(dY, s));
             if (dW) KF_CUDA(cudaFreeAsync(dW, s));
             KF_CUDA(cudaStreamSynchronize(s));
         } else {
-            kf::drive_apply(H0, E0, nports, ports, coef, omega, t, (const double *)X, ldx, (double *)Y, ldy, m);
+            kf::drive_apply(H0, E0, nports, ports, ports_im, coef, omega, t, (const double *)X, ldx, (double *)Y, ldy,
+                            m);
         }
     });
 }

@@ -6,11 +6,14 @@
 //   H(t) = 2 pi [H0 - E0 + sum_k f_k(t) O_k]        (rad/ns; f_k in GHz, E0 the node's lowest energy)
 //   interaction frame: H_I(t) = e^{i Omega t} (H(t) - diag Omega) e^{-i Omega t},   psi_lab = e^{-i Omega t} psi_I
 //
-// H0 and the ports are real operators (the real-by-structure circuits: every measured one), so on a
-// complex block they act on the real and the imaginary parts alike: the block of m complex columns
-// is stored as 2m FP64 columns (real parts, then imaginary parts) and every product is one real
-// apply of the existing kernels over 2m columns.  The rotations and the accumulation of the port
-// terms are elementwise kernels here.
+// H0 is a real operator (the real-by-structure circuits: every measured one), so on a complex block
+// it acts on the real and the imaginary parts alike: the block of m complex columns is stored as 2m
+// FP64 columns (real parts, then imaginary parts) and every product is one real apply of the
+// existing kernels over 2m columns.  A port of complex character (e^{i phi}, e^{2 pi i n k}: the
+// reference's real-character ports are the real ones) is given as its real and imaginary
+// components, two real operators O = O_re + i O_im: i O_im psi is O_im applied to the same 2m
+// columns with its halves exchanged and one negated.  The rotations and the accumulation of the
+// port terms are elementwise kernels here.
 #include "kf_internal.h"
 
 namespace kf {
@@ -39,6 +42,17 @@ __global__ void k_rotate(const double *X, int64_t ldx, double *Y, int64_t ldy, c
     Y[r + ldy * (m + j)] = a * sn + b * cs;
 }
 
+// Y += i T for complex blocks of m columns (real halves first): Y_re -= T_im, Y_im += T_re
+__global__ void k_drive_acc_i(double *__restrict__ Y, int64_t ldy, const double *__restrict__ T, int64_t ldt,
+                              int64_t N, int m) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y;
+    if (i >= N || j >= m) return;
+    const double tr = T[i + ldt * j], ti = T[i + ldt * (m + j)];
+    Y[i + ldy * j] -= ti;
+    Y[i + ldy * (m + j)] += tr;
+}
+
 // Y <- e^{i omega_r t} (Y - omega_r U), row r: the interaction frame's last step
 __global__ void k_rotate_sub(double *__restrict__ Y, int64_t ldy, const double *__restrict__ U, int64_t ldu,
                              const double *__restrict__ omega, double t, int64_t N, int m) {
@@ -64,8 +78,8 @@ void rotate_rows(const double *omega, int64_t N, double t, double sign, double *
     KF_LAUNCH_CHECK();
 }
 
-void drive_apply(kf_op *H0, double E0, int nports, kf_op *const *ports, const double *coef, const double *omega,
-                 double t, const double *X, int64_t ldx, double *Y, int64_t ldy, int64_t m) {
+void drive_apply(kf_op *H0, double E0, int nports, kf_op *const *ports, kf_op *const *ports_im, const double *coef,
+                 const double *omega, double t, const double *X, int64_t ldx, double *Y, int64_t ldy, int64_t m) {
     const int64_t N = H0->N, w = 2 * m;
     cudaStream_t s = H0->stream;
     if (N == 0 || m == 0) return;
@@ -96,10 +110,17 @@ void drive_apply(kf_op *H0, double E0, int nports, kf_op *const *ports, const do
     launch_apply(H0, false, src, Y, lds, ldy, w, TWO_PI, -TWO_PI * E0, nullptr, 0, 0.0, s);
     for (int k = 0; k < nports; ++k) {
         if (coef[k] == 0.0) continue;
-        // the port's product on H0's stream, then accumulated
-        launch_apply(ports[k], false, src, T, lds, N, w, TWO_PI * coef[k], 0.0, nullptr, 0, 0.0, s);
-        k_drive_acc<<<g2, 256, 0, s>>>(Y, ldy, T, N, N, (int)w);
-        KF_LAUNCH_CHECK();
+        // the port's products on H0's stream, then accumulated (the imaginary component times i)
+        if (ports[k]) {
+            launch_apply(ports[k], false, src, T, lds, N, w, TWO_PI * coef[k], 0.0, nullptr, 0, 0.0, s);
+            k_drive_acc<<<g2, 256, 0, s>>>(Y, ldy, T, N, N, (int)w);
+            KF_LAUNCH_CHECK();
+        }
+        if (ports_im && ports_im[k]) {
+            launch_apply(ports_im[k], false, src, T, lds, N, w, TWO_PI * coef[k], 0.0, nullptr, 0, 0.0, s);
+            k_drive_acc_i<<<g, 256, 0, s>>>(Y, ldy, T, N, N, (int)m);
+            KF_LAUNCH_CHECK();
+        }
     }
     if (omega) {
         k_rotate_sub<<<g, 256, 0, s>>>(Y, ldy, U, N, omega, t, N, (int)m);     // e^{i Omega t} (Y - Omega U)

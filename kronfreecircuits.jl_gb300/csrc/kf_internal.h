@@ -255,8 +255,9 @@ bool rr_eig_device(const double *G, int ldg, bool packed, int na, int k, double 
 // basis = :free): Y = H(t) X, H(t) = 2 pi [H0 - E0 + sum_k coef_k O_k] (rad/ns), X a complex block of m
 // columns stored as 2m FP64 columns (real parts, then imaginary parts); omega != nullptr: the
 // interaction frame e^{i Omega t} (H(t) - diag Omega) e^{-i Omega t}.  Device pointers, H0's stream.
-void drive_apply(kf_op *H0, double E0, int nports, kf_op *const *ports, const double *coef, const double *omega,
-                 double t, const double *X, int64_t ldx, double *Y, int64_t ldy, int64_t m);
+// ports_im (may be NULL): the imaginary components of ports of complex character (entries may be NULL)
+void drive_apply(kf_op *H0, double E0, int nports, kf_op *const *ports, kf_op *const *ports_im, const double *coef,
+                 const double *omega, double t, const double *X, int64_t ldx, double *Y, int64_t ldy, int64_t m);
 // X <- e^{sign i Omega t} X in place (complex block of m columns as above)
 void rotate_rows(const double *omega, int64_t N, double t, double sign, double *X, int64_t ldx, int64_t m,
                  cudaStream_t s);

@@ -108,7 +108,7 @@ def lib():
         "kf_op_sandwich": (C.c_int, [P, P, C.c_int64, C.c_int32, P, C.c_int64, C.c_int32, P, C.c_int32]),
         "kf_complement_solve": (C.c_int, [P, P, C.c_int64, C.c_int32, P, C.c_int64, C.c_int32, P, P, C.c_double,
                                           C.c_int32, C.c_double, P, C.c_int64, P, P, P, P, C.c_int32]),
-        "kf_drive_apply": (C.c_int, [P, C.c_double, C.c_int32, P, P, P, C.c_double, P, C.c_int64, P, C.c_int64,
+        "kf_drive_apply": (C.c_int, [P, C.c_double, C.c_int32, P, P, P, P, C.c_double, P, C.c_int64, P, C.c_int64,
                                      C.c_int64, C.c_int32]),
         "kf_to_lab": (C.c_int, [P, C.c_int64, C.c_double, P, C.c_int64, C.c_int64, C.c_int32]),
         "kf_op_diagonal": (C.c_int, [P, C.POINTER(C.c_double)]),

@@ -6,7 +6,9 @@
                                             its QobjEvo to QuantumToolbox's adaptive sesolve)
 
 H(t) = 2 pi [H0 - E0 + sum_k f_k(t) O_k] in rad/ns (t in ns, f_k in GHz, E0 the node's lowest
-energy), for real H0 and real port operators O_k (KronFreeOperator on the same product basis).
+energy), for a real H0 and port operators O_k on the same product basis: a KronFreeOperator (a port
+of real character) or a pair (O_re, O_im) of its real and imaginary components (complex character,
+e^{i phi} or e^{2 pi i n k}; either may be None).
 frame = "interaction": H_I(t) = e^{i Omega t} (H(t) - diag Omega) e^{-i Omega t} with Omega the
 diagonal of 2 pi (H0 - E0); to_lab takes its states back to the lab frame.  States are complex
 (N,) kets or (N, m) blocks; on the device they are torch complex128 tensors, shape (m, N).
@@ -37,20 +39,27 @@ def _unpack(P, m):
 
 class DriveHamiltonian:
     """The drive Hamiltonian of src/quantumtoolbox.jl:84-99 on a node's product basis.  drives: a list
-    of (O_k, f_k) pairs, O_k a KronFreeOperator on H0's basis (a port operator), f_k(t) its
-    coefficient in GHz.  frame: "lab" or "interaction"."""
+    of (O_k, f_k) pairs, O_k a KronFreeOperator on H0's basis (a port operator) or a pair of its real
+    and imaginary components, f_k(t) its coefficient in GHz.  frame: "lab" or "interaction"."""
 
     def __init__(self, H0, drives, E0, frame="lab"):
         if frame not in ("lab", "interaction"):
             raise _abi.ArgumentError(_abi.KF_EINVAL, f"drive_hamiltonian: frame must be lab or interaction, got {frame!r}")
         self.H0 = H0
         self.E0 = float(E0)
-        self.ports = [O for O, _ in drives]
+        self.ports, self.ports_im = [], []
+        for O, _ in drives:
+            re, im = (O if isinstance(O, tuple) else (O, None))
+            self.ports.append(re)
+            self.ports_im.append(im)
         self.funcs = [f for _, f in drives]
-        for k, O in enumerate(self.ports):
-            if O.N != H0.N:
-                raise _abi.DimensionMismatch(_abi.KF_EDIM, f"drive_hamiltonian: port operator {k} has size {O.N}, "
-                                                           f"H0 {H0.N}")
+        for k, (re, im) in enumerate(zip(self.ports, self.ports_im)):
+            if re is None and im is None:
+                raise _abi.ArgumentError(_abi.KF_EINVAL, f"drive_hamiltonian: port {k} has neither component")
+            for O in (re, im):
+                if O is not None and O.N != H0.N:
+                    raise _abi.DimensionMismatch(_abi.KF_EDIM, f"drive_hamiltonian: port operator {k} has size "
+                                                               f"{O.N}, H0 {H0.N}")
         self.frame = frame
         self.omega = None
         self._omega_dev = None
@@ -78,13 +87,21 @@ class DriveHamiltonian:
         m = P.shape[0] // 2
         if Y is None:
             Y = torch.empty_like(P)
-        coef = (C.c_double * max(1, len(self.funcs)))(*[float(f(t)) for f in self.funcs])
-        ports = (C.c_void_p * max(1, len(self.ports)))(*[O.handle for O in self.ports])
+        coef, ports, pim = self._args(t)
         om = self._omega_device().data_ptr() if self.omega is not None else None
-        _abi.check(_abi.lib().kf_drive_apply(self.H0.handle, self.E0, len(self.ports), C.cast(ports, C.c_void_p),
-                                             C.cast(coef, C.c_void_p), om, float(t), P.data_ptr(), self.N,
-                                             Y.data_ptr(), self.N, m, _abi.KF_DEVICE | _abi.KF_F64))
+        _abi.check(_abi.lib().kf_drive_apply(self.H0.handle, self.E0, len(self.ports), ports, pim, coef, om, float(t),
+                                             P.data_ptr(), self.N, Y.data_ptr(), self.N, m,
+                                             _abi.KF_DEVICE | _abi.KF_F64))
         return Y
+
+    def _args(self, t):
+        """(coefficients, real components, imaginary components) as C arrays for kf_drive_apply."""
+        n = max(1, len(self.funcs))
+        coef = (C.c_double * n)(*[float(f(t)) for f in self.funcs])
+        re = (C.c_void_p * n)(*[O.handle if O is not None else None for O in self.ports])
+        im = (C.c_void_p * n)(*[O.handle if O is not None else None for O in self.ports_im])
+        has_im = any(O is not None for O in self.ports_im)
+        return C.cast(coef, C.c_void_p), C.cast(re, C.c_void_p), (C.cast(im, C.c_void_p) if has_im else None)
 
     def apply(self, t, psi):
         """H(t) psi for a host complex ket (N,) or block (N, m)."""
@@ -94,13 +111,11 @@ class DriveHamiltonian:
         m = X.shape[1]
         P = np.asfortranarray(np.concatenate([X.real, X.imag], axis=1))
         Y = np.empty_like(P, order="F")
-        coef = (C.c_double * max(1, len(self.funcs)))(*[float(f(t)) for f in self.funcs])
-        ports = (C.c_void_p * max(1, len(self.ports)))(*[O.handle for O in self.ports])
+        coef, ports, pim = self._args(t)
         om = self.omega.ctypes.data_as(C.c_void_p) if self.omega is not None else None
-        _abi.check(_abi.lib().kf_drive_apply(self.H0.handle, self.E0, len(self.ports), C.cast(ports, C.c_void_p),
-                                             C.cast(coef, C.c_void_p), om, float(t), P.ctypes.data_as(C.c_void_p),
-                                             self.N, Y.ctypes.data_as(C.c_void_p), self.N, m,
-                                             _abi.KF_HOST | _abi.KF_F64))
+        _abi.check(_abi.lib().kf_drive_apply(self.H0.handle, self.E0, len(self.ports), ports, pim, coef, om, float(t),
+                                             P.ctypes.data_as(C.c_void_p), self.N, Y.ctypes.data_as(C.c_void_p),
+                                             self.N, m, _abi.KF_HOST | _abi.KF_F64))
         out = Y[:, :m] + 1j * Y[:, m:]
         return out[:, 0] if one else out
 

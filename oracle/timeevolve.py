@@ -23,10 +23,11 @@ TWO_PI = 2.0 * math.pi
 
 
 def drive_matrix(H0, E0, ports, coefs):
-    """2 pi [H0 - E0 + sum_k coefs[k] ports[k]] as a dense matrix (src/quantumtoolbox.jl:84-99)."""
-    M = np.array(H0, dtype=np.float64) - E0 * np.eye(H0.shape[0])
+    """2 pi [H0 - E0 + sum_k coefs[k] ports[k]] as a dense matrix (src/quantumtoolbox.jl:84-99); a port
+    of complex character is a complex matrix."""
+    M = np.array(H0, dtype=np.complex128) - E0 * np.eye(H0.shape[0])
     for O, c in zip(ports, coefs):
-        M = M + c * np.asarray(O, dtype=np.float64)
+        M = M + c * np.asarray(O, dtype=np.complex128)
     return TWO_PI * M
 
 

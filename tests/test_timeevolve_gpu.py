@@ -133,10 +133,46 @@ def test_drive_errors(cuda):
     X = np.zeros((H0.N, 2), order="F")
     ports = (C.c_void_p * 1)(small.handle)
     coef = (C.c_double * 1)(1.0)
-    st = _abi.lib().kf_drive_apply(H0.handle, 0.0, 1, C.cast(ports, C.c_void_p), C.cast(coef, C.c_void_p), None, 0.0,
-                                   X.ctypes.data_as(C.c_void_p), H0.N, X.ctypes.data_as(C.c_void_p), H0.N, 1,
+    st = _abi.lib().kf_drive_apply(H0.handle, 0.0, 1, C.cast(ports, C.c_void_p), None, C.cast(coef, C.c_void_p), None,
+                                   0.0, X.ctypes.data_as(C.c_void_p), H0.N, X.ctypes.data_as(C.c_void_p), H0.N, 1,
                                    _abi.KF_HOST | _abi.KF_F64)
     assert st == _abi.KF_EDIM
-    st = _abi.lib().kf_drive_apply(H0.handle, 0.0, 0, None, None, None, 0.0, X.ctypes.data_as(C.c_void_p), H0.N,
+    st = _abi.lib().kf_drive_apply(H0.handle, 0.0, 0, None, None, None, None, 0.0, X.ctypes.data_as(C.c_void_p), H0.N,
                                    X.ctypes.data_as(C.c_void_p), H0.N, 1, _abi.KF_HOST | _abi.KF_F32)
     assert st == _abi.KF_EINVAL
+    with pytest.raises(_abi.ArgumentError, match="neither"):
+        te.DriveHamiltonian(H0, [((None, None), lambda t: 1.0)], E[0])
+
+
+def _complex_ports(ncut=4):
+    """e^{2 pi i n k} on mode 1 (k = 0.1: a port of complex character on the charge basis, as the
+    reference's tests drive the real system) as (cos, sin) components, and an imaginary-only port."""
+    from kfgpu import KronFreeOperator
+    from kfgpu.ops import DiagonalOp
+    n = np.arange(-ncut, ncut + 1, dtype=np.float64)
+    d = 2 * ncut + 1
+    c, sn = np.cos(2 * np.pi * 0.1 * n), np.sin(2 * np.pi * 0.1 * n)
+    re = KronFreeOperator([d, d], [(1.0, [(0, DiagonalOp(c))])])
+    im = KronFreeOperator([d, d], [(1.0, [(0, DiagonalOp(sn))])])
+    im2 = KronFreeOperator([d, d], [(1.0, [(1, DiagonalOp(n))])])
+    dense = np.kron(np.eye(d), np.diag(c + 1j * sn))          # axis 0 fastest
+    dense2 = 1j * np.kron(np.diag(n), np.eye(d))
+    return (re, im), (None, im2), dense, dense2
+
+
+@pytest.mark.parametrize("frame", ["lab", "interaction"])
+def test_complex_character_ports(cuda, frame):
+    from kfgpu import timeevolve as te
+    H0, Ps, H0d, Pd, E, V = _setup()
+    p1, p2, d1, d2 = _complex_ports()
+    funcs = [lambda t: 0.05 * math.cos(3.0 * t), lambda t: 0.02 * math.sin(2.0 * t)]
+    H = te.DriveHamiltonian(H0, [(p1, funcs[0]), (p2, funcs[1])], E[0], frame=frame)
+    om = ote.omega_of(H0d, E[0]) if frame == "interaction" else None
+    X = _rand_block(H0.N, 2, 5)
+    for t in (0.1, 1.3):
+        ref = ote.apply(H0d, E[0], [d1, d2], funcs, t, X, omega=om)
+        assert np.max(np.abs(H.apply(t, X) - ref)) / np.max(np.abs(ref)) < 1e-12, (frame, t)
+    psi0 = (V[:, 0] + 0.5j * V[:, 1]).astype(np.complex128)
+    got = te.sesolve(H, psi0, [0.0, 0.02, 0.04], 2e-3)
+    ref = ote.rk4(H0d, E[0], [d1, d2], funcs, psi0, [0.0, 0.02, 0.04], 2e-3, omega=om)
+    assert np.max(np.abs(got - ref)) < 1e-10
