@@ -2,7 +2,8 @@
 (oracle/timeevolve.py; src/quantumtoolbox.jl), pinned by the properties the reference's own tests
 check (test/quantumtoolbox/test_quantumtoolbox.jl): to_lab's known answers on arrays (:102-107), the
 interaction frame taken back to the lab frame equal to the lab-frame evolution, for a ket and for a
-block (:109-128), and with no drives the product-basis evolution e^{-i 2 pi (H0 - E0) T} (:137-149).
+block (:109-128), and with no drives the product-basis evolution e^{-i 2 pi (H0 - E0) T} (:137-149);
+and a Hermitian port of complex character keeps the evolution unitary.
 The system: two transmons on the flat product of two small charge bases (9 x 9), driven through the
 charge port of the first, f(t) = 0.05 cos(2 pi (E1 - E0) t) GHz, as the reference's tests drive.
 """
@@ -84,3 +85,26 @@ def test_no_drives_is_the_product_basis_propagator():
     # dressed amplitudes pick up e^{-i 2 pi (E_i - E_0) T}
     amp = V.conj().T @ ex
     assert np.allclose(amp, np.exp(-1j * 2 * math.pi * (E - E[0]) * T) * (V.conj().T @ psi0), atol=1e-10)
+
+
+def test_complex_character_port_is_unitary():
+    """A Hermitian port of complex character -- the charge n = -i d/dphi on a phase grid, purely
+    imaginary -- keeps the evolution unitary, and the fixed-step evolution matches e^{-i H T} for a
+    constant coefficient."""
+    from kfgpu import circuits
+    from kfgpu.ops import PhaseGrid, localop
+    rng = np.random.default_rng(9)
+    dims, terms = circuits.fluxonium_leaf(circuits.fluxonium_theta(rng), 101)
+    H0 = _dense(dims, terms)
+    basis = PhaseGrid(-5 * math.pi, 5 * math.pi, 101, 4)        # the fluxonium leaf's grid
+    n_im = _dense(dims, [(1.0, [(0, localop(basis, "n", part="im"))])])
+    O = 1j * n_im
+    assert np.allclose(O, O.conj().T, atol=1e-12)
+    E = np.linalg.eigvalsh(H0)
+    V = np.linalg.eigh(H0)[1]
+    psi0 = (V[:, 0] + V[:, 1]).astype(np.complex128) / math.sqrt(2)
+    T = 0.05
+    ex = ote.expm_evolve(H0, E[0], [O], [0.03], psi0, T)
+    r = ote.rk4(H0, E[0], [O], [lambda t: 0.03], psi0, [0.0, T], 1e-5)[-1]
+    assert abs(np.linalg.norm(ex) - 1.0) < 1e-12
+    assert np.max(np.abs(r - ex)) < 1e-7
